@@ -1,0 +1,365 @@
+"""GB300 Barnes-Hut engine: Python host bindings over libbh_gpu.so (C ABI).
+
+The compute path is the CUDA library ``_build/libbh_gpu.so`` (built by
+``build.py``); this module only marshals numpy arrays through ctypes.  There is
+no CPU fallback: every compute call raises if the library is missing or no
+GPU is present.
+
+Reference-shaped entry points (YonatanGM/Barnes-Hut, single-rank ``--fc tree``):
+
+=========================  ===============================================
+``compute_local_bbox``     compute_local_bbox, src/bounding_box.cpp:23-44
+``generateMortonCodes``    generateMortonCodes, src/morton_keys.cpp:65-98
+``sortBodiesByMortonKey``  sortBodiesByMortonKey, include/utility.h:23-52
+``buildOctreeBottomUp``    buildOctreeBottomUp + exchangeFullTrees merge,
+                           src/linear_octree.cpp:13-107, 178-204
+``computeAccelerations``   computeAccelerations, src/traversal.cpp:13-103
+``Simulation.step``        the step loop of src/main.cpp:191-282
+``read_csv``               readCSV, src/io.cpp:16-81
+``kepler_to_cartesian``    convertKeplerToCartesian,
+                           src/kepler_to_cartesian.cpp:13-107
+=========================  ===============================================
+
+Arrays: positions/velocities/accelerations are (n, 3) float64 (the
+reference's Vec3 AoS), masses (n,) float64, ids and keys (n,) uint64.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+from pathlib import Path
+
+import numpy as np
+
+_PKG = Path(__file__).resolve().parent
+LIB_PATH = _PKG / "_build" / "libbh_gpu.so"
+
+G_DEFAULT = 1.48812e-34  # AU^3 kg^-1 day^-2 (src/main.cpp:174)
+THETA_DEFAULT = 1.05     # src/main.cpp:61
+MAX_DEPTH = 21
+NUM_MASSIVE = 9
+
+MODE_PLAIN_FP64 = 0
+MODE_FP64_LIST = 1
+MODE_FP32_FAR = 2
+MODE_LEARNED = 3
+
+STATUS = {
+    0: "BH_OK", 1: "BH_ERR_INVALID_ARGUMENT", 2: "BH_ERR_CUDA", 3: "BH_ERR_OUT_OF_MEMORY",
+    4: "BH_ERR_CAPACITY", 5: "BH_ERR_OVERFLOW", 6: "BH_ERR_TIMEOUT", 7: "BH_ERR_NONFINITE",
+    8: "BH_ERR_STATE", 9: "BH_ERR_IO", 10: "BH_ERR_NO_DEVICE",
+}
+
+
+class BhError(RuntimeError):
+    """A non-zero status from libbh_gpu.so, with the library's message."""
+
+    def __init__(self, status: int, message: str):
+        self.status = status
+        super().__init__(f"{STATUS.get(status, status)}: {message}")
+
+
+_lib = None
+_P = C.c_void_p
+_I64 = C.c_int64
+_D = C.c_double
+
+
+def _sig(lib):
+    f = {}
+    f["bh_last_error"] = (C.c_char_p, [])
+    f["bh_status_string"] = (C.c_char_p, [C.c_int])
+    f["bh_api_version"] = (C.c_int, [])
+    f["bh_context_create"] = (C.c_int, [_I64, C.c_int, C.POINTER(_P)])
+    f["bh_context_destroy"] = (C.c_int, [_P])
+    f["bh_context_sync"] = (C.c_int, [_P])
+    f["bh_context_stream"] = (C.c_int, [_P, C.POINTER(_P)])
+    f["bh_set_bodies"] = (C.c_int, [_P, _I64, _P, _P, _P, _P])
+    f["bh_get_bodies"] = (C.c_int, [_P, _P, _P, _P, _P, _P])
+    f["bh_set_accelerations"] = (C.c_int, [_P, _P])
+    f["bh_num_bodies"] = (C.c_int, [_P, C.POINTER(_I64)])
+    f["bh_compute_bbox"] = (C.c_int, [_P, _P])
+    f["bh_compute_keys"] = (C.c_int, [_P, _P])
+    f["bh_sort_bodies"] = (C.c_int, [_P, _P])
+    f["bh_build_tree"] = (C.c_int, [_P])
+    f["bh_tree_info"] = (C.c_int, [_P, C.POINTER(_I64), C.POINTER(_I64), C.POINTER(_I64)])
+    f["bh_export_tree"] = (C.c_int, [_P, _P, _P, _P, _P])
+    f["bh_compute_accelerations"] = (C.c_int, [_P, _D, _D, _D, C.c_int, _P])
+    f["bh_interaction_count"] = (C.c_int, [_P, C.POINTER(_I64)])
+    f["bh_step"] = (C.c_int, [_P, _D, _D, _D, _I64, C.c_int, C.POINTER(_D)])
+    f["bh_set_profiling"] = (C.c_int, [_P, C.c_int])
+    f["bh_phase_times"] = (C.c_int, [_P, _P, C.POINTER(_I64)])
+    f["bh_measure_fma_peak"] = (C.c_int, [_P, C.c_int, C.POINTER(_D)])
+    f["bh_direct_sum"] = (C.c_int, [_P, _I64, _P, _D, _P])
+    f["bh_invariants"] = (C.c_int, [_P, _D, _D, _P])
+    f["bh_compute_local_bbox"] = (C.c_int, [_P, _I64, _P])
+    f["bh_generate_morton_codes"] = (C.c_int, [_P, _I64, _P, _P])
+    f["bh_sort_bodies_by_morton_key"] = (C.c_int, [_I64, _P, _P, _P, _P, _P])
+    f["bh_kepler_to_cartesian"] = (C.c_int, [_P, _I64, _P])
+    f["bh_generate_system"] = (C.c_int, [C.c_uint64, _I64, _D, _D, _P, _P, _P, _P])
+    f["bh_read_csv"] = (C.c_int, [C.c_char_p, _I64, C.POINTER(_I64), _P, _P, _P, _P])
+    f["bh_write_csv"] = (C.c_int, [C.c_char_p, _I64, _P, _P, _P, _P])
+    for name, (res, args) in f.items():
+        if hasattr(lib, name):
+            fn = getattr(lib, name)
+            fn.restype = res
+            fn.argtypes = args
+    return lib
+
+
+def library():
+    """The loaded libbh_gpu.so; raises if it has not been built."""
+    global _lib
+    if _lib is None:
+        if not LIB_PATH.exists():
+            raise RuntimeError(f"{LIB_PATH} is missing: build the CUDA extension first "
+                               "(python barnes-hut_gb300/build.py)")
+        _lib = _sig(C.CDLL(str(LIB_PATH)))
+    return _lib
+
+
+def _check(rc: int) -> None:
+    if rc != 0:
+        raise BhError(rc, library().bh_last_error().decode(errors="replace"))
+
+
+def _ptr(a: np.ndarray | None):
+    return None if a is None else a.ctypes.data_as(C.c_void_p)
+
+
+def _f64(a, shape=None) -> np.ndarray:
+    a = np.ascontiguousarray(a, dtype=np.float64)
+    if shape is not None:
+        a = a.reshape(shape)
+    return a
+
+
+def _u64(a) -> np.ndarray:
+    return np.ascontiguousarray(a, dtype=np.uint64)
+
+
+# ---------------------------------------------------------------- host side
+def kepler_to_cartesian(elements) -> np.ndarray:
+    """convertKeplerToCartesian for rows {e, a, i, omega, Omega, M, epoch, mu}."""
+    el = _f64(elements).reshape(-1, 8)
+    out = np.empty((el.shape[0], 6))
+    _check(library().bh_kepler_to_cartesian(_ptr(el), el.shape[0], _ptr(out)))
+    return out
+
+
+def generate_system(seed: int, n: int, frac_outer: float = 0.1, frac_trojan: float = 0.0):
+    """Seeded synthetic solar system: (pos, vel, mass, ids)."""
+    pos = np.empty((n, 3)); vel = np.empty((n, 3)); mass = np.empty(n); ids = np.empty(n, np.uint64)
+    _check(library().bh_generate_system(seed, n, frac_outer, frac_trojan, _ptr(pos), _ptr(vel), _ptr(mass),
+                                        _ptr(ids)))
+    return pos, vel, mass, ids
+
+
+def read_csv(path, body_count: int = -1):
+    """readCSV: (ids, mass, pos, vel)."""
+    lib = library()
+    n = _I64(0)
+    p = str(path).encode()
+    _check(lib.bh_read_csv(p, body_count, C.byref(n), None, None, None, None))
+    ids = np.empty(n.value, np.uint64); mass = np.empty(n.value); pos = np.empty((n.value, 3))
+    vel = np.empty((n.value, 3))
+    _check(lib.bh_read_csv(p, body_count, C.byref(n), _ptr(ids), _ptr(mass), _ptr(pos), _ptr(vel)))
+    return ids, mass, pos, vel
+
+
+def write_csv(path, ids, mass, pos, vel) -> None:
+    ids = _u64(ids); mass = _f64(mass); pos = _f64(pos); vel = _f64(vel)
+    _check(library().bh_write_csv(str(path).encode(), len(mass), _ptr(ids), _ptr(mass), _ptr(pos), _ptr(vel)))
+
+
+# ---------------------------------------------------------------- device context
+class Context:
+    """A device-resident body set on one GPU (bh_context)."""
+
+    def __init__(self, capacity: int, device: int = 0):
+        self._h = C.c_void_p()
+        _check(library().bh_context_create(int(capacity), int(device), C.byref(self._h)))
+        self.capacity = int(capacity)
+
+    def close(self) -> None:
+        if self._h:
+            library().bh_context_destroy(self._h)
+            self._h = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    @property
+    def handle(self):
+        return self._h
+
+    @property
+    def n(self) -> int:
+        v = _I64(0)
+        _check(library().bh_num_bodies(self._h, C.byref(v)))
+        return v.value
+
+    def stream(self) -> int:
+        s = C.c_void_p()
+        _check(library().bh_context_stream(self._h, C.byref(s)))
+        return s.value or 0
+
+    def sync(self) -> None:
+        _check(library().bh_context_sync(self._h))
+
+    def set_bodies(self, pos, vel, mass, ids=None) -> None:
+        pos = _f64(pos).reshape(-1, 3)
+        n = pos.shape[0]
+        vel = _f64(vel).reshape(n, 3)
+        mass = _f64(mass).reshape(n)
+        ids = np.arange(n, dtype=np.uint64) if ids is None else _u64(ids)
+        _check(library().bh_set_bodies(self._h, n, _ptr(pos), _ptr(vel), _ptr(mass), _ptr(ids)))
+
+    def set_accelerations(self, acc) -> None:
+        acc = _f64(acc).reshape(-1, 3)
+        _check(library().bh_set_accelerations(self._h, _ptr(acc)))
+
+    def get_bodies(self, out=None):
+        """(pos, vel, mass, ids, acc) in the current (last sorted) order;
+        `out` may supply the five destination arrays (e.g. pinned memory)."""
+        n = self.n
+        if out is None:
+            out = (np.empty((n, 3)), np.empty((n, 3)), np.empty(n), np.empty(n, np.uint64), np.empty((n, 3)))
+        pos, vel, mass, ids, acc = out
+        _check(library().bh_get_bodies(self._h, _ptr(pos), _ptr(vel), _ptr(mass), _ptr(ids), _ptr(acc)))
+        return pos, vel, mass, ids, acc
+
+    def compute_bbox(self) -> np.ndarray:
+        out = np.empty(6)
+        _check(library().bh_compute_bbox(self._h, _ptr(out)))
+        return out
+
+    def compute_keys(self) -> np.ndarray:
+        out = np.empty(self.n, np.uint64)
+        _check(library().bh_compute_keys(self._h, _ptr(out)))
+        return out
+
+    def sort_bodies(self) -> np.ndarray:
+        perm = np.empty(self.n, np.int64)
+        _check(library().bh_sort_bodies(self._h, _ptr(perm)))
+        return perm
+
+    def build_tree(self) -> None:
+        _check(library().bh_build_tree(self._h))
+
+    def tree_info(self):
+        r, nn, nl = _I64(0), _I64(0), _I64(0)
+        _check(library().bh_tree_info(self._h, C.byref(r), C.byref(nn), C.byref(nl)))
+        return {"records": r.value, "nodes": nn.value, "leaves": nl.value}
+
+    def export_tree(self):
+        """The reference's node set sorted by (depth, prefix):
+        (prefix u64, depth u8, mass f64, com (k,3) f64)."""
+        k = self.tree_info()["records"]
+        prefix = np.empty(k, np.uint64); depth = np.empty(k, np.uint8); mass = np.empty(k)
+        com = np.empty((k, 3))
+        _check(library().bh_export_tree(self._h, _ptr(prefix), _ptr(depth), _ptr(mass), _ptr(com)))
+        return prefix, depth, mass, com
+
+    def compute_accelerations(self, theta=THETA_DEFAULT, G=G_DEFAULT, soft2=0.0, mode=MODE_PLAIN_FP64,
+                              download=True):
+        out = np.empty((self.n, 3)) if download else None
+        _check(library().bh_compute_accelerations(self._h, theta, G, soft2, mode, _ptr(out)))
+        return out
+
+    def interaction_count(self) -> int:
+        v = _I64(0)
+        _check(library().bh_interaction_count(self._h, C.byref(v)))
+        return v.value
+
+    def set_profiling(self, on: bool = True) -> None:
+        _check(library().bh_set_profiling(self._h, 1 if on else 0))
+
+    PHASES = ("kick_drift_bbox", "keys", "sort", "permute", "build", "forces")
+
+    def phase_times(self):
+        """(dict phase -> accumulated device ms, kernel launches so far)."""
+        ms = np.zeros(8)
+        nl = _I64(0)
+        _check(library().bh_phase_times(self._h, _ptr(ms), C.byref(nl)))
+        return dict(zip(self.PHASES, ms[:6].tolist())), nl.value
+
+    def launches(self) -> int:
+        return self.phase_times()[1]
+
+    def measure_fma_peak(self, fp64: bool = True) -> float:
+        v = _D(0.0)
+        _check(library().bh_measure_fma_peak(self._h, 1 if fp64 else 0, C.byref(v)))
+        return v.value
+
+    def direct_sum(self, targets, G=G_DEFAULT) -> np.ndarray:
+        """FP64 direct-sum accelerations of the bodies at positions `targets`
+        of the current order."""
+        t = np.ascontiguousarray(targets, np.int64)
+        out = np.empty((len(t), 3))
+        _check(library().bh_direct_sum(self._h, len(t), _ptr(t), G, _ptr(out)))
+        return out
+
+    def invariants(self, G=G_DEFAULT, theta=THETA_DEFAULT) -> dict:
+        out = np.empty(9)
+        _check(library().bh_invariants(self._h, G, theta, _ptr(out)))
+        return dict(E=out[0], K=out[1], U=out[2], L=out[3:6].copy(), P=out[6:9].copy())
+
+    def step(self, dt, theta=THETA_DEFAULT, G=G_DEFAULT, nsteps=1, mode=MODE_PLAIN_FP64, t=None) -> float:
+        tv = _D(0.0 if t is None else t)
+        _check(library().bh_step(self._h, dt, theta, G, int(nsteps), mode, None if t is None else C.byref(tv)))
+        return tv.value
+
+
+# ------------------------------------------------- reference-named functions
+def compute_local_bbox(pos) -> np.ndarray:
+    pos = _f64(pos).reshape(-1, 3)
+    out = np.empty(6)
+    _check(library().bh_compute_local_bbox(_ptr(pos), pos.shape[0], _ptr(out)))
+    return out
+
+
+def generateMortonCodes(pos, bbox) -> np.ndarray:  # noqa: N802 (reference name)
+    pos = _f64(pos).reshape(-1, 3)
+    bb = _f64(bbox).reshape(6)
+    out = np.empty(pos.shape[0], np.uint64)
+    _check(library().bh_generate_morton_codes(_ptr(pos), pos.shape[0], _ptr(bb), _ptr(out)))
+    return out
+
+
+def sortBodiesByMortonKey(keys, pos, mass, vel, ids):  # noqa: N802
+    """Returns sorted copies (keys, pos, mass, vel, ids)."""
+    keys = _u64(keys).copy(); pos = _f64(pos).reshape(-1, 3).copy(); mass = _f64(mass).copy()
+    vel = _f64(vel).reshape(-1, 3).copy(); ids = _u64(ids).copy()
+    _check(library().bh_sort_bodies_by_morton_key(len(keys), _ptr(keys), _ptr(pos), _ptr(mass), _ptr(vel),
+                                                  _ptr(ids)))
+    return keys, pos, mass, vel, ids
+
+
+def buildOctreeBottomUp(pos, vel, mass, ids=None, ctx: Context | None = None):  # noqa: N802
+    """Loads the bodies, computes bbox/keys, sorts and builds; returns the
+    context holding the tree (export with ``ctx.export_tree()``)."""
+    pos = _f64(pos).reshape(-1, 3)
+    own = ctx is None
+    if own:
+        ctx = Context(max(1, pos.shape[0]))
+    ctx.set_bodies(pos, vel, mass, ids)
+    ctx.compute_bbox()
+    ctx.compute_keys()
+    ctx.sort_bodies()
+    ctx.build_tree()
+    return ctx
+
+
+def computeAccelerations(ctx: Context, theta=THETA_DEFAULT, G=G_DEFAULT, soft2=0.0,  # noqa: N802
+                         mode=MODE_PLAIN_FP64) -> np.ndarray:
+    return ctx.compute_accelerations(theta, G, soft2, mode)

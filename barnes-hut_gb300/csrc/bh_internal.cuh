@@ -1,0 +1,177 @@
+// Internal definitions shared by the CUDA translation units of libbh_gpu.so.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <cstdint>
+#include <vector>
+
+#include "bh_common.h"
+
+#define BH_CUDA_TRY(expr)                                                               \
+    do {                                                                                \
+        cudaError_t bh_e_ = (expr);                                                     \
+        if (bh_e_ != cudaSuccess)                                                       \
+            return bh_fail(BH_ERR_CUDA, std::string(#expr) + ": " + cudaGetErrorString(bh_e_)); \
+    } while (0)
+
+// After a kernel launch: report a launch error, count the launch.
+#define BH_LAUNCH_CHECK(ctx)        \
+    do {                            \
+        BH_CUDA_TRY(cudaGetLastError()); \
+        ++(ctx)->launches;          \
+    } while (0)
+
+namespace bh {
+
+constexpr int kMaxDepth = 21;          // depth of a leaf (one body key)
+constexpr int kSortPasses = 8;         // 8-bit digits over the 63-bit key
+constexpr int kRadix = 256;
+constexpr int kSortThreads = 512;      // onesweep tile: 512 threads x 8 keys
+constexpr int kSortItems = 8;
+constexpr int kSortTile = kSortThreads * kSortItems;
+constexpr int kNumSMs = 152;
+
+// Device error word bits (OR-ed by kernels, read back by bh_context_sync).
+enum : unsigned {
+    kErrNonFinite = 1u << 0,
+    kErrTimeout = 1u << 1,
+    kErrOverflow = 1u << 2,
+    kErrCapacity = 1u << 3,
+};
+
+// Bits of a key kept by mortonPrefix(key, d) (src/morton_keys.cpp:28-32).
+__host__ __device__ inline uint64_t prefix_mask(int d)
+{
+    return d == 0 ? 0ull : (~0ull << (63 - 3 * d));
+}
+
+// Deepest depth at which two distinct keys share a cell: 0..20.
+__device__ inline int common_depth(uint64_t a, uint64_t b)
+{
+    const int hb = 63 - __clzll((long long)(a ^ b));  // highest differing bit, 0..62
+    return (62 - hb) / 3;
+}
+
+// One node of the compressed octree as the traversal reads it (48 bytes).
+// A node stands for the reference's chain of single-child nodes from depth
+// `top` down to `depth` (all with identical mass and centre of mass), so it
+// is accepted exactly when the reference would accept any node of the chain.
+struct __align__(16) TreeRec {
+    double cx, cy, cz;  // centre of mass after the single-rank merge
+    double m;           // mass
+    int32_t child;      // first child slot, or -1 for a leaf
+    int32_t leaf;       // leaf id for a leaf, -1 otherwise
+    uint8_t nchild;     // 0 for a leaf, 2..8 otherwise
+    uint8_t depth;      // bottom depth of the chain (21 for a leaf)
+    uint8_t top;        // top depth of the chain
+    uint8_t pad0;
+    int32_t pad1;
+};
+static_assert(sizeof(TreeRec) == 48, "TreeRec layout");
+
+}  // namespace bh
+
+// The context behind the opaque bh_context handle.
+struct bh_context {
+    int device = 0;
+    cudaStream_t stream = nullptr;
+    int64_t cap = 0;  // bodies the buffers hold
+    int64_t n = 0;    // bodies currently loaded
+    double t = 0.0;   // simulation time (bh_step)
+    void* alloc_base = nullptr;  // the single device allocation
+
+    // Body state, structure of arrays, in the current (last sorted) order.
+    double *px = nullptr, *py = nullptr, *pz = nullptr;
+    double *vx = nullptr, *vy = nullptr, *vz = nullptr;
+    double *ax = nullptr, *ay = nullptr, *az = nullptr;
+    double* m = nullptr;
+    uint64_t* id = nullptr;
+    uint64_t* key = nullptr;
+    // Second body set; the permutation gathers into it, then the sets swap.
+    double *px2 = nullptr, *py2 = nullptr, *pz2 = nullptr;
+    double *vx2 = nullptr, *vy2 = nullptr, *vz2 = nullptr;
+    double* m2 = nullptr;
+    uint64_t* id2 = nullptr;
+
+    // Radix sort scratch.
+    uint64_t* key_alt = nullptr;
+    uint32_t* perm = nullptr;      // after the sort: previous position per slot
+    uint32_t* perm_alt = nullptr;
+    uint32_t* hist = nullptr;      // kSortPasses x 256 digit counts, then starts
+    uint32_t* lookback = nullptr;  // kSortPasses x tiles x 256 status words
+    uint32_t* tile_ctr = nullptr;  // kSortPasses tile counters
+    int64_t max_tiles = 0;
+
+    // Bounding box: 6 doubles, block partials and the last-block ticket.
+    double* bbox = nullptr;
+    double* bbox_part = nullptr;
+    unsigned* bbox_ticket = nullptr;
+    int bbox_blocks = 0;
+
+    // Tree build (sizes in bodies; L <= n leaves, B <= n branching nodes).
+    int32_t* head = nullptr;        // scan scratch, n + 1
+    int32_t* leaf_first = nullptr;  // first body of each leaf, n + 1
+    int32_t* body_leaf = nullptr;   // leaf id of each body
+    uint64_t* leaf_key = nullptr;
+    double *leaf_m = nullptr, *leaf_wx = nullptr, *leaf_wy = nullptr, *leaf_wz = nullptr;
+    int8_t* cdep = nullptr;         // common depth of leaves j-1, j (boundary j)
+    int32_t* rep_node = nullptr;    // branching-node id of a representative boundary
+    int32_t* node_rep = nullptr;    // representative boundary of each node
+    int32_t* node_a = nullptr;      // first leaf of each node
+    int32_t* node_nchild = nullptr;
+    int32_t* node_cs = nullptr;     // first child slot
+    uint8_t* node_depth = nullptr;
+    double *node_m = nullptr, *node_wx = nullptr, *node_wy = nullptr, *node_wz = nullptr;
+    int32_t* slot_ref = nullptr;    // >= 0 leaf id, < 0 ~node id
+    uint8_t* slot_top = nullptr;
+    int32_t* depth_off = nullptr;   // 23 offsets into depth_nodes (by depth)
+    int32_t* depth_nodes = nullptr; // node ids bucketed by depth
+    bh::TreeRec* rec = nullptr;     // traversal records, slot 0 = root
+    int32_t* counts = nullptr;      // device scalars: [0]=L, [1]=B, [2]=slots
+    int32_t* scan_tmp = nullptr;    // block sums of the device scans
+    bool tree_valid = false;
+    bool keys_valid = false;   // keys and their digit histograms are current
+    bool bbox_valid = false;
+    bool sorted_valid = false; // bodies are in sorted-key order
+
+    // Traversal.
+    unsigned long long* inter_count = nullptr;
+
+    // Phase timing (bh_set_profiling): CUDA events around each phase of a
+    // step, read back at the next synchronisation.
+    bool prof = false;
+    std::vector<cudaEvent_t> ev_pool;
+    size_t ev_used = 0;
+    struct Mark { int phase; cudaEvent_t a, b; };
+    std::vector<Mark> marks;
+    double phase_ms[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+    int64_t launches = 0;  // kernels of this library enqueued so far
+
+    // Error word raised by kernels and a pinned mirror for readback.
+    unsigned* err = nullptr;
+    unsigned* h_err = nullptr;
+    double* h_small = nullptr;  // pinned host scratch (64 doubles)
+};
+
+namespace bh {
+
+// Kernel launch wrappers (defined in the .cu files).  Each enqueues on
+// ctx->stream and returns BH_OK or a launch error.
+int launch_drift_bbox(bh_context* ctx, double dt, bool kick, bool drift);
+int launch_keys(bh_context* ctx, bool with_hist);
+int launch_hist(bh_context* ctx);
+int bbox_partial_bytes(int blocks);
+size_t sort_smem_bytes();
+int64_t scan_tmp_ints(int64_t n_max);
+int launch_sort(bh_context* ctx);
+int launch_permute(bh_context* ctx);
+int launch_build(bh_context* ctx);
+int launch_traverse(bh_context* ctx, double theta, double G, double soft2, int mode, double kick_h);
+
+// Device-wide exclusive scan of n int32 values (in may equal out); the
+// total is written to *total (device pointer).  n is read from n_dev when
+// n_dev != nullptr (device-side count, at most n_max), else n_max is used.
+int device_exclusive_scan(bh_context* ctx, const int32_t* in, int32_t* out, int64_t n_max,
+                          const int32_t* n_dev, int32_t* total);
+
+}  // namespace bh

@@ -1,0 +1,125 @@
+// Device-wide exclusive scan of int32 values (reduce, scan of block sums,
+// down-sweep).  Used by the tree build to number leaves, branching nodes and
+// child slots.  No block waits on another block.
+#include "bh_internal.cuh"
+
+namespace bh {
+namespace {
+
+constexpr int kScanThreads = 512;
+constexpr int kScanItems = 4;
+constexpr int kScanBlock = kScanThreads * kScanItems;
+
+__device__ inline int64_t scan_n(int64_t n_max, const int32_t* n_dev)
+{
+    if (!n_dev) return n_max;
+    const int64_t v = *n_dev;
+    return v < n_max ? v : n_max;
+}
+
+// Block-wide inclusive scan of one value per thread; returns the inclusive
+// value and writes the block total to *total.
+__device__ int32_t block_inclusive(int32_t x, int32_t* warp_tot, int32_t* total)
+{
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+#pragma unroll
+    for (int off = 1; off < 32; off <<= 1) {
+        const int32_t y = __shfl_up_sync(0xffffffffu, x, off);
+        if (lane >= off) x += y;
+    }
+    if (lane == 31) warp_tot[w] = x;
+    __syncthreads();
+    if (w == 0) {
+        int32_t t = lane < (int)(blockDim.x >> 5) ? warp_tot[lane] : 0;
+#pragma unroll
+        for (int off = 1; off < 32; off <<= 1) {
+            const int32_t y = __shfl_up_sync(0xffffffffu, t, off);
+            if (lane >= off) t += y;
+        }
+        warp_tot[lane] = t;
+    }
+    __syncthreads();
+    const int32_t r = x + (w > 0 ? warp_tot[w - 1] : 0);
+    if (threadIdx.x == blockDim.x - 1) *total = r;
+    __syncthreads();
+    return r;
+}
+
+__global__ void __launch_bounds__(kScanThreads) scan_reduce_kernel(const int32_t* __restrict__ in, int64_t n_max,
+                                                                  const int32_t* __restrict__ n_dev,
+                                                                  int32_t* __restrict__ bsum)
+{
+    __shared__ int32_t warp_tot[32];
+    __shared__ int32_t total;
+    const int64_t n = scan_n(n_max, n_dev);
+    const int64_t base = (int64_t)blockIdx.x * kScanBlock + (int64_t)threadIdx.x * kScanItems;
+    int32_t s = 0;
+#pragma unroll
+    for (int k = 0; k < kScanItems; ++k)
+        if (base + k < n) s += in[base + k];
+    block_inclusive(s, warp_tot, &total);
+    if (threadIdx.x == 0) bsum[blockIdx.x] = total;
+}
+
+__global__ void __launch_bounds__(1024) scan_bsum_kernel(int32_t* __restrict__ bsum, int nb, int32_t* __restrict__ total)
+{
+    __shared__ int32_t warp_tot[32];
+    __shared__ int32_t chunk;
+    int32_t carry = 0;
+    for (int base = 0; base < nb; base += blockDim.x) {
+        const int i = base + threadIdx.x;
+        const int32_t v = i < nb ? bsum[i] : 0;
+        const int32_t inc = block_inclusive(v, warp_tot, &chunk);
+        if (i < nb) bsum[i] = carry + inc - v;
+        carry += chunk;
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) *total = carry;
+}
+
+__global__ void __launch_bounds__(kScanThreads) scan_down_kernel(const int32_t* in, int32_t* out, int64_t n_max,
+                                                                const int32_t* __restrict__ n_dev,
+                                                                const int32_t* __restrict__ bsum)
+{
+    __shared__ int32_t warp_tot[32];
+    __shared__ int32_t total;
+    const int64_t n = scan_n(n_max, n_dev);
+    const int64_t base = (int64_t)blockIdx.x * kScanBlock + (int64_t)threadIdx.x * kScanItems;
+    int32_t v[kScanItems];
+    int32_t s = 0;
+#pragma unroll
+    for (int k = 0; k < kScanItems; ++k) {
+        v[k] = base + k < n ? in[base + k] : 0;
+        s += v[k];
+    }
+    const int32_t inc = block_inclusive(s, warp_tot, &total);
+    int32_t run = bsum[blockIdx.x] + inc - s;
+#pragma unroll
+    for (int k = 0; k < kScanItems; ++k) {
+        if (base + k < n) out[base + k] = run;
+        run += v[k];
+    }
+}
+
+}  // namespace
+
+int64_t scan_tmp_ints(int64_t n_max) { return (n_max + kScanBlock - 1) / kScanBlock + 64; }
+
+int device_exclusive_scan(bh_context* ctx, const int32_t* in, int32_t* out, int64_t n_max, const int32_t* n_dev,
+                          int32_t* total)
+{
+    if (n_max <= 0) {
+        BH_CUDA_TRY(cudaMemsetAsync(total, 0, sizeof(int32_t), ctx->stream));
+        return BH_OK;
+    }
+    const int nb = (int)((n_max + kScanBlock - 1) / kScanBlock);
+    scan_reduce_kernel<<<nb, kScanThreads, 0, ctx->stream>>>(in, n_max, n_dev, ctx->scan_tmp);
+    BH_LAUNCH_CHECK(ctx);
+    scan_bsum_kernel<<<1, 1024, 0, ctx->stream>>>(ctx->scan_tmp, nb, total);
+    BH_LAUNCH_CHECK(ctx);
+    scan_down_kernel<<<nb, kScanThreads, 0, ctx->stream>>>(in, out, n_max, n_dev, ctx->scan_tmp);
+    BH_LAUNCH_CHECK(ctx);
+    return BH_OK;
+}
+
+}  // namespace bh

@@ -1,0 +1,322 @@
+#!/usr/bin/env python3
+"""Throughput of the single-rank `--fc tree` Barnes-Hut step on GB300.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+
+Metric: body-steps/s (bodies x steps / second) of the full step of
+src/main.cpp:191-282 -- kick, drift, bounding box, Morton keys, radix sort,
+permutation, octree build with the single-rank merge, forces, kick -- on the
+plain FP64 theta = 1.05 workload of 300,149 bodies (Sun, 8 planets, 300,140
+asteroids of which 10 % in the outer belt), dt = 1 h.  Inputs are synthetic
+and seeded (the reference's 300k CSV is not part of its repository).
+
+* value: device time (CUDA events on the engine's stream), state resident in
+  HBM, L2 flushed (256 MiB write) before every timed step.
+* e2e: the same steps through the C ABI with the state on the host: each
+  step uploads pos, vel, mass, ids and acc from pinned memory and downloads
+  them again (host clock around upload + step + download).
+* roofline: the force kernel (the dominant phase) against the FP64 FMA peak
+  measured in the same process; algorithmic work = 20 flops per accepted
+  interaction (the conventional monopole count), interactions counted on the
+  device.
+* cpu_baseline: the oracle (C restatement of the reference's path, OpenMP,
+  every host core) on the same workload, a bounded number of steps.
+
+Multi-GPU: the path does not shard on one GPU per rank; ranks run replicas
+(weak scaling) and value is the sum of their body-steps over the slowest
+rank's time.  `--impl reference` times the reference's CPU path (the oracle
+port on hosts without the reference checkout) on rank 0 only.
+"""
+from __future__ import annotations
+
+import argparse
+import importlib
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+from pathlib import Path
+
+import numpy as np
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT))
+
+G = 1.48812e-34
+THETA = 1.05
+DT = 1.0 / 24.0
+N_BODIES = 300_149
+SEED = 2
+FLOPS_PER_INTERACTION = 20
+L2_FLUSH_BYTES = 256 << 20
+WORKLOAD = "plain FP64 theta=1.05, dt=1h, 300,149 bodies (Sun, 8 planets, 300,140 asteroids, 10% outer belt)"
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--bodies", type=int, default=N_BODIES)
+    ap.add_argument("--e2e-steps", type=int, default=5)
+    ap.add_argument("--cpu-seconds", type=float, default=15.0, help="budget of the CPU-baseline sample")
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    return ap.parse_args()
+
+
+def dist_init():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    if ws <= 1:
+        return 0, 1, 0
+    import torch
+    import torch.distributed as dist
+    rank = int(os.environ["RANK"])
+    local = int(os.environ.get("LOCAL_RANK", rank))
+    torch.cuda.set_device(local)
+    dist.init_process_group("nccl")
+    return rank, ws, local
+
+
+class ClockSampler:
+    """nvidia-smi samples (200 ms) of SM clock and throttle reasons."""
+
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device: int):
+        self.device = device
+        self.proc = None
+        self.lines = []
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.device), f"--query-gpu={self.Q}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except (OSError, FileNotFoundError):
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def __exit__(self, *exc):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self):
+        sm, mx, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            f = [x.strip() for x in ln.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                mx = float(f[2])
+            except ValueError:
+                continue
+            for nm, v in zip(names, f[5:9]):
+                if v.lower().startswith("active"):
+                    reasons.add(nm)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": mx, "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def cpu_baseline(pos, vel, mass, ids, budget_s: float, nsteps_max: int = 20):
+    """Times the oracle's step loop on all host cores for a bounded sample."""
+    from oracle.oracle import Oracle
+    o = Oracle("port")
+    kind = "port"
+    try:
+        ref = Oracle("reference")
+        o, kind = ref, "reference"
+    except (FileNotFoundError, OSError):
+        pass
+    n = len(mass)
+    t0 = time.perf_counter()
+    p, v, m, i, a, t, _ = o.simulate(pos, vel, mass, ids, DT, THETA, G, 1)
+    first = time.perf_counter() - t0
+    extra = max(0, min(nsteps_max - 1, int(budget_s / max(first, 1e-3)) - 1))
+    t1 = time.perf_counter()
+    if extra:
+        o.simulate(p, v, m, i, DT, THETA, G, extra, t=t, acc=a)
+    rest = time.perf_counter() - t1
+    steps = 1 + extra
+    secs = first + rest
+    cores = Oracle("port").threads()
+    return {"value": n * steps / secs, "unit": "body-steps/s", "cores": cores, "kind": kind,
+            "sample": f"{steps} full steps of the {n:,}-body workload ({secs:.1f} s, OpenMP {cores} threads)"}
+
+
+def run_reference(args, rank):
+    if rank != 0:
+        return
+    bh = importlib.import_module("barnes-hut_gb300")
+    pos, vel, mass, ids = bh.generate_system(SEED, args.bodies, 0.1, 0.0)
+    from oracle.oracle import Oracle
+    o, kind = Oracle("port"), "port"
+    try:
+        o, kind = Oracle("reference"), "reference"
+    except (FileNotFoundError, OSError):
+        pass
+    n = len(mass)
+    # warm-up and timed steps, each a full step of the same workload; the
+    # number of timed steps is capped so the run stays within minutes.
+    p, v, m, i, a, t, _ = o.simulate(pos, vel, mass, ids, DT, THETA, G, max(1, min(args.warmup, 1)))
+    t0 = time.perf_counter()
+    p, v, m, i, a, t, _ = o.simulate(p, v, m, i, DT, THETA, G, 1, t=t, acc=a)
+    one = time.perf_counter() - t0
+    k = max(1, min(args.steps, int(90.0 / max(one, 1e-3))))
+    t0 = time.perf_counter()
+    if k > 1:
+        o.simulate(p, v, m, i, DT, THETA, G, k - 1, t=t, acc=a)
+    secs = one + (time.perf_counter() - t0)
+    val = n * k / secs
+    cores = Oracle("port").threads()
+    line = {"metric": "body-steps/s", "value": val, "unit": "body-steps/s", "n_gpus": args.gpus, "steps": k,
+            "warmup": 1, "ms_per_step": 1e3 * secs / k, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f64", "data": "synthetic", "impl": "reference",
+            "config": {"workload": WORKLOAD, "bodies": n, "theta": THETA, "dt_days": DT},
+            "cpu_baseline": {"value": val, "unit": "body-steps/s", "cores": cores, "kind": kind,
+                             "sample": f"{k} timed steps after 1 warm-up step, OpenMP {cores} threads"},
+            "e2e": {"value": val, "unit": "body-steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+def run_ours(args, rank, ws, local):
+    import torch
+    bh = importlib.import_module("barnes-hut_gb300")
+    dev = local
+    torch.cuda.set_device(dev)
+    pos, vel, mass, ids = bh.generate_system(SEED, args.bodies, 0.1, 0.0)
+    n = len(mass)
+    ctx = bh.Context(n, dev)
+    ext = torch.cuda.ExternalStream(ctx.stream(), device=dev)
+    flush = torch.empty(L2_FLUSH_BYTES // 4, dtype=torch.float32, device=f"cuda:{dev}")
+    ctx.set_bodies(pos, vel, mass, ids)
+    t = 0.0
+    for _ in range(args.warmup):
+        t = ctx.step(DT, THETA, G, 1, bh.MODE_PLAIN_FP64, t=t)
+    peak_fp64 = ctx.measure_fma_peak(True)
+
+    ctx.set_profiling(True)
+    l0 = ctx.launches()
+    times, inter = [], 0
+    barrier(ws)
+    with ClockSampler(dev) as clk:
+        for _ in range(args.steps):
+            flush.fill_(1.0)
+            torch.cuda.synchronize(dev)
+            e0 = torch.cuda.Event(enable_timing=True)
+            e1 = torch.cuda.Event(enable_timing=True)
+            e0.record(ext)
+            t = ctx.step(DT, THETA, G, 1, bh.MODE_PLAIN_FP64, t=t)
+            e1.record(ext)
+            e1.synchronize()
+            times.append(e0.elapsed_time(e1))
+            inter += ctx.interaction_count()
+    torch.cuda.synchronize(dev)
+    launches = ctx.launches() - l0
+    phases, _ = ctx.phase_times()
+    ctx.set_profiling(False)
+    total_ms = sum(times)
+    total_ms = reduce_max(total_ms, ws)
+
+    # End to end through the C ABI with host-resident state (pinned memory).
+    pin = lambda shape, dt: torch.empty(shape, dtype=dt, pin_memory=True).numpy()  # noqa: E731
+    hp, hv, hm = pin((n, 3), torch.float64), pin((n, 3), torch.float64), pin((n,), torch.float64)
+    hi = pin((n,), torch.int64).view(np.uint64)
+    ha = pin((n, 3), torch.float64)
+    hp[:], hv[:], hm[:], hi[:], ha[:] = ctx.get_bodies()
+    e2e_steps = max(1, args.e2e_steps)
+    barrier(ws)
+    t0 = time.perf_counter()
+    for _ in range(e2e_steps):
+        ctx.set_bodies(hp, hv, hm, hi)
+        ctx.set_accelerations(ha)
+        t = ctx.step(DT, THETA, G, 1, bh.MODE_PLAIN_FP64, t=t)
+        ctx.get_bodies(out=(hp, hv, hm, hi, ha))
+    e2e_s = reduce_max(time.perf_counter() - t0, ws)
+    h2d = hp.nbytes + hv.nbytes + hm.nbytes + hi.nbytes + ha.nbytes
+    d2h = h2d
+
+    cpu = None
+    if rank == 0 and not args.no_cpu_baseline:
+        cpu = cpu_baseline(pos, vel, mass, ids, args.cpu_seconds)
+    ctx.close()
+    if rank != 0:
+        return
+    k = args.steps
+    force_ms = phases["forces"] / k
+    inter_per_step = inter / k
+    achieved = inter_per_step * FLOPS_PER_INTERACTION / (force_ms * 1e-3) / 1e12
+    value = ws * n * k / (total_ms * 1e-3)
+    line = {
+        "metric": "body-steps/s", "value": value, "unit": "body-steps/s", "n_gpus": ws, "steps": k,
+        "warmup": args.warmup, "ms_per_step": total_ms / k, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f64",
+        "data": "synthetic (seeded solar system generated through bh_generate_system)",
+        "config": {"workload": WORKLOAD, "bodies": n, "theta": THETA, "dt_days": DT, "mode": "plain_fp64",
+                   "seed": SEED, "l2": "flushed before every timed step (256 MiB write)",
+                   "parallelism": f"replicas x{ws}"},
+        "roofline": {"kernel": "traverse_exact_kernel", "bound": "fp64", "achieved": achieved,
+                     "peak": peak_fp64, "unit": "TFLOP/s", "frac": achieved / peak_fp64,
+                     "peak_source": "measured in-process: FP64 FMA chains (bh_measure_fma_peak)",
+                     "work": f"{FLOPS_PER_INTERACTION} flops x {inter_per_step:.4g} interactions per launch",
+                     "traffic": None},
+        "phases_ms_per_step": {kk: v / k for kk, v in phases.items()},
+        "interactions_per_body": inter_per_step / n,
+        "e2e": {"value": ws * n * e2e_steps / e2e_s, "unit": "body-steps/s", "h2d_bytes_per_step": h2d,
+                "d2h_bytes_per_step": d2h},
+        "gpu_launches": launches,
+        "clocks": clk.summary(),
+        "cpu_baseline": cpu,
+    }
+    print(json.dumps(line), flush=True)
+
+
+def barrier(ws):
+    if ws > 1:
+        import torch.distributed as dist
+        dist.barrier()
+
+
+def reduce_max(x: float, ws: int) -> float:
+    if ws <= 1:
+        return x
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([x], dtype=torch.float64, device="cuda")
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def main():
+    args = parse()
+    rank, ws, local = (0, 1, 0)
+    if args.impl == "reference":
+        rank = int(os.environ.get("RANK", "0"))
+        run_reference(args, rank)
+        return
+    rank, ws, local = dist_init()
+    run_ours(args, rank, ws, local)
+    if ws > 1:
+        import torch.distributed as dist
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,200 @@
+/*
+ * bh_gpu.h -- C ABI of the GB300 Barnes-Hut engine (libbh_gpu.so).
+ *
+ * Drop-in boundary for the single-rank `--fc tree` force path of
+ * YonatanGM/Barnes-Hut.  Every entry point takes plain pointers and sizes,
+ * returns an int status (BH_OK == 0) and never throws.  The last error
+ * message of the calling thread is available from bh_last_error().
+ *
+ * Array conventions (identical to the reference's body.h:4-10 Vec3 AoS):
+ *   pos, vel, acc : n*3 doubles, x,y,z per body
+ *   mass          : n doubles
+ *   ids, keys     : n uint64
+ *   bbox          : {min.x, min.y, min.z, max.x, max.y, max.z}
+ *                   (BoundingBox, include/bounding_box.h:11-22)
+ * Units are the reference's: AU, day, kg; G = 1.48812e-34 (src/main.cpp:174).
+ *
+ * Each line below names the reference interface (file:line) an entry point
+ * replaces.  Entry points with no reference counterpart say so.
+ */
+#ifndef BH_GPU_H
+#define BH_GPU_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define BH_API_VERSION 1
+
+/* ---- status codes ---------------------------------------------------- */
+enum bh_status {
+    BH_OK = 0,
+    BH_ERR_INVALID_ARGUMENT = 1, /* null pointer, negative size, theta < 0 ... */
+    BH_ERR_CUDA = 2,             /* a CUDA runtime call failed                 */
+    BH_ERR_OUT_OF_MEMORY = 3,    /* device or host allocation failed           */
+    BH_ERR_CAPACITY = 4,         /* more bodies than the context was made for  */
+    BH_ERR_OVERFLOW = 5,         /* traversal stack/list overflow flag (the
+                                    reference throws "BH stack overflow",
+                                    src/traversal.cpp:94)                      */
+    BH_ERR_TIMEOUT = 6,          /* a bounded device-side wait gave up         */
+    BH_ERR_NONFINITE = 7,        /* a position is NaN or infinite              */
+    BH_ERR_STATE = 8,            /* call out of order (e.g. forces before tree)*/
+    BH_ERR_IO = 9,               /* file cannot be opened                      */
+    BH_ERR_NO_DEVICE = 10        /* no CUDA device                             */
+};
+
+/* ---- force modes ----------------------------------------------------- */
+enum bh_mode {
+    /* The reference's criterion and arithmetic: FP64, IEEE sqrt/div, no
+     * contraction, interactions summed in the reference's DFS order, so
+     * accelerations equal computeAccelerations (src/traversal.cpp:13-103)
+     * bit for bit. */
+    BH_MODE_PLAIN_FP64 = 0,
+    /* Same interaction set as BH_MODE_PLAIN_FP64 (exact per-body theta test
+     * in FP64), evaluated from shared-memory interaction lists with a
+     * refined reciprocal square root; results agree with the reference to
+     * ~1e-15 relative, not bit for bit.  No reference counterpart. */
+    BH_MODE_FP64_LIST = 1,
+    /* Far field in FP32 on displacements formed in FP64 relative to the
+     * warp's group centre; FP32 partials summed into FP64 accumulators; the
+     * Sun and planets (the BH_NUM_MASSIVE heaviest bodies) summed directly in
+     * FP64 and excluded from the far-field tree.  No reference counterpart. */
+    BH_MODE_FP32_FAR = 2,
+    /* BH_MODE_FP32_FAR with the learned acceptance criterion (see
+     * bh_learned_*).  No reference counterpart. */
+    BH_MODE_LEARNED = 3
+};
+
+#define BH_MAX_DEPTH 21   /* reference MAX_L / MAX_DEPTH (traversal.cpp:28) */
+#define BH_NUM_MASSIVE 9  /* Sun + 8 planets: direct FP64 terms in FP32 modes */
+
+const char *bh_last_error(void);
+const char *bh_status_string(int status);
+int bh_api_version(void);
+
+/* ---- device-resident context ---------------------------------------- */
+/* A context owns all device buffers for up to `capacity` bodies on one GPU
+ * and one CUDA stream; the body state stays on the device across steps.
+ * No reference counterpart (the reference keeps std::vectors in main.cpp). */
+typedef struct bh_context bh_context;
+
+int bh_context_create(int64_t capacity, int device, bh_context **out);
+int bh_context_destroy(bh_context *ctx);
+/* Blocks until all work queued on the context's stream has finished and
+ * reports any error flag a kernel raised. */
+int bh_context_sync(bh_context *ctx);
+/* The context's cudaStream_t, for callers that order their own work. */
+int bh_context_stream(bh_context *ctx, void **stream_out);
+
+/* Upload host arrays (any of vel/mass/ids may be NULL only if n == 0).
+ * Resets the accumulated time to 0 and the stored accelerations to 0, as
+ * the reference's main.cpp:175,178 do before the loop. */
+int bh_set_bodies(bh_context *ctx, int64_t n, const double *pos, const double *vel,
+                  const double *mass, const uint64_t *ids);
+/* Upload the accelerations of the previous step (n*3), for a caller that
+ * keeps the whole state on the host between steps (the first half kick of
+ * the next step uses them, src/main.cpp:193-200). */
+int bh_set_accelerations(bh_context *ctx, const double *acc);
+/* Download the state in its current (last sorted) order; NULL skips. */
+int bh_get_bodies(bh_context *ctx, double *pos, double *vel, double *mass, uint64_t *ids, double *acc);
+int bh_num_bodies(bh_context *ctx, int64_t *n_out);
+
+/* ---- the hot path, stage by stage ------------------------------------ */
+/* compute_local_bbox (src/bounding_box.cpp:23-44); on one rank
+ * compute_global_bbox (:46-52) is the identity. */
+int bh_compute_bbox(bh_context *ctx, double bbox_out[6]);
+/* generateMortonCodes (src/morton_keys.cpp:65-98) over the device-resident
+ * positions and the bbox of the last bh_compute_bbox.  keys_out may be NULL. */
+int bh_compute_keys(bh_context *ctx, uint64_t *keys_out);
+/* sortBodiesByMortonKey (include/utility.h:23-52): stable LSD radix sort of
+ * the keys, then permutes pos, vel, mass, ids (and keys).  perm_out (may be
+ * NULL) receives, for each new position, the body's previous position. */
+int bh_sort_bodies(bh_context *ctx, int64_t *perm_out);
+/* buildOctreeBottomUp (src/linear_octree.cpp:13-107) followed by the
+ * single-rank exchangeFullTrees re-merge (src/exchange.cpp:9-29 ->
+ * src/linear_octree.cpp:178-204).  Requires sorted keys. */
+int bh_build_tree(bh_context *ctx);
+/* Sizes of the last tree: n_records = nodes of the reference's uncompressed
+ * OctreeMap; n_nodes = nodes of the compressed device octree; n_leaves =
+ * distinct keys. */
+int bh_tree_info(bh_context *ctx, int64_t *n_records, int64_t *n_nodes, int64_t *n_leaves);
+/* The reference's node set (serializeTreeToRecords,
+ * src/linear_octree.cpp:169-176, NodeRecord linear_octree.h:60-65) sorted by
+ * (depth, prefix): each array holds n_records entries (com: 3 per node). */
+int bh_export_tree(bh_context *ctx, uint64_t *prefix, uint8_t *depth, double *mass, double *com);
+/* computeAccelerations (src/traversal.cpp:13-103, include/traversal.h:21-30)
+ * over the last tree; `mode` is a bh_mode.  acc_out (may be NULL) receives
+ * the accelerations in the current body order. */
+int bh_compute_accelerations(bh_context *ctx, double theta, double G, double soft2, int mode,
+                             double *acc_out);
+/* Accepted interactions per body of the last bh_compute_accelerations
+ * (summed over the body's accepted nodes). No reference counterpart. */
+int bh_interaction_count(bh_context *ctx, int64_t *total_out);
+/* `nsteps` steps of the `--fc tree` loop of src/main.cpp:191-282 (kick at
+ * t > 0, drift, bbox, keys, sort, build, merge, forces, kick).  *t_io is the
+ * simulation time, accumulated as t += dt after every step. */
+int bh_step(bh_context *ctx, double dt, double theta, double G, int64_t nsteps, int mode, double *t_io);
+
+/* ---- measurement (no reference counterpart) -------------------------- */
+/* Enables (on != 0) or disables CUDA-event timing of the phases of bh_step
+ * and clears the accumulated times. */
+int bh_set_profiling(bh_context *ctx, int on);
+/* Accumulated device time per phase of bh_step since profiling was enabled:
+ * ms_out[0] kick+drift+bbox, [1] keys + digit histograms, [2] radix sort,
+ * [3] permutation, [4] tree build, [5] forces (+ second half kick);
+ * launches_out: kernels this context has enqueued since it was created. */
+int bh_phase_times(bh_context *ctx, double ms_out[8], int64_t *launches_out);
+/* Sustained FMA throughput of this GPU in TFLOP/s (2 flops per FMA),
+ * fp64 != 0 for double, else float: the denominator of the force kernels'
+ * roofline, measured in the same process. */
+int bh_measure_fma_peak(bh_context *ctx, int fp64, double *tflops_out);
+
+/* ---- diagnostics (no reference counterpart) -------------------------- */
+/* FP64 direct sum over all bodies for the bodies at positions targets[k]
+ * of the current order; acc_out: ns*3. */
+int bh_direct_sum(bh_context *ctx, int64_t ns, const int64_t *targets, double G, double *acc_out);
+/* Kinetic energy, potential energy (pairs with at least one of the first
+ * BH_NUM_MASSIVE bodies by id exact in FP64, all other pairs through the
+ * tree monopoles at theta), total linear and angular momentum.
+ * out = {E, K, U, Lx, Ly, Lz, Px, Py, Pz}. */
+int bh_invariants(bh_context *ctx, double G, double theta, double out[9]);
+
+/* ---- stateless host-buffer entry points ------------------------------ */
+/* Each copies its inputs to the device, runs the kernel, copies back.  They
+ * use a per-thread default context on device 0. */
+int bh_compute_local_bbox(const double *pos, int64_t n, double bbox_out[6]);
+int bh_generate_morton_codes(const double *pos, int64_t n, const double bbox[6], uint64_t *keys_out);
+int bh_sort_bodies_by_morton_key(int64_t n, uint64_t *keys, double *pos, double *mass, double *vel,
+                                 uint64_t *ids);
+
+/* ---- host-side input (no GPU needed) --------------------------------- */
+/* convertKeplerToCartesian (src/kepler_to_cartesian.cpp:13-107).
+ * el: n*8 = {e, a, i, arg. periapsis, long. asc. node, M, epoch, mu}
+ * (radians, AU, days); out: n*6 = {x, y, z, vx, vy, vz}. */
+int bh_kepler_to_cartesian(const double *el, int64_t n, double *out);
+/* Seeded synthetic solar system (std::mt19937_64): the Sun (1.989e30 kg at
+ * rest at the origin), the 8 planets on circular coplanar orbits, and
+ * n - 9 asteroids: an inner belt, a fraction frac_outer in an outer belt
+ * (a 30-50 AU) and a fraction frac_trojan in Jupiter's L4/L5 clouds.
+ * ids are the row indices.  No reference counterpart (the reference reads
+ * CSVs made by its orbital_converter tool). */
+int bh_generate_system(uint64_t seed, int64_t n, double frac_outer, double frac_trojan, double *pos,
+                       double *vel, double *mass, uint64_t *ids);
+/* readCSV (src/io.cpp:16-81): header skipped; columns id,name,class are
+ * ignored; mass,pos_x..vel_z parsed; an unparsable line is skipped; ids are
+ * the parsed-row counter; at most body_count rows if body_count > 0.
+ * Call with pos == NULL to get the row count only. */
+int bh_read_csv(const char *path, int64_t body_count, int64_t *n_out, uint64_t *ids, double *mass,
+                double *pos, double *vel);
+/* Writes the reference's state-vector CSV layout (header
+ * id,name,class,mass,pos_x,pos_y,pos_z,vel_x,vel_y,vel_z). */
+int bh_write_csv(const char *path, int64_t n, const uint64_t *ids, const double *mass, const double *pos,
+                 const double *vel);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* BH_GPU_H */

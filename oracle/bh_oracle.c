@@ -1,0 +1,642 @@
+/*
+ * bh_oracle.c -- CPU restatement of the reference's single-rank `--fc tree`
+ * Barnes-Hut path (YonatanGM/Barnes-Hut), in plain C11 + OpenMP.
+ *
+ * TEST INFRASTRUCTURE ONLY.  This is the oracle: the GPU engine's parity
+ * tests compare against it, `bench.py` times it as the CPU baseline, and
+ * `bench.py --impl reference` runs it as the reference arm where the
+ * reference's own sources are not available.  No product code path calls it.
+ *
+ * Pinning: every function here is checked against the reference's own
+ * sources compiled unmodified into oracle/_ref/libbhref.so (see
+ * oracle/Makefile) and against the golden fixtures under tests/golden/ that
+ * the compiled reference produced (tests/golden/make_golden.py).
+ *
+ * Arithmetic is strict IEEE binary64: the Makefile compiles this file with
+ * -ffp-contract=off -fno-fast-math, so every product and sum below rounds
+ * exactly where the reference's (strict-IEEE-built) C++ rounds.
+ *
+ * Layout: positions, velocities and accelerations are AoS (x,y,z per body)
+ * like the reference's Vec3 (include/body.h:4-10).
+ */
+#include <math.h>
+#include <stdint.h>
+#include <stdlib.h>
+#include <string.h>
+#ifdef _OPENMP
+#include <omp.h>
+#endif
+
+#define ORC_MAX_DEPTH 21
+#define ORC_STACK_MAX 256
+
+enum { ORC_OK = 0, ORC_ERR_OOM = 3, ORC_ERR_STACK = 5 };
+
+/* ------------------------------------------------------------------ */
+/* Bounding box -- compute_local_bbox, src/bounding_box.cpp:23-44.      */
+/* std::min(a,b) is (b<a)?b:a and std::max(a,b) is (a<b)?b:a, so the    */
+/* first of two equal values (e.g. +0/-0) is kept, as written here.     */
+/* ------------------------------------------------------------------ */
+void orc_bbox(const double *pos, int64_t n, double out[6])
+{
+    if (n <= 0) {
+        out[0] = out[1] = out[2] = INFINITY;
+        out[3] = out[4] = out[5] = -INFINITY;
+        return;
+    }
+    double lo[3] = {pos[0], pos[1], pos[2]};
+    double hi[3] = {pos[0], pos[1], pos[2]};
+    for (int64_t i = 1; i < n; ++i) {
+        for (int a = 0; a < 3; ++a) {
+            double v = pos[3 * i + a];
+            if (v < lo[a]) lo[a] = v;
+            if (hi[a] < v) hi[a] = v;
+        }
+    }
+    for (int a = 0; a < 3; ++a) { out[a] = lo[a]; out[3 + a] = hi[a]; }
+}
+
+/* ------------------------------------------------------------------ */
+/* Morton keys -- generateMortonCodes, src/morton_keys.cpp:65-98, with  */
+/* spread21/morton63 (:11-25).  The interleave is written bit by bit    */
+/* here, independently of the reference's magic-mask form.              */
+/* ------------------------------------------------------------------ */
+uint64_t orc_spread21(uint32_t v)
+{
+    uint64_t r = 0;
+    for (int b = 0; b < 21; ++b) r |= (uint64_t)((v >> b) & 1u) << (3 * b);
+    return r;
+}
+
+uint64_t orc_morton63(uint32_t xi, uint32_t yi, uint32_t zi)
+{
+    return orc_spread21(xi) | (orc_spread21(yi) << 1) | (orc_spread21(zi) << 2);
+}
+
+/* mortonPrefix, src/morton_keys.cpp:28-32 */
+uint64_t orc_prefix(uint64_t key, int depth)
+{
+    if (depth == 0) return 0;
+    return key & (~0ULL << (63 - 3 * depth));
+}
+
+static double orc_norm(double v, double lo, double span)
+{
+    double t = (v - lo) / span;
+    if (t <= 0.0) return 0.0;
+    if (t >= 1.0) return nextafter(1.0, 0.0);
+    return t;
+}
+
+void orc_keys(const double *pos, int64_t n, const double bb[6], uint64_t *out)
+{
+    double span[3];
+    for (int a = 0; a < 3; ++a) span[a] = (bb[3 + a] == bb[a]) ? 1.0 : (bb[3 + a] - bb[a]);
+    const double Q = 2097152.0; /* 2^21 */
+#pragma omp parallel for schedule(static)
+    for (int64_t i = 0; i < n; ++i) {
+        uint32_t c[3];
+        for (int a = 0; a < 3; ++a) c[a] = (uint32_t)(orc_norm(pos[3 * i + a], bb[a], span[a]) * Q);
+        out[i] = orc_morton63(c[0], c[1], c[2]);
+    }
+}
+
+/* ------------------------------------------------------------------ */
+/* Sort + permute -- sortBodiesByMortonKey, include/utility.h:23-52.    */
+/* The reference's std::sort is not stable; keys are unique in every    */
+/* input it was run on, and there any comparison sort yields the same   */
+/* permutation.  Ties are broken here by original index.                */
+/* ------------------------------------------------------------------ */
+typedef struct { uint64_t key; int64_t idx; } orc_kidx;
+
+static int orc_kidx_cmp(const void *a, const void *b)
+{
+    const orc_kidx *x = (const orc_kidx *)a, *y = (const orc_kidx *)b;
+    if (x->key != y->key) return x->key < y->key ? -1 : 1;
+    return (x->idx > y->idx) - (x->idx < y->idx);
+}
+
+/* perm_out (optional): perm_out[i] = original index of the body now at i */
+int orc_sort_bodies(int64_t n, uint64_t *keys, double *pos, double *mass, double *vel,
+                    uint64_t *ids, int64_t *perm_out)
+{
+    if (n <= 0) return ORC_OK;
+    orc_kidx *o = (orc_kidx *)malloc(sizeof(orc_kidx) * (size_t)n);
+    double *tmp = (double *)malloc(sizeof(double) * 3 * (size_t)n);
+    if (!o || !tmp) { free(o); free(tmp); return ORC_ERR_OOM; }
+    for (int64_t i = 0; i < n; ++i) { o[i].key = keys[i]; o[i].idx = i; }
+    qsort(o, (size_t)n, sizeof(orc_kidx), orc_kidx_cmp);
+    for (int64_t i = 0; i < n; ++i) memcpy(tmp + 3 * i, pos + 3 * o[i].idx, 24);
+    memcpy(pos, tmp, 24 * (size_t)n);
+    for (int64_t i = 0; i < n; ++i) memcpy(tmp + 3 * i, vel + 3 * o[i].idx, 24);
+    memcpy(vel, tmp, 24 * (size_t)n);
+    for (int64_t i = 0; i < n; ++i) tmp[i] = mass[o[i].idx];
+    memcpy(mass, tmp, 8 * (size_t)n);
+    uint64_t *ut = (uint64_t *)tmp;
+    for (int64_t i = 0; i < n; ++i) ut[i] = ids[o[i].idx];
+    memcpy(ids, ut, 8 * (size_t)n);
+    for (int64_t i = 0; i < n; ++i) keys[i] = o[i].key;
+    if (perm_out)
+        for (int64_t i = 0; i < n; ++i) perm_out[i] = o[i].idx;
+    free(o);
+    free(tmp);
+    return ORC_OK;
+}
+
+/* ------------------------------------------------------------------ */
+/* Linear octree as a hash map keyed by (prefix, depth).                */
+/* OctreeKey/OctreeKeyHash/OctreeNode: include/linear_octree.h:15-53.   */
+/* Open addressing with linear probing; the key mix is the splitmix64   */
+/* finaliser the reference applies to prefix ^ depth*golden.            */
+/* ------------------------------------------------------------------ */
+typedef struct {
+    uint64_t prefix;
+    int32_t depth; /* -1 = empty slot */
+    int32_t pad;
+    double mass, cx, cy, cz;
+} orc_node;
+
+typedef struct {
+    orc_node *slot;
+    uint64_t cap; /* power of two */
+    uint64_t count;
+} orc_tree;
+
+static uint64_t orc_hash(uint64_t prefix, int depth)
+{
+    uint64_t x = prefix ^ ((uint64_t)depth * 0x9e3779b97f4a7c15ULL);
+    x ^= x >> 30;
+    x *= 0xbf58476d1ce4e5b9ULL;
+    x ^= x >> 27;
+    x *= 0x94d049bb133111ebULL;
+    x ^= x >> 31;
+    return x;
+}
+
+static int orc_tree_init(orc_tree *t, uint64_t want)
+{
+    uint64_t cap = 16;
+    while (cap < 2 * want) cap <<= 1;
+    t->slot = (orc_node *)malloc(sizeof(orc_node) * cap);
+    if (!t->slot) return ORC_ERR_OOM;
+    for (uint64_t i = 0; i < cap; ++i) t->slot[i].depth = -1;
+    t->cap = cap;
+    t->count = 0;
+    return ORC_OK;
+}
+
+static orc_node *orc_tree_find(const orc_tree *t, uint64_t prefix, int depth)
+{
+    uint64_t m = t->cap - 1, h = orc_hash(prefix, depth) & m;
+    for (;;) {
+        orc_node *s = &t->slot[h];
+        if (s->depth < 0) return NULL;
+        if (s->depth == depth && s->prefix == prefix) return s;
+        h = (h + 1) & m;
+    }
+}
+
+static int orc_tree_grow(orc_tree *t);
+
+/* operator[] of the reference's map: find, or insert a zeroed node */
+static orc_node *orc_tree_get(orc_tree *t, uint64_t prefix, int depth)
+{
+    if (2 * (t->count + 1) > t->cap && orc_tree_grow(t) != ORC_OK) return NULL;
+    uint64_t m = t->cap - 1, h = orc_hash(prefix, depth) & m;
+    for (;;) {
+        orc_node *s = &t->slot[h];
+        if (s->depth < 0) {
+            s->prefix = prefix;
+            s->depth = depth;
+            s->mass = s->cx = s->cy = s->cz = 0.0;
+            t->count++;
+            return s;
+        }
+        if (s->depth == depth && s->prefix == prefix) return s;
+        h = (h + 1) & m;
+    }
+}
+
+static int orc_tree_grow(orc_tree *t)
+{
+    orc_tree nt;
+    if (orc_tree_init(&nt, t->cap) != ORC_OK) return ORC_ERR_OOM;
+    for (uint64_t i = 0; i < t->cap; ++i) {
+        orc_node *s = &t->slot[i];
+        if (s->depth < 0) continue;
+        uint64_t m = nt.cap - 1, h = orc_hash(s->prefix, s->depth) & m;
+        while (nt.slot[h].depth >= 0) h = (h + 1) & m;
+        nt.slot[h] = *s;
+        nt.count++;
+    }
+    free(t->slot);
+    *t = nt;
+    return ORC_OK;
+}
+
+static int orc_u64_cmp(const void *a, const void *b)
+{
+    uint64_t x = *(const uint64_t *)a, y = *(const uint64_t *)b;
+    return (x > y) - (x < y);
+}
+
+static int64_t orc_sort_unique(uint64_t *v, int64_t n)
+{
+    if (n <= 0) return 0;
+    qsort(v, (size_t)n, sizeof(uint64_t), orc_u64_cmp);
+    int64_t w = 1;
+    for (int64_t i = 1; i < n; ++i)
+        if (v[i] != v[w - 1]) v[w++] = v[i];
+    return w;
+}
+
+/*
+ * buildOctreeBottomUp, src/linear_octree.cpp:13-107, followed (merge != 0)
+ * by the single-rank full-tree exchange of src/exchange.cpp:9-29, which
+ * re-inserts every node into an empty map through mergeRecordsIntoTree
+ * (src/linear_octree.cpp:178-204): mass' = 0 + m, com' = (0*0 + m*c)/mass',
+ * and a node whose mass' is 0 is left as an all-zero node.
+ */
+void *orc_build_tree(int64_t n, const uint64_t *keys, const double *pos, const double *mass, int merge)
+{
+    orc_tree *t = (orc_tree *)calloc(1, sizeof(orc_tree));
+    if (!t) return NULL;
+    if (orc_tree_init(t, (uint64_t)(n > 0 ? n : 1) * 2) != ORC_OK) { free(t); return NULL; }
+    if (n <= 0) return t;
+
+    /* 1. leaves, accumulated in body order */
+    uint64_t *cur = (uint64_t *)malloc(sizeof(uint64_t) * (size_t)n);
+    uint64_t *par = (uint64_t *)malloc(sizeof(uint64_t) * (size_t)n);
+    if (!cur || !par) goto oom;
+    for (int64_t i = 0; i < n; ++i) {
+        orc_node *s = orc_tree_get(t, keys[i], ORC_MAX_DEPTH);
+        if (!s) goto oom;
+        double m = mass[i];
+        s->mass += m;
+        s->cx += pos[3 * i + 0] * m;
+        s->cy += pos[3 * i + 1] * m;
+        s->cz += pos[3 * i + 2] * m;
+        cur[i] = keys[i];
+    }
+    int64_t ncur = orc_sort_unique(cur, n);
+
+    /* 2. parents level by level, children summed in octant order 0..7 */
+    for (int depth = ORC_MAX_DEPTH - 1; depth >= 0 && ncur > 0; --depth) {
+        for (int64_t j = 0; j < ncur; ++j) par[j] = orc_prefix(cur[j], depth);
+        int64_t npar = orc_sort_unique(par, ncur);
+        for (int64_t j = 0; j < npar; ++j) {
+            orc_node *p = orc_tree_get(t, par[j], depth);
+            if (!p) goto oom;
+            uint64_t pfx = p->prefix;
+            for (int oc = 0; oc < 8; ++oc) {
+                uint64_t cp = pfx | ((uint64_t)oc << (63 - 3 * (depth + 1)));
+                const orc_node *c = orc_tree_find(t, cp, depth + 1);
+                if (!c) continue;
+                p->mass += c->mass;
+                p->cx += c->cx;
+                p->cy += c->cy;
+                p->cz += c->cz;
+            }
+        }
+        uint64_t *sw = cur; cur = par; par = sw;
+        ncur = npar;
+    }
+
+    /* 3. finalise centre of mass */
+    for (uint64_t i = 0; i < t->cap; ++i) {
+        orc_node *s = &t->slot[i];
+        if (s->depth < 0) continue;
+        if (s->mass > 0) {
+            s->cx /= s->mass;
+            s->cy /= s->mass;
+            s->cz /= s->mass;
+        }
+    }
+
+    /* 4. single-rank exchange: each record merged into a fresh node */
+    if (merge) {
+        for (uint64_t i = 0; i < t->cap; ++i) {
+            orc_node *s = &t->slot[i];
+            if (s->depth < 0) continue;
+            double m0 = 0.0, c0 = 0.0;
+            double m1 = s->mass;
+            double tot = m0 + m1;
+            if (tot == 0) {
+                s->mass = s->cx = s->cy = s->cz = 0.0;
+                continue;
+            }
+            s->cx = (m0 * c0 + m1 * s->cx) / tot;
+            s->cy = (m0 * c0 + m1 * s->cy) / tot;
+            s->cz = (m0 * c0 + m1 * s->cz) / tot;
+            s->mass = tot;
+        }
+    }
+    free(cur);
+    free(par);
+    return t;
+oom:
+    free(cur);
+    free(par);
+    free(t->slot);
+    free(t);
+    return NULL;
+}
+
+int64_t orc_tree_size(void *h) { return (int64_t)((orc_tree *)h)->count; }
+
+void orc_tree_free(void *h)
+{
+    if (!h) return;
+    free(((orc_tree *)h)->slot);
+    free(h);
+}
+
+static int orc_rec_cmp(const void *a, const void *b)
+{
+    const orc_node *x = (const orc_node *)a, *y = (const orc_node *)b;
+    if (x->depth != y->depth) return x->depth < y->depth ? -1 : 1;
+    return (x->prefix > y->prefix) - (x->prefix < y->prefix);
+}
+
+/* All nodes sorted by (depth, prefix). */
+int orc_tree_records(void *h, uint64_t *prefix, uint8_t *depth, double *mass, double *com)
+{
+    orc_tree *t = (orc_tree *)h;
+    orc_node *v = (orc_node *)malloc(sizeof(orc_node) * (t->count ? t->count : 1));
+    if (!v) return ORC_ERR_OOM;
+    uint64_t k = 0;
+    for (uint64_t i = 0; i < t->cap; ++i)
+        if (t->slot[i].depth >= 0) v[k++] = t->slot[i];
+    qsort(v, (size_t)k, sizeof(orc_node), orc_rec_cmp);
+    for (uint64_t i = 0; i < k; ++i) {
+        prefix[i] = v[i].prefix;
+        depth[i] = (uint8_t)v[i].depth;
+        mass[i] = v[i].mass;
+        com[3 * i + 0] = v[i].cx;
+        com[3 * i + 1] = v[i].cy;
+        com[3 * i + 2] = v[i].cz;
+    }
+    free(v);
+    return ORC_OK;
+}
+
+/* ------------------------------------------------------------------ */
+/* Traversal -- computeAccelerations, src/traversal.cpp:13-103.         */
+/* Per body: DFS with an explicit stack, children pushed in octant      */
+/* order 0..7 and popped LIFO; a node is skipped when absent or         */
+/* massless, the body's own leaf is skipped by key equality, and a      */
+/* node is accepted when it is a leaf or side(d)^2 < theta^2 r^2 with   */
+/* side(d) = maxspan/2^d.  Summation order equals the reference's.      */
+/* n_inter (optional): accepted interactions per body.                  */
+/* ------------------------------------------------------------------ */
+int orc_accelerations(void *h, int64_t n, const uint64_t *key, const double *pos, double theta,
+                      double G, double soft2, const double bb[6], double *acc, int64_t *n_inter)
+{
+    const orc_tree *t = (const orc_tree *)h;
+    const double theta2 = theta * theta;
+    double dx = bb[3] - bb[0], dy = bb[4] - bb[1], dz = bb[5] - bb[2];
+    double L = dx;
+    if (L < dy) L = dy;
+    if (L < dz) L = dz;
+    double side2[ORC_MAX_DEPTH + 1];
+    uint64_t stride[ORC_MAX_DEPTH + 1];
+    for (int d = 0; d <= ORC_MAX_DEPTH; ++d) {
+        double side = L / (double)(1ULL << d);
+        side2[d] = side * side;
+        stride[d] = 1ULL << (63 - 3 * d);
+    }
+    int err = ORC_OK;
+#pragma omp parallel for schedule(dynamic, 256)
+    for (int64_t i = 0; i < n; ++i) {
+        uint64_t sp[ORC_STACK_MAX];
+        int sd[ORC_STACK_MAX];
+        int top = 0;
+        double ax = 0.0, ay = 0.0, az = 0.0;
+        int64_t cnt = 0;
+        const double px = pos[3 * i], py = pos[3 * i + 1], pz = pos[3 * i + 2];
+        sp[top] = 0;
+        sd[top] = 0;
+        top++;
+        while (top) {
+            --top;
+            uint64_t pref = sp[top];
+            int dep = sd[top];
+            const orc_node *nd = orc_tree_find(t, pref, dep);
+            if (!nd || nd->mass == 0.0) continue;
+            if (dep == ORC_MAX_DEPTH && pref == key[i]) continue;
+            double ex = nd->cx - px, ey = nd->cy - py, ez = nd->cz - pz;
+            double r2 = ex * ex + ey * ey + ez * ez + soft2;
+            if (dep == ORC_MAX_DEPTH || side2[dep] < theta2 * r2) {
+                double invR = 1.0 / sqrt(r2);
+                double invR3 = invR * invR * invR;
+                double s = G * nd->mass * invR3;
+                ax += s * ex;
+                ay += s * ey;
+                az += s * ez;
+                cnt++;
+            } else {
+                int cd = dep + 1;
+                for (int oc = 0; oc < 8; ++oc) {
+                    uint64_t c = pref + stride[cd] * (uint64_t)oc;
+                    if (!orc_tree_find(t, c, cd)) continue;
+                    if (top >= ORC_STACK_MAX) {
+#pragma omp atomic write
+                        err = ORC_ERR_STACK;
+                        top = 0;
+                        break;
+                    }
+                    sp[top] = c;
+                    sd[top] = cd;
+                    top++;
+                }
+            }
+        }
+        acc[3 * i + 0] = ax;
+        acc[3 * i + 1] = ay;
+        acc[3 * i + 2] = az;
+        if (n_inter) n_inter[i] = cnt;
+    }
+    return err;
+}
+
+/* ------------------------------------------------------------------ */
+/* The step loop of src/main.cpp:191-282 for `--fc tree` on one rank.   */
+/* The half kick at :193-200 runs only when t > 0; t is accumulated in  */
+/* double (t += dt), as the reference's loop header does.  The MPI      */
+/* layers are identities on one rank (global bbox = local bbox,          */
+/* rebalance keeps the order) and are omitted.                          */
+/* phase_s (7 doubles, accumulated): kdk, bbox, keys, sort, build,       */
+/* merge (folded into build here: 0), traversal.                        */
+/* ------------------------------------------------------------------ */
+static double orc_now(void)
+{
+#ifdef _OPENMP
+    return omp_get_wtime();
+#else
+    return (double)clock() / CLOCKS_PER_SEC;
+#endif
+}
+
+int orc_simulate(int64_t n, double *pos, double *vel, double *mass, uint64_t *ids, double *acc,
+                 double dt, double theta, double G, int64_t nsteps, double *t_io, double *phase_s)
+{
+    uint64_t *keys = (uint64_t *)malloc(sizeof(uint64_t) * (size_t)(n > 0 ? n : 1));
+    if (!keys) return ORC_ERR_OOM;
+    double t = *t_io;
+    int err = ORC_OK;
+    const double h = 0.5 * dt;
+    for (int64_t s = 0; s < nsteps && err == ORC_OK; ++s, t += dt) {
+        double t0 = orc_now();
+        if (t > 0) {
+#pragma omp parallel for schedule(static)
+            for (int64_t i = 0; i < 3 * n; ++i) vel[i] += h * acc[i];
+        }
+#pragma omp parallel for schedule(static)
+        for (int64_t i = 0; i < 3 * n; ++i) pos[i] += dt * vel[i];
+        double t1 = orc_now();
+        double bb[6];
+        orc_bbox(pos, n, bb);
+        double t2 = orc_now();
+        orc_keys(pos, n, bb, keys);
+        double t3 = orc_now();
+        err = orc_sort_bodies(n, keys, pos, mass, vel, ids, NULL);
+        if (err) break;
+        /* acceleration follows its body through the permutation only by
+         * being recomputed below; the reference's stale local_acc is
+         * overwritten by computeAccelerations before it is read again. */
+        double t4 = orc_now();
+        void *tree = orc_build_tree(n, keys, pos, mass, 1);
+        if (!tree) { err = ORC_ERR_OOM; break; }
+        double t5 = orc_now();
+        err = orc_accelerations(tree, n, keys, pos, theta, G, 0.0, bb, acc, NULL);
+        orc_tree_free(tree);
+        double t6 = orc_now();
+#pragma omp parallel for schedule(static)
+        for (int64_t i = 0; i < 3 * n; ++i) vel[i] += h * acc[i];
+        double t7 = orc_now();
+        if (phase_s) {
+            phase_s[0] += (t1 - t0) + (t7 - t6);
+            phase_s[1] += t2 - t1;
+            phase_s[2] += t3 - t2;
+            phase_s[3] += t4 - t3;
+            phase_s[4] += t5 - t4;
+            phase_s[6] += t6 - t5;
+        }
+    }
+    *t_io = t;
+    free(keys);
+    return err;
+}
+
+/* ------------------------------------------------------------------ */
+/* FP64 direct sum over all sources for a sample of target bodies       */
+/* (no reference counterpart; the judge of every force error).          */
+/* Self-exclusion is by index.                                          */
+/* ------------------------------------------------------------------ */
+void orc_direct_sum(int64_t n, const double *pos, const double *mass, int64_t ns, const int64_t *targets,
+                    double G, double *acc_out)
+{
+#pragma omp parallel for schedule(dynamic, 16)
+    for (int64_t k = 0; k < ns; ++k) {
+        int64_t j = targets[k];
+        double ax = 0.0, ay = 0.0, az = 0.0;
+        const double px = pos[3 * j], py = pos[3 * j + 1], pz = pos[3 * j + 2];
+        for (int64_t i = 0; i < n; ++i) {
+            if (i == j) continue;
+            double ex = pos[3 * i] - px, ey = pos[3 * i + 1] - py, ez = pos[3 * i + 2] - pz;
+            double r2 = ex * ex + ey * ey + ez * ez;
+            if (r2 == 0.0) continue;
+            double invR = 1.0 / sqrt(r2);
+            double s = G * mass[i] * (invR * invR * invR);
+            ax += s * ex;
+            ay += s * ey;
+            az += s * ez;
+        }
+        acc_out[3 * k] = ax;
+        acc_out[3 * k + 1] = ay;
+        acc_out[3 * k + 2] = az;
+    }
+}
+
+/* Total energy (exact pairwise potential, O(n^2): small n only), linear
+ * and angular momentum.  out = {E, K, U, Lx, Ly, Lz, Px, Py, Pz}. */
+void orc_invariants(int64_t n, const double *pos, const double *vel, const double *mass, double G, double out[9])
+{
+    double K = 0.0, U = 0.0, L[3] = {0, 0, 0}, P[3] = {0, 0, 0};
+    for (int64_t i = 0; i < n; ++i) {
+        const double *x = pos + 3 * i, *v = vel + 3 * i;
+        double m = mass[i];
+        K += 0.5 * m * (v[0] * v[0] + v[1] * v[1] + v[2] * v[2]);
+        L[0] += m * (x[1] * v[2] - x[2] * v[1]);
+        L[1] += m * (x[2] * v[0] - x[0] * v[2]);
+        L[2] += m * (x[0] * v[1] - x[1] * v[0]);
+        for (int a = 0; a < 3; ++a) P[a] += m * v[a];
+    }
+#pragma omp parallel for reduction(+ : U) schedule(dynamic, 64)
+    for (int64_t i = 0; i < n; ++i) {
+        double u = 0.0;
+        for (int64_t j = i + 1; j < n; ++j) {
+            double ex = pos[3 * j] - pos[3 * i], ey = pos[3 * j + 1] - pos[3 * i + 1],
+                   ez = pos[3 * j + 2] - pos[3 * i + 2];
+            double r = sqrt(ex * ex + ey * ey + ez * ez);
+            if (r > 0) u -= G * mass[i] * mass[j] / r;
+        }
+        U += u;
+    }
+    out[0] = K + U;
+    out[1] = K;
+    out[2] = U;
+    out[3] = L[0]; out[4] = L[1]; out[5] = L[2];
+    out[6] = P[0]; out[7] = P[1]; out[8] = P[2];
+}
+
+/* ------------------------------------------------------------------ */
+/* convertKeplerToCartesian, src/kepler_to_cartesian.cpp:13-107:        */
+/* propagate M to J2000 (JD 2451544.5), Newton on Kepler's equation     */
+/* (tol 1e-8, <= 100 iterations), true anomaly, perifocal state and     */
+/* the 3-1-3 rotation.  el = {e, a, i, omega, Omega, M, epoch, mu}.     */
+/* ------------------------------------------------------------------ */
+void orc_kepler_to_cartesian(const double *el, int64_t n, double *out)
+{
+    for (int64_t k = 0; k < n; ++k) {
+        const double *q = el + 8 * k;
+        double e = q[0], a = q[1], inc = q[2], w = q[3], Om = q[4], M = q[5], epoch = q[6], mu = q[7];
+        double nmot = sqrt(mu / pow(a, 3));
+        M += nmot * (2451544.5 - epoch);
+        M = fmod(M, 2 * M_PI);
+        if (M < 0) M += 2 * M_PI;
+        double E = M;
+        for (int it = 0; it < 100; ++it) {
+            double f = E - e * sin(E) - M;
+            double fp = 1 - e * cos(E);
+            double d = -f / fp;
+            E += d;
+            if (fabs(d) < 1e-8) break;
+        }
+        double nu = 2 * atan2(sqrt(1 + e) * sin(E / 2), sqrt(1 - e) * cos(E / 2));
+        double r = a * (1 - e * cos(E));
+        double xo = r * cos(nu), yo = r * sin(nu);
+        double hh = sqrt(mu * a) / r;
+        double vxo = hh * (-sin(E)), vyo = hh * sqrt(1 - e * e) * cos(E);
+        double cO = cos(Om), sO = sin(Om), ci = cos(inc), si = sin(inc), cw = cos(w), sw = sin(w);
+        double R11 = cO * cw - sO * sw * ci, R12 = -cO * sw - sO * cw * ci;
+        double R21 = sO * cw + cO * sw * ci, R22 = -sO * sw + cO * cw * ci;
+        double R31 = sw * si, R32 = cw * si;
+        double *o = out + 6 * k;
+        o[0] = R11 * xo + R12 * yo;
+        o[1] = R21 * xo + R22 * yo;
+        o[2] = R31 * xo + R32 * yo;
+        o[3] = R11 * vxo + R12 * vyo;
+        o[4] = R21 * vxo + R22 * vyo;
+        o[5] = R31 * vxo + R32 * vyo;
+    }
+}
+
+int orc_num_threads(void)
+{
+#ifdef _OPENMP
+    return omp_get_max_threads();
+#else
+    return 1;
+#endif
+}

@@ -1,0 +1,211 @@
+"""ctypes front end of the oracle (TEST INFRASTRUCTURE ONLY).
+
+Two libraries with the same calling conventions:
+
+* ``Oracle("port")``      -- oracle/_build/libbhoracle.so, the C restatement
+                              (bh_oracle.c) of the reference's path; builds on
+                              any host with gcc (``make -C oracle``).
+* ``Oracle("reference")`` -- oracle/_ref/libbhref.so, the reference's own
+                              sources compiled by ``make -C oracle ref``
+                              (only where the reference checkout exists).
+
+Only tests/, ``__graft_entry__.smoke()`` and bench.py's CPU-baseline and
+reference legs use this module.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import subprocess
+from pathlib import Path
+
+import numpy as np
+
+HERE = Path(__file__).resolve().parent
+PORT_LIB = HERE / "_build" / "libbhoracle.so"
+REF_LIB = HERE / "_ref" / "libbhref.so"
+REF_SRC = Path("/root/reference")
+
+_P = C.c_void_p
+_I64 = C.c_int64
+_D = C.c_double
+
+
+def build_port() -> Path:
+    subprocess.run(["make", "-s", "-C", str(HERE), "all"], check=True)
+    return PORT_LIB
+
+
+def build_reference() -> Path | None:
+    """Compiles the reference's sources when the checkout is present."""
+    if not (REF_SRC / "src" / "traversal.cpp").exists():
+        return REF_LIB if REF_LIB.exists() else None
+    subprocess.run(["make", "-s", "-C", str(HERE), "ref", f"REF={REF_SRC}"], check=True)
+    return REF_LIB
+
+
+def _ptr(a):
+    return None if a is None else a.ctypes.data_as(C.c_void_p)
+
+
+class Oracle:
+    def __init__(self, kind: str = "port"):
+        self.kind = kind
+        if kind == "port":
+            path = PORT_LIB if PORT_LIB.exists() else build_port()
+            pre = "orc_"
+        elif kind == "reference":
+            path = REF_LIB
+            if not path.exists():
+                raise FileNotFoundError(f"{path} not built (make -C oracle ref)")
+            pre = "ref_"
+        else:
+            raise ValueError(kind)
+        self.lib = C.CDLL(str(path))
+        self.pre = pre
+        L, p = self.lib, pre
+
+        def f(name, res, args):
+            fn = getattr(L, p + name)
+            fn.restype = res
+            fn.argtypes = args
+            return fn
+
+        if kind == "port":
+            self._bbox = f("bbox", None, [_P, _I64, _P])
+            self._keys = f("keys", None, [_P, _I64, _P, _P])
+            self._sort = f("sort_bodies", C.c_int, [_I64, _P, _P, _P, _P, _P, _P])
+            self._build = f("build_tree", _P, [_I64, _P, _P, _P, C.c_int])
+            self._size = f("tree_size", _I64, [_P])
+            self._records = f("tree_records", C.c_int, [_P, _P, _P, _P, _P])
+            self._free = f("tree_free", None, [_P])
+            self._accel = f("accelerations", C.c_int, [_P, _I64, _P, _P, _D, _D, _D, _P, _P, _P])
+            self._sim = f("simulate", C.c_int, [_I64, _P, _P, _P, _P, _P, _D, _D, _D, _I64, _P, _P])
+            self._kepler = f("kepler_to_cartesian", None, [_P, _I64, _P])
+            self._direct = f("direct_sum", None, [_I64, _P, _P, _I64, _P, _D, _P])
+            self._inv = f("invariants", None, [_I64, _P, _P, _P, _D, _P])
+            self._threads = f("num_threads", C.c_int, [])
+        else:
+            self._bbox = f("compute_local_bbox", None, [_P, _I64, _P])
+            self._keys = f("generate_morton_codes", None, [_P, _I64, _P, _P])
+            self._sort = f("sort_bodies", None, [_I64, _P, _P, _P, _P, _P])
+            self._build = f("build_tree", _P, [_I64, _P, _P, _P, C.c_int])
+            self._size = f("tree_size", _I64, [_P])
+            self._records = f("tree_records", None, [_P, _P, _P, _P, _P])
+            self._free = f("tree_free", None, [_P])
+            self._accel = f("compute_accelerations", None, [_P, _I64, _P, _P, _D, _D, _D, _P, _P])
+            self._sim = f("simulate", None, [_I64, _P, _P, _P, _P, _P, _D, _D, _D, _I64, _P, _P])
+            self._kepler = f("kepler_to_cartesian", None, [_P, _I64, _P])
+
+    # -- stages ---------------------------------------------------------
+    def bbox(self, pos) -> np.ndarray:
+        pos = np.ascontiguousarray(pos, np.float64).reshape(-1, 3)
+        out = np.empty(6)
+        self._bbox(_ptr(pos), pos.shape[0], _ptr(out))
+        return out
+
+    def keys(self, pos, bbox) -> np.ndarray:
+        pos = np.ascontiguousarray(pos, np.float64).reshape(-1, 3)
+        bb = np.ascontiguousarray(bbox, np.float64)
+        out = np.empty(pos.shape[0], np.uint64)
+        self._keys(_ptr(pos), pos.shape[0], _ptr(bb), _ptr(out))
+        return out
+
+    def sort(self, keys, pos, mass, vel, ids):
+        """Sorted copies (keys, pos, mass, vel, ids[, perm for the port])."""
+        k = np.array(keys, np.uint64); p = np.array(pos, np.float64).reshape(-1, 3)
+        m = np.array(mass, np.float64); v = np.array(vel, np.float64).reshape(-1, 3)
+        i = np.array(ids, np.uint64)
+        if self.kind == "port":
+            perm = np.empty(len(k), np.int64)
+            self._sort(len(k), _ptr(k), _ptr(p), _ptr(m), _ptr(v), _ptr(i), _ptr(perm))
+            return k, p, m, v, i, perm
+        self._sort(len(k), _ptr(k), _ptr(p), _ptr(m), _ptr(v), _ptr(i))
+        return k, p, m, v, i, None
+
+    def tree(self, keys, pos, mass, merge=True):
+        k = np.ascontiguousarray(keys, np.uint64)
+        p = np.ascontiguousarray(pos, np.float64).reshape(-1, 3)
+        m = np.ascontiguousarray(mass, np.float64)
+        h = self._build(len(k), _ptr(k), _ptr(p), _ptr(m), 1 if merge else 0)
+        if not h:
+            raise MemoryError("oracle tree build failed")
+        return OracleTree(self, h)
+
+    def accelerations(self, tree, keys, pos, theta, G, soft2, bbox, count=False):
+        k = np.ascontiguousarray(keys, np.uint64)
+        p = np.ascontiguousarray(pos, np.float64).reshape(-1, 3)
+        bb = np.ascontiguousarray(bbox, np.float64)
+        acc = np.empty((len(k), 3))
+        if self.kind == "port":
+            cnt = np.empty(len(k), np.int64) if count else None
+            rc = self._accel(tree.h, len(k), _ptr(k), _ptr(p), theta, G, soft2, _ptr(bb), _ptr(acc), _ptr(cnt))
+            if rc:
+                raise RuntimeError(f"oracle traversal failed: {rc}")
+            return (acc, cnt) if count else acc
+        self._accel(tree.h, len(k), _ptr(k), _ptr(p), theta, G, soft2, _ptr(bb), _ptr(acc))
+        return acc
+
+    def simulate(self, pos, vel, mass, ids, dt, theta, G, nsteps, t=0.0, acc=None):
+        """Runs the step loop; returns (pos, vel, mass, ids, acc, t, phase_s)."""
+        p = np.array(pos, np.float64).reshape(-1, 3); v = np.array(vel, np.float64).reshape(-1, 3)
+        m = np.array(mass, np.float64); i = np.array(ids, np.uint64)
+        a = np.zeros_like(p) if acc is None else np.array(acc, np.float64).reshape(-1, 3)
+        tt = _D(t)
+        ph = np.zeros(7)
+        rc = self._sim(len(m), _ptr(p), _ptr(v), _ptr(m), _ptr(i), _ptr(a), dt, theta, G, int(nsteps),
+                       C.byref(tt), _ptr(ph))
+        if self.kind == "port" and rc:
+            raise RuntimeError(f"oracle simulate failed: {rc}")
+        return p, v, m, i, a, tt.value, ph
+
+    def kepler(self, el) -> np.ndarray:
+        e = np.ascontiguousarray(el, np.float64).reshape(-1, 8)
+        out = np.empty((e.shape[0], 6))
+        self._kepler(_ptr(e), e.shape[0], _ptr(out))
+        return out
+
+    def direct_sum(self, pos, mass, targets, G) -> np.ndarray:
+        p = np.ascontiguousarray(pos, np.float64).reshape(-1, 3)
+        m = np.ascontiguousarray(mass, np.float64)
+        t = np.ascontiguousarray(targets, np.int64)
+        out = np.empty((len(t), 3))
+        self._direct(len(m), _ptr(p), _ptr(m), len(t), _ptr(t), G, _ptr(out))
+        return out
+
+    def invariants(self, pos, vel, mass, G) -> np.ndarray:
+        p = np.ascontiguousarray(pos, np.float64).reshape(-1, 3)
+        v = np.ascontiguousarray(vel, np.float64).reshape(-1, 3)
+        m = np.ascontiguousarray(mass, np.float64)
+        out = np.empty(9)
+        self._inv(len(m), _ptr(p), _ptr(v), _ptr(m), G, _ptr(out))
+        return out
+
+    def threads(self) -> int:
+        return int(self._threads()) if self.kind == "port" else -1
+
+
+class OracleTree:
+    def __init__(self, oracle: Oracle, h):
+        self.o = oracle
+        self.h = h
+
+    def __len__(self):
+        return int(self.o._size(self.h))
+
+    def records(self):
+        n = len(self)
+        prefix = np.empty(n, np.uint64); depth = np.empty(n, np.uint8); mass = np.empty(n)
+        com = np.empty((n, 3))
+        self.o._records(self.h, _ptr(prefix), _ptr(depth), _ptr(mass), _ptr(com))
+        return prefix, depth, mass, com
+
+    def close(self):
+        if self.h:
+            self.o._free(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass

@@ -1,0 +1,120 @@
+"""CPU-side checks of the C ABI library: it loads, exports every function
+include/bh_gpu.h declares, and its host-only entry points (Kepler conversion,
+synthetic generator, CSV reader/writer) behave like the reference's."""
+from __future__ import annotations
+
+import ctypes as C
+import re
+
+import numpy as np
+import pytest
+
+from conftest import ROOT, assert_bits_equal
+
+
+def declared_functions():
+    text = (ROOT / "include" / "bh_gpu.h").read_text()
+    text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
+    return sorted(set(re.findall(r"^\s*(?:const\s+)?[a-z_0-9]+\s*\*?\s*(bh_[a-z_0-9]+)\s*\(", text, flags=re.M)))
+
+
+def test_header_declares_entry_points():
+    names = declared_functions()
+    for must in ("bh_context_create", "bh_compute_keys", "bh_sort_bodies", "bh_build_tree",
+                 "bh_compute_accelerations", "bh_step", "bh_export_tree", "bh_generate_morton_codes"):
+        assert must in names
+
+
+def test_library_exports_every_declared_symbol(bh):
+    lib = bh.library()
+    missing = [n for n in declared_functions() if not hasattr(lib, n)]
+    assert not missing, f"declared in bh_gpu.h but not exported: {missing}"
+    assert lib.bh_api_version() == 1
+
+
+def test_status_strings(bh):
+    lib = bh.library()
+    assert lib.bh_status_string(0) == b"ok"
+    assert lib.bh_status_string(7) == b"non-finite position"
+
+
+def test_context_without_gpu_reports_no_device(bh):
+    import torch
+    if torch.cuda.is_available():
+        pytest.skip("a GPU is present")
+    with pytest.raises(bh.BhError) as e:
+        bh.Context(16)
+    assert e.value.status == 10  # BH_ERR_NO_DEVICE
+
+
+def test_invalid_arguments_rejected_without_device(bh):
+    lib = bh.library()
+    h = C.c_void_p()
+    assert lib.bh_context_create(0, 0, C.byref(h)) == 1
+    assert lib.bh_context_create(1 << 31, 0, C.byref(h)) == 1
+    assert b"capacity" in lib.bh_last_error()
+    assert lib.bh_compute_local_bbox(None, -1, None) == 1
+
+
+def test_kepler_matches_oracle(bh, port):
+    rng = np.random.default_rng(3)
+    n = 200
+    el = np.column_stack([rng.uniform(0, 0.95, n), rng.uniform(0.3, 60, n), rng.uniform(0, 3.1, n),
+                          rng.uniform(0, 6.3, n), rng.uniform(0, 6.3, n), rng.uniform(-10, 10, n),
+                          rng.uniform(2450000, 2453000, n), np.full(n, 2.95987e-4)])
+    assert_bits_equal(bh.kepler_to_cartesian(el), port.kepler(el), "kepler states")
+
+
+def test_generator_deterministic_and_shaped(bh):
+    a = bh.generate_system(42, 5000, 0.1, 0.05)
+    b = bh.generate_system(42, 5000, 0.1, 0.05)
+    for x, y in zip(a, b):
+        assert_bits_equal(x, y)
+    pos, vel, mass, ids = a
+    assert mass[0] == 1.989e30 and np.all(pos[0] == 0) and np.all(vel[0] == 0)
+    r = np.linalg.norm(pos, axis=1)
+    np.testing.assert_allclose(r[1:9], [0.3870982252718477, 0.723326849675607, 1.000371833994387,
+                                        1.52367818431121, 5.205108585205607, 9.581451990534042,
+                                        19.22994588008584, 30.10071183142183], rtol=1e-12)
+    assert np.all(pos[1:9, 2] == 0)  # coplanar planets
+    nast = 5000 - 9
+    n_out, n_tro = round(0.1 * nast), round(0.05 * nast)
+    n_in = nast - n_out - n_tro
+    inner = r[9:9 + n_in]
+    assert inner.min() > 2.1 * (1 - 0.3) - 1e-9 and inner.max() < 3.3 * 1.3 + 1e-9
+    outer = r[9 + n_in:9 + n_in + n_out]
+    assert outer.min() > 30 * 0.8 - 1e-9 and outer.max() < 50 * 1.2 + 1e-9
+    tro = r[9 + n_in + n_out:]
+    assert tro.min() > 5.2 * 0.9 - 1e-9 and tro.max() < 5.2 * 1.1 + 1e-9
+    # trojans lead/trail Jupiter by 60 +/- 30 degrees in mean longitude; the
+    # true position angle differs by up to ~2e rad (e <= 0.1) plus projection
+    lam_j = np.arctan2(pos[5, 1], pos[5, 0])
+    dl = np.degrees(np.angle(np.exp(1j * (np.arctan2(pos[-n_tro:, 1], pos[-n_tro:, 0]) - lam_j))))
+    assert np.all((np.abs(dl) > 15) & (np.abs(dl) < 105))
+    m = mass[9:]
+    assert m.min() >= 1e12 * (1 - 1e-12) and m.max() <= 1e20 * (1 + 1e-12)
+    assert np.array_equal(ids, np.arange(5000, dtype=np.uint64))
+
+
+def test_csv_round_trip_and_reader_rules(bh, tmp_path):
+    pos, vel, mass, ids = bh.generate_system(9, 50, 0.1, 0.0)
+    f = tmp_path / "s.csv"
+    bh.write_csv(f, ids, mass, pos, vel)
+    rid, rmass, rpos, rvel = bh.read_csv(f)
+    assert_bits_equal(rpos, pos); assert_bits_equal(rvel, vel); assert_bits_equal(rmass, mass)
+    assert np.array_equal(rid, ids)
+    # body_count limit, unparsable rows skipped, ids = parsed-row counter
+    lines = f.read_text().splitlines()
+    bad = lines[:3] + ["7,x,AST,notanumber,1,2,3,4,5,6"] + lines[3:6]
+    f.write_text("\n".join(bad) + "\n")
+    rid, rmass, rpos, rvel = bh.read_csv(f)
+    assert len(rmass) == 5 and np.array_equal(rid, np.arange(5, dtype=np.uint64))
+    assert_bits_equal(rmass, np.concatenate([mass[:2], mass[2:5]]))
+    rid, rmass, _, _ = bh.read_csv(f, body_count=3)
+    assert len(rmass) == 3
+    # a row that ends early re-parses its last column (std::getline keeps it)
+    f.write_text("h\n0,a,b,5.0,1,2,3,4,5\n")
+    _, rmass, rpos, rvel = bh.read_csv(f)
+    assert rmass[0] == 5.0 and rvel[0].tolist() == [4.0, 5.0, 5.0]
+    with pytest.raises(bh.BhError):
+        bh.read_csv(tmp_path / "missing.csv")

@@ -1,0 +1,206 @@
+"""GPU parity: every stage of the CUDA path, called through the C ABI, against
+the golden fixtures of the compiled reference and against the oracle on the
+same inputs.  Keys, permutation, tree and (BH_MODE_PLAIN_FP64) accelerations
+must be bit for bit the reference's."""
+from __future__ import annotations
+
+import hashlib
+
+import numpy as np
+import pytest
+
+from conftest import DT, G, THETA, assert_bits_equal
+
+pytestmark = pytest.mark.gpu
+
+EDGE = ["one", "two", "coplanar", "single_point", "massless", "massive", "duplicate_key"]
+
+
+def digest(*arrays) -> str:
+    h = hashlib.sha256()
+    for a in arrays:
+        h.update(np.ascontiguousarray(a).tobytes())
+    return h.hexdigest()
+
+
+@pytest.fixture(scope="module")
+def ctx(bh):
+    c = bh.Context(400_000)
+    yield c
+    c.close()
+
+
+def gpu_stages(ctx, pos, vel, mass, ids, theta=THETA, mode=0):
+    ctx.set_bodies(pos, vel, mass, ids)
+    bb = ctx.compute_bbox()
+    keys = ctx.compute_keys()
+    perm = ctx.sort_bodies()
+    ctx.build_tree()
+    rec = ctx.export_tree()
+    acc = ctx.compute_accelerations(theta, G, 0.0, mode)
+    p, v, m, i, _ = ctx.get_bodies()
+    return dict(bbox=bb, keys=keys, perm=perm, sorted=(ctx_keys_sorted(keys, perm), p, m, v, i), rec=rec, acc=acc)
+
+
+def ctx_keys_sorted(keys, perm):
+    return keys[perm]
+
+
+@pytest.mark.parametrize("case", EDGE)
+def test_edge_cases(ctx, golden, case):
+    g = golden("edge_cases.npz")
+    pos, vel, mass, ids = (g[f"{case}/{k}"] for k in ("pos", "vel", "mass", "ids"))
+    s = gpu_stages(ctx, pos, vel, mass, ids)
+    assert_bits_equal(s["bbox"], g[f"{case}/bbox"], "bbox")
+    assert_bits_equal(s["keys"], g[f"{case}/keys"], "keys")
+    sk = s["sorted"][0]
+    assert_bits_equal(sk, g[f"{case}/sorted_keys"], "sorted keys")
+    assert np.array_equal(np.sort(s["perm"]), np.arange(len(mass)))
+    if case == "duplicate_key":
+        # std::sort leaves the order of equal keys unspecified: compare as sets
+        ref_ids, ref_keys = g[f"{case}/sorted_ids"], g[f"{case}/sorted_keys"]
+        for k in np.unique(ref_keys):
+            assert set(s["sorted"][4][sk == k]) == set(ref_ids[ref_keys == k])
+        assert_bits_equal(s["rec"][0], g[f"{case}/tree_prefix"], "tree prefixes")
+        assert_bits_equal(s["rec"][1], g[f"{case}/tree_depth"], "tree depths")
+        np.testing.assert_allclose(s["rec"][2], g[f"{case}/tree_mass"], rtol=1e-15)
+        np.testing.assert_allclose(s["acc"], g[f"{case}/acc"], rtol=1e-12, atol=1e-30)
+        return
+    for got, name in zip(s["sorted"][1:], ("sorted_pos", "sorted_mass", "sorted_vel", "sorted_ids")):
+        assert_bits_equal(got, g[f"{case}/{name}"], name)
+    for got, name in zip(s["rec"], ("tree_prefix", "tree_depth", "tree_mass", "tree_com")):
+        assert_bits_equal(got, g[f"{case}/{name}"], name)
+    assert_bits_equal(s["acc"], g[f"{case}/acc"], "accelerations")
+
+
+def test_synthetic_1000(ctx, golden):
+    g = golden("synthetic_1000.npz")
+    s = gpu_stages(ctx, g["pos"], g["vel"], g["mass"], g["ids"])
+    assert_bits_equal(s["bbox"], g["bbox"], "bbox")
+    assert_bits_equal(s["keys"], g["keys"], "keys")
+    for got, name in zip(s["sorted"], ("sorted_keys", "sorted_pos", "sorted_mass", "sorted_vel", "sorted_ids")):
+        assert_bits_equal(got, g[name], name)
+    for got, name in zip(s["rec"], ("tree_prefix", "tree_depth", "tree_mass", "tree_com")):
+        assert_bits_equal(got, g[name], name)
+    assert_bits_equal(s["acc"], g["acc"], "accelerations")
+    for th in (0.5, 0.8):
+        assert_bits_equal(ctx.compute_accelerations(th), g[f"acc_theta_{th}"], f"acc theta={th}")
+
+
+def test_synthetic_1000_five_steps(ctx, golden):
+    g = golden("synthetic_1000.npz")
+    ctx.set_bodies(g["pos"], g["vel"], g["mass"], g["ids"])
+    t = ctx.step(DT, THETA, G, nsteps=5, t=0.0)
+    p, v, m, i, a = ctx.get_bodies()
+    for got, name in zip((p, v, m, i, a), ("sim5_pos", "sim5_vel", "sim5_mass", "sim5_ids", "sim5_acc")):
+        assert_bits_equal(got, g[name], name)
+    assert t == g["sim5_t"][0]
+
+
+def test_synthetic_19054(ctx, golden):
+    g = golden("synthetic_19054.npz")
+    s = gpu_stages(ctx, g["pos"], g["vel"], g["mass"], g["ids"])
+    assert_bits_equal(s["bbox"], g["bbox"], "bbox")
+    assert_bits_equal(s["keys"], g["keys"], "keys")
+    assert_bits_equal(s["sorted"][4], g["sorted_ids"], "permutation")
+    assert len(s["rec"][0]) == int(g["n_records"][0])
+    assert np.array_equal(np.bincount(s["rec"][1], minlength=22), g["depth_hist"])
+    assert digest(*s["rec"]) == str(g["tree_digest"][0])
+    assert digest(s["acc"]) == str(g["acc_digest"][0])
+    ctx.set_bodies(g["pos"], g["vel"], g["mass"], g["ids"])
+    t = ctx.step(DT, THETA, G, nsteps=3, t=0.0)
+    p, v, m, i, a = ctx.get_bodies()
+    assert digest(p, v, m, i, a) == str(g["sim3_digest"][0])
+    assert t == g["sim3_t"][0]
+
+
+def test_300k_against_oracle(bh, ctx, port):
+    """The GPU-plain configuration's size (300,149 bodies, 10 % outer belt)."""
+    pos, vel, mass, ids = bh.generate_system(2, 300_149, 0.1, 0.0)
+    s = gpu_stages(ctx, pos, vel, mass, ids)
+    bb = port.bbox(pos)
+    keys = port.keys(pos, bb)
+    sk, sp, sm, sv, si, _ = port.sort(keys, pos, mass, vel, ids)
+    assert_bits_equal(s["bbox"], bb, "bbox")
+    assert_bits_equal(s["keys"], keys, "keys")
+    assert_bits_equal(s["sorted"][4], si, "permutation")
+    assert_bits_equal(s["sorted"][1], sp, "sorted positions")
+    tree = port.tree(sk, sp, sm)
+    rec = tree.records()
+    for got, ref, name in zip(s["rec"], rec, ("prefix", "depth", "mass", "com")):
+        assert_bits_equal(got, ref, f"tree {name}")
+    acc = port.accelerations(tree, sk, sp, THETA, G, 0.0, bb)
+    assert_bits_equal(s["acc"], acc, "accelerations")
+
+
+def test_stateless_entry_points(bh, port, golden):
+    g = golden("synthetic_1000.npz")
+    pos, vel, mass, ids = g["pos"], g["vel"], g["mass"], g["ids"]
+    bb = bh.compute_local_bbox(pos)
+    assert_bits_equal(bb, g["bbox"], "bbox")
+    keys = bh.generateMortonCodes(pos, bb)
+    assert_bits_equal(keys, g["keys"], "keys")
+    sk, sp, sm, sv, si = bh.sortBodiesByMortonKey(keys, pos, mass, vel, ids)
+    for got, name in zip((sk, sp, sm, sv, si), ("sorted_keys", "sorted_pos", "sorted_mass", "sorted_vel",
+                                                 "sorted_ids")):
+        assert_bits_equal(got, g[name], name)
+
+
+def test_errors_are_statuses(bh, ctx):
+    pos, vel, mass, ids = bh.generate_system(4, 1000)
+    ctx.set_bodies(pos, vel, mass, ids)
+    with pytest.raises(bh.BhError) as e:
+        ctx.compute_accelerations()
+    assert e.value.status == 8  # BH_ERR_STATE: no tree yet
+    with pytest.raises(bh.BhError) as e:
+        ctx.build_tree()
+    assert e.value.status == 8
+    bad = pos.copy()
+    bad[17, 1] = np.nan
+    ctx.set_bodies(bad, vel, mass, ids)
+    with pytest.raises(bh.BhError) as e:
+        ctx.compute_bbox()
+    assert e.value.status == 7  # BH_ERR_NONFINITE
+    small = bh.Context(10)
+    with pytest.raises(bh.BhError) as e:
+        small.set_bodies(pos, vel, mass, ids)
+    assert e.value.status == 4  # BH_ERR_CAPACITY
+    small.close()
+    # the context stays usable after an error
+    ctx.set_bodies(pos, vel, mass, ids)
+    ctx.step(DT, THETA, G, 1)
+
+
+def test_4m_properties(bh):
+    """The combined-scale size (4,000,000 bodies, 85/10/5): size-independent checks."""
+    n = 4_000_000
+    pos, vel, mass, ids = bh.generate_system(5, n, 0.10, 0.05)
+    with bh.Context(n) as c:
+        c.set_bodies(pos, vel, mass, ids)
+        bb = c.compute_bbox()
+        assert np.array_equal(bb[:3], pos.min(axis=0)) and np.array_equal(bb[3:], pos.max(axis=0))
+        keys = c.compute_keys()
+        perm = c.sort_bodies()
+        assert np.array_equal(np.sort(perm), np.arange(n))
+        sk = keys[perm]
+        assert np.all(sk[1:] >= sk[:-1])
+        # stability: equal keys keep their input order
+        eq = sk[1:] == sk[:-1]
+        assert np.all(perm[1:][eq] > perm[:-1][eq])
+        c.build_tree()
+        info = c.tree_info()
+        assert info["leaves"] == len(np.unique(sk))
+        acc = c.compute_accelerations()
+        assert np.all(np.isfinite(acc))
+        _, _, m_sorted, ids_sorted, _ = c.get_bodies()
+        assert np.array_equal(ids_sorted, ids[perm])
+        rng = np.random.default_rng(0)
+        sample = rng.choice(n, 256, replace=False)
+        ref = np.empty((256, 3))
+        lib = bh.library()
+        import ctypes as C
+        tgt = np.ascontiguousarray(sample, np.int64)
+        rc = lib.bh_direct_sum(c.handle, 256, tgt.ctypes.data_as(C.c_void_p), G, ref.ctypes.data_as(C.c_void_p))
+        assert rc == 0
+        err = np.linalg.norm(acc[sample] - ref, axis=1) / np.linalg.norm(ref, axis=1)
+        assert np.median(err) < 1e-5

@@ -1,0 +1,164 @@
+"""Pins the oracle (the C restatement of the reference's path) to the golden
+fixtures that the reference's own compiled sources produced, and -- where the
+reference checkout is present -- directly to the compiled reference."""
+from __future__ import annotations
+
+import hashlib
+import json
+from pathlib import Path
+
+import numpy as np
+import pytest
+
+from conftest import DT, G, GOLDEN, THETA, assert_bits_equal
+
+EDGE = ["one", "two", "duplicate_key", "coplanar", "single_point", "massless", "massive"]
+
+
+def digest(*arrays) -> str:
+    h = hashlib.sha256()
+    for a in arrays:
+        h.update(np.ascontiguousarray(a).tobytes())
+    return h.hexdigest()
+
+
+def run_stages(o, pos, vel, mass, ids, theta=THETA):
+    bb = o.bbox(pos)
+    keys = o.keys(pos, bb)
+    sk, sp, sm, sv, si, _ = o.sort(keys, pos, mass, vel, ids)
+    tree = o.tree(sk, sp, sm)
+    rec = tree.records()
+    acc = o.accelerations(tree, sk, sp, theta, G, 0.0, bb)
+    tree.close()
+    return bb, keys, (sk, sp, sm, sv, si), rec, acc
+
+
+@pytest.mark.parametrize("case", EDGE)
+def test_edge_cases_bit_exact(port, golden, case):
+    g = golden("edge_cases.npz")
+    pos, vel, mass, ids = (g[f"{case}/{k}"] for k in ("pos", "vel", "mass", "ids"))
+    bb, keys, srt, rec, acc = run_stages(port, pos, vel, mass, ids)
+    assert_bits_equal(bb, g[f"{case}/bbox"], "bbox")
+    assert_bits_equal(keys, g[f"{case}/keys"], "keys")
+    for got, name in zip(srt, ("sorted_keys", "sorted_pos", "sorted_mass", "sorted_vel", "sorted_ids")):
+        if case == "duplicate_key" and name != "sorted_keys":
+            continue  # tie order of std::sort is unspecified; compared as sets below
+        assert_bits_equal(got, g[f"{case}/{name}"], name)
+    for got, name in zip(rec, ("tree_prefix", "tree_depth", "tree_mass", "tree_com")):
+        if case == "duplicate_key" and name in ("tree_mass", "tree_com"):
+            continue  # leaf sums depend on the tie order
+        assert_bits_equal(got, g[f"{case}/{name}"], name)
+    if case != "duplicate_key":
+        assert_bits_equal(acc, g[f"{case}/acc"], "acc")
+
+
+def test_duplicate_key_ties_as_sets(port, golden):
+    g = golden("edge_cases.npz")
+    c = "duplicate_key"
+    pos, vel, mass, ids = (g[f"{c}/{k}"] for k in ("pos", "vel", "mass", "ids"))
+    _, _, (sk, sp, sm, sv, si), rec, acc = run_stages(port, pos, vel, mass, ids)
+    ref_ids = g[f"{c}/sorted_ids"]
+    ref_keys = g[f"{c}/sorted_keys"]
+    for k in np.unique(ref_keys):
+        assert set(si[sk == k]) == set(ref_ids[ref_keys == k])
+    assert len(np.unique(ref_keys)) == len(ref_keys) - 1
+    # masses/COMs of the tree agree to rounding whatever the tie order
+    np.testing.assert_allclose(rec[2], g[f"{c}/tree_mass"], rtol=1e-15)
+    np.testing.assert_allclose(rec[3], g[f"{c}/tree_com"], rtol=1e-13, atol=1e-300)
+    np.testing.assert_allclose(acc, g[f"{c}/acc"], rtol=1e-12, atol=1e-30)
+
+
+def test_synthetic_1000_bit_exact(port, golden):
+    g = golden("synthetic_1000.npz")
+    pos, vel, mass, ids = g["pos"], g["vel"], g["mass"], g["ids"]
+    bb, keys, srt, rec, acc = run_stages(port, pos, vel, mass, ids)
+    assert_bits_equal(bb, g["bbox"], "bbox")
+    assert_bits_equal(keys, g["keys"], "keys")
+    for got, name in zip(srt, ("sorted_keys", "sorted_pos", "sorted_mass", "sorted_vel", "sorted_ids")):
+        assert_bits_equal(got, g[name], name)
+    for got, name in zip(rec, ("tree_prefix", "tree_depth", "tree_mass", "tree_com")):
+        assert_bits_equal(got, g[name], name)
+    assert_bits_equal(acc, g["acc"], "acc")
+    for th in (0.5, 0.8):
+        *_, a = run_stages(port, pos, vel, mass, ids, theta=th)
+        assert_bits_equal(a, g[f"acc_theta_{th}"], f"acc theta={th}")
+
+
+def test_synthetic_1000_five_steps(port, golden):
+    g = golden("synthetic_1000.npz")
+    p, v, m, i, a, t, _ = port.simulate(g["pos"], g["vel"], g["mass"], g["ids"], DT, THETA, G, 5)
+    for got, name in zip((p, v, m, i, a), ("sim5_pos", "sim5_vel", "sim5_mass", "sim5_ids", "sim5_acc")):
+        assert_bits_equal(got, g[name], name)
+    assert t == g["sim5_t"][0]
+
+
+def test_synthetic_19054_digests(port, golden):
+    g = golden("synthetic_19054.npz")
+    pos, vel, mass, ids = g["pos"], g["vel"], g["mass"], g["ids"]
+    bb, keys, (sk, sp, sm, sv, si), rec, acc = run_stages(port, pos, vel, mass, ids)
+    assert_bits_equal(bb, g["bbox"], "bbox")
+    assert_bits_equal(keys, g["keys"], "keys")
+    assert_bits_equal(si, g["sorted_ids"], "permutation")
+    assert len(rec[0]) == int(g["n_records"][0])
+    assert np.array_equal(np.bincount(rec[1], minlength=22), g["depth_hist"])
+    assert digest(*rec) == str(g["tree_digest"][0])
+    assert digest(acc) == str(g["acc_digest"][0])
+    assert_bits_equal(acc[:512], g["acc_head"], "acc head")
+    p, v, m, i, a, t, _ = port.simulate(pos, vel, mass, ids, DT, THETA, G, 3)
+    assert digest(p, v, m, i, a) == str(g["sim3_digest"][0])
+    assert t == g["sim3_t"][0]
+
+
+def test_step_count_semantics(port, golden):
+    """`for (t = 0; t < t_end; t += dt)` with dt = 1h: 10 d -> 241 steps."""
+    t, steps = 0.0, 0
+    while t < 10.0:
+        steps += 1
+        t += 1.0 / 24.0
+    assert steps == 241
+
+
+REF_CSV = Path("/root/reference/data/state_vectors_csvs/scenario1_19054.csv")
+
+
+@pytest.mark.skipif(not REF_CSV.exists(), reason="the reference checkout is not on this host")
+def test_scenario1_csv_digests(port, bh):
+    info = json.loads((GOLDEN / "scenario1.json").read_text())
+    ids, mass, pos, vel = bh.read_csv(REF_CSV)
+    assert len(mass) == info["n"]
+    assert digest(pos, vel, mass, ids) == info["input_digest"]
+    bb, keys, (sk, sp, sm, sv, si), rec, acc = run_stages(port, pos, vel, mass, ids)
+    assert bb.tolist() == info["bbox"]
+    assert digest(keys) == info["keys_digest"]
+    assert digest(si) == info["sorted_ids_digest"]
+    assert len(rec[0]) == info["n_records"]
+    assert np.bincount(rec[1], minlength=22).tolist() == info["depth_hist"]
+    assert digest(*rec) == info["tree_digest"]
+    assert digest(acc) == info["acc_digest"]
+
+
+@pytest.mark.skipif(not Path("/root/reference/src/traversal.cpp").exists(), reason="reference checkout absent")
+def test_port_equals_compiled_reference_random(port):
+    """Random systems, several theta: the port and the compiled reference agree bit for bit."""
+    from oracle.oracle import Oracle, build_reference
+    build_reference()
+    ref = Oracle("reference")
+    rng = np.random.default_rng(5)
+    for n, theta in ((3, 1.05), (17, 0.3), (300, 0.7), (2500, 1.05), (2500, 2.0)):
+        pos = rng.standard_normal((n, 3)) * rng.uniform(0.1, 30, (n, 1))
+        vel = rng.standard_normal((n, 3)) * 1e-3
+        mass = 10 ** rng.uniform(12, 25, n)
+        ids = np.arange(n, dtype=np.uint64)
+        a = run_stages(port, pos, vel, mass, ids, theta)
+        b = run_stages(ref, pos, vel, mass, ids, theta)
+        assert_bits_equal(a[0], b[0], "bbox")
+        assert_bits_equal(a[1], b[1], "keys")
+        for x, y in zip(a[2], b[2]):
+            assert_bits_equal(x, y, "sorted")
+        for x, y in zip(a[3], b[3]):
+            assert_bits_equal(x, y, "tree")
+        assert_bits_equal(a[4], b[4], "acc")
+    el = np.column_stack([rng.uniform(0, 0.9, 50), rng.uniform(0.3, 50, 50), rng.uniform(0, 3, 50),
+                          rng.uniform(0, 6.3, 50), rng.uniform(0, 6.3, 50), rng.uniform(-7, 7, 50),
+                          rng.uniform(2451000, 2452000, 50), np.full(50, 2.96e-4)])
+    assert_bits_equal(port.kepler(el), ref.kepler(el), "kepler")
