@@ -165,6 +165,10 @@ size_t sort_smem_bytes();
 int64_t scan_tmp_ints(int64_t n_max);
 int launch_sort(bh_context* ctx);
 int launch_permute(bh_context* ctx);
+// The onesweep passes over raw buffers (the allocation-free sort entry).
+int sort_passes_raw(int64_t n, const uint64_t* keys_in, uint64_t* keys_out, uint32_t* vals_out, uint64_t* key_alt,
+                    uint32_t* val_alt, uint32_t* hist, uint32_t* lookback, uint32_t* tile_ctr, unsigned* err,
+                    cudaStream_t stream);
 int launch_build(bh_context* ctx);
 int launch_traverse(bh_context* ctx, double theta, double G, double soft2, int mode, double kick_h);
 

@@ -250,6 +250,39 @@ int launch_sort(bh_context* ctx)
     return BH_OK;
 }
 
+int sort_passes_raw(int64_t n, const uint64_t* keys_in, uint64_t* keys_out, uint32_t* vals_out, uint64_t* key_alt,
+                    uint32_t* val_alt, uint32_t* hist, uint32_t* lookback, uint32_t* tile_ctr, unsigned* err,
+                    cudaStream_t stream)
+{
+    // The eight onesweep passes over caller-provided buffers: digit starts
+    // from `hist` (counts on entry), pass 0 reads keys_in and writes the
+    // alternate buffers, the last pass writes keys_out / vals_out.
+    const size_t smem = sizeof(SortSmem);
+    BH_CUDA_TRY(cudaFuncSetAttribute(onesweep_kernel<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    BH_CUDA_TRY(cudaFuncSetAttribute(onesweep_kernel<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    const int64_t tiles = (n + kSortTile - 1) / kSortTile;
+    hist_scan_kernel<<<kSortPasses, kRadix, 0, stream>>>(hist);
+    BH_CUDA_TRY(cudaGetLastError());
+    const uint64_t* kin = keys_in;
+    const uint32_t* vin = nullptr;
+    for (int p = 0; p < kSortPasses; ++p) {
+        const bool to_out = (p & 1) != 0;
+        uint64_t* kout = to_out ? keys_out : key_alt;
+        uint32_t* vout = to_out ? vals_out : val_alt;
+        uint32_t* lb = lookback + (size_t)p * tiles * kRadix;
+        if (p == 0)
+            onesweep_kernel<true><<<(unsigned)tiles, kSortThreads, smem, stream>>>(
+                n, 8 * p, kin, vin, kout, vout, hist + p * kRadix, lb, tile_ctr + p, err);
+        else
+            onesweep_kernel<false><<<(unsigned)tiles, kSortThreads, smem, stream>>>(
+                n, 8 * p, kin, vin, kout, vout, hist + p * kRadix, lb, tile_ctr + p, err);
+        BH_CUDA_TRY(cudaGetLastError());
+        kin = kout;
+        vin = vout;
+    }
+    return BH_OK;
+}
+
 int launch_permute(bh_context* ctx)
 {
     const int64_t n = ctx->n;

@@ -170,6 +170,27 @@ int bh_generate_morton_codes(const double *pos, int64_t n, const double bbox[6],
 int bh_sort_bodies_by_morton_key(int64_t n, uint64_t *keys, double *pos, double *mass, double *vel,
                                  uint64_t *ids);
 
+/* ---- allocation-free sort (no counterpart in the reference) ---------- */
+/* For callers that cannot let the library call cudaMalloc: a host code whose
+ * device memory belongs to its own pool hands over buffers it already owns,
+ * and a time-critical loop cannot take cudaMalloc's implicit device
+ * synchronisation or its failure under memory pressure.  Sorts n 63-bit
+ * Morton keys already on the device (stable LSD radix sort, the same result
+ * as bh_sort_bodies): keys_out receives the sorted keys and perm_out, for
+ * each sorted position, the key's input position.  keys_in may equal
+ * keys_out.  All three are device pointers; `stream` is a cudaStream_t (NULL
+ * for the default stream).  The call allocates nothing: its scratch is a
+ * fixed file-scope device array of about 15 MB, held by every GPU that loads
+ * the library until the process exits, and n is limited to
+ * BH_NOALLOC_MAX_KEYS (larger n returns BH_ERR_CAPACITY).  The first call on
+ * a device looks the array's device address up (cudaGetSymbolAddress), so make
+ * that first call before any stream capture.  Calls share the array: calls
+ * that overlap on the GPU race.  Returns after the sort has finished (it
+ * synchronises `stream`). */
+#define BH_NOALLOC_MAX_KEYS (1 << 20)
+int bh_sort_keys_noalloc(const uint64_t *keys_in, uint64_t *keys_out, uint32_t *perm_out, int64_t n,
+                         void *stream);
+
 /* ---- host-side input (no GPU needed) --------------------------------- */
 /* convertKeplerToCartesian (src/kepler_to_cartesian.cpp:13-107).
  * el: n*8 = {e, a, i, arg. periapsis, long. asc. node, M, epoch, mu}
