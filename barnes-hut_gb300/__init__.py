@@ -86,6 +86,7 @@ def _sig(lib):
     f["bh_export_tree"] = (C.c_int, [_P, _P, _P, _P, _P])
     f["bh_compute_accelerations"] = (C.c_int, [_P, _D, _D, _D, C.c_int, _P])
     f["bh_interaction_count"] = (C.c_int, [_P, C.POINTER(_I64)])
+    f["bh_interaction_counts"] = (C.c_int, [_P, _P])
     f["bh_step"] = (C.c_int, [_P, _D, _D, _D, _I64, C.c_int, C.POINTER(_D)])
     f["bh_set_profiling"] = (C.c_int, [_P, C.c_int])
     f["bh_phase_times"] = (C.c_int, [_P, _P, C.POINTER(_I64)])
@@ -274,6 +275,12 @@ class Context:
                               download=True):
         out = np.empty((self.n, 3)) if download else None
         _check(library().bh_compute_accelerations(self._h, theta, G, soft2, mode, _ptr(out)))
+        return out
+
+    def interaction_counts(self) -> np.ndarray:
+        """Accepted interactions per body of the last force evaluation."""
+        out = np.empty(self.n, np.int32)
+        _check(library().bh_interaction_counts(self._h, _ptr(out)))
         return out
 
     def interaction_count(self) -> int:

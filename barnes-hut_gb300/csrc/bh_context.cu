@@ -120,6 +120,12 @@ void layout(bh_context* ctx, Carver& c)
     const int64_t nblk = (n + 1023) / 1024;
     ctx->scan_tmp = c.take<int32_t>(std::max<int64_t>(bh::scan_tmp_ints(2 * n), 21 * nblk + 64));
     ctx->inter_count = c.take<unsigned long long>(1);
+    ctx->body_count = c.take<int32_t>(n);
+    ctx->fA = c.take<float4>(2 * n);
+    ctx->fB = c.take<float4>(2 * n);
+    ctx->fmeta = c.take<uint32_t>(2 * n);
+    ctx->direct = c.take<double>(4 * 64);
+    ctx->direct_present = c.take<int32_t>(64);
     ctx->err = c.take<unsigned>(1);
 }
 
@@ -211,6 +217,7 @@ void collect_phases(bh_context* ctx)
 int step_once(bh_context* ctx, double dt, double theta, double G, int mode)
 {
     const bool kick = ctx->t > 0;
+    const bool far = mode >= BH_MODE_FP32_FAR;
     cudaEvent_t e = phase_begin(ctx);
     int rc = bh::launch_drift_bbox(ctx, dt, kick, true);
     phase_end(ctx, 0, e);
@@ -224,7 +231,9 @@ int step_once(bh_context* ctx, double dt, double theta, double G, int mode)
     if (!rc) rc = bh::launch_permute(ctx);
     phase_end(ctx, 3, e);
     e = phase_begin(ctx);
-    if (!rc) rc = bh::launch_build(ctx);
+    if (!rc && far) rc = bh::launch_far_mass(ctx);
+    if (!rc) rc = bh::launch_build(ctx, far ? ctx->m2 : ctx->m);
+    ctx->tree_far = far;
     phase_end(ctx, 4, e);
     e = phase_begin(ctx);
     if (!rc) rc = bh::launch_traverse(ctx, theta, G, 0.0, mode, 0.5 * dt);
@@ -473,7 +482,8 @@ int bh_build_tree(bh_context* ctx)
     int rc = check_ctx(ctx, "bh_build_tree");
     if (rc) return rc;
     if (!ctx->sorted_valid && ctx->n > 0) return bh_fail(BH_ERR_STATE, "bh_build_tree: call bh_sort_bodies first");
-    if ((rc = bh::launch_build(ctx))) return rc;
+    if ((rc = bh::launch_build(ctx, ctx->m))) return rc;
+    ctx->tree_far = false;
     rc = finish(ctx, "bh_build_tree");
     ctx->tree_valid = rc == BH_OK;
     return rc;
@@ -541,6 +551,10 @@ int bh_export_tree(bh_context* ctx, uint64_t* prefix, uint8_t* depth, double* ma
     if (rc) return rc;
     if (!ctx->tree_valid) return ctx->n == 0 ? BH_OK : bh_fail(BH_ERR_STATE, "bh_export_tree: no tree built");
     if (!prefix || !depth || !mass || !com) return bh_fail(BH_ERR_INVALID_ARGUMENT, "bh_export_tree: null array");
+    if (ctx->tree_far) {  // the export is the reference's tree: real masses
+        if ((rc = bh::launch_build(ctx, ctx->m))) return rc;
+        ctx->tree_far = false;
+    }
     HostTree h;
     if ((rc = fetch_tree(ctx, h))) return rc;
     struct Out { uint64_t p; uint8_t d; int32_t s; };
@@ -572,9 +586,28 @@ int bh_compute_accelerations(bh_context* ctx, double theta, double G, double sof
     if (!(theta >= 0.0) || !(soft2 >= 0.0)) return bh_fail(BH_ERR_INVALID_ARGUMENT, "bh_compute_accelerations: theta and soft2 must be >= 0");
     if (ctx->n == 0) return BH_OK;
     if (!ctx->tree_valid) return bh_fail(BH_ERR_STATE, "bh_compute_accelerations: call bh_build_tree first");
+    // The FP32 modes read a tree built over the far-field masses (direct
+    // bodies zeroed); the FP64 modes the reference's tree.  Rebuild the
+    // node values when the tree in place is the other kind.
+    const bool far = mode >= BH_MODE_FP32_FAR;
+    if (far != ctx->tree_far) {
+        if (far && (rc = bh::launch_far_mass(ctx))) return rc;
+        if ((rc = bh::launch_build(ctx, far ? ctx->m2 : ctx->m))) return rc;
+        ctx->tree_far = far;
+    }
     if ((rc = bh::launch_traverse(ctx, theta, G, soft2, mode, 0.0))) return rc;
     if (acc_out && (rc = download_vec3(ctx, acc_out, ctx->px2, ctx->ax, ctx->ay, ctx->az, ctx->n))) return rc;
     return finish(ctx, "bh_compute_accelerations");
+}
+
+int bh_interaction_counts(bh_context* ctx, int32_t* per_body)
+{
+    int rc = check_ctx(ctx, "bh_interaction_counts");
+    if (rc) return rc;
+    if (!per_body) return bh_fail(BH_ERR_INVALID_ARGUMENT, "bh_interaction_counts: null out");
+    if (ctx->n == 0) return BH_OK;
+    BH_CUDA_TRY(cudaMemcpyAsync(per_body, ctx->body_count, sizeof(int32_t) * ctx->n, cudaMemcpyDeviceToHost, ctx->stream));
+    return finish(ctx, "bh_interaction_counts");
 }
 
 int bh_interaction_count(bh_context* ctx, int64_t* total_out)

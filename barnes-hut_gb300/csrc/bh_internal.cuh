@@ -134,8 +134,19 @@ struct bh_context {
     bool bbox_valid = false;
     bool sorted_valid = false; // bodies are in sorted-key order
 
+    bool tree_far = false;      // the tree holds far-field masses (FP32 modes)
+    int num_direct = BH_NUM_MASSIVE;  // bodies with id < num_direct: FP64 direct terms in FP32 modes
+
     // Traversal.
     unsigned long long* inter_count = nullptr;
+    int32_t* body_count = nullptr;  // accepted interactions per body (last traversal)
+    // FP32 node records (FP32 modes): centre of mass as hi + lo floats, G m,
+    // and the topology word; 2n entries each.
+    float4* fA = nullptr;   // {hi.x, hi.y, hi.z, G m}
+    float4* fB = nullptr;   // {lo.x, lo.y, lo.z, bits of ref (child or leaf id)}
+    uint32_t* fmeta = nullptr;  // nchild | depth << 8 | leaf << 16
+    double* direct = nullptr;   // 4 doubles per direct body: x, y, z, G m (by id)
+    int32_t* direct_present = nullptr;  // 1 when body id k was found
 
     // Phase timing (bh_set_profiling): CUDA events around each phase of a
     // step, read back at the next synchronisation.
@@ -169,8 +180,13 @@ int launch_permute(bh_context* ctx);
 int sort_passes_raw(int64_t n, const uint64_t* keys_in, uint64_t* keys_out, uint32_t* vals_out, uint64_t* key_alt,
                     uint32_t* val_alt, uint32_t* hist, uint32_t* lookback, uint32_t* tile_ctr, unsigned* err,
                     cudaStream_t stream);
-int launch_build(bh_context* ctx);
+// Builds the octree over the sorted bodies with the given masses (ctx->m
+// for the reference's tree; the far-field masses for the FP32 modes).
+int launch_build(bh_context* ctx, const double* mass);
+// FP32 modes: far-field masses (direct bodies zeroed) into ctx->m2.
+int launch_far_mass(bh_context* ctx);
 int launch_traverse(bh_context* ctx, double theta, double G, double soft2, int mode, double kick_h);
+int launch_traverse_masked(bh_context* ctx, double theta, double G, double soft2, double kick_h, bool fp64);
 
 // Device-wide exclusive scan of n int32 values (in may equal out); the
 // total is written to *total (device pointer).  n is read from n_dev when

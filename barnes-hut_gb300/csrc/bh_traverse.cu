@@ -46,6 +46,7 @@ struct TravParams {
     double* vy;
     double* vz;
     unsigned long long* inter_count;
+    int32_t* body_count;
     unsigned* err;
 };
 
@@ -162,6 +163,7 @@ __global__ void __launch_bounds__(kTravThreads) traverse_exact_kernel(TravParams
         p.ax[i] = ax;
         p.ay[i] = ay;
         p.az[i] = az;
+        if (p.body_count) p.body_count[i] = (int32_t)cnt;
         if (p.kick_h > 0.0) {
             p.vx[i] = __dadd_rn(p.vx[i], __dmul_rn(p.kick_h, ax));
             p.vy[i] = __dadd_rn(p.vy[i], __dmul_rn(p.kick_h, ay));
@@ -196,6 +198,7 @@ int launch_traverse(bh_context* ctx, double theta, double G, double soft2, int m
     p.ax = ctx->ax; p.ay = ctx->ay; p.az = ctx->az;
     p.vx = ctx->vx; p.vy = ctx->vy; p.vz = ctx->vz;
     p.inter_count = ctx->inter_count;
+    p.body_count = ctx->body_count;
     p.err = ctx->err;
     BH_CUDA_TRY(cudaMemsetAsync(ctx->inter_count, 0, sizeof(unsigned long long), ctx->stream));
     const int64_t groups = (n + 31) / 32;
@@ -204,6 +207,10 @@ int launch_traverse(bh_context* ctx, double theta, double G, double soft2, int m
     case BH_MODE_PLAIN_FP64:
         traverse_exact_kernel<<<(unsigned)blocks, kTravThreads, 0, ctx->stream>>>(p);
         break;
+    case BH_MODE_FP64_LIST:
+        return launch_traverse_masked(ctx, theta, G, soft2, kick_h, true);
+    case BH_MODE_FP32_FAR:
+        return launch_traverse_masked(ctx, theta, G, soft2, kick_h, false);
     default:
         return bh_fail(BH_ERR_INVALID_ARGUMENT, "bh_compute_accelerations: mode not available");
     }

@@ -1,0 +1,449 @@
+// FP32 far-field traversal with FP64 direct terms for the dominant bodies
+// (BH_MODE_FP32_FAR; the learned acceptance reuses it).  No reference
+// counterpart: the reference evaluates every interaction in FP64
+// (src/traversal.cpp:72-82).
+//
+// Precision form:
+//  * The bodies with id < num_direct (the Sun and the 8 planets in the
+//    solar-system inputs) are taken out of the far-field tree (their masses
+//    are zeroed before the build) and summed directly in FP64 for every body.
+//  * Far-field node-body interactions run in FP32 on displacements relative
+//    to the warp's group centre g.  A node's centre of mass is stored as a
+//    pair of floats hi + lo (hi = fl32(c), lo = fl32(c - hi), formed in FP64
+//    once per node), and g is a float, so (hi - g) + lo is the FP64
+//    displacement c - g rounded to FP32 (within an ulp) without one FP64
+//    instruction per visit: on this GPU the FP64 pipe is 1/60 of the FP32
+//    one and three FP64 subtractions per visit would cost more than the
+//    whole FP32 interaction.  Body positions relative to g are formed in FP64
+//    once per body and rounded.
+//  * FP32 partial sums over each staged list of nodes (at most kList) are
+//    added into FP64 accumulators.
+//
+// Warp-cooperative walk: a warp owns 32 Morton-consecutive bodies.  Up to 32
+// nodes are popped at a time, one per lane; a node is accepted for the whole
+// group when side(depth)^2 < theta^2 d^2 with d the distance from its centre
+// of mass to the group's bounding box (every body is at least that far, so
+// each body's own test would accept it too), leaves are always accepted,
+// other nodes are opened.  Accepted nodes are staged in shared memory
+// (group-relative centre + G m) and evaluated by all 32 lanes.
+#include "bh_internal.cuh"
+
+namespace bh {
+namespace {
+
+constexpr int kWarps = 4;
+constexpr int kThreads = 32 * kWarps;
+constexpr int kStack = 1024;  // (slot, lane mask) entries per warp
+constexpr int kList = 128;    // staged interactions per warp
+
+__global__ void far_mass_kernel(int64_t n, const double* __restrict__ m, const uint64_t* __restrict__ id, int nd,
+                                double* __restrict__ m_far)
+{
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+        m_far[i] = id[i] < (uint64_t)nd ? 0.0 : m[i];
+}
+
+// FP32 node records from the FP64 ones.
+__global__ void fp32_nodes_kernel(const int32_t* __restrict__ counts, const TreeRec* __restrict__ rec, double G,
+                                  float4* __restrict__ A, float4* __restrict__ B, uint32_t* __restrict__ meta)
+{
+    const int S = counts[2];
+    for (int s = blockIdx.x * blockDim.x + threadIdx.x; s < S; s += gridDim.x * blockDim.x) {
+        const TreeRec r = rec[s];
+        const float hx = __double2float_rn(r.cx), hy = __double2float_rn(r.cy), hz = __double2float_rn(r.cz);
+        const float lx = __double2float_rn(r.cx - (double)hx);
+        const float ly = __double2float_rn(r.cy - (double)hy);
+        const float lz = __double2float_rn(r.cz - (double)hz);
+        const bool leaf = r.child < 0;
+        A[s] = make_float4(hx, hy, hz, __double2float_rn(G * r.m));
+        B[s] = make_float4(lx, ly, lz, __int_as_float(leaf ? r.leaf : r.child));
+        meta[s] = (uint32_t)r.nchild | ((uint32_t)r.depth << 8) | ((leaf ? 1u : 0u) << 16) |
+                  ((r.m == 0.0 ? 1u : 0u) << 17);
+    }
+}
+
+// Positions and G m of the direct bodies, indexed by id.
+__global__ void direct_extract_kernel(int64_t n, const double* __restrict__ px, const double* __restrict__ py,
+                                      const double* __restrict__ pz, const double* __restrict__ m,
+                                      const uint64_t* __restrict__ id, int nd, double G, double* __restrict__ direct,
+                                      int32_t* __restrict__ present)
+{
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+        const uint64_t k = id[i];
+        if (k < (uint64_t)nd) {
+            direct[4 * k] = px[i];
+            direct[4 * k + 1] = py[i];
+            direct[4 * k + 2] = pz[i];
+            direct[4 * k + 3] = G * m[i];
+            present[k] = 1;
+        }
+    }
+}
+
+struct FParams {
+    int64_t n;
+    const double* px;
+    const double* py;
+    const double* pz;
+    const uint64_t* id;
+    const int32_t* body_leaf;
+    const float4* A;
+    const float4* B;
+    const uint32_t* meta;
+    const TreeRec* rec;
+    const double* bbox;
+    double theta2;
+    double soft2;
+    double G;
+    const double* direct;
+    const int32_t* present;
+    int nd;
+    double kick_h;
+    double* ax;
+    double* ay;
+    double* az;
+    double* vx;
+    double* vy;
+    double* vz;
+    unsigned long long* inter_count;
+    int32_t* body_count;
+    unsigned* err;
+    int64_t max_pops;
+};
+
+// Relative safety margin of the FP32 group tests: a node is accept-all /
+// open-all only when the FP32 test clears the threshold by this factor, so
+// every body's own FP64 test agrees; otherwise it is resolved lane by lane.
+constexpr float kMargin = 1e-4f;
+
+// The masked warp walk.  Stack entries are (slot, lane mask of the bodies that
+// still need the subtree).  Up to 32 entries are classified per iteration,
+// one per lane, against the group's bounding box:
+//   accept-all : side^2 < theta^2 dmin^2 (every body is at least dmin away),
+//   open-all   : side^2 > theta^2 dmax^2 (no body is farther than dmax),
+//   mixed      : each lane of the mask applies its own body's test.
+// Lanes that accept a node take it into the staged interaction list with
+// their mask bit; the others carry it down to the children.  Every body thus
+// interacts with exactly the nodes its own per-body walk accepts
+// (src/traversal.cpp:63-99), in some order.
+//
+// kFP64 = true  (BH_MODE_FP64_LIST): per-lane tests in FP64 with the
+//   reference's rounding; interactions in FP64 from the FP64 node records.
+// kFP64 = false (BH_MODE_FP32_FAR): per-lane tests and interactions in FP32
+//   on group-relative displacements; FP32 partials summed into FP64 per
+//   staged list; FP64 direct terms from the direct bodies at the end.
+template <bool kFP64>
+__global__ void __launch_bounds__(kThreads) traverse_masked_kernel(FParams p)
+{
+    __shared__ int2 stack[kWarps][kStack];
+    __shared__ float4 lst[kWarps][kList];
+    __shared__ int lst_node[kWarps][kList];
+    __shared__ int lst_leaf[kWarps][kList];
+    __shared__ unsigned lst_mask[kWarps][kList];
+    __shared__ float side2f[kMaxDepth + 1];
+    __shared__ double side2d[kMaxDepth + 1];
+    if (threadIdx.x <= kMaxDepth) {
+        const double dx = __dsub_rn(p.bbox[3], p.bbox[0]);
+        const double dy = __dsub_rn(p.bbox[4], p.bbox[1]);
+        const double dz = __dsub_rn(p.bbox[5], p.bbox[2]);
+        double L = dx;
+        if (L < dy) L = dy;
+        if (L < dz) L = dz;
+        const double side = __ddiv_rn(L, (double)(1ull << threadIdx.x));
+        side2d[threadIdx.x] = __dmul_rn(side, side);
+        side2f[threadIdx.x] = (float)side2d[threadIdx.x];
+    }
+    __syncthreads();
+
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    const int64_t base = ((int64_t)blockIdx.x * kWarps + w) * 32;
+    if (base >= p.n) return;
+    const int64_t i = base + lane;
+    const bool valid = i < p.n;
+    const int64_t ii = valid ? i : base;  // idle lanes shadow the group's first body
+    const double x = p.px[ii], y = p.py[ii], z = p.pz[ii];
+    const float gx = __double2float_rn(__shfl_sync(0xffffffffu, x, 0));
+    const float gy = __double2float_rn(__shfl_sync(0xffffffffu, y, 0));
+    const float gz = __double2float_rn(__shfl_sync(0xffffffffu, z, 0));
+    const float rx = __double2float_rn(x - (double)gx);
+    const float ry = __double2float_rn(y - (double)gy);
+    const float rz = __double2float_rn(z - (double)gz);
+    float bminx = rx, bminy = ry, bminz = rz, bmaxx = rx, bmaxy = ry, bmaxz = rz;
+#pragma unroll
+    for (int off = 16; off > 0; off >>= 1) {
+        bminx = fminf(bminx, __shfl_xor_sync(0xffffffffu, bminx, off));
+        bminy = fminf(bminy, __shfl_xor_sync(0xffffffffu, bminy, off));
+        bminz = fminf(bminz, __shfl_xor_sync(0xffffffffu, bminz, off));
+        bmaxx = fmaxf(bmaxx, __shfl_xor_sync(0xffffffffu, bmaxx, off));
+        bmaxy = fmaxf(bmaxy, __shfl_xor_sync(0xffffffffu, bmaxy, off));
+        bmaxz = fmaxf(bmaxz, __shfl_xor_sync(0xffffffffu, bmaxz, off));
+    }
+    const unsigned full = __ballot_sync(0xffffffffu, valid);
+    const int my_leaf = valid ? p.body_leaf[i] : -2;
+    const float theta2f = (float)p.theta2;
+    const double theta2 = p.theta2, soft2 = p.soft2, G = p.G;
+    int2* stk = stack[w];
+    float4* L = lst[w];
+    int* LN = lst_node[w];
+    int* LL = lst_leaf[w];
+    unsigned* LM = lst_mask[w];
+    const unsigned me = 1u << lane;
+    const unsigned lt = me - 1u;
+
+    double adx = 0.0, ady = 0.0, adz = 0.0;
+    unsigned cnt = 0;
+    int nlist = 0;
+    int sp = 1;
+    if (lane == 0) stk[0] = make_int2(0, (int)full);
+    __syncwarp();
+    bool overflow = false;
+    int64_t pops = 0;
+
+    while (sp > 0 || nlist > 0) {
+        if (sp > 0) {
+            int k = (kStack - sp) / 7;  // up to 8 children per popped entry must fit
+            k = k < 32 ? k : 32;
+            k = k < sp ? k : sp;
+            pops += k;
+            if (k == 0 || pops > p.max_pops) {
+                overflow = true;
+                break;
+            }
+            int node = -1;
+            unsigned M = 0, A = 0;
+            int nc = 0, ref = 0, depth = 0;
+            bool leaf = false, mixed = false;
+            float4 e = make_float4(0.f, 0.f, 0.f, 0.f);
+            if (lane < k) {
+                const int2 ent = stk[sp - k + lane];
+                node = ent.x;
+                M = (unsigned)ent.y;
+                const float4 a = __ldg(p.A + node);
+                const float4 b = __ldg(p.B + node);
+                const uint32_t mt = __ldg(p.meta + node);
+                const float cx = (a.x - gx) + b.x, cy = (a.y - gy) + b.y, cz = (a.z - gz) + b.z;
+                e = make_float4(cx, cy, cz, a.w);
+                ref = __float_as_int(b.w);
+                leaf = (mt >> 16) & 1u;
+                depth = (mt >> 8) & 0xFF;
+                if ((mt >> 17) & 1u) {
+                    M = 0;  // skipped with its subtree (traversal.cpp:66)
+                } else if (leaf) {
+                    A = M;  // leaves are always accepted; the own leaf is handled at evaluation
+                } else {
+                    const float ex = fmaxf(0.0f, fmaxf(bminx - cx, cx - bmaxx));
+                    const float ey = fmaxf(0.0f, fmaxf(bminy - cy, cy - bmaxy));
+                    const float ez = fmaxf(0.0f, fmaxf(bminz - cz, cz - bmaxz));
+                    const float fx = fmaxf(fabsf(cx - bminx), fabsf(cx - bmaxx));
+                    const float fy = fmaxf(fabsf(cy - bminy), fabsf(cy - bmaxy));
+                    const float fz = fmaxf(fabsf(cz - bminz), fabsf(cz - bmaxz));
+                    const float dmin2 = ex * ex + ey * ey + ez * ez;
+                    const float dmax2 = fx * fx + fy * fy + fz * fz;
+                    const float s2 = side2f[depth];
+                    if (s2 < theta2f * dmin2 * (1.0f - kMargin)) A = M;
+                    else if (s2 > theta2f * dmax2 * (1.0f + kMargin)) A = 0;
+                    else mixed = true;
+                    nc = (int)(mt & 0xFF);
+                }
+            }
+            __syncwarp();
+            sp -= k;
+            // Mixed nodes: every lane of the mask applies its own test.
+            unsigned mb = __ballot_sync(0xffffffffu, mixed);
+            while (mb) {
+                const int j = __ffs(mb) - 1;
+                mb &= mb - 1;
+                const unsigned Mj = __shfl_sync(0xffffffffu, M, j);
+                bool acc = false;
+                if (kFP64) {
+                    const int nj = __shfl_sync(0xffffffffu, node, j);
+                    const int dj = __shfl_sync(0xffffffffu, depth, j);
+                    const TreeRec r = p.rec[nj];
+                    const double dx = __dsub_rn(r.cx, x), dy = __dsub_rn(r.cy, y), dz = __dsub_rn(r.cz, z);
+                    const double r2 = __dadd_rn(
+                        __dadd_rn(__dadd_rn(__dmul_rn(dx, dx), __dmul_rn(dy, dy)), __dmul_rn(dz, dz)), soft2);
+                    acc = side2d[dj] < __dmul_rn(theta2, r2);
+                } else {
+                    const float cx = __shfl_sync(0xffffffffu, e.x, j);
+                    const float cy = __shfl_sync(0xffffffffu, e.y, j);
+                    const float cz = __shfl_sync(0xffffffffu, e.z, j);
+                    const int dj = __shfl_sync(0xffffffffu, depth, j);
+                    const float dx = cx - rx, dy = cy - ry, dz = cz - rz;
+                    acc = side2f[dj] < theta2f * (dx * dx + dy * dy + dz * dz);
+                }
+                const unsigned Aj = __ballot_sync(0xffffffffu, acc) & Mj;
+                if (lane == j) A = Aj;
+            }
+            // Stage the accepted (node, lanes) entries.
+            const bool stage = A != 0;
+            const unsigned am = __ballot_sync(0xffffffffu, stage);
+            if (stage) {
+                const int pos = nlist + __popc(am & lt);
+                L[pos] = e;
+                LN[pos] = node;
+                LL[pos] = leaf ? ref : -1;  // leaf id for the own-leaf test
+                LM[pos] = A;
+            }
+            nlist += __popc(am);
+            // Push the children with the lanes that still need them.
+            const unsigned rest = M & ~A;
+            if (leaf || rest == 0) nc = 0;
+            int incl = nc;
+#pragma unroll
+            for (int off = 1; off < 32; off <<= 1) {
+                const int t = __shfl_up_sync(0xffffffffu, incl, off);
+                if (lane >= off) incl += t;
+            }
+            const int total = __shfl_sync(0xffffffffu, incl, 31);
+            const int at = sp + incl - nc;
+            for (int c = 0; c < nc; ++c) stk[at + c] = make_int2(ref + c, (int)rest);
+            sp += total;
+            __syncwarp();
+        }
+        if (nlist > kList - 32 || (sp == 0 && nlist > 0)) {
+            if (kFP64) {
+                for (int j = 0; j < nlist; ++j) {
+                    const unsigned mj = LM[j];
+                    const TreeRec r = p.rec[LN[j]];
+                    const double dx = r.cx - x, dy = r.cy - y, dz = r.cz - z;
+                    bool take = (mj & me) != 0;
+                    if (LL[j] == my_leaf) {
+                        // Own leaf: skipped at depth 21 unless a chain cell above
+                        // it (depths top..20) accepts (traversal.cpp:70,78).
+                        const double r2e = __dadd_rn(__dadd_rn(__dadd_rn(__dmul_rn(dx, dx), __dmul_rn(dy, dy)),
+                                                               __dmul_rn(dz, dz)), soft2);
+                        take = take && r.top <= kMaxDepth - 1 && side2d[kMaxDepth - 1] < __dmul_rn(theta2, r2e);
+                    }
+                    const double r2 = fma(dx, dx, fma(dy, dy, fma(dz, dz, soft2)));
+                    const double inv = rsqrt(r2);
+                    double sc = (G * r.m) * (inv * inv * inv);
+                    if (!take) sc = 0.0;
+                    adx = fma(sc, dx, adx);
+                    ady = fma(sc, dy, ady);
+                    adz = fma(sc, dz, adz);
+                    cnt += take ? 1u : 0u;
+                }
+            } else {
+                float fx = 0.f, fy = 0.f, fz = 0.f;
+                for (int j = 0; j < nlist; ++j) {
+                    const float4 q = L[j];
+                    const unsigned mj = LM[j];
+                    const bool take = (mj & me) && LL[j] != my_leaf;
+                    const float dx = q.x - rx, dy = q.y - ry, dz = q.z - rz;
+                    const float r2 = fmaf(dx, dx, fmaf(dy, dy, fmaf(dz, dz, (float)soft2)));
+                    const float inv = rsqrtf(r2);
+                    float sc = q.w * (inv * inv * inv);
+                    if (!take) sc = 0.0f;
+                    fx = fmaf(sc, dx, fx);
+                    fy = fmaf(sc, dy, fy);
+                    fz = fmaf(sc, dz, fz);
+                    cnt += take ? 1u : 0u;
+                }
+                adx += (double)fx;
+                ady += (double)fy;
+                adz += (double)fz;
+            }
+            nlist = 0;
+            __syncwarp();
+        }
+    }
+    if (overflow && lane == 0) atomicOr(p.err, kErrOverflow);
+
+    if (!kFP64) {
+        // FP64 direct terms from the direct bodies (not in the far-field tree).
+        const uint64_t my_id = valid ? p.id[i] : ~0ull;
+        for (int kk = 0; kk < p.nd; ++kk) {
+            if (!p.present[kk] || my_id == (uint64_t)kk) continue;
+            const double dx = p.direct[4 * kk] - x, dy = p.direct[4 * kk + 1] - y, dz = p.direct[4 * kk + 2] - z;
+            const double r2 = fma(dx, dx, fma(dy, dy, fma(dz, dz, soft2)));
+            const double inv = rsqrt(r2);
+            const double sc = p.direct[4 * kk + 3] * (inv * inv * inv);
+            adx = fma(sc, dx, adx);
+            ady = fma(sc, dy, ady);
+            adz = fma(sc, dz, adz);
+            ++cnt;
+        }
+    }
+    if (valid) {
+        p.ax[i] = adx;
+        p.ay[i] = ady;
+        p.az[i] = adz;
+        if (p.body_count) p.body_count[i] = (int32_t)cnt;
+        if (p.kick_h > 0.0) {
+            p.vx[i] = p.vx[i] + p.kick_h * adx;
+            p.vy[i] = p.vy[i] + p.kick_h * ady;
+            p.vz[i] = p.vz[i] + p.kick_h * adz;
+        }
+    }
+    if (p.inter_count) {
+        unsigned long long c = valid ? cnt : 0ull;
+#pragma unroll
+        for (int off = 16; off > 0; off >>= 1) c += __shfl_down_sync(0xffffffffu, c, off);
+        if (lane == 0) atomicAdd(p.inter_count, c);
+    }
+}
+
+int grid_n(int64_t n)
+{
+    int64_t b = (n + 255) / 256;
+    if (b < 1) b = 1;
+    return (int)(b > 8 * kNumSMs ? 8 * kNumSMs : b);
+}
+
+}  // namespace
+
+int launch_far_mass(bh_context* ctx)
+{
+    if (ctx->n == 0) return BH_OK;
+    const int nd = ctx->num_direct < 64 ? ctx->num_direct : 64;
+    far_mass_kernel<<<grid_n(ctx->n), 256, 0, ctx->stream>>>(ctx->n, ctx->m, ctx->id, nd, ctx->m2);
+    BH_LAUNCH_CHECK(ctx);
+    return BH_OK;
+}
+
+int launch_traverse_masked(bh_context* ctx, double theta, double G, double soft2, double kick_h, bool fp64)
+{
+    const int64_t n = ctx->n;
+    if (n == 0) return BH_OK;
+    const int nd = fp64 ? 0 : (ctx->num_direct < 64 ? ctx->num_direct : 64);
+    fp32_nodes_kernel<<<grid_n(2 * n), 256, 0, ctx->stream>>>(ctx->counts, ctx->rec, G, ctx->fA, ctx->fB, ctx->fmeta);
+    BH_LAUNCH_CHECK(ctx);
+    if (nd > 0) {
+        BH_CUDA_TRY(cudaMemsetAsync(ctx->direct_present, 0, sizeof(int32_t) * 64, ctx->stream));
+        direct_extract_kernel<<<grid_n(n), 256, 0, ctx->stream>>>(n, ctx->px, ctx->py, ctx->pz, ctx->m, ctx->id, nd, G,
+                                                                  ctx->direct, ctx->direct_present);
+        BH_LAUNCH_CHECK(ctx);
+    }
+    FParams p;
+    p.n = n;
+    p.px = ctx->px; p.py = ctx->py; p.pz = ctx->pz;
+    p.id = ctx->id;
+    p.body_leaf = ctx->body_leaf;
+    p.A = ctx->fA; p.B = ctx->fB; p.meta = ctx->fmeta;
+    p.rec = ctx->rec;
+    p.bbox = ctx->bbox;
+    p.theta2 = theta * theta;
+    p.soft2 = soft2;
+    p.G = G;
+    p.direct = ctx->direct;
+    p.present = ctx->direct_present;
+    p.nd = nd;
+    p.kick_h = kick_h;
+    p.ax = ctx->ax; p.ay = ctx->ay; p.az = ctx->az;
+    p.vx = ctx->vx; p.vy = ctx->vy; p.vz = ctx->vz;
+    p.inter_count = ctx->inter_count;
+    p.body_count = ctx->body_count;
+    p.err = ctx->err;
+    p.max_pops = 2 * n + 2;
+    BH_CUDA_TRY(cudaMemsetAsync(ctx->inter_count, 0, sizeof(unsigned long long), ctx->stream));
+    const int64_t groups = (n + 31) / 32;
+    const int64_t blocks = (groups + kWarps - 1) / kWarps;
+    if (fp64)
+        traverse_masked_kernel<true><<<(unsigned)blocks, kThreads, 0, ctx->stream>>>(p);
+    else
+        traverse_masked_kernel<false><<<(unsigned)blocks, kThreads, 0, ctx->stream>>>(p);
+    BH_LAUNCH_CHECK(ctx);
+    return BH_OK;
+}
+
+}  // namespace bh

@@ -372,7 +372,7 @@ __global__ void slot_count_kernel(int32_t* counts, const int32_t* __restrict__ c
 
 }  // namespace
 
-int launch_build(bh_context* ctx)
+int launch_build(bh_context* ctx, const double* mass)
 {
     const int64_t n = ctx->n;
     if (n == 0) return BH_OK;
@@ -388,7 +388,7 @@ int launch_build(bh_context* ctx)
     leaf_scatter_kernel<<<g, kThreads, 0, st>>>(n, ctx->key, ctx->head, ctx->body_leaf, ctx->leaf_first, ctx->leaf_key);
     BH_LAUNCH_CHECK(ctx);
     leaf_sum_kernel<<<g, kThreads, 0, st>>>(ctx->counts, ctx->leaf_first, ctx->leaf_key, ctx->px, ctx->py, ctx->pz,
-                                            ctx->m, ctx->leaf_m, ctx->leaf_wx, ctx->leaf_wy, ctx->leaf_wz, ctx->cdep);
+                                            mass, ctx->leaf_m, ctx->leaf_wx, ctx->leaf_wy, ctx->leaf_wz, ctx->cdep);
     BH_LAUNCH_CHECK(ctx);
 
     // 2. branching nodes: representative flags -> ids -> ranges/child counts

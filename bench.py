@@ -53,6 +53,16 @@ SEED = 2
 FLOPS_PER_INTERACTION = 20
 L2_FLUSH_BYTES = 256 << 20
 WORKLOAD = "plain FP64 theta=1.05, dt=1h, 300,149 bodies (Sun, 8 planets, 300,140 asteroids, 10% outer belt)"
+MODES = {"plain": 0, "fp64_list": 1, "fp32": 2, "learned": 3}
+KERNEL = {0: "traverse_exact_kernel", 1: "traverse_list_kernel", 2: "traverse_fp32_kernel", 3: "traverse_fp32_kernel"}
+
+
+def workload_name(args) -> str:
+    if args.bodies == N_BODIES and args.mode == "fp64_list" and args.theta == THETA and args.outer == 0.1 \
+            and args.trojan == 0.0:
+        return WORKLOAD
+    return (f"{args.mode} theta={args.theta}, dt=1h, {args.bodies:,} bodies (Sun, 8 planets, "
+            f"{args.bodies - 9:,} asteroids, {args.outer:.0%} outer belt, {args.trojan:.0%} trojans)")
 
 
 def parse():
@@ -62,6 +72,10 @@ def parse():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--bodies", type=int, default=N_BODIES)
+    ap.add_argument("--mode", default="fp64_list", choices=list(MODES))
+    ap.add_argument("--outer", type=float, default=0.10, help="outer-belt fraction of the asteroids")
+    ap.add_argument("--trojan", type=float, default=0.0, help="Jupiter-trojan fraction of the asteroids")
+    ap.add_argument("--theta", type=float, default=THETA)
     ap.add_argument("--e2e-steps", type=int, default=5)
     ap.add_argument("--cpu-seconds", type=float, default=15.0, help="budget of the CPU-baseline sample")
     ap.add_argument("--no-cpu-baseline", action="store_true")
@@ -135,7 +149,7 @@ class ClockSampler:
                 "samples": len(sm)}
 
 
-def cpu_baseline(pos, vel, mass, ids, budget_s: float, nsteps_max: int = 20):
+def cpu_baseline(pos, vel, mass, ids, budget_s: float, theta: float = THETA, nsteps_max: int = 20):
     """Times the oracle's step loop on all host cores for a bounded sample."""
     from oracle.oracle import Oracle
     o = Oracle("port")
@@ -147,12 +161,12 @@ def cpu_baseline(pos, vel, mass, ids, budget_s: float, nsteps_max: int = 20):
         pass
     n = len(mass)
     t0 = time.perf_counter()
-    p, v, m, i, a, t, _ = o.simulate(pos, vel, mass, ids, DT, THETA, G, 1)
+    p, v, m, i, a, t, _ = o.simulate(pos, vel, mass, ids, DT, theta, G, 1)
     first = time.perf_counter() - t0
     extra = max(0, min(nsteps_max - 1, int(budget_s / max(first, 1e-3)) - 1))
     t1 = time.perf_counter()
     if extra:
-        o.simulate(p, v, m, i, DT, THETA, G, extra, t=t, acc=a)
+        o.simulate(p, v, m, i, DT, theta, G, extra, t=t, acc=a)
     rest = time.perf_counter() - t1
     steps = 1 + extra
     secs = first + rest
@@ -162,10 +176,12 @@ def cpu_baseline(pos, vel, mass, ids, budget_s: float, nsteps_max: int = 20):
 
 
 def run_reference(args, rank):
+    """The reference arm: the reference's CPU path (compiled sources where the
+    checkout exists, else the oracle port) on every host core, rank 0 only."""
     if rank != 0:
         return
     bh = importlib.import_module("barnes-hut_gb300")
-    pos, vel, mass, ids = bh.generate_system(SEED, args.bodies, 0.1, 0.0)
+    pos, vel, mass, ids = bh.generate_system(SEED, args.bodies, args.outer, args.trojan)
     from oracle.oracle import Oracle
     o, kind = Oracle("port"), "port"
     try:
@@ -173,25 +189,26 @@ def run_reference(args, rank):
     except (FileNotFoundError, OSError):
         pass
     n = len(mass)
-    # warm-up and timed steps, each a full step of the same workload; the
-    # number of timed steps is capped so the run stays within minutes.
-    p, v, m, i, a, t, _ = o.simulate(pos, vel, mass, ids, DT, THETA, G, max(1, min(args.warmup, 1)))
+    theta = args.theta
+    # Warm-up steps, then timed steps; both capped so the run ends in minutes.
     t0 = time.perf_counter()
-    p, v, m, i, a, t, _ = o.simulate(p, v, m, i, DT, THETA, G, 1, t=t, acc=a)
+    p, v, m, i, a, t, _ = o.simulate(pos, vel, mass, ids, DT, theta, G, 1)
     one = time.perf_counter() - t0
-    k = max(1, min(args.steps, int(90.0 / max(one, 1e-3))))
+    warm = 1 + max(0, min(args.warmup - 1, int(30.0 / max(one, 1e-3))))
+    if warm > 1:
+        p, v, m, i, a, t, _ = o.simulate(p, v, m, i, DT, theta, G, warm - 1, t=t, acc=a)
+    k = max(1, min(args.steps, int(120.0 / max(one, 1e-3))))
     t0 = time.perf_counter()
-    if k > 1:
-        o.simulate(p, v, m, i, DT, THETA, G, k - 1, t=t, acc=a)
-    secs = one + (time.perf_counter() - t0)
+    o.simulate(p, v, m, i, DT, theta, G, k, t=t, acc=a)
+    secs = time.perf_counter() - t0
     val = n * k / secs
     cores = Oracle("port").threads()
     line = {"metric": "body-steps/s", "value": val, "unit": "body-steps/s", "n_gpus": args.gpus, "steps": k,
-            "warmup": 1, "ms_per_step": 1e3 * secs / k, "higher_is_better": True, "scaling": "weak",
+            "warmup": warm, "ms_per_step": 1e3 * secs / k, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f64", "data": "synthetic", "impl": "reference",
-            "config": {"workload": WORKLOAD, "bodies": n, "theta": THETA, "dt_days": DT},
+            "config": {"workload": workload_name(args), "bodies": n, "theta": theta, "dt_days": DT},
             "cpu_baseline": {"value": val, "unit": "body-steps/s", "cores": cores, "kind": kind,
-                             "sample": f"{k} timed steps after 1 warm-up step, OpenMP {cores} threads"},
+                             "sample": f"{k} timed full steps after {warm} warm-up steps, OpenMP {cores} threads"},
             "e2e": {"value": val, "unit": "body-steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
 
@@ -201,16 +218,18 @@ def run_ours(args, rank, ws, local):
     bh = importlib.import_module("barnes-hut_gb300")
     dev = local
     torch.cuda.set_device(dev)
-    pos, vel, mass, ids = bh.generate_system(SEED, args.bodies, 0.1, 0.0)
+    pos, vel, mass, ids = bh.generate_system(SEED, args.bodies, args.outer, args.trojan)
     n = len(mass)
+    mode = MODES[args.mode]
+    theta = args.theta
     ctx = bh.Context(n, dev)
     ext = torch.cuda.ExternalStream(ctx.stream(), device=dev)
     flush = torch.empty(L2_FLUSH_BYTES // 4, dtype=torch.float32, device=f"cuda:{dev}")
     ctx.set_bodies(pos, vel, mass, ids)
     t = 0.0
     for _ in range(args.warmup):
-        t = ctx.step(DT, THETA, G, 1, bh.MODE_PLAIN_FP64, t=t)
-    peak_fp64 = ctx.measure_fma_peak(True)
+        t = ctx.step(DT, theta, G, 1, mode, t=t)
+    peak = ctx.measure_fma_peak(mode <= 1)
 
     ctx.set_profiling(True)
     l0 = ctx.launches()
@@ -223,7 +242,7 @@ def run_ours(args, rank, ws, local):
             e0 = torch.cuda.Event(enable_timing=True)
             e1 = torch.cuda.Event(enable_timing=True)
             e0.record(ext)
-            t = ctx.step(DT, THETA, G, 1, bh.MODE_PLAIN_FP64, t=t)
+            t = ctx.step(DT, theta, G, 1, mode, t=t)
             e1.record(ext)
             e1.synchronize()
             times.append(e0.elapsed_time(e1))
@@ -247,15 +266,24 @@ def run_ours(args, rank, ws, local):
     for _ in range(e2e_steps):
         ctx.set_bodies(hp, hv, hm, hi)
         ctx.set_accelerations(ha)
-        t = ctx.step(DT, THETA, G, 1, bh.MODE_PLAIN_FP64, t=t)
+        t = ctx.step(DT, theta, G, 1, mode, t=t)
         ctx.get_bodies(out=(hp, hv, hm, hi, ha))
     e2e_s = reduce_max(time.perf_counter() - t0, ws)
     h2d = hp.nbytes + hv.nbytes + hm.nbytes + hi.nbytes + ha.nbytes
     d2h = h2d
 
+    # Accuracy of this mode against the FP64 direct-sum sampler (4,096 bodies).
+    rng = np.random.default_rng(0)
+    sample = np.sort(rng.choice(n, min(n, 4096), replace=False))
+    ref = ctx.direct_sum(sample, G)
+    acc = ctx.compute_accelerations(theta, G, 0.0, mode)
+    err = np.linalg.norm(acc[sample] - ref, axis=1) / np.linalg.norm(ref, axis=1)
+    accuracy = {"median_rel_err": float(np.median(err)), "p99_rel_err": float(np.quantile(err, 0.99)),
+                "sample": int(len(sample)), "judge": "FP64 direct sum"}
+
     cpu = None
     if rank == 0 and not args.no_cpu_baseline:
-        cpu = cpu_baseline(pos, vel, mass, ids, args.cpu_seconds)
+        cpu = cpu_baseline(pos, vel, mass, ids, args.cpu_seconds, theta)
     ctx.close()
     if rank != 0:
         return
@@ -263,22 +291,24 @@ def run_ours(args, rank, ws, local):
     force_ms = phases["forces"] / k
     inter_per_step = inter / k
     achieved = inter_per_step * FLOPS_PER_INTERACTION / (force_ms * 1e-3) / 1e12
+    fp = "fp64" if mode <= 1 else "fp32"
     value = ws * n * k / (total_ms * 1e-3)
     line = {
         "metric": "body-steps/s", "value": value, "unit": "body-steps/s", "n_gpus": ws, "steps": k,
         "warmup": args.warmup, "ms_per_step": total_ms / k, "higher_is_better": True, "scaling": "weak",
-        "vs_baseline": None, "dtype": "f64",
+        "vs_baseline": None, "dtype": "f64" if mode <= 1 else "f32 far field + f64 state/direct terms",
         "data": "synthetic (seeded solar system generated through bh_generate_system)",
-        "config": {"workload": WORKLOAD, "bodies": n, "theta": THETA, "dt_days": DT, "mode": "plain_fp64",
+        "config": {"workload": workload_name(args), "bodies": n, "theta": theta, "dt_days": DT, "mode": args.mode,
                    "seed": SEED, "l2": "flushed before every timed step (256 MiB write)",
                    "parallelism": f"replicas x{ws}"},
-        "roofline": {"kernel": "traverse_exact_kernel", "bound": "fp64", "achieved": achieved,
-                     "peak": peak_fp64, "unit": "TFLOP/s", "frac": achieved / peak_fp64,
-                     "peak_source": "measured in-process: FP64 FMA chains (bh_measure_fma_peak)",
+        "roofline": {"kernel": KERNEL[mode], "bound": fp, "achieved": achieved,
+                     "peak": peak, "unit": "TFLOP/s", "frac": achieved / peak,
+                     "peak_source": f"measured in-process: {fp.upper()} FMA chains (bh_measure_fma_peak)",
                      "work": f"{FLOPS_PER_INTERACTION} flops x {inter_per_step:.4g} interactions per launch",
                      "traffic": None},
         "phases_ms_per_step": {kk: v / k for kk, v in phases.items()},
         "interactions_per_body": inter_per_step / n,
+        "accuracy": accuracy,
         "e2e": {"value": ws * n * e2e_steps / e2e_s, "unit": "body-steps/s", "h2d_bytes_per_step": h2d,
                 "d2h_bytes_per_step": d2h},
         "gpu_launches": launches,

@@ -53,10 +53,12 @@ enum bh_mode {
      * accelerations equal computeAccelerations (src/traversal.cpp:13-103)
      * bit for bit. */
     BH_MODE_PLAIN_FP64 = 0,
-    /* Same interaction set as BH_MODE_PLAIN_FP64 (exact per-body theta test
-     * in FP64), evaluated from shared-memory interaction lists with a
-     * refined reciprocal square root; results agree with the reference to
-     * ~1e-15 relative, not bit for bit.  No reference counterpart. */
+    /* Same interaction set as BH_MODE_PLAIN_FP64: the warp's group box
+     * classifies nodes, undecided ones get each body's exact FP64 test, and
+     * lane masks carry which bodies still need a subtree.  Interactions are
+     * evaluated in FP64 from shared-memory lists with rsqrt and FMA, so
+     * results agree with the reference to ~1e-15 relative, not bit for bit.
+     * No reference counterpart. */
     BH_MODE_FP64_LIST = 1,
     /* Far field in FP32 on displacements formed in FP64 relative to the
      * warp's group centre; FP32 partials summed into FP64 accumulators; the
@@ -133,6 +135,9 @@ int bh_compute_accelerations(bh_context *ctx, double theta, double G, double sof
 /* Accepted interactions per body of the last bh_compute_accelerations
  * (summed over the body's accepted nodes). No reference counterpart. */
 int bh_interaction_count(bh_context *ctx, int64_t *total_out);
+/* Accepted interactions of every body (n int32, current order) in the last
+ * bh_compute_accelerations / bh_step.  No reference counterpart. */
+int bh_interaction_counts(bh_context *ctx, int32_t *per_body);
 /* `nsteps` steps of the `--fc tree` loop of src/main.cpp:191-282 (kick at
  * t > 0, drift, bbox, keys, sort, build, merge, forces, kick).  *t_io is the
  * simulation time, accumulated as t += dt after every step. */

@@ -204,3 +204,38 @@ def test_4m_properties(bh):
         assert rc == 0
         err = np.linalg.norm(acc[sample] - ref, axis=1) / np.linalg.norm(ref, axis=1)
         assert np.median(err) < 1e-5
+
+
+def test_fp64_list_mode_same_interaction_set(bh, ctx, golden, port):
+    """BH_MODE_FP64_LIST: the masked group walk gives every body exactly the
+    reference's interaction set (per-body counts equal the oracle's), and the
+    accelerations agree with the bit-exact mode to FP64 rounding."""
+    g = golden("synthetic_19054.npz")
+    pos, vel, mass, ids = g["pos"], g["vel"], g["mass"], g["ids"]
+    s = gpu_stages(ctx, pos, vel, mass, ids)
+    exact_counts = ctx.interaction_counts()
+    acc_list = ctx.compute_accelerations(THETA, G, 0.0, bh.MODE_FP64_LIST)
+    list_counts = ctx.interaction_counts()
+    bb = port.bbox(pos)
+    sk, sp, sm, sv, si, _ = port.sort(port.keys(pos, bb), pos, mass, vel, ids)
+    tree = port.tree(sk, sp, sm)
+    _, ref_counts = port.accelerations(tree, sk, sp, THETA, G, 0.0, bb, count=True)
+    assert np.array_equal(exact_counts, ref_counts)
+    assert np.array_equal(list_counts, ref_counts)
+    # Tolerance: different summation order and rsqrt/FMA -> relative 1e-13.
+    err = np.linalg.norm(acc_list - s["acc"], axis=1) / np.linalg.norm(s["acc"], axis=1)
+    assert err.max() < 1e-13
+
+
+def test_fp64_list_mode_300k_counts(bh, ctx, port):
+    pos, vel, mass, ids = bh.generate_system(21, 300_149, 0.1, 0.0)
+    s = gpu_stages(ctx, pos, vel, mass, ids)
+    acc_list = ctx.compute_accelerations(THETA, G, 0.0, bh.MODE_FP64_LIST)
+    counts = ctx.interaction_counts()
+    bb = port.bbox(pos)
+    sk, sp, sm, sv, si, _ = port.sort(port.keys(pos, bb), pos, mass, vel, ids)
+    tree = port.tree(sk, sp, sm)
+    _, ref_counts = port.accelerations(tree, sk, sp, THETA, G, 0.0, bb, count=True)
+    assert np.array_equal(counts, ref_counts)
+    err = np.linalg.norm(acc_list - s["acc"], axis=1) / np.linalg.norm(s["acc"], axis=1)
+    assert err.max() < 1e-13

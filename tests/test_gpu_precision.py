@@ -1,0 +1,92 @@
+"""The FP32 far-field precision form (BH_MODE_FP32_FAR): accelerations judged
+against the FP64 direct-sum sampler, and against the plain FP64 mode."""
+from __future__ import annotations
+
+import numpy as np
+import pytest
+
+from conftest import DT, G, THETA
+
+pytestmark = pytest.mark.gpu
+
+
+def rel_err(a, ref):
+    return np.linalg.norm(a - ref, axis=1) / np.linalg.norm(ref, axis=1)
+
+
+@pytest.fixture(scope="module")
+def system(bh):
+    pos, vel, mass, ids = bh.generate_system(11, 300_149, 0.1, 0.0)
+    ctx = bh.Context(len(mass))
+    ctx.set_bodies(pos, vel, mass, ids)
+    ctx.compute_bbox(); ctx.compute_keys(); ctx.sort_bodies(); ctx.build_tree()
+    rng = np.random.default_rng(1)
+    sample = np.sort(rng.choice(len(mass), 2048, replace=False))
+    sample = np.unique(np.concatenate([sample, np.arange(9)]))  # include the Sun and planets' slots
+    ref = ctx.direct_sum(sample, G)
+    yield ctx, sample, ref
+    ctx.close()
+
+
+@pytest.mark.parametrize("theta", [0.5, 0.8, 1.05])
+def test_fp32_far_error_vs_direct_sum(bh, system, theta):
+    ctx, sample, ref = system
+    a32 = ctx.compute_accelerations(theta, G, 0.0, bh.MODE_FP32_FAR)
+    a64 = ctx.compute_accelerations(theta, G, 0.0, bh.MODE_PLAIN_FP64)
+    e32 = rel_err(a32[sample], ref)
+    e64 = rel_err(a64[sample], ref)
+    # Tolerance: the metric's budget, median relative error <= 1e-5.
+    assert np.median(e32) <= 1e-5
+    assert np.all(np.isfinite(a32))
+    # The group acceptance is at least as strict as the per-body test, and
+    # the dominant Sun/planet terms are exact FP64, so the FP32 form is not
+    # less accurate than the plain FP64 form beyond FP32 rounding.
+    assert np.median(e32) <= np.median(e64) + 1e-6
+    assert np.quantile(e32, 0.99) <= max(1e-4, 2 * np.quantile(e64, 0.99))
+
+
+def test_fp32_far_tree_rebuild_restores_reference_tree(bh, system, golden):
+    ctx, _, _ = system
+    ctx.compute_accelerations(THETA, G, 0.0, bh.MODE_FP32_FAR)
+    # export always reports the reference's tree (real masses)
+    prefix, depth, mass, com = ctx.export_tree()
+    assert depth[0] == 0 and mass[0] > 1.9e30  # the root holds the Sun again
+
+
+def test_fp32_far_trajectory_close_to_fp64(bh):
+    pos, vel, mass, ids = bh.generate_system(12, 50_000, 0.1, 0.05)
+    out = {}
+    for mode in (bh.MODE_PLAIN_FP64, bh.MODE_FP32_FAR):
+        with bh.Context(len(mass)) as c:
+            c.set_bodies(pos, vel, mass, ids)
+            c.step(DT, THETA, G, nsteps=20, mode=mode, t=0.0)
+            p, v, m, i, a = c.get_bodies()
+            o = np.argsort(i)
+            out[mode] = (p[o], v[o])
+    dp = np.abs(out[0][0] - out[2][0]).max()
+    assert dp < 1e-9  # AU after 20 one-hour steps
+
+
+def test_direct_bodies_summed_exactly(bh):
+    """Nine massive bodies only: no far field at all, FP64 direct sums."""
+    pos, vel, mass, ids = bh.generate_system(3, 9, 0.0, 0.0)
+    with bh.Context(9) as c:
+        c.set_bodies(pos, vel, mass, ids)
+        c.compute_bbox(); c.compute_keys(); c.sort_bodies(); c.build_tree()
+        a = c.compute_accelerations(THETA, G, 0.0, bh.MODE_FP32_FAR)
+        ref = c.direct_sum(np.arange(9), G)
+    assert np.all(rel_err(a, ref) < 1e-14)
+
+
+def test_fp32_far_interaction_set_tracks_per_body_theta(bh, system, port):
+    """The FP32 walk applies each body's own theta test on the far-field tree
+    (the direct bodies' masses removed, which moves the centres of mass of
+    the cells around them): the typical body has exactly the FP64 interaction
+    count plus its direct terms, and the totals stay within 15 %."""
+    ctx, _, _ = system
+    ctx.compute_accelerations(THETA, G, 0.0, bh.MODE_FP64_LIST)
+    c64 = ctx.interaction_counts().astype(np.int64)
+    ctx.compute_accelerations(THETA, G, 0.0, bh.MODE_FP32_FAR)
+    c32 = ctx.interaction_counts().astype(np.int64)
+    assert np.median(c32 - c64) == 9
+    assert abs(c32.sum() / c64.sum() - 1) < 0.15
