@@ -93,6 +93,12 @@ def _sig(lib):
     f["bh_measure_fma_peak"] = (C.c_int, [_P, C.c_int, C.POINTER(_D)])
     f["bh_direct_sum"] = (C.c_int, [_P, _I64, _P, _D, _P])
     f["bh_invariants"] = (C.c_int, [_P, _D, _D, _P])
+    f["bh_mlp_gradient"] = (C.c_int, [_P, _P, _P, _I64, _P, _P])
+    f["bh_mlp_train"] = (C.c_int, [_P, _P, _I64, C.c_int, C.c_int, C.c_float, C.c_uint64, _P, _P, _P])
+    f["bh_mlp_predict"] = (C.c_int, [_P, _P, _P, _I64, _P, _P])
+    f["bh_learned_collect"] = (C.c_int, [_P, _D, _D, _D, _D, _I64, _P, _P, C.POINTER(_I64)])
+    f["bh_learned_set_model"] = (C.c_int, [_P, _P, _P, _D, _D])
+    f["bh_learned_stats"] = (C.c_int, [_P, _P])
     f["bh_compute_local_bbox"] = (C.c_int, [_P, _I64, _P])
     f["bh_generate_morton_codes"] = (C.c_int, [_P, _I64, _P, _P])
     f["bh_sort_bodies_by_morton_key"] = (C.c_int, [_I64, _P, _P, _P, _P, _P])
@@ -321,10 +327,66 @@ class Context:
         _check(library().bh_invariants(self._h, G, theta, _ptr(out)))
         return dict(E=out[0], K=out[1], U=out[2], L=out[3:6].copy(), P=out[6:9].copy())
 
+    def learned_collect(self, theta=THETA_DEFAULT, theta_label=0.5, theta_max=3.0, G=G_DEFAULT,
+                        max_pairs=2_000_000):
+        """(features (k, 8), labels (k,)) training pairs from the current tree."""
+        F = np.empty((max_pairs, 8), np.float32); L = np.empty(max_pairs, np.float32)
+        k = _I64(0)
+        _check(library().bh_learned_collect(self._h, theta, theta_label, theta_max, G, max_pairs, _ptr(F), _ptr(L),
+                                            C.byref(k)))
+        return F[:k.value].copy(), L[:k.value].copy()
+
+    def learned_set_model(self, params, scale, budget=1e-5, theta_max=3.0) -> None:
+        p = np.ascontiguousarray(params, np.float32); sc = np.ascontiguousarray(scale, np.float32)
+        _check(library().bh_learned_set_model(self._h, _ptr(p), _ptr(sc), budget, theta_max))
+
+    def learned_stats(self) -> dict:
+        v = np.zeros(3, np.int64)
+        _check(library().bh_learned_stats(self._h, _ptr(v)))
+        return {"candidates": int(v[0]), "accepted": int(v[1]), "fallback": int(v[2])}
+
     def step(self, dt, theta=THETA_DEFAULT, G=G_DEFAULT, nsteps=1, mode=MODE_PLAIN_FP64, t=None) -> float:
         tv = _D(0.0 if t is None else t)
         _check(library().bh_step(self._h, dt, theta, G, int(nsteps), mode, None if t is None else C.byref(tv)))
         return tv.value
+
+
+# ------------------------------------------------- learned acceptance network
+MLP_PARAMS = 4801
+MLP_SCALE = 34
+
+
+def mlp_gradient(params, X, T):
+    """(loss, gradient) of the network on standardised X (n, 8), targets T."""
+    p = np.ascontiguousarray(params, np.float32)
+    X = np.ascontiguousarray(X, np.float32).reshape(-1, 8)
+    T = np.ascontiguousarray(T, np.float32)
+    g = np.empty(MLP_PARAMS, np.float32)
+    loss = C.c_float(0.0)
+    _check(library().bh_mlp_gradient(_ptr(p), _ptr(X), _ptr(T), len(T), _ptr(g), C.byref(loss)))
+    return loss.value, g
+
+
+def mlp_train(features, labels, epochs=20, batch=4096, lr=2e-3, seed=0):
+    """Trains the acceptance network on the GPU: (params, scale, losses)."""
+    F = np.ascontiguousarray(features, np.float32).reshape(-1, 8)
+    L = np.ascontiguousarray(labels, np.float32)
+    params = np.empty(MLP_PARAMS, np.float32)
+    scale = np.empty(MLP_SCALE, np.float32)
+    losses = np.empty(epochs, np.float32)
+    _check(library().bh_mlp_train(_ptr(F), _ptr(L), len(L), epochs, batch, lr, seed, _ptr(params), _ptr(scale),
+                                  _ptr(losses)))
+    return params, scale, losses
+
+
+def mlp_predict(params, scale, features):
+    """Predicted log10 error of raw feature rows (fused inference path) and
+    the in-training-range flags."""
+    p = np.ascontiguousarray(params, np.float32); sc = np.ascontiguousarray(scale, np.float32)
+    F = np.ascontiguousarray(features, np.float32).reshape(-1, 8)
+    out = np.empty(len(F), np.float32); inr = np.empty(len(F), np.int32)
+    _check(library().bh_mlp_predict(_ptr(p), _ptr(sc), _ptr(F), len(F), _ptr(out), _ptr(inr)))
+    return out, inr.astype(bool)
 
 
 # ------------------------------------------------- reference-named functions

@@ -124,6 +124,10 @@ void layout(bh_context* ctx, Carver& c)
     ctx->fA = c.take<float4>(2 * n);
     ctx->fB = c.take<float4>(2 * n);
     ctx->fmeta = c.take<uint32_t>(2 * n);
+    ctx->fspread = c.take<float>(2 * n);
+    ctx->leaf_q = c.take<double>(n);
+    ctx->node_q = c.take<double>(n);
+    ctx->lstats = c.take<unsigned long long>(4);
     ctx->direct = c.take<double>(4 * 64);
     ctx->direct_present = c.take<int32_t>(64);
     ctx->err = c.take<unsigned>(1);
@@ -329,6 +333,7 @@ int bh_context_destroy(bh_context* ctx)
     if (ctx->h_err) cudaFreeHost(ctx->h_err);
     if (ctx->h_small) cudaFreeHost(ctx->h_small);
     for (cudaEvent_t e : ctx->ev_pool) cudaEventDestroy(e);
+    if (ctx->mlp_dev) cudaFree(ctx->mlp_dev);
     delete ctx;
     return BH_OK;
 }

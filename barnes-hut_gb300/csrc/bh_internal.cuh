@@ -22,6 +22,7 @@
     } while (0)
 
 namespace bh {
+struct MlpDev;
 
 constexpr int kMaxDepth = 21;          // depth of a leaf (one body key)
 constexpr int kSortPasses = 8;         // 8-bit digits over the 63-bit key
@@ -145,6 +146,12 @@ struct bh_context {
     float4* fA = nullptr;   // {hi.x, hi.y, hi.z, G m}
     float4* fB = nullptr;   // {lo.x, lo.y, lo.z, bits of ref (child or leaf id)}
     uint32_t* fmeta = nullptr;  // nchild | depth << 8 | leaf << 16
+    float* fspread = nullptr;   // sqrt(Q / m) per slot (second moment about the centre of mass)
+    double* leaf_q = nullptr;   // second moments of leaves and branching nodes
+    double* node_q = nullptr;
+    bh::MlpDev* mlp_dev = nullptr;      // learned model (bh_learned_set_model)
+    double learn_theta_max = 0.0;
+    unsigned long long* lstats = nullptr;  // candidates, accepted, fallbacks
     double* direct = nullptr;   // 4 doubles per direct body: x, y, z, G m (by id)
     int32_t* direct_present = nullptr;  // 1 when body id k was found
 
@@ -185,8 +192,11 @@ int sort_passes_raw(int64_t n, const uint64_t* keys_in, uint64_t* keys_out, uint
 int launch_build(bh_context* ctx, const double* mass);
 // FP32 modes: far-field masses (direct bodies zeroed) into ctx->m2.
 int launch_far_mass(bh_context* ctx);
+// Second moments of every node of the last build (same masses), into fspread.
+int launch_second_moments(bh_context* ctx, const double* mass);
 int launch_traverse(bh_context* ctx, double theta, double G, double soft2, int mode, double kick_h);
 int launch_traverse_masked(bh_context* ctx, double theta, double G, double soft2, double kick_h, bool fp64);
+int launch_traverse_learned(bh_context* ctx, double theta, double G, double soft2, double kick_h);
 
 // Device-wide exclusive scan of n int32 values (in may equal out); the
 // total is written to *total (device pointer).  n is read from n_dev when

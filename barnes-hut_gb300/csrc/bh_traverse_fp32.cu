@@ -1,32 +1,45 @@
-// FP32 far-field traversal with FP64 direct terms for the dominant bodies
-// (BH_MODE_FP32_FAR; the learned acceptance reuses it).  No reference
-// counterpart: the reference evaluates every interaction in FP64
-// (src/traversal.cpp:72-82).
+// The masked warp walk behind BH_MODE_FP64_LIST, BH_MODE_FP32_FAR and
+// BH_MODE_LEARNED, and the collection of training pairs for the learned
+// criterion.  No reference counterpart: the reference walks one body at a
+// time (src/traversal.cpp:53-102).
 //
-// Precision form:
-//  * The bodies with id < num_direct (the Sun and the 8 planets in the
-//    solar-system inputs) are taken out of the far-field tree (their masses
-//    are zeroed before the build) and summed directly in FP64 for every body.
-//  * Far-field node-body interactions run in FP32 on displacements relative
-//    to the warp's group centre g.  A node's centre of mass is stored as a
-//    pair of floats hi + lo (hi = fl32(c), lo = fl32(c - hi), formed in FP64
-//    once per node), and g is a float, so (hi - g) + lo is the FP64
-//    displacement c - g rounded to FP32 (within an ulp) without one FP64
-//    instruction per visit: on this GPU the FP64 pipe is 1/60 of the FP32
-//    one and three FP64 subtractions per visit would cost more than the
-//    whole FP32 interaction.  Body positions relative to g are formed in FP64
-//    once per body and rounded.
-//  * FP32 partial sums over each staged list of nodes (at most kList) are
-//    added into FP64 accumulators.
+// A warp owns 32 Morton-consecutive bodies.  Stack entries are
+// (slot, mask of the lanes that still need the subtree).  Up to 32 entries
+// are classified per iteration, one per lane, against the group's bounding
+// box (group-relative FP32 coordinates):
+//   accept-all : side^2 < theta^2 dmin^2 (every body is at least dmin away),
+//   open-all   : side^2 > theta^2 dmax^2 (no body is farther than dmax),
+//   mixed      : each lane of the mask applies its own body's test.
+// (both group tests carry a 1e-4 relative margin, so every body's own test
+// agrees with them).  Lanes that accept a node take it into a staged
+// interaction list with their mask bit; the others carry it down to the
+// children.  Each body therefore interacts with exactly the nodes its own
+// walk at theta accepts.
 //
-// Warp-cooperative walk: a warp owns 32 Morton-consecutive bodies.  Up to 32
-// nodes are popped at a time, one per lane; a node is accepted for the whole
-// group when side(depth)^2 < theta^2 d^2 with d the distance from its centre
-// of mass to the group's bounding box (every body is at least that far, so
-// each body's own test would accept it too), leaves are always accepted,
-// other nodes are opened.  Accepted nodes are staged in shared memory
-// (group-relative centre + G m) and evaluated by all 32 lanes.
+// BH_MODE_FP64_LIST: per-lane tests in FP64 with the reference's rounding,
+//   interactions in FP64 (rsqrt + FMA) from the FP64 node records, on the
+//   reference's tree.
+// BH_MODE_FP32_FAR: precision form.  The bodies with id < num_direct (Sun and
+//   planets) are taken out of the tree (masses zeroed before the build) and
+//   summed directly in FP64.  Far-field interactions run in FP32 on
+//   displacements relative to the warp's group centre g: node centres are
+//   stored as float pairs hi + lo (formed in FP64 once per node), g is a
+//   float, so (hi - g) + lo is the FP64 displacement rounded to FP32 without
+//   one FP64 instruction per visit (the FP64 pipe is 1/60 of the FP32 one
+//   here, and three FP64 subtractions per visit would cost more than the
+//   interaction).  FP32 partials of each staged list are added into FP64
+//   accumulators.
+// BH_MODE_LEARNED: BH_MODE_FP32_FAR plus the learned criterion: a node the
+//   theta test would not accept for the whole group, but which is within
+//   theta_max (side < theta_max dmin), is a candidate; the warp evaluates
+//   the network on its up-to-32 candidates at once (mma.sync, BF16) and
+//   accepts a candidate for all its lanes when the predicted log10 error is
+//   below the threshold.  Candidates whose features fall outside the
+//   training range use the theta test (the fallback), and are counted.
+// Collection (bh_learned_collect): the FP32 walk with the theta test only,
+//   recording every candidate's group, slot, lane mask and raw features.
 #include "bh_internal.cuh"
+#include "bh_mlp.cuh"
 
 namespace bh {
 namespace {
@@ -35,6 +48,9 @@ constexpr int kWarps = 4;
 constexpr int kThreads = 32 * kWarps;
 constexpr int kStack = 1024;  // (slot, lane mask) entries per warp
 constexpr int kList = 128;    // staged interactions per warp
+constexpr float kMargin = 1e-4f;
+
+enum { kLearnNone = 0, kLearnInfer = 1, kLearnCollect = 2 };
 
 __global__ void far_mass_kernel(int64_t n, const double* __restrict__ m, const uint64_t* __restrict__ id, int nd,
                                 double* __restrict__ m_far)
@@ -80,6 +96,8 @@ __global__ void direct_extract_kernel(int64_t n, const double* __restrict__ px, 
     }
 }
 
+}  // namespace
+
 struct FParams {
     int64_t n;
     const double* px;
@@ -91,6 +109,7 @@ struct FParams {
     const float4* B;
     const uint32_t* meta;
     const TreeRec* rec;
+    const float* spread;
     const double* bbox;
     double theta2;
     double soft2;
@@ -109,39 +128,39 @@ struct FParams {
     int32_t* body_count;
     unsigned* err;
     int64_t max_pops;
+    // learned criterion
+    const MlpDev* mlp;
+    float theta_max2;
+    unsigned long long* lstats;  // candidates, accepted by the network, fallbacks
+    // collection
+    int32_t* c_group;
+    int32_t* c_slot;
+    uint32_t* c_mask;
+    float* c_feat;
+    float* c_ascale;
+    unsigned long long* c_count;
+    int64_t c_cap;
 };
 
-// Relative safety margin of the FP32 group tests: a node is accept-all /
-// open-all only when the FP32 test clears the threshold by this factor, so
-// every body's own FP64 test agrees; otherwise it is resolved lane by lane.
-constexpr float kMargin = 1e-4f;
+namespace {
 
-// The masked warp walk.  Stack entries are (slot, lane mask of the bodies that
-// still need the subtree).  Up to 32 entries are classified per iteration,
-// one per lane, against the group's bounding box:
-//   accept-all : side^2 < theta^2 dmin^2 (every body is at least dmin away),
-//   open-all   : side^2 > theta^2 dmax^2 (no body is farther than dmax),
-//   mixed      : each lane of the mask applies its own body's test.
-// Lanes that accept a node take it into the staged interaction list with
-// their mask bit; the others carry it down to the children.  Every body thus
-// interacts with exactly the nodes its own per-body walk accepts
-// (src/traversal.cpp:63-99), in some order.
-//
-// kFP64 = true  (BH_MODE_FP64_LIST): per-lane tests in FP64 with the
-//   reference's rounding; interactions in FP64 from the FP64 node records.
-// kFP64 = false (BH_MODE_FP32_FAR): per-lane tests and interactions in FP32
-//   on group-relative displacements; FP32 partials summed into FP64 per
-//   staged list; FP64 direct terms from the direct bodies at the end.
-template <bool kFP64>
+template <int kLearn>
+struct WalkSmem {
+    int2 stack[kWarps][kStack];
+    float4 lst[kWarps][kList];
+    int lst_node[kWarps][kList];
+    int lst_leaf[kWarps][kList];
+    unsigned lst_mask[kWarps][kList];
+    float side2f[kMaxDepth + 1];
+    double side2d[kMaxDepth + 1];
+    float feat[kLearn ? kWarps : 1][32][9];
+};
+
+template <bool kFP64, int kLearn>
 __global__ void __launch_bounds__(kThreads) traverse_masked_kernel(FParams p)
 {
-    __shared__ int2 stack[kWarps][kStack];
-    __shared__ float4 lst[kWarps][kList];
-    __shared__ int lst_node[kWarps][kList];
-    __shared__ int lst_leaf[kWarps][kList];
-    __shared__ unsigned lst_mask[kWarps][kList];
-    __shared__ float side2f[kMaxDepth + 1];
-    __shared__ double side2d[kMaxDepth + 1];
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    WalkSmem<kLearn>& sm = *reinterpret_cast<WalkSmem<kLearn>*>(smem_raw);
     if (threadIdx.x <= kMaxDepth) {
         const double dx = __dsub_rn(p.bbox[3], p.bbox[0]);
         const double dy = __dsub_rn(p.bbox[4], p.bbox[1]);
@@ -150,13 +169,14 @@ __global__ void __launch_bounds__(kThreads) traverse_masked_kernel(FParams p)
         if (L < dy) L = dy;
         if (L < dz) L = dz;
         const double side = __ddiv_rn(L, (double)(1ull << threadIdx.x));
-        side2d[threadIdx.x] = __dmul_rn(side, side);
-        side2f[threadIdx.x] = (float)side2d[threadIdx.x];
+        sm.side2d[threadIdx.x] = __dmul_rn(side, side);
+        sm.side2f[threadIdx.x] = (float)sm.side2d[threadIdx.x];
     }
     __syncthreads();
 
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
-    const int64_t base = ((int64_t)blockIdx.x * kWarps + w) * 32;
+    const int64_t group = (int64_t)blockIdx.x * kWarps + w;
+    const int64_t base = group * 32;
     if (base >= p.n) return;
     const int64_t i = base + lane;
     const bool valid = i < p.n;
@@ -182,16 +202,45 @@ __global__ void __launch_bounds__(kThreads) traverse_masked_kernel(FParams p)
     const int my_leaf = valid ? p.body_leaf[i] : -2;
     const float theta2f = (float)p.theta2;
     const double theta2 = p.theta2, soft2 = p.soft2, G = p.G;
-    int2* stk = stack[w];
-    float4* L = lst[w];
-    int* LN = lst_node[w];
-    int* LL = lst_leaf[w];
-    unsigned* LM = lst_mask[w];
+    int2* stk = sm.stack[w];
+    float4* L = sm.lst[w];
+    int* LN = sm.lst_node[w];
+    int* LL = sm.lst_leaf[w];
+    unsigned* LM = sm.lst_mask[w];
     const unsigned me = 1u << lane;
     const unsigned lt = me - 1u;
 
     double adx = 0.0, ady = 0.0, adz = 0.0;
     unsigned cnt = 0;
+
+    // FP64 direct terms from the direct bodies first (FP32 modes): they set
+    // the group's acceleration scale for the learned criterion.
+    float ascale = 0.0f;
+    if (!kFP64) {
+        const uint64_t my_id = valid ? p.id[i] : ~0ull;
+        for (int kk = 0; kk < p.nd; ++kk) {
+            if (!p.present[kk] || my_id == (uint64_t)kk) continue;
+            const double dx = p.direct[4 * kk] - x, dy = p.direct[4 * kk + 1] - y, dz = p.direct[4 * kk + 2] - z;
+            const double r2 = fma(dx, dx, fma(dy, dy, fma(dz, dz, soft2)));
+            const double inv = rsqrt(r2);
+            const double sc = p.direct[4 * kk + 3] * (inv * inv * inv);
+            adx = fma(sc, dx, adx);
+            ady = fma(sc, dy, ady);
+            adz = fma(sc, dz, adz);
+            ++cnt;
+        }
+        if (kLearn) {
+            float a = valid ? (float)sqrt(adx * adx + ady * ady + adz * adz) : 3.0e38f;
+#pragma unroll
+            for (int off = 16; off > 0; off >>= 1) a = fminf(a, __shfl_xor_sync(0xffffffffu, a, off));
+            ascale = a < 3.0e38f ? a : 0.0f;
+        }
+    }
+    const float gextent = sqrtf((bmaxx - bminx) * (bmaxx - bminx) + (bmaxy - bminy) * (bmaxy - bminy) +
+                                (bmaxz - bminz) * (bmaxz - bminz));
+    const float bcx = 0.5f * (bminx + bmaxx), bcy = 0.5f * (bminy + bmaxy), bcz = 0.5f * (bminz + bmaxz);
+    unsigned long long ncand = 0, nacc = 0, nfall = 0;
+
     int nlist = 0;
     int sp = 1;
     if (lane == 0) stk[0] = make_int2(0, (int)full);
@@ -212,7 +261,8 @@ __global__ void __launch_bounds__(kThreads) traverse_masked_kernel(FParams p)
             int node = -1;
             unsigned M = 0, A = 0;
             int nc = 0, ref = 0, depth = 0;
-            bool leaf = false, mixed = false;
+            bool leaf = false, mixed = false, cand = false;
+            float dmin2 = 0.f, dmax2 = 0.f, s2 = 0.f;
             float4 e = make_float4(0.f, 0.f, 0.f, 0.f);
             if (lane < k) {
                 const int2 ent = stk[sp - k + lane];
@@ -227,7 +277,7 @@ __global__ void __launch_bounds__(kThreads) traverse_masked_kernel(FParams p)
                 leaf = (mt >> 16) & 1u;
                 depth = (mt >> 8) & 0xFF;
                 if ((mt >> 17) & 1u) {
-                    M = 0;  // skipped with its subtree (traversal.cpp:66)
+                    M = 0;  // massless: skipped with its subtree (traversal.cpp:66)
                 } else if (leaf) {
                     A = M;  // leaves are always accepted; the own leaf is handled at evaluation
                 } else {
@@ -237,39 +287,101 @@ __global__ void __launch_bounds__(kThreads) traverse_masked_kernel(FParams p)
                     const float fx = fmaxf(fabsf(cx - bminx), fabsf(cx - bmaxx));
                     const float fy = fmaxf(fabsf(cy - bminy), fabsf(cy - bmaxy));
                     const float fz = fmaxf(fabsf(cz - bminz), fabsf(cz - bmaxz));
-                    const float dmin2 = ex * ex + ey * ey + ez * ez;
-                    const float dmax2 = fx * fx + fy * fy + fz * fz;
-                    const float s2 = side2f[depth];
-                    if (s2 < theta2f * dmin2 * (1.0f - kMargin)) A = M;
-                    else if (s2 > theta2f * dmax2 * (1.0f + kMargin)) A = 0;
-                    else mixed = true;
+                    dmin2 = ex * ex + ey * ey + ez * ez;
+                    dmax2 = fx * fx + fy * fy + fz * fz;
+                    s2 = sm.side2f[depth];
                     nc = (int)(mt & 0xFF);
+                    if (s2 < theta2f * dmin2 * (1.0f - kMargin)) {
+                        A = M;
+                    } else {
+                        if (kLearn) cand = M != 0 && dmin2 > 0.0f && s2 < p.theta_max2 * dmin2;
+                        if (s2 > theta2f * dmax2 * (1.0f + kMargin)) A = 0;
+                        else mixed = true;
+                    }
                 }
             }
             __syncwarp();
             sp -= k;
+            if (kLearn && !kFP64) {
+                const unsigned cb = __ballot_sync(0xffffffffu, cand);
+                if (cb) {
+                    float f[kFeat];
+#pragma unroll
+                    for (int q = 0; q < kFeat; ++q) f[q] = 0.0f;
+                    if (cand) {
+                        const float dmin = sqrtf(dmin2), side = sqrtf(s2);
+                        const float spr = fmaxf(__ldg(p.spread + node), 1e-8f * side);
+                        const float dcx = e.x - bcx, dcy = e.y - bcy, dcz = e.z - bcz;
+                        f[0] = log10f(side / dmin);
+                        f[1] = log10f(spr / dmin);
+                        f[2] = log10f(fmaxf(gextent, 1e-30f) / dmin);
+                        f[3] = log10f(e.w / (dmin2 * ascale));
+                        f[4] = log10f(sqrtf(dmax2) / dmin);
+                        f[5] = (float)depth * (1.0f / kMaxDepth);
+                        f[6] = log10f(spr / side);
+                        f[7] = log10f(fmaxf(sqrtf(dcx * dcx + dcy * dcy + dcz * dcz), 1e-30f) / dmin);
+                    }
+                    if (kLearn == kLearnCollect) {
+                        const int leader = __ffs(cb) - 1;
+                        unsigned long long basec = 0;
+                        if (lane == leader) basec = atomicAdd(p.c_count, (unsigned long long)__popc(cb));
+                        basec = __shfl_sync(0xffffffffu, basec, leader);
+                        const unsigned long long slot = basec + __popc(cb & lt);
+                        if (cand && (int64_t)slot < p.c_cap) {
+                            p.c_group[slot] = (int32_t)group;
+                            p.c_slot[slot] = node;
+                            p.c_mask[slot] = M;
+                            p.c_ascale[slot] = ascale;
+#pragma unroll
+                            for (int q = 0; q < kFeat; ++q) p.c_feat[slot * kFeat + q] = f[q];
+                        }
+                    } else {
+                        const MlpDev* md = p.mlp;
+                        float (*F)[9] = sm.feat[w];
+                        bool inr = cand;
+#pragma unroll
+                        for (int q = 0; q < kFeat; ++q) {
+                            const float zq = (f[q] - md->sc.mean[q]) * md->sc.inv_std[q];
+                            inr = inr && zq >= md->sc.lo[q] && zq <= md->sc.hi[q];
+                            F[lane][q] = cand ? fminf(fmaxf(zq, -64.0f), 64.0f) : 0.0f;
+                        }
+                        __syncwarp();
+                        const float yhat = mlp_predict_warp(md, F, lane);
+                        __syncwarp();
+                        if (cand) {
+                            ++ncand;
+                            if (!inr) {
+                                ++nfall;
+                            } else if (yhat * md->sc.lstd + md->sc.lmean < md->log_thresh) {
+                                A = M;
+                                mixed = false;
+                                ++nacc;
+                            }
+                        }
+                    }
+                }
+            }
             // Mixed nodes: every lane of the mask applies its own test.
             unsigned mb = __ballot_sync(0xffffffffu, mixed);
             while (mb) {
                 const int j = __ffs(mb) - 1;
                 mb &= mb - 1;
                 const unsigned Mj = __shfl_sync(0xffffffffu, M, j);
+                const int dj = __shfl_sync(0xffffffffu, depth, j);
                 bool acc = false;
                 if (kFP64) {
                     const int nj = __shfl_sync(0xffffffffu, node, j);
-                    const int dj = __shfl_sync(0xffffffffu, depth, j);
                     const TreeRec r = p.rec[nj];
                     const double dx = __dsub_rn(r.cx, x), dy = __dsub_rn(r.cy, y), dz = __dsub_rn(r.cz, z);
                     const double r2 = __dadd_rn(
                         __dadd_rn(__dadd_rn(__dmul_rn(dx, dx), __dmul_rn(dy, dy)), __dmul_rn(dz, dz)), soft2);
-                    acc = side2d[dj] < __dmul_rn(theta2, r2);
+                    acc = sm.side2d[dj] < __dmul_rn(theta2, r2);
                 } else {
                     const float cx = __shfl_sync(0xffffffffu, e.x, j);
                     const float cy = __shfl_sync(0xffffffffu, e.y, j);
                     const float cz = __shfl_sync(0xffffffffu, e.z, j);
-                    const int dj = __shfl_sync(0xffffffffu, depth, j);
                     const float dx = cx - rx, dy = cy - ry, dz = cz - rz;
-                    acc = side2f[dj] < theta2f * (dx * dx + dy * dy + dz * dz);
+                    acc = sm.side2f[dj] < theta2f * (dx * dx + dy * dy + dz * dz);
                 }
                 const unsigned Aj = __ballot_sync(0xffffffffu, acc) & Mj;
                 if (lane == j) A = Aj;
@@ -301,6 +413,11 @@ __global__ void __launch_bounds__(kThreads) traverse_masked_kernel(FParams p)
             __syncwarp();
         }
         if (nlist > kList - 32 || (sp == 0 && nlist > 0)) {
+            if (kLearn == kLearnCollect) {
+                nlist = 0;  // collection evaluates nothing
+                __syncwarp();
+                continue;
+            }
             if (kFP64) {
                 for (int j = 0; j < nlist; ++j) {
                     const unsigned mj = LM[j];
@@ -312,7 +429,7 @@ __global__ void __launch_bounds__(kThreads) traverse_masked_kernel(FParams p)
                         // it (depths top..20) accepts (traversal.cpp:70,78).
                         const double r2e = __dadd_rn(__dadd_rn(__dadd_rn(__dmul_rn(dx, dx), __dmul_rn(dy, dy)),
                                                                __dmul_rn(dz, dz)), soft2);
-                        take = take && r.top <= kMaxDepth - 1 && side2d[kMaxDepth - 1] < __dmul_rn(theta2, r2e);
+                        take = take && r.top <= kMaxDepth - 1 && sm.side2d[kMaxDepth - 1] < __dmul_rn(theta2, r2e);
                     }
                     const double r2 = fma(dx, dx, fma(dy, dy, fma(dz, dz, soft2)));
                     const double inv = rsqrt(r2);
@@ -348,22 +465,8 @@ __global__ void __launch_bounds__(kThreads) traverse_masked_kernel(FParams p)
         }
     }
     if (overflow && lane == 0) atomicOr(p.err, kErrOverflow);
+    if (kLearn == kLearnCollect) return;
 
-    if (!kFP64) {
-        // FP64 direct terms from the direct bodies (not in the far-field tree).
-        const uint64_t my_id = valid ? p.id[i] : ~0ull;
-        for (int kk = 0; kk < p.nd; ++kk) {
-            if (!p.present[kk] || my_id == (uint64_t)kk) continue;
-            const double dx = p.direct[4 * kk] - x, dy = p.direct[4 * kk + 1] - y, dz = p.direct[4 * kk + 2] - z;
-            const double r2 = fma(dx, dx, fma(dy, dy, fma(dz, dz, soft2)));
-            const double inv = rsqrt(r2);
-            const double sc = p.direct[4 * kk + 3] * (inv * inv * inv);
-            adx = fma(sc, dx, adx);
-            ady = fma(sc, dy, ady);
-            adz = fma(sc, dz, adz);
-            ++cnt;
-        }
-    }
     if (valid) {
         p.ax[i] = adx;
         p.ay[i] = ady;
@@ -381,6 +484,19 @@ __global__ void __launch_bounds__(kThreads) traverse_masked_kernel(FParams p)
         for (int off = 16; off > 0; off >>= 1) c += __shfl_down_sync(0xffffffffu, c, off);
         if (lane == 0) atomicAdd(p.inter_count, c);
     }
+    if (kLearn == kLearnInfer && p.lstats) {
+#pragma unroll
+        for (int off = 16; off > 0; off >>= 1) {
+            ncand += __shfl_down_sync(0xffffffffu, ncand, off);
+            nacc += __shfl_down_sync(0xffffffffu, nacc, off);
+            nfall += __shfl_down_sync(0xffffffffu, nfall, off);
+        }
+        if (lane == 0) {
+            atomicAdd(p.lstats, ncand);
+            atomicAdd(p.lstats + 1, nacc);
+            atomicAdd(p.lstats + 2, nfall);
+        }
+    }
 }
 
 int grid_n(int64_t n)
@@ -388,6 +504,19 @@ int grid_n(int64_t n)
     int64_t b = (n + 255) / 256;
     if (b < 1) b = 1;
     return (int)(b > 8 * kNumSMs ? 8 * kNumSMs : b);
+}
+
+template <bool kFP64, int kLearn>
+int launch_walk(bh_context* ctx, const FParams& p)
+{
+    const size_t smem = sizeof(WalkSmem<kLearn>);
+    BH_CUDA_TRY(cudaFuncSetAttribute(traverse_masked_kernel<kFP64, kLearn>,
+                                     cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    const int64_t groups = (p.n + 31) / 32;
+    const int64_t blocks = (groups + kWarps - 1) / kWarps;
+    traverse_masked_kernel<kFP64, kLearn><<<(unsigned)blocks, kThreads, smem, ctx->stream>>>(p);
+    BH_LAUNCH_CHECK(ctx);
+    return BH_OK;
 }
 
 }  // namespace
@@ -401,10 +530,11 @@ int launch_far_mass(bh_context* ctx)
     return BH_OK;
 }
 
-int launch_traverse_masked(bh_context* ctx, double theta, double G, double soft2, double kick_h, bool fp64)
+// Prepares the FP32 node records and the direct bodies and fills the walk's
+// parameters (kick_h and the learned/collection fields are the caller's).
+int prepare_walk(bh_context* ctx, double theta, double G, double soft2, bool fp64, FParams& p)
 {
     const int64_t n = ctx->n;
-    if (n == 0) return BH_OK;
     const int nd = fp64 ? 0 : (ctx->num_direct < 64 ? ctx->num_direct : 64);
     fp32_nodes_kernel<<<grid_n(2 * n), 256, 0, ctx->stream>>>(ctx->counts, ctx->rec, G, ctx->fA, ctx->fB, ctx->fmeta);
     BH_LAUNCH_CHECK(ctx);
@@ -414,13 +544,14 @@ int launch_traverse_masked(bh_context* ctx, double theta, double G, double soft2
                                                                   ctx->direct, ctx->direct_present);
         BH_LAUNCH_CHECK(ctx);
     }
-    FParams p;
+    p = FParams{};
     p.n = n;
     p.px = ctx->px; p.py = ctx->py; p.pz = ctx->pz;
     p.id = ctx->id;
     p.body_leaf = ctx->body_leaf;
     p.A = ctx->fA; p.B = ctx->fB; p.meta = ctx->fmeta;
     p.rec = ctx->rec;
+    p.spread = ctx->fspread;
     p.bbox = ctx->bbox;
     p.theta2 = theta * theta;
     p.soft2 = soft2;
@@ -428,7 +559,6 @@ int launch_traverse_masked(bh_context* ctx, double theta, double G, double soft2
     p.direct = ctx->direct;
     p.present = ctx->direct_present;
     p.nd = nd;
-    p.kick_h = kick_h;
     p.ax = ctx->ax; p.ay = ctx->ay; p.az = ctx->az;
     p.vx = ctx->vx; p.vy = ctx->vy; p.vz = ctx->vz;
     p.inter_count = ctx->inter_count;
@@ -436,14 +566,49 @@ int launch_traverse_masked(bh_context* ctx, double theta, double G, double soft2
     p.err = ctx->err;
     p.max_pops = 2 * n + 2;
     BH_CUDA_TRY(cudaMemsetAsync(ctx->inter_count, 0, sizeof(unsigned long long), ctx->stream));
-    const int64_t groups = (n + 31) / 32;
-    const int64_t blocks = (groups + kWarps - 1) / kWarps;
-    if (fp64)
-        traverse_masked_kernel<true><<<(unsigned)blocks, kThreads, 0, ctx->stream>>>(p);
-    else
-        traverse_masked_kernel<false><<<(unsigned)blocks, kThreads, 0, ctx->stream>>>(p);
-    BH_LAUNCH_CHECK(ctx);
     return BH_OK;
+}
+
+int launch_traverse_masked(bh_context* ctx, double theta, double G, double soft2, double kick_h, bool fp64)
+{
+    if (ctx->n == 0) return BH_OK;
+    FParams p;
+    int rc = prepare_walk(ctx, theta, G, soft2, fp64, p);
+    if (rc) return rc;
+    p.kick_h = kick_h;
+    return fp64 ? launch_walk<true, kLearnNone>(ctx, p) : launch_walk<false, kLearnNone>(ctx, p);
+}
+
+int launch_traverse_learned(bh_context* ctx, double theta, double G, double soft2, double kick_h)
+{
+    if (ctx->n == 0) return BH_OK;
+    if (!ctx->mlp_dev) return bh_fail(BH_ERR_STATE, "learned mode: no model set (bh_learned_set_model)");
+    int rc = launch_second_moments(ctx, ctx->tree_far ? ctx->m2 : ctx->m);
+    if (rc) return rc;
+    FParams p;
+    if ((rc = prepare_walk(ctx, theta, G, soft2, false, p))) return rc;
+    p.kick_h = kick_h;
+    p.mlp = ctx->mlp_dev;
+    p.theta_max2 = (float)(ctx->learn_theta_max * ctx->learn_theta_max);
+    p.lstats = ctx->lstats;
+    BH_CUDA_TRY(cudaMemsetAsync(ctx->lstats, 0, 3 * sizeof(unsigned long long), ctx->stream));
+    return launch_walk<false, kLearnInfer>(ctx, p);
+}
+
+int launch_collect(bh_context* ctx, double theta, double G, double theta_max, int32_t* c_group, int32_t* c_slot,
+                   uint32_t* c_mask, float* c_feat, float* c_ascale, unsigned long long* c_count, int64_t cap)
+{
+    if (ctx->n == 0) return BH_OK;
+    int rc = launch_second_moments(ctx, ctx->m2);
+    if (rc) return rc;
+    FParams p;
+    if ((rc = prepare_walk(ctx, theta, G, 0.0, false, p))) return rc;
+    p.kick_h = 0.0;
+    p.theta_max2 = (float)(theta_max * theta_max);
+    p.c_group = c_group; p.c_slot = c_slot; p.c_mask = c_mask; p.c_feat = c_feat; p.c_ascale = c_ascale;
+    p.c_count = c_count;
+    p.c_cap = cap;
+    return launch_walk<false, kLearnCollect>(ctx, p);
 }
 
 }  // namespace bh

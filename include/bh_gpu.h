@@ -167,6 +167,50 @@ int bh_direct_sum(bh_context *ctx, int64_t ns, const int64_t *targets, double G,
  * out = {E, K, U, Lx, Ly, Lz, Px, Py, Pz}. */
 int bh_invariants(bh_context *ctx, double G, double theta, double out[9]);
 
+/* ---- learned acceptance (no reference counterpart) ------------------- */
+/* The network 8 -> 64 -> 64 -> 1 (ReLU; BF16 weights, FP32 accumulation)
+ * predicts log10 of the relative force error of accepting a tree node
+ * unopened for a warp's group of bodies.  Parameters are BH_MLP_PARAMS
+ * floats: W1[64][8] b1[64] W2[64][64] b2[64] W3[64] b3.  A model's feature
+ * scaling is BH_MLP_SCALE floats: per feature mean, 1/std, lowest and
+ * highest standardised value seen in training (4 x 8), then the label's mean
+ * and std. */
+#define BH_MLP_PARAMS 4801
+#define BH_MLP_SCALE 34
+#define BH_LEARNED_FEATURES 8
+/* Loss (mean squared error) and its gradient over n standardised samples
+ * X[n][8], targets T[n], computed by the GPU training kernels (for checks). */
+int bh_mlp_gradient(const float *params, const float *X, const float *T, int64_t n, float *grad_out,
+                    float *loss_out);
+/* Trains a network on raw features[n][8] and log10-error labels[n] with
+ * Adam (epochs over shuffled mini-batches of `batch`), all on the GPU;
+ * returns the parameters, the feature scaling and the last loss of each
+ * epoch (loss_out: epochs floats, may be NULL). */
+int bh_mlp_train(const float *features, const float *labels, int64_t n, int epochs, int batch, float lr,
+                 uint64_t seed, float *params_out, float *scale_out, float *loss_out);
+
+/* Network outputs (predicted log10 error) for raw feature rows through the
+ * same fused mma.sync inference the traversal uses; in_range (may be NULL)
+ * flags rows inside the model's training range. */
+int bh_mlp_predict(const float *params, const float *scale, const float *features, int64_t n, float *out,
+                   int32_t *in_range);
+/* Training pairs from the context's bodies (tree built): the FP32 walk with
+ * the theta test records every (group, node) the test would not accept for
+ * the whole group but theta_max would, with its 8 features
+ * (features_out: max_pairs x 8) and its label (labels_out), log10 of the
+ * largest relative force error over the group of accepting the node unopened
+ * instead of walking its subtree at theta_label.  *n_out pairs are written. */
+int bh_learned_collect(bh_context *ctx, double theta, double theta_label, double theta_max, double G,
+                       int64_t max_pairs, float *features_out, float *labels_out, int64_t *n_out);
+/* Model for BH_MODE_LEARNED: a candidate node (side < theta_max d_min) is
+ * accepted for the whole group when the predicted error is below `budget`
+ * (relative, per node) and its features are inside the training range;
+ * otherwise the theta criterion decides. */
+int bh_learned_set_model(bh_context *ctx, const float *params, const float *scale, double budget, double theta_max);
+/* Counters of the last BH_MODE_LEARNED traversal: candidates, candidates
+ * accepted by the network, candidates that fell back to theta. */
+int bh_learned_stats(bh_context *ctx, int64_t out[3]);
+
 /* ---- stateless host-buffer entry points ------------------------------ */
 /* Each copies its inputs to the device, runs the kernel, copies back.  They
  * use a per-thread default context on device 0. */
