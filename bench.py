@@ -79,6 +79,11 @@ def parse():
     ap.add_argument("--e2e-steps", type=int, default=5)
     ap.add_argument("--cpu-seconds", type=float, default=15.0, help="budget of the CPU-baseline sample")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-north-star", action="store_true",
+                    help="skip the 4M-body comparison of the FP32+learned form against plain FP64")
+    ap.add_argument("--ns-bodies", type=int, default=4_000_000)
+    ap.add_argument("--ns-steps", type=int, default=3)
+    ap.add_argument("--theta-max", type=float, default=3.0, help="learned criterion: candidate range")
     return ap.parse_args()
 
 
@@ -213,6 +218,88 @@ def run_reference(args, rank):
     print(json.dumps(line), flush=True)
 
 
+def time_steps(ctx, ext, flush, mode, theta, steps, warmup, t=0.0):
+    """Device ms per step (CUDA events on the engine's stream, L2 flushed
+    before each step) and accepted interactions per body of the last step."""
+    import torch
+    for _ in range(warmup):
+        t = ctx.step(DT, theta, G, 1, mode, t=t)
+    ms = []
+    for _ in range(steps):
+        flush.fill_(1.0)
+        torch.cuda.synchronize()
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record(ext)
+        t = ctx.step(DT, theta, G, 1, mode, t=t)
+        e1.record(ext)
+        e1.synchronize()
+        ms.append(e0.elapsed_time(e1))
+    return sum(ms) / len(ms), ctx.interaction_count() / ctx.n
+
+
+def north_star(args, dev):
+    """The 4M-body combined-scale system (85 % inner belt, 10 % outer belt, 5 %
+    trojans): plain FP64 theta=1.05 (fp64_list: the reference's interaction
+    set in FP64) against FP32 far field and FP32 + learned criterion, each
+    with its median relative error against the FP64 direct sum on a 4,096-body
+    sample (evaluated on the same initial state)."""
+    import torch
+    bh = importlib.import_module("barnes-hut_gb300")
+    from importlib import import_module
+    learned = import_module("barnes-hut_gb300.learned")
+    n = args.ns_bodies
+    t0 = time.perf_counter()
+    params, scale, losses, npairs = learned.train(seeds=range(9001, 9005), n_bodies=min(n, 1_000_000), epochs=6,
+                                                  theta_max=args.theta_max, max_pairs=4_000_000)
+    train_s = time.perf_counter() - t0
+    pos, vel, mass, ids = bh.generate_system(SEED + 1, n, 0.10, 0.05)
+    out = {"workload": f"{n:,} bodies (Sun, 8 planets, 85% inner belt, 10% outer belt, 5% trojans), theta=1.05, dt=1h",
+           "training": {"pairs": npairs, "systems": 4, "system_bodies": min(n, 1_000_000), "epochs": 6,
+                        "final_loss": float(losses[-1]), "seconds": train_s, "label_theta": 0.5,
+                        "theta_max": args.theta_max}}
+    with bh.Context(n, dev) as ctx:
+        ext = torch.cuda.ExternalStream(ctx.stream(), device=dev)
+        flush = torch.empty(L2_FLUSH_BYTES // 4, dtype=torch.float32, device=f"cuda:{dev}")
+        ctx.set_bodies(pos, vel, mass, ids)
+        ctx.compute_bbox(); ctx.compute_keys(); ctx.sort_bodies(); ctx.build_tree()
+        rng = np.random.default_rng(0)
+        sample = np.sort(rng.choice(n, 4096, replace=False))
+        ref = ctx.direct_sum(sample, G)
+
+        def err(a):
+            e = np.linalg.norm(a[sample] - ref, axis=1) / np.linalg.norm(ref, axis=1)
+            return float(np.median(e)), float(np.quantile(e, 0.99))
+
+        rows = {}
+        cases = [("plain_fp64", bh.MODE_FP64_LIST, None), ("fp32_far", bh.MODE_FP32_FAR, None)]
+        cases += [(f"fp32_learned_budget_{b:g}", bh.MODE_LEARNED, b) for b in (1e-4, 1e-5, 1e-6)]
+        for name, mode, budget in cases:
+            if budget is not None:
+                ctx.learned_set_model(params, scale, budget=budget, theta_max=args.theta_max)
+            ctx.set_bodies(pos, vel, mass, ids)
+            ctx.compute_bbox(); ctx.compute_keys(); ctx.sort_bodies(); ctx.build_tree()
+            a = ctx.compute_accelerations(THETA, G, 0.0, mode)
+            med, p99 = err(a)
+            row = {"median_rel_err": med, "p99_rel_err": p99}
+            if budget is not None:
+                st = ctx.learned_stats()
+                row["fallback_rate"] = st["fallback"] / max(1, st["candidates"])
+                row["network_accept_rate"] = st["accepted"] / max(1, st["candidates"])
+            ctx.set_bodies(pos, vel, mass, ids)
+            ms, ipb = time_steps(ctx, ext, flush, mode, THETA, args.ns_steps, 2)
+            row.update({"ms_per_step": ms, "body_steps_per_s": n / (ms * 1e-3), "interactions_per_body": ipb})
+            rows[name] = row
+    base = rows["plain_fp64"]
+    out["forms"] = rows
+    eligible = [k for k, r in rows.items() if k.startswith("fp32_learned") and
+                r["median_rel_err"] <= base["median_rel_err"]]
+    best = max(eligible, key=lambda k: rows[k]["body_steps_per_s"]) if eligible else None
+    out["best_learned_at_equal_or_lower_error"] = best
+    out["speedup_vs_plain_fp64"] = (rows[best]["body_steps_per_s"] / base["body_steps_per_s"]) if best else None
+    return out
+
+
 def run_ours(args, rank, ws, local):
     import torch
     bh = importlib.import_module("barnes-hut_gb300")
@@ -281,6 +368,10 @@ def run_ours(args, rank, ws, local):
     accuracy = {"median_rel_err": float(np.median(err)), "p99_rel_err": float(np.quantile(err, 0.99)),
                 "sample": int(len(sample)), "judge": "FP64 direct sum"}
 
+    ns = None
+    if rank == 0 and ws == 1 and not args.no_north_star:
+        ns = north_star(args, dev)
+
     cpu = None
     if rank == 0 and not args.no_cpu_baseline:
         cpu = cpu_baseline(pos, vel, mass, ids, args.cpu_seconds, theta)
@@ -314,6 +405,7 @@ def run_ours(args, rank, ws, local):
         "gpu_launches": launches,
         "clocks": clk.summary(),
         "cpu_baseline": cpu,
+        "north_star": ns,
     }
     print(json.dumps(line), flush=True)
 
