@@ -236,8 +236,10 @@ int step_once(bh_context* ctx, double dt, double theta, double G, int mode)
     phase_end(ctx, 3, e);
     e = phase_begin(ctx);
     if (!rc && far) rc = bh::launch_far_mass(ctx);
-    if (!rc) rc = bh::launch_build(ctx, far ? ctx->m2 : ctx->m);
+    const bool moments = mode == BH_MODE_LEARNED;
+    if (!rc) rc = bh::launch_build(ctx, far ? ctx->m2 : ctx->m, moments);
     ctx->tree_far = far;
+    ctx->tree_moments = moments;
     phase_end(ctx, 4, e);
     e = phase_begin(ctx);
     if (!rc) rc = bh::launch_traverse(ctx, theta, G, 0.0, mode, 0.5 * dt);
@@ -488,7 +490,7 @@ int bh_build_tree(bh_context* ctx)
     if (rc) return rc;
     if (!ctx->sorted_valid && ctx->n > 0) return bh_fail(BH_ERR_STATE, "bh_build_tree: call bh_sort_bodies first");
     if ((rc = bh::launch_build(ctx, ctx->m))) return rc;
-    ctx->tree_far = false;
+    ctx->tree_far = ctx->tree_moments = false;
     rc = finish(ctx, "bh_build_tree");
     ctx->tree_valid = rc == BH_OK;
     return rc;
@@ -558,7 +560,7 @@ int bh_export_tree(bh_context* ctx, uint64_t* prefix, uint8_t* depth, double* ma
     if (!prefix || !depth || !mass || !com) return bh_fail(BH_ERR_INVALID_ARGUMENT, "bh_export_tree: null array");
     if (ctx->tree_far) {  // the export is the reference's tree: real masses
         if ((rc = bh::launch_build(ctx, ctx->m))) return rc;
-        ctx->tree_far = false;
+        ctx->tree_far = ctx->tree_moments = false;
     }
     HostTree h;
     if ((rc = fetch_tree(ctx, h))) return rc;
@@ -595,10 +597,12 @@ int bh_compute_accelerations(bh_context* ctx, double theta, double G, double sof
     // bodies zeroed); the FP64 modes the reference's tree.  Rebuild the
     // node values when the tree in place is the other kind.
     const bool far = mode >= BH_MODE_FP32_FAR;
-    if (far != ctx->tree_far) {
+    const bool moments = mode == BH_MODE_LEARNED;
+    if (far != ctx->tree_far || (moments && !ctx->tree_moments)) {
         if (far && (rc = bh::launch_far_mass(ctx))) return rc;
-        if ((rc = bh::launch_build(ctx, far ? ctx->m2 : ctx->m))) return rc;
+        if ((rc = bh::launch_build(ctx, far ? ctx->m2 : ctx->m, moments))) return rc;
         ctx->tree_far = far;
+        ctx->tree_moments = moments;
     }
     if ((rc = bh::launch_traverse(ctx, theta, G, soft2, mode, 0.0))) return rc;
     if (acc_out && (rc = download_vec3(ctx, acc_out, ctx->px2, ctx->ax, ctx->ay, ctx->az, ctx->n))) return rc;

@@ -136,6 +136,7 @@ struct bh_context {
     bool sorted_valid = false; // bodies are in sorted-key order
 
     bool tree_far = false;      // the tree holds far-field masses (FP32 modes)
+    bool tree_moments = false;  // the tree's second moments are current
     int num_direct = BH_NUM_MASSIVE;  // bodies with id < num_direct: FP64 direct terms in FP32 modes
 
     // Traversal.
@@ -188,12 +189,12 @@ int sort_passes_raw(int64_t n, const uint64_t* keys_in, uint64_t* keys_out, uint
                     uint32_t* val_alt, uint32_t* hist, uint32_t* lookback, uint32_t* tile_ctr, unsigned* err,
                     cudaStream_t stream);
 // Builds the octree over the sorted bodies with the given masses (ctx->m
-// for the reference's tree; the far-field masses for the FP32 modes).
-int launch_build(bh_context* ctx, const double* mass);
+// for the reference's tree; the far-field masses for the FP32 modes);
+// `moments` also computes the second moments (spread per slot).
+int launch_build(bh_context* ctx, const double* mass, bool moments = false);
 // FP32 modes: far-field masses (direct bodies zeroed) into ctx->m2.
 int launch_far_mass(bh_context* ctx);
-// Second moments of every node of the last build (same masses), into fspread.
-int launch_second_moments(bh_context* ctx, const double* mass);
+
 int launch_traverse(bh_context* ctx, double theta, double G, double soft2, int mode, double kick_h);
 int launch_traverse_masked(bh_context* ctx, double theta, double G, double soft2, double kick_h, bool fp64);
 int launch_traverse_learned(bh_context* ctx, double theta, double G, double soft2, double kick_h);

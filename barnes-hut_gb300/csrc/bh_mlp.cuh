@@ -83,18 +83,19 @@ __device__ inline void mma_bf16_16816(float& c0, float& c1, float& c2, float& c3
         : "r"(a0), "r"(a1), "r"(a2), "r"(a3), "r"(b0), "r"(b1));
 }
 
-// Warp-wide inference on 32 standardised feature rows F[lane][0..7] (shared
-// memory, row stride 9): returns each lane's network output (standardised
-// log10 error).  All 32 lanes must call it.  Two 16-row tiles; layer 1 is
+// Warp-wide inference on standardised feature rows F[r][0..7] (shared
+// memory, row stride 9), r < rows: lane r receives row r's network output
+// (standardised log10 error).  All 32 lanes must call it with the same rows.  Two 16-row tiles; layer 1 is
 // 8 mma (K = 8 padded to 16), layer 2 is 32 mma; the layer-1 accumulator
 // fragments are reused in registers as layer-2 A fragments; layer 3 is a
 // per-thread dot product reduced over the four lanes of a row group.
-__device__ inline float mlp_predict_warp(const MlpDev* __restrict__ M, const float (*F)[9], int lane)
+__device__ inline float mlp_predict_warp(const MlpDev* __restrict__ M, const float (*F)[9], int lane, int rows = 32)
 {
     const int g = lane >> 2, t = lane & 3;
-    float out[2][2];
-#pragma unroll
-    for (int mt = 0; mt < 2; ++mt) {
+    float out[2][2] = {{0.f, 0.f}, {0.f, 0.f}};
+    const int ntiles = rows > 16 ? 2 : 1;  // warp-uniform: skip the second tile when unused
+#pragma unroll 1
+    for (int mt = 0; mt < ntiles; ++mt) {
         const int r0 = 16 * mt + g, r1 = r0 + 8;
         const uint32_t a0 = pack_bf16(F[r0][2 * t], F[r0][2 * t + 1]);
         const uint32_t a1 = pack_bf16(F[r1][2 * t], F[r1][2 * t + 1]);
@@ -109,7 +110,7 @@ __device__ inline float mlp_predict_warp(const MlpDev* __restrict__ M, const flo
             A2[j >> 1][(j & 1) * 2 + 1] = hi;
         }
         float pg = 0.f, pg8 = 0.f;
-#pragma unroll
+#pragma unroll 2
         for (int j = 0; j < 8; ++j) {
             float c0 = M->b2[8 * j + 2 * t], c1 = M->b2[8 * j + 2 * t + 1], c2 = c0, c3 = c1;
 #pragma unroll
@@ -127,8 +128,8 @@ __device__ inline float mlp_predict_warp(const MlpDev* __restrict__ M, const flo
         pg += __shfl_xor_sync(0xffffffffu, pg, 2);
         pg8 += __shfl_xor_sync(0xffffffffu, pg8, 1);
         pg8 += __shfl_xor_sync(0xffffffffu, pg8, 2);
-        out[mt][0] = pg + M->b3;
-        out[mt][1] = pg8 + M->b3;
+        if (mt == 0) { out[0][0] = pg + M->b3; out[0][1] = pg8 + M->b3; }
+        else { out[1][0] = pg + M->b3; out[1][1] = pg8 + M->b3; }
     }
     const int src = 4 * (lane & 7);
     const float v00 = __shfl_sync(0xffffffffu, out[0][0], src);

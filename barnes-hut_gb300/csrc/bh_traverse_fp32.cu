@@ -3,10 +3,11 @@
 // criterion.  No reference counterpart: the reference walks one body at a
 // time (src/traversal.cpp:53-102).
 //
-// A warp owns 32 Morton-consecutive bodies.  Stack entries are
-// (slot, mask of the lanes that still need the subtree).  Up to 32 entries
-// are classified per iteration, one per lane, against the group's bounding
-// box (group-relative FP32 coordinates):
+// A warp owns 32 Morton-consecutive bodies.  Stack entries are sibling
+// ranges (first child slot, number of children, mask of the lanes that still
+// need them): an opened node pushes one entry.  Each iteration pops whole
+// ranges from the top, up to 32 nodes, and classifies them one per lane
+// against the group's bounding box (group-relative FP32 coordinates):
 //   accept-all : side^2 < theta^2 dmin^2 (every body is at least dmin away),
 //   open-all   : side^2 > theta^2 dmax^2 (no body is farther than dmax),
 //   mixed      : each lane of the mask applies its own body's test.
@@ -46,8 +47,9 @@ namespace {
 
 constexpr int kWarps = 4;
 constexpr int kThreads = 32 * kWarps;
-constexpr int kStack = 1024;  // (slot, lane mask) entries per warp
-constexpr int kList = 128;    // staged interactions per warp
+constexpr int kStack = 512;   // sibling-range entries per warp
+constexpr int kList = 96;     // staged interactions per warp
+constexpr int kSlotBits = 28; // slot index bits of a stack entry (count - 1 in the top 3)
 constexpr float kMargin = 1e-4f;
 
 enum { kLearnNone = 0, kLearnInfer = 1, kLearnCollect = 2 };
@@ -146,7 +148,7 @@ namespace {
 
 template <int kLearn>
 struct WalkSmem {
-    int2 stack[kWarps][kStack];
+    int2 stack[kWarps][kStack];  // sibling ranges: {first | (count - 1) << 28, lane mask}
     float4 lst[kWarps][kList];
     int lst_node[kWarps][kList];
     int lst_leaf[kWarps][kList];
@@ -243,21 +245,44 @@ __global__ void __launch_bounds__(kThreads) traverse_masked_kernel(FParams p)
 
     int nlist = 0;
     int sp = 1;
-    if (lane == 0) stk[0] = make_int2(0, (int)full);
+    if (lane == 0) stk[0] = make_int2(0, (int)full);  // the root: a range of one slot
     __syncwarp();
     bool overflow = false;
     int64_t pops = 0;
 
     while (sp > 0 || nlist > 0) {
         if (sp > 0) {
-            int k = (kStack - sp) / 7;  // up to 8 children per popped entry must fit
-            k = k < 32 ? k : 32;
-            k = k < sp ? k : sp;
-            pops += k;
-            if (k == 0 || pops > p.max_pops) {
+            // Pop whole ranges from the top while they fit in 32 lanes.
+            const int avail = sp < 32 ? sp : 32;
+            int rfirst = 0, rcnt = 0;
+            unsigned rmask = 0;
+            if (lane < avail) {
+                const int2 ent = stk[sp - 1 - lane];
+                rfirst = ent.x & ((1 << kSlotBits) - 1);
+                rcnt = (int)((unsigned)ent.x >> kSlotBits) + 1;
+                rmask = (unsigned)ent.y;
+            }
+            int incl = rcnt;
+#pragma unroll
+            for (int off = 1; off < 32; off <<= 1) {
+                const int t = __shfl_up_sync(0xffffffffu, incl, off);
+                if (lane >= off) incl += t;
+            }
+            const bool take = lane < avail && incl <= 32;
+            const int R = __popc(__ballot_sync(0xffffffffu, take));
+            const int T = __shfl_sync(0xffffffffu, incl, R - 1);
+            const int rstart = incl - rcnt;
+            const unsigned starts = __reduce_or_sync(0xffffffffu, take ? (1u << rstart) : 0u);
+            const int rj = __popc(starts & ((2u << lane) - 1u)) - 1;
+            const int f_r = __shfl_sync(0xffffffffu, rfirst, rj);
+            const int s_r = __shfl_sync(0xffffffffu, rstart, rj);
+            const unsigned m_r = __shfl_sync(0xffffffffu, rmask, rj);
+            pops += T;
+            if (sp - R + T > kStack || pops > p.max_pops) {
                 overflow = true;
                 break;
             }
+            const int k = T;
             int node = -1;
             unsigned M = 0, A = 0;
             int nc = 0, ref = 0, depth = 0;
@@ -265,9 +290,8 @@ __global__ void __launch_bounds__(kThreads) traverse_masked_kernel(FParams p)
             float dmin2 = 0.f, dmax2 = 0.f, s2 = 0.f;
             float4 e = make_float4(0.f, 0.f, 0.f, 0.f);
             if (lane < k) {
-                const int2 ent = stk[sp - k + lane];
-                node = ent.x;
-                M = (unsigned)ent.y;
+                node = f_r + (lane - s_r);
+                M = m_r;
                 const float4 a = __ldg(p.A + node);
                 const float4 b = __ldg(p.B + node);
                 const uint32_t mt = __ldg(p.meta + node);
@@ -301,7 +325,7 @@ __global__ void __launch_bounds__(kThreads) traverse_masked_kernel(FParams p)
                 }
             }
             __syncwarp();
-            sp -= k;
+            sp -= R;
             if (kLearn && !kFP64) {
                 const unsigned cb = __ballot_sync(0xffffffffu, cand);
                 if (cb) {
@@ -336,17 +360,22 @@ __global__ void __launch_bounds__(kThreads) traverse_masked_kernel(FParams p)
                             for (int q = 0; q < kFeat; ++q) p.c_feat[slot * kFeat + q] = f[q];
                         }
                     } else {
+                        // Candidates are packed into rows 0..ncand-1 so that
+                        // one 16-row tile suffices for up to 16 of them.
                         const MlpDev* md = p.mlp;
                         float (*F)[9] = sm.feat[w];
+                        const int row = __popc(cb & lt);
+                        const int nrows = __popc(cb);
                         bool inr = cand;
 #pragma unroll
                         for (int q = 0; q < kFeat; ++q) {
                             const float zq = (f[q] - md->sc.mean[q]) * md->sc.inv_std[q];
                             inr = inr && zq >= md->sc.lo[q] && zq <= md->sc.hi[q];
-                            F[lane][q] = cand ? fminf(fmaxf(zq, -64.0f), 64.0f) : 0.0f;
+                            if (cand) F[row][q] = fminf(fmaxf(zq, -64.0f), 64.0f);
                         }
                         __syncwarp();
-                        const float yhat = mlp_predict_warp(md, F, lane);
+                        const float yrow = mlp_predict_warp(md, F, lane, nrows);
+                        const float yhat = __shfl_sync(0xffffffffu, yrow, row);
                         __syncwarp();
                         if (cand) {
                             ++ncand;
@@ -397,19 +426,13 @@ __global__ void __launch_bounds__(kThreads) traverse_masked_kernel(FParams p)
                 LM[pos] = A;
             }
             nlist += __popc(am);
-            // Push the children with the lanes that still need them.
+            // Push one sibling range per opened node, with the lanes that
+            // still need it.
             const unsigned rest = M & ~A;
-            if (leaf || rest == 0) nc = 0;
-            int incl = nc;
-#pragma unroll
-            for (int off = 1; off < 32; off <<= 1) {
-                const int t = __shfl_up_sync(0xffffffffu, incl, off);
-                if (lane >= off) incl += t;
-            }
-            const int total = __shfl_sync(0xffffffffu, incl, 31);
-            const int at = sp + incl - nc;
-            for (int c = 0; c < nc; ++c) stk[at + c] = make_int2(ref + c, (int)rest);
-            sp += total;
+            const bool push = !leaf && nc > 0 && rest != 0;
+            const unsigned pm = __ballot_sync(0xffffffffu, push);
+            if (push) stk[sp + __popc(pm & lt)] = make_int2(ref | ((nc - 1) << kSlotBits), (int)rest);
+            sp += __popc(pm);
             __syncwarp();
         }
         if (nlist > kList - 32 || (sp == 0 && nlist > 0)) {
@@ -572,6 +595,8 @@ int prepare_walk(bh_context* ctx, double theta, double G, double soft2, bool fp6
 int launch_traverse_masked(bh_context* ctx, double theta, double G, double soft2, double kick_h, bool fp64)
 {
     if (ctx->n == 0) return BH_OK;
+    if (2 * ctx->n >= (int64_t(1) << kSlotBits))
+        return bh_fail(BH_ERR_CAPACITY, "masked walk: more than 2^27 bodies");
     FParams p;
     int rc = prepare_walk(ctx, theta, G, soft2, fp64, p);
     if (rc) return rc;
@@ -582,11 +607,13 @@ int launch_traverse_masked(bh_context* ctx, double theta, double G, double soft2
 int launch_traverse_learned(bh_context* ctx, double theta, double G, double soft2, double kick_h)
 {
     if (ctx->n == 0) return BH_OK;
+    if (2 * ctx->n >= (int64_t(1) << kSlotBits))
+        return bh_fail(BH_ERR_CAPACITY, "masked walk: more than 2^27 bodies");
     if (!ctx->mlp_dev) return bh_fail(BH_ERR_STATE, "learned mode: no model set (bh_learned_set_model)");
-    int rc = launch_second_moments(ctx, ctx->tree_far ? ctx->m2 : ctx->m);
-    if (rc) return rc;
+    if (!ctx->tree_moments) return bh_fail(BH_ERR_STATE, "learned mode: the tree was built without second moments");
     FParams p;
-    if ((rc = prepare_walk(ctx, theta, G, soft2, false, p))) return rc;
+    int rc = prepare_walk(ctx, theta, G, soft2, false, p);
+    if (rc) return rc;
     p.kick_h = kick_h;
     p.mlp = ctx->mlp_dev;
     p.theta_max2 = (float)(ctx->learn_theta_max * ctx->learn_theta_max);
@@ -599,10 +626,12 @@ int launch_collect(bh_context* ctx, double theta, double G, double theta_max, in
                    uint32_t* c_mask, float* c_feat, float* c_ascale, unsigned long long* c_count, int64_t cap)
 {
     if (ctx->n == 0) return BH_OK;
-    int rc = launch_second_moments(ctx, ctx->m2);
-    if (rc) return rc;
+    if (2 * ctx->n >= (int64_t(1) << kSlotBits))
+        return bh_fail(BH_ERR_CAPACITY, "masked walk: more than 2^27 bodies");
+    if (!ctx->tree_moments) return bh_fail(BH_ERR_STATE, "collection: the tree was built without second moments");
     FParams p;
-    if ((rc = prepare_walk(ctx, theta, G, 0.0, false, p))) return rc;
+    int rc = prepare_walk(ctx, theta, G, 0.0, false, p);
+    if (rc) return rc;
     p.kick_h = 0.0;
     p.theta_max2 = (float)(theta_max * theta_max);
     p.c_group = c_group; p.c_slot = c_slot; p.c_mask = c_mask; p.c_feat = c_feat; p.c_ascale = c_ascale;

@@ -109,16 +109,21 @@ __global__ void leaf_scatter_kernel(int64_t n, const uint64_t* __restrict__ key,
 }
 
 // Leaf sums in body order (linear_octree.cpp:28-38) and boundary depths.
+// kMoments: also the leaf's second moment about its centre of mass (the
+// learned criterion's spread feature), sum_b m_b |x_b - c|^2.
+template <bool kMoments>
 __global__ void leaf_sum_kernel(const int32_t* __restrict__ counts, const int32_t* __restrict__ leaf_first,
                                 const uint64_t* __restrict__ leaf_key, const double* __restrict__ px,
                                 const double* __restrict__ py, const double* __restrict__ pz,
                                 const double* __restrict__ m, double* __restrict__ lm, double* __restrict__ lwx,
-                                double* __restrict__ lwy, double* __restrict__ lwz, int8_t* __restrict__ cdep)
+                                double* __restrict__ lwy, double* __restrict__ lwz, int8_t* __restrict__ cdep,
+                                double* __restrict__ lq)
 {
     const int L = counts[0];
     for (int l = blockIdx.x * blockDim.x + threadIdx.x; l < L; l += gridDim.x * blockDim.x) {
         double sm = 0.0, sx = 0.0, sy = 0.0, sz = 0.0;
-        for (int b = leaf_first[l]; b < leaf_first[l + 1]; ++b) {
+        const int b0 = leaf_first[l], b1 = leaf_first[l + 1];
+        for (int b = b0; b < b1; ++b) {
             const double mb = m[b];
             sm = __dadd_rn(sm, mb);
             sx = __dadd_rn(sx, __dmul_rn(px[b], mb));
@@ -127,6 +132,17 @@ __global__ void leaf_sum_kernel(const int32_t* __restrict__ counts, const int32_
         }
         lm[l] = sm; lwx[l] = sx; lwy[l] = sy; lwz[l] = sz;
         cdep[l] = l == 0 ? (int8_t)-1 : (int8_t)common_depth(leaf_key[l - 1], leaf_key[l]);
+        if (kMoments) {
+            double q = 0.0;
+            if (b1 - b0 > 1 && sm > 0) {
+                const double cx = sx / sm, cy = sy / sm, cz = sz / sm;
+                for (int b = b0; b < b1; ++b) {
+                    const double dx = px[b] - cx, dy = py[b] - cy, dz = pz[b] - cz;
+                    q += m[b] * (dx * dx + dy * dy + dz * dz);
+                }
+            }
+            lq[l] = q;
+        }
     }
 }
 
@@ -285,14 +301,18 @@ __global__ void bucket_place_kernel(const int32_t* __restrict__ counts, const ui
 }
 
 // Monopole of the branching nodes at one depth: children summed in key
-// (= octant) order from 0.0 (linear_octree.cpp:69-87).
+// (= octant) order from 0.0 (linear_octree.cpp:69-87).  kMoments: also the
+// second moment by the parallel-axis rule, Q = sum_c (Q_c + m_c |c_c - c|^2)
+// (it reads only the sums above, so the monopole bits are unchanged).
+template <bool kMoments>
 __global__ void monopole_level_kernel(int depth, const int32_t* __restrict__ depth_off,
                                       const int32_t* __restrict__ depth_nodes, const int32_t* __restrict__ node_cs,
                                       const int32_t* __restrict__ node_nchild, const int32_t* __restrict__ slot_ref,
                                       const double* __restrict__ lm, const double* __restrict__ lwx,
                                       const double* __restrict__ lwy, const double* __restrict__ lwz,
                                       double* __restrict__ nm, double* __restrict__ nwx, double* __restrict__ nwy,
-                                      double* __restrict__ nwz)
+                                      double* __restrict__ nwz, const double* __restrict__ lq,
+                                      double* __restrict__ nq)
 {
     const int lo = depth_off[depth], hi = depth_off[depth + 1];
     for (int k = lo + blockIdx.x * blockDim.x + threadIdx.x; k < hi; k += gridDim.x * blockDim.x) {
@@ -310,6 +330,23 @@ __global__ void monopole_level_kernel(int depth, const int32_t* __restrict__ dep
             sz = __dadd_rn(sz, cz);
         }
         nm[b] = sm; nwx[b] = sx; nwy[b] = sy; nwz[b] = sz;
+        if (kMoments) {
+            double q = 0.0;
+            if (sm > 0) {
+                const double gx = sx / sm, gy = sy / sm, gz = sz / sm;
+                for (int s = s0; s < s1; ++s) {
+                    const int r = slot_ref[s];
+                    double cm, wx, wy, wz, cq;
+                    if (r >= 0) { cm = lm[r]; wx = lwx[r]; wy = lwy[r]; wz = lwz[r]; cq = lq[r]; }
+                    else { const int c = ~r; cm = nm[c]; wx = nwx[c]; wy = nwy[c]; wz = nwz[c]; cq = nq[c]; }
+                    if (cm > 0) {
+                        const double dx = wx / cm - gx, dy = wy / cm - gy, dz = wz / cm - gz;
+                        q += cq + cm * (dx * dx + dy * dy + dz * dz);
+                    }
+                }
+            }
+            nq[b] = q;
+        }
     }
 }
 
@@ -330,6 +367,7 @@ __device__ inline void finish_com(double m, double wx, double wy, double wz, Tre
     r.m = tot;
 }
 
+template <bool kMoments>
 __global__ void finalize_kernel(const int32_t* __restrict__ counts, const int32_t* __restrict__ slot_ref,
                                 const uint8_t* __restrict__ slot_top, const double* __restrict__ lm,
                                 const double* __restrict__ lwx, const double* __restrict__ lwy,
@@ -337,7 +375,8 @@ __global__ void finalize_kernel(const int32_t* __restrict__ counts, const int32_
                                 const double* __restrict__ nwx, const double* __restrict__ nwy,
                                 const double* __restrict__ nwz, const int32_t* __restrict__ node_cs,
                                 const int32_t* __restrict__ node_nchild, const uint8_t* __restrict__ node_depth,
-                                TreeRec* __restrict__ rec)
+                                TreeRec* __restrict__ rec, const double* __restrict__ lq,
+                                const double* __restrict__ nq, float* __restrict__ spread)
 {
     const int S = counts[2];
     for (int s = blockIdx.x * blockDim.x + threadIdx.x; s < S; s += gridDim.x * blockDim.x) {
@@ -361,79 +400,11 @@ __global__ void finalize_kernel(const int32_t* __restrict__ counts, const int32_
             o.depth = node_depth[b];
         }
         rec[s] = o;
-    }
-}
-
-// Second moments (the learned criterion's spread feature).  Q of a cell is
-// sum_b m_b |x_b - c|^2 about its centre of mass c; a leaf sums its bodies, a
-// parent combines its children with the parallel-axis rule
-// Q = sum_c (Q_c + m_c |c_c - c|^2).  Level-synchronous like the monopole pass.
-__global__ void leaf_moment_kernel(const int32_t* __restrict__ counts, const int32_t* __restrict__ leaf_first,
-                                   const double* __restrict__ px, const double* __restrict__ py,
-                                   const double* __restrict__ pz, const double* __restrict__ m,
-                                   const double* __restrict__ lm, const double* __restrict__ lwx,
-                                   const double* __restrict__ lwy, const double* __restrict__ lwz,
-                                   double* __restrict__ lq)
-{
-    const int L = counts[0];
-    for (int l = blockIdx.x * blockDim.x + threadIdx.x; l < L; l += gridDim.x * blockDim.x) {
-        double q = 0.0;
-        const double ml = lm[l];
-        if (leaf_first[l + 1] - leaf_first[l] > 1 && ml > 0) {
-            const double cx = lwx[l] / ml, cy = lwy[l] / ml, cz = lwz[l] / ml;
-            for (int b = leaf_first[l]; b < leaf_first[l + 1]; ++b) {
-                const double dx = px[b] - cx, dy = py[b] - cy, dz = pz[b] - cz;
-                q += m[b] * (dx * dx + dy * dy + dz * dz);
-            }
+        if (kMoments) {
+            const double m = r >= 0 ? lm[r] : nm[~r];
+            const double q = r >= 0 ? lq[r] : nq[~r];
+            spread[s] = m > 0 ? (float)sqrt(q / m) : 0.0f;
         }
-        lq[l] = q;
-    }
-}
-
-__global__ void moment_level_kernel(int depth, const int32_t* __restrict__ depth_off,
-                                    const int32_t* __restrict__ depth_nodes, const int32_t* __restrict__ node_cs,
-                                    const int32_t* __restrict__ node_nchild, const int32_t* __restrict__ slot_ref,
-                                    const double* __restrict__ lm, const double* __restrict__ lwx,
-                                    const double* __restrict__ lwy, const double* __restrict__ lwz,
-                                    const double* __restrict__ lq, const double* __restrict__ nm,
-                                    const double* __restrict__ nwx, const double* __restrict__ nwy,
-                                    const double* __restrict__ nwz, double* __restrict__ nq)
-{
-    const int lo = depth_off[depth], hi = depth_off[depth + 1];
-    for (int k = lo + blockIdx.x * blockDim.x + threadIdx.x; k < hi; k += gridDim.x * blockDim.x) {
-        const int b = depth_nodes[k];
-        const double mb = nm[b];
-        double q = 0.0;
-        if (mb > 0) {
-            const double cx = nwx[b] / mb, cy = nwy[b] / mb, cz = nwz[b] / mb;
-            const int s0 = node_cs[b] + 1, s1 = s0 + node_nchild[b];
-            for (int s = s0; s < s1; ++s) {
-                const int r = slot_ref[s];
-                double cm, wx, wy, wz, cq;
-                if (r >= 0) { cm = lm[r]; wx = lwx[r]; wy = lwy[r]; wz = lwz[r]; cq = lq[r]; }
-                else { const int c = ~r; cm = nm[c]; wx = nwx[c]; wy = nwy[c]; wz = nwz[c]; cq = nq[c]; }
-                if (cm > 0) {
-                    const double dx = wx / cm - cx, dy = wy / cm - cy, dz = wz / cm - cz;
-                    q += cq + cm * (dx * dx + dy * dy + dz * dz);
-                }
-            }
-        }
-        nq[b] = q;
-    }
-}
-
-// Spread radius sqrt(Q / m) of every slot, as float.
-__global__ void slot_spread_kernel(const int32_t* __restrict__ counts, const int32_t* __restrict__ slot_ref,
-                                   const double* __restrict__ lm, const double* __restrict__ lq,
-                                   const double* __restrict__ nm, const double* __restrict__ nq,
-                                   float* __restrict__ spread)
-{
-    const int S = counts[2];
-    for (int s = blockIdx.x * blockDim.x + threadIdx.x; s < S; s += gridDim.x * blockDim.x) {
-        const int r = slot_ref[s];
-        const double m = r >= 0 ? lm[r] : nm[~r];
-        const double q = r >= 0 ? lq[r] : nq[~r];
-        spread[s] = m > 0 ? (float)sqrt(q / m) : 0.0f;
     }
 }
 
@@ -445,7 +416,7 @@ __global__ void slot_count_kernel(int32_t* counts, const int32_t* __restrict__ c
 
 }  // namespace
 
-int launch_build(bh_context* ctx, const double* mass)
+int launch_build(bh_context* ctx, const double* mass, bool moments)
 {
     const int64_t n = ctx->n;
     if (n == 0) return BH_OK;
@@ -460,8 +431,14 @@ int launch_build(bh_context* ctx, const double* mass)
     if (rc) return rc;
     leaf_scatter_kernel<<<g, kThreads, 0, st>>>(n, ctx->key, ctx->head, ctx->body_leaf, ctx->leaf_first, ctx->leaf_key);
     BH_LAUNCH_CHECK(ctx);
-    leaf_sum_kernel<<<g, kThreads, 0, st>>>(ctx->counts, ctx->leaf_first, ctx->leaf_key, ctx->px, ctx->py, ctx->pz,
-                                            mass, ctx->leaf_m, ctx->leaf_wx, ctx->leaf_wy, ctx->leaf_wz, ctx->cdep);
+    if (moments)
+        leaf_sum_kernel<true><<<g, kThreads, 0, st>>>(ctx->counts, ctx->leaf_first, ctx->leaf_key, ctx->px, ctx->py,
+                                                      ctx->pz, mass, ctx->leaf_m, ctx->leaf_wx, ctx->leaf_wy,
+                                                      ctx->leaf_wz, ctx->cdep, ctx->leaf_q);
+    else
+        leaf_sum_kernel<false><<<g, kThreads, 0, st>>>(ctx->counts, ctx->leaf_first, ctx->leaf_key, ctx->px, ctx->py,
+                                                       ctx->pz, mass, ctx->leaf_m, ctx->leaf_wx, ctx->leaf_wy,
+                                                       ctx->leaf_wz, ctx->cdep, ctx->leaf_q);
     BH_LAUNCH_CHECK(ctx);
 
     // 2. branching nodes: representative flags -> ids -> ranges/child counts
@@ -495,41 +472,33 @@ int launch_build(bh_context* ctx, const double* mass)
 
     // 4. level-synchronous monopole pass, deepest level first
     for (int d = kMaxDepth - 1; d >= 0; --d) {
-        monopole_level_kernel<<<g, kThreads, 0, st>>>(d, ctx->depth_off, ctx->depth_nodes, ctx->node_cs,
-                                                      ctx->node_nchild, ctx->slot_ref, ctx->leaf_m, ctx->leaf_wx,
-                                                      ctx->leaf_wy, ctx->leaf_wz, ctx->node_m, ctx->node_wx,
-                                                      ctx->node_wy, ctx->node_wz);
+        if (moments)
+            monopole_level_kernel<true><<<g, kThreads, 0, st>>>(
+                d, ctx->depth_off, ctx->depth_nodes, ctx->node_cs, ctx->node_nchild, ctx->slot_ref, ctx->leaf_m,
+                ctx->leaf_wx, ctx->leaf_wy, ctx->leaf_wz, ctx->node_m, ctx->node_wx, ctx->node_wy, ctx->node_wz,
+                ctx->leaf_q, ctx->node_q);
+        else
+            monopole_level_kernel<false><<<g, kThreads, 0, st>>>(
+                d, ctx->depth_off, ctx->depth_nodes, ctx->node_cs, ctx->node_nchild, ctx->slot_ref, ctx->leaf_m,
+                ctx->leaf_wx, ctx->leaf_wy, ctx->leaf_wz, ctx->node_m, ctx->node_wx, ctx->node_wy, ctx->node_wz,
+                ctx->leaf_q, ctx->node_q);
         BH_LAUNCH_CHECK(ctx);
     }
 
     // 5. traversal records
     const int gs = grid_for(2 * n, kThreads, maxb);
-    finalize_kernel<<<gs, kThreads, 0, st>>>(ctx->counts, ctx->slot_ref, ctx->slot_top, ctx->leaf_m, ctx->leaf_wx,
-                                             ctx->leaf_wy, ctx->leaf_wz, ctx->node_m, ctx->node_wx, ctx->node_wy,
-                                             ctx->node_wz, ctx->node_cs, ctx->node_nchild, ctx->node_depth, ctx->rec);
-    BH_LAUNCH_CHECK(ctx);
-    return BH_OK;
-}
-
-int launch_second_moments(bh_context* ctx, const double* mass)
-{
-    const int64_t n = ctx->n;
-    if (n == 0) return BH_OK;
-    cudaStream_t st = ctx->stream;
-    const int g = grid_for(n, kThreads, 8 * kNumSMs);
-    leaf_moment_kernel<<<g, kThreads, 0, st>>>(ctx->counts, ctx->leaf_first, ctx->px, ctx->py, ctx->pz, mass,
-                                               ctx->leaf_m, ctx->leaf_wx, ctx->leaf_wy, ctx->leaf_wz, ctx->leaf_q);
-    BH_LAUNCH_CHECK(ctx);
-    for (int d = kMaxDepth - 1; d >= 0; --d) {
-        moment_level_kernel<<<g, kThreads, 0, st>>>(d, ctx->depth_off, ctx->depth_nodes, ctx->node_cs,
-                                                    ctx->node_nchild, ctx->slot_ref, ctx->leaf_m, ctx->leaf_wx,
-                                                    ctx->leaf_wy, ctx->leaf_wz, ctx->leaf_q, ctx->node_m,
-                                                    ctx->node_wx, ctx->node_wy, ctx->node_wz, ctx->node_q);
-        BH_LAUNCH_CHECK(ctx);
-    }
-    const int gs = grid_for(2 * n, kThreads, 8 * kNumSMs);
-    slot_spread_kernel<<<gs, kThreads, 0, st>>>(ctx->counts, ctx->slot_ref, ctx->leaf_m, ctx->leaf_q, ctx->node_m,
-                                                ctx->node_q, ctx->fspread);
+    if (moments)
+        finalize_kernel<true><<<gs, kThreads, 0, st>>>(ctx->counts, ctx->slot_ref, ctx->slot_top, ctx->leaf_m,
+                                                       ctx->leaf_wx, ctx->leaf_wy, ctx->leaf_wz, ctx->node_m,
+                                                       ctx->node_wx, ctx->node_wy, ctx->node_wz, ctx->node_cs,
+                                                       ctx->node_nchild, ctx->node_depth, ctx->rec, ctx->leaf_q,
+                                                       ctx->node_q, ctx->fspread);
+    else
+        finalize_kernel<false><<<gs, kThreads, 0, st>>>(ctx->counts, ctx->slot_ref, ctx->slot_top, ctx->leaf_m,
+                                                        ctx->leaf_wx, ctx->leaf_wy, ctx->leaf_wz, ctx->node_m,
+                                                        ctx->node_wx, ctx->node_wy, ctx->node_wz, ctx->node_cs,
+                                                        ctx->node_nchild, ctx->node_depth, ctx->rec, ctx->leaf_q,
+                                                        ctx->node_q, ctx->fspread);
     BH_LAUNCH_CHECK(ctx);
     return BH_OK;
 }

@@ -54,7 +54,8 @@ FLOPS_PER_INTERACTION = 20
 L2_FLUSH_BYTES = 256 << 20
 WORKLOAD = "plain FP64 theta=1.05, dt=1h, 300,149 bodies (Sun, 8 planets, 300,140 asteroids, 10% outer belt)"
 MODES = {"plain": 0, "fp64_list": 1, "fp32": 2, "learned": 3}
-KERNEL = {0: "traverse_exact_kernel", 1: "traverse_list_kernel", 2: "traverse_fp32_kernel", 3: "traverse_fp32_kernel"}
+KERNEL = {0: "traverse_exact_kernel", 1: "traverse_masked_kernel<fp64>", 2: "traverse_masked_kernel<fp32>",
+          3: "traverse_masked_kernel<fp32, learned>"}
 
 
 def workload_name(args) -> str:
@@ -84,6 +85,7 @@ def parse():
     ap.add_argument("--ns-bodies", type=int, default=4_000_000)
     ap.add_argument("--ns-steps", type=int, default=3)
     ap.add_argument("--theta-max", type=float, default=3.0, help="learned criterion: candidate range")
+    ap.add_argument("--budget", type=float, default=1e-7, help="learned criterion: per-node error threshold")
     return ap.parse_args()
 
 
@@ -273,7 +275,7 @@ def north_star(args, dev):
 
         rows = {}
         cases = [("plain_fp64", bh.MODE_FP64_LIST, None), ("fp32_far", bh.MODE_FP32_FAR, None)]
-        cases += [(f"fp32_learned_budget_{b:g}", bh.MODE_LEARNED, b) for b in (1e-4, 1e-5, 1e-6)]
+        cases += [(f"fp32_learned_budget_{b:g}", bh.MODE_LEARNED, b) for b in (1e-4, 1e-5, 1e-6, 1e-7)]
         for name, mode, budget in cases:
             if budget is not None:
                 ctx.learned_set_model(params, scale, budget=budget, theta_max=args.theta_max)
@@ -312,6 +314,11 @@ def run_ours(args, rank, ws, local):
     ctx = bh.Context(n, dev)
     ext = torch.cuda.ExternalStream(ctx.stream(), device=dev)
     flush = torch.empty(L2_FLUSH_BYTES // 4, dtype=torch.float32, device=f"cuda:{dev}")
+    if mode == bh.MODE_LEARNED:
+        learned = importlib.import_module("barnes-hut_gb300.learned")
+        params, scale, _, _ = learned.train(seeds=range(9001, 9005), n_bodies=min(n, 1_000_000), epochs=6,
+                                            theta_max=args.theta_max, max_pairs=4_000_000)
+        ctx.learned_set_model(params, scale, budget=args.budget, theta_max=args.theta_max)
     ctx.set_bodies(pos, vel, mass, ids)
     t = 0.0
     for _ in range(args.warmup):
