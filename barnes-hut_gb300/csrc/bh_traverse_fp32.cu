@@ -146,7 +146,7 @@ struct FParams {
 
 namespace {
 
-template <int kLearn>
+template <bool kFP64, int kLearn>
 struct WalkSmem {
     int2 stack[kWarps][kStack];  // sibling ranges: {first | (count - 1) << 28, lane mask}
     float4 lst[kWarps][kList];
@@ -156,13 +156,14 @@ struct WalkSmem {
     float side2f[kMaxDepth + 1];
     double side2d[kMaxDepth + 1];
     float feat[kLearn ? kWarps : 1][32][9];
+    uint8_t plist[kFP64 ? kWarps : 1][kList][32];  // FP64: each lane's own entries, in order
 };
 
 template <bool kFP64, int kLearn>
 __global__ void __launch_bounds__(kThreads) traverse_masked_kernel(FParams p)
 {
     extern __shared__ __align__(16) unsigned char smem_raw[];
-    WalkSmem<kLearn>& sm = *reinterpret_cast<WalkSmem<kLearn>*>(smem_raw);
+    WalkSmem<kFP64, kLearn>& sm = *reinterpret_cast<WalkSmem<kFP64, kLearn>*>(smem_raw);
     if (threadIdx.x <= kMaxDepth) {
         const double dx = __dsub_rn(p.bbox[3], p.bbox[0]);
         const double dy = __dsub_rn(p.bbox[4], p.bbox[1]);
@@ -442,17 +443,29 @@ __global__ void __launch_bounds__(kThreads) traverse_masked_kernel(FParams p)
                 continue;
             }
             if (kFP64) {
-                for (int j = 0; j < nlist; ++j) {
-                    const unsigned mj = LM[j];
+                // Each lane compacts the entries it takes into its own list,
+                // then all lanes walk their lists in lockstep: the FP64 pipe
+                // then serves (nearly) only lanes with work, instead of every
+                // lane for every partly-accepted entry.
+                uint8_t (*PL)[32] = sm.plist[w];
+                int mine = 0;
+                for (int j = 0; j < nlist; ++j)
+                    if (LM[j] & me) PL[mine++][lane] = (uint8_t)j;
+                int most = mine;
+#pragma unroll
+                for (int off = 16; off > 0; off >>= 1) most = max(most, __shfl_xor_sync(0xffffffffu, most, off));
+                for (int q = 0; q < most; ++q) {
+                    const bool on = q < mine;
+                    const int j = on ? PL[q][lane] : 0;
                     const TreeRec r = p.rec[LN[j]];
                     const double dx = r.cx - x, dy = r.cy - y, dz = r.cz - z;
-                    bool take = (mj & me) != 0;
-                    if (LL[j] == my_leaf) {
+                    bool take = on;
+                    if (on && LL[j] == my_leaf) {
                         // Own leaf: skipped at depth 21 unless a chain cell above
                         // it (depths top..20) accepts (traversal.cpp:70,78).
                         const double r2e = __dadd_rn(__dadd_rn(__dadd_rn(__dmul_rn(dx, dx), __dmul_rn(dy, dy)),
                                                                __dmul_rn(dz, dz)), soft2);
-                        take = take && r.top <= kMaxDepth - 1 && sm.side2d[kMaxDepth - 1] < __dmul_rn(theta2, r2e);
+                        take = r.top <= kMaxDepth - 1 && sm.side2d[kMaxDepth - 1] < __dmul_rn(theta2, r2e);
                     }
                     const double r2 = fma(dx, dx, fma(dy, dy, fma(dz, dz, soft2)));
                     const double inv = rsqrt(r2);
@@ -532,7 +545,7 @@ int grid_n(int64_t n)
 template <bool kFP64, int kLearn>
 int launch_walk(bh_context* ctx, const FParams& p)
 {
-    const size_t smem = sizeof(WalkSmem<kLearn>);
+    const size_t smem = sizeof(WalkSmem<kFP64, kLearn>);
     BH_CUDA_TRY(cudaFuncSetAttribute(traverse_masked_kernel<kFP64, kLearn>,
                                      cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     const int64_t groups = (p.n + 31) / 32;
