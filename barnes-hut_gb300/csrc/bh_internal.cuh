@@ -198,6 +198,8 @@ int launch_far_mass(bh_context* ctx);
 int launch_traverse(bh_context* ctx, double theta, double G, double soft2, int mode, double kick_h);
 int launch_traverse_masked(bh_context* ctx, double theta, double G, double soft2, double kick_h, bool fp64);
 int launch_traverse_learned(bh_context* ctx, double theta, double G, double soft2, double kick_h);
+// FP32 node records (hi/lo centres, G m, topology) from the FP64 records.
+int launch_fp32_nodes(bh_context* ctx, double G);
 
 // Device-wide exclusive scan of n int32 values (in may equal out); the
 // total is written to *total (device pointer).  n is read from n_dev when

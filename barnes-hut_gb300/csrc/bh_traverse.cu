@@ -13,8 +13,13 @@
 // rejoins when the stack falls back below it.  Each lane applies the
 // reference's test to its own body: leaf -> accept (own leaf -> skip),
 // else side(depth)^2 < theta^2 r^2 with r the distance to the centre of
-// mass; accepted nodes contribute G m d / r^3 with IEEE sqrt and division
-// and no contraction.  The result equals the reference bit for bit.
+// mass.  Because every lane sees the same node, the node is first classified
+// against the group's bounding box in FP32 (with allowances for rounding):
+// accepted by all, opened by all, or undecided -- only then does each lane
+// run the FP64 test.  Accepted nodes go to a per-lane list in walk order;
+// the lists are evaluated in lockstep (each lane its own next node) with
+// IEEE sqrt and division and no contraction, so every lane adds its terms in
+// the reference's order and the result equals the reference bit for bit.
 #include "bh_internal.cuh"
 
 namespace bh {
@@ -33,6 +38,9 @@ struct TravParams {
     const double* pz;
     const int32_t* body_leaf;
     const TreeRec* rec;
+    const float4* A;        // FP32 node records (group tests)
+    const float4* B;
+    const uint32_t* meta;
     const double* bbox;
     double theta2;
     double G;
@@ -81,34 +89,90 @@ __device__ inline TreeRec load_rec(const TreeRec* __restrict__ rec, int s)
     return r;
 }
 
+// Per-lane ordered interaction lists of the exact walk (slots).
+constexpr int kPList = 48;
+constexpr float kMargin = 1e-5f;
+constexpr float kAbsErr = 1e-6f;
+
 __global__ void __launch_bounds__(kTravThreads) traverse_exact_kernel(TravParams p)
 {
     __shared__ int stack[kTravWarps][kStackCap];
+    __shared__ int plist[kTravWarps][kPList][32];
     __shared__ double side2[kMaxDepth + 1];
+    __shared__ float side2f[kMaxDepth + 1];
     fill_side2(p.bbox, side2);
+    __syncthreads();
+    if (threadIdx.x <= kMaxDepth) side2f[threadIdx.x] = (float)side2[threadIdx.x];
     __syncthreads();
 
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
     const int64_t group = (int64_t)blockIdx.x * kTravWarps + w;
-    const int64_t i = group * 32 + lane;
-    if (group * 32 >= p.n) return;  // whole warp past the end
+    const int64_t base = group * 32;
+    if (base >= p.n) return;  // whole warp past the end
+    const int64_t i = base + lane;
     const bool valid = i < p.n;
-    const double px = valid ? p.px[i] : 0.0, py = valid ? p.py[i] : 0.0, pz = valid ? p.pz[i] : 0.0;
+    const int64_t ii = valid ? i : base;
+    const double px = p.px[ii], py = p.py[ii], pz = p.pz[ii];
     const int my_leaf = valid ? p.body_leaf[i] : -2;
     const double theta2 = p.theta2, G = p.G, soft2 = p.soft2;
+    const float theta2f = (float)theta2;
+    // Group box in group-relative FP32 coordinates (for the group tests).
+    const float gx = __double2float_rn(__shfl_sync(0xffffffffu, px, 0));
+    const float gy = __double2float_rn(__shfl_sync(0xffffffffu, py, 0));
+    const float gz = __double2float_rn(__shfl_sync(0xffffffffu, pz, 0));
+    const float rx = __double2float_rn(px - (double)gx);
+    const float ry = __double2float_rn(py - (double)gy);
+    const float rz = __double2float_rn(pz - (double)gz);
+    float bminx = rx, bminy = ry, bminz = rz, bmaxx = rx, bmaxy = ry, bmaxz = rz;
+#pragma unroll
+    for (int off = 16; off > 0; off >>= 1) {
+        bminx = fminf(bminx, __shfl_xor_sync(0xffffffffu, bminx, off));
+        bminy = fminf(bminy, __shfl_xor_sync(0xffffffffu, bminy, off));
+        bminz = fminf(bminz, __shfl_xor_sync(0xffffffffu, bminz, off));
+        bmaxx = fmaxf(bmaxx, __shfl_xor_sync(0xffffffffu, bmaxx, off));
+        bmaxy = fmaxf(bmaxy, __shfl_xor_sync(0xffffffffu, bmaxy, off));
+        bmaxz = fmaxf(bmaxz, __shfl_xor_sync(0xffffffffu, bmaxz, off));
+    }
+    const float bmag = fmaxf(fmaxf(fmaxf(fabsf(bminx), fabsf(bmaxx)), fmaxf(fabsf(bminy), fabsf(bmaxy))),
+                             fmaxf(fabsf(bminz), fabsf(bmaxz)));
     int* stk = stack[w];
+    int (*PL)[32] = plist[w];
 
     double ax = 0.0, ay = 0.0, az = 0.0;
     unsigned cnt = 0;
-    int sp = 0;
+    int mine = 0;  // entries in this lane's list
+    int sp = 1;
     int skip_sp = 0x7fffffff;
     if (lane == 0) stk[0] = 0;
-    sp = 1;
     __syncwarp();
     bool overflow = false;
-    // Each slot is pushed at most once per warp in a well-formed tree, so a
-    // walk longer than max_pops means a malformed tree: stop and report.
     int64_t pops = 0;
+
+    // Evaluates every lane's list in order with the reference's arithmetic.
+    auto flush = [&]() {
+        int most = mine;
+#pragma unroll
+        for (int off = 16; off > 0; off >>= 1) most = max(most, __shfl_xor_sync(0xffffffffu, most, off));
+        for (int q = 0; q < most; ++q) {
+            const bool on = q < mine;
+            const int s = on ? PL[q][lane] : 0;
+            const TreeRec r = load_rec(p.rec, s);
+            const double dx = __dsub_rn(r.cx, px), dy = __dsub_rn(r.cy, py), dz = __dsub_rn(r.cz, pz);
+            const double r2 =
+                __dadd_rn(__dadd_rn(__dadd_rn(__dmul_rn(dx, dx), __dmul_rn(dy, dy)), __dmul_rn(dz, dz)), soft2);
+            const double invR = __drcp_rn(__dsqrt_rn(r2));
+            const double invR3 = __dmul_rn(__dmul_rn(invR, invR), invR);
+            const double sc = __dmul_rn(__dmul_rn(G, r.m), invR3);
+            if (on) {
+                ax = __dadd_rn(ax, __dmul_rn(sc, dx));
+                ay = __dadd_rn(ay, __dmul_rn(sc, dy));
+                az = __dadd_rn(az, __dmul_rn(sc, dz));
+            }
+        }
+        mine = 0;
+        __syncwarp();
+    };
+
     while (sp > 0) {
         if (++pops > p.max_pops) {
             overflow = true;
@@ -117,47 +181,78 @@ __global__ void __launch_bounds__(kTravThreads) traverse_exact_kernel(TravParams
         --sp;
         const int s = stk[sp];
         __syncwarp();
-        const TreeRec r = load_rec(p.rec, s);
+        const float4 a = __ldg(p.A + s);
+        const float4 b = __ldg(p.B + s);
+        const uint32_t mt = __ldg(p.meta + s);
         if (sp < skip_sp) skip_sp = 0x7fffffff;
-        if (r.m == 0.0) continue;  // massless: skipped with its subtree (traversal.cpp:66)
+        if ((mt >> 17) & 1u) continue;  // massless: skipped with its subtree (traversal.cpp:66)
         const bool active = valid && skip_sp == 0x7fffffff;
-        const bool leaf = r.child < 0;
+        const bool leaf = (mt >> 16) & 1u;
+        const int depth = (mt >> 8) & 0xFF;
         bool accept = false, open = false;
-        if (active) {
-            const double dx = __dsub_rn(r.cx, px), dy = __dsub_rn(r.cy, py), dz = __dsub_rn(r.cz, pz);
-            const double r2 = __dadd_rn(__dadd_rn(__dadd_rn(__dmul_rn(dx, dx), __dmul_rn(dy, dy)), __dmul_rn(dz, dz)), soft2);
-            const double t2r2 = __dmul_rn(theta2, r2);
-            if (leaf) {
-                // Own leaf: the reference skips it at depth 21, but a chain
-                // cell above it (depths top..20) may already accept.
-                accept = (r.leaf != my_leaf) || (r.top <= kMaxDepth - 1 && side2[kMaxDepth - 1] < t2r2);
-            } else {
-                accept = side2[r.depth] < t2r2;
-                open = !accept;
+        if (leaf) {
+            if (active) {
+                if (__float_as_int(b.w) != my_leaf) {
+                    accept = true;
+                } else {
+                    // Own leaf: the reference skips it at depth 21, but a chain
+                    // cell above it (depths top..20) may already accept.
+                    const TreeRec r = load_rec(p.rec, s);
+                    const double dx = __dsub_rn(r.cx, px), dy = __dsub_rn(r.cy, py), dz = __dsub_rn(r.cz, pz);
+                    const double r2 = __dadd_rn(
+                        __dadd_rn(__dadd_rn(__dmul_rn(dx, dx), __dmul_rn(dy, dy)), __dmul_rn(dz, dz)), soft2);
+                    accept = r.top <= kMaxDepth - 1 && side2[kMaxDepth - 1] < __dmul_rn(theta2, r2);
+                }
             }
-            if (accept) {
-                const double invR = __drcp_rn(__dsqrt_rn(r2));
-                const double invR3 = __dmul_rn(__dmul_rn(invR, invR), invR);
-                const double sc = __dmul_rn(__dmul_rn(G, r.m), invR3);
-                ax = __dadd_rn(ax, __dmul_rn(sc, dx));
-                ay = __dadd_rn(ay, __dmul_rn(sc, dy));
-                az = __dadd_rn(az, __dmul_rn(sc, dz));
-                ++cnt;
+        } else {
+            // The same node for every lane: classify it against the group box
+            // (with allowances for FP32 rounding), test lane by lane in FP64
+            // only when the box cannot decide.
+            const float cx = (a.x - gx) + b.x, cy = (a.y - gy) + b.y, cz = (a.z - gz) + b.z;
+            const float ex = fmaxf(0.0f, fmaxf(bminx - cx, cx - bmaxx));
+            const float ey = fmaxf(0.0f, fmaxf(bminy - cy, cy - bmaxy));
+            const float ez = fmaxf(0.0f, fmaxf(bminz - cz, cz - bmaxz));
+            const float fx = fmaxf(fabsf(cx - bminx), fabsf(cx - bmaxx));
+            const float fy = fmaxf(fabsf(cy - bminy), fabsf(cy - bmaxy));
+            const float fz = fmaxf(fabsf(cz - bminz), fabsf(cz - bmaxz));
+            const float err = kAbsErr * (fmaxf(fabsf(cx), fmaxf(fabsf(cy), fabsf(cz))) + bmag);
+            const float dlo = fmaxf(sqrtf(ex * ex + ey * ey + ez * ez) - err, 0.0f);
+            const float dhi = sqrtf(fx * fx + fy * fy + fz * fz) + err;
+            const float s2 = side2f[depth];
+            if (s2 * (1.0f + kMargin) < theta2f * dlo * dlo) {
+                accept = active;
+            } else if (s2 * (1.0f - kMargin) > theta2f * dhi * dhi) {
+                open = active;
+            } else if (__any_sync(0xffffffffu, active)) {
+                const TreeRec r = load_rec(p.rec, s);
+                if (active) {
+                    const double dx = __dsub_rn(r.cx, px), dy = __dsub_rn(r.cy, py), dz = __dsub_rn(r.cz, pz);
+                    const double r2 = __dadd_rn(
+                        __dadd_rn(__dadd_rn(__dmul_rn(dx, dx), __dmul_rn(dy, dy)), __dmul_rn(dz, dz)), soft2);
+                    accept = side2[depth] < __dmul_rn(theta2, r2);
+                    open = !accept;
+                }
             }
+        }
+        if (accept) {
+            PL[mine++][lane] = s;
+            ++cnt;
         }
         const unsigned opened = __ballot_sync(0xffffffffu, open);
         if (opened) {
             if (accept) skip_sp = sp;  // sit out this node's subtree
-            const int nc = r.nchild;
+            const int nc = (int)(mt & 0xFF);
             if (sp + nc > kStackCap) {
                 overflow = true;
                 break;
             }
-            if (lane < nc) stk[sp + lane] = r.child + lane;
+            if (lane < nc) stk[sp + lane] = __float_as_int(b.w) + lane;
             __syncwarp();
             sp += nc;
         }
+        if (__any_sync(0xffffffffu, mine == kPList)) flush();
     }
+    flush();
     if (overflow && lane == 0) atomicOr(p.err, kErrOverflow);
     if (valid) {
         p.ax[i] = ax;
@@ -171,7 +266,7 @@ __global__ void __launch_bounds__(kTravThreads) traverse_exact_kernel(TravParams
         }
     }
     if (p.inter_count) {
-        unsigned long long c = cnt;
+        unsigned long long c = valid ? cnt : 0ull;
 #pragma unroll
         for (int off = 16; off > 0; off >>= 1) c += __shfl_down_sync(0xffffffffu, c, off);
         if (lane == 0) atomicAdd(p.inter_count, c);
@@ -189,6 +284,7 @@ int launch_traverse(bh_context* ctx, double theta, double G, double soft2, int m
     p.px = ctx->px; p.py = ctx->py; p.pz = ctx->pz;
     p.body_leaf = ctx->body_leaf;
     p.rec = ctx->rec;
+    p.A = ctx->fA; p.B = ctx->fB; p.meta = ctx->fmeta;
     p.bbox = ctx->bbox;
     p.theta2 = theta * theta;
     p.G = G;
@@ -204,9 +300,12 @@ int launch_traverse(bh_context* ctx, double theta, double G, double soft2, int m
     const int64_t groups = (n + 31) / 32;
     const int64_t blocks = (groups + kTravWarps - 1) / kTravWarps;
     switch (mode) {
-    case BH_MODE_PLAIN_FP64:
+    case BH_MODE_PLAIN_FP64: {
+        const int rc = launch_fp32_nodes(ctx, G);
+        if (rc) return rc;
         traverse_exact_kernel<<<(unsigned)blocks, kTravThreads, 0, ctx->stream>>>(p);
         break;
+    }
     case BH_MODE_FP64_LIST:
         return launch_traverse_masked(ctx, theta, G, soft2, kick_h, true);
     case BH_MODE_FP32_FAR:

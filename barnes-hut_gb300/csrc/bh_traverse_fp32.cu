@@ -11,8 +11,9 @@
 //   accept-all : side^2 < theta^2 dmin^2 (every body is at least dmin away),
 //   open-all   : side^2 > theta^2 dmax^2 (no body is farther than dmax),
 //   mixed      : each lane of the mask applies its own body's test.
-// (both group tests carry a 1e-4 relative margin, so every body's own test
-// agrees with them).  Lanes that accept a node take it into a staged
+// (both group tests allow for the FP32 rounding of the coordinates with an
+// absolute bound and a relative margin, so every body's own FP64 test agrees
+// with them).  Lanes that accept a node take it into a staged
 // interaction list with their mask bit; the others carry it down to the
 // children.  Each body therefore interacts with exactly the nodes its own
 // walk at theta accepts.
@@ -50,7 +51,8 @@ constexpr int kThreads = 32 * kWarps;
 constexpr int kStack = 512;   // sibling-range entries per warp
 constexpr int kList = 96;     // staged interactions per warp
 constexpr int kSlotBits = 28; // slot index bits of a stack entry (count - 1 in the top 3)
-constexpr float kMargin = 1e-4f;
+constexpr float kMargin = 1e-5f;  // relative margin of the FP32 group tests
+constexpr float kAbsErr = 1e-6f;  // bound on FP32 coordinate error, relative to magnitudes
 
 enum { kLearnNone = 0, kLearnInfer = 1, kLearnCollect = 2 };
 
@@ -239,6 +241,8 @@ __global__ void __launch_bounds__(kThreads) traverse_masked_kernel(FParams p)
             ascale = a < 3.0e38f ? a : 0.0f;
         }
     }
+    const float bmag = fmaxf(fmaxf(fmaxf(fabsf(bminx), fabsf(bmaxx)), fmaxf(fabsf(bminy), fabsf(bmaxy))),
+                             fmaxf(fabsf(bminz), fabsf(bmaxz)));
     const float gextent = sqrtf((bmaxx - bminx) * (bmaxx - bminx) + (bmaxy - bminy) * (bmaxy - bminy) +
                                 (bmaxz - bminz) * (bmaxz - bminz));
     const float bcx = 0.5f * (bminx + bmaxx), bcy = 0.5f * (bminy + bmaxy), bcz = 0.5f * (bminz + bmaxz);
@@ -316,11 +320,14 @@ __global__ void __launch_bounds__(kThreads) traverse_masked_kernel(FParams p)
                     dmax2 = fx * fx + fy * fy + fz * fz;
                     s2 = sm.side2f[depth];
                     nc = (int)(mt & 0xFF);
-                    if (s2 < theta2f * dmin2 * (1.0f - kMargin)) {
+                    // Absolute error of the FP32 group-relative distances.
+                    const float err = kAbsErr * (fmaxf(fabsf(cx), fmaxf(fabsf(cy), fabsf(cz))) + bmag);
+                    const float dlo = fmaxf(sqrtf(dmin2) - err, 0.0f), dhi = sqrtf(dmax2) + err;
+                    if (s2 * (1.0f + kMargin) < theta2f * dlo * dlo) {
                         A = M;
                     } else {
                         if (kLearn) cand = M != 0 && dmin2 > 0.0f && s2 < p.theta_max2 * dmin2;
-                        if (s2 > theta2f * dmax2 * (1.0f + kMargin)) A = 0;
+                        if (s2 * (1.0f - kMargin) > theta2f * dhi * dhi) A = 0;
                         else mixed = true;
                     }
                 }
@@ -556,6 +563,15 @@ int launch_walk(bh_context* ctx, const FParams& p)
 }
 
 }  // namespace
+
+int launch_fp32_nodes(bh_context* ctx, double G)
+{
+    if (ctx->n == 0) return BH_OK;
+    fp32_nodes_kernel<<<grid_n(2 * ctx->n), 256, 0, ctx->stream>>>(ctx->counts, ctx->rec, G, ctx->fA, ctx->fB,
+                                                                    ctx->fmeta);
+    BH_LAUNCH_CHECK(ctx);
+    return BH_OK;
+}
 
 int launch_far_mass(bh_context* ctx)
 {
