@@ -1,6 +1,8 @@
 """Builds libbh_gpu.so in-tree (``barnes-hut_gb300/_build/``) with nvcc for
-sm_103a.  Each translation unit compiles in its own process, in parallel;
-objects newer than their sources and headers are reused.
+sm_103a, then the reference-API shim (libbh_reference_api.so) and the
+``simulate`` driver over it with g++.  Each translation unit compiles in its
+own process, in parallel; objects newer than their sources and headers are
+reused.
 
 Usage: ``python barnes-hut_gb300/build.py`` or ``build.build()``.
 """
@@ -17,6 +19,8 @@ PKG = Path(__file__).resolve().parent
 CSRC = PKG / "csrc"
 OUT = PKG / "_build"
 LIB = OUT / "libbh_gpu.so"
+SHIM = PKG / "shim"
+SHIM_LIB = OUT / "libbh_reference_api.so"
 INCLUDE = PKG.parent / "include"
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
@@ -69,7 +73,22 @@ def build(verbose: bool = False, force: bool = False) -> Path:
         r = subprocess.run(cmd, capture_output=True, text=True)
         if r.returncode != 0:
             raise RuntimeError(f"link failed: {' '.join(cmd)}\n{r.stdout}\n{r.stderr}")
+    # The reference's C++ call surface over the library, and the
+    # reference-compatible driver.
+    _host_link(SHIM_LIB, [SHIM / "bh_reference_api.cpp"], ["-shared"], force)
+    _host_link(OUT / "simulate", [SHIM / "simulate.cpp"], [], force)
     return LIB
+
+
+def _host_link(out: Path, srcs: list[Path], extra: list[str], force: bool) -> None:
+    deps = [*srcs, *SHIM.glob("*.hpp"), LIB]
+    if not force and out.exists() and out.stat().st_mtime >= max(d.stat().st_mtime for d in deps):
+        return
+    cmd = [shutil.which("g++") or "g++", *CXX_FLAGS, f"-I{SHIM}", *extra, *map(str, srcs), "-o", str(out),
+           f"-L{OUT}", "-lbh_gpu", "-Wl,-rpath,$ORIGIN"]
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    if r.returncode != 0:
+        raise RuntimeError(f"build failed: {' '.join(cmd)}\n{r.stdout}\n{r.stderr}")
 
 
 if __name__ == "__main__":

@@ -484,6 +484,41 @@ int bh_sort_bodies(bh_context* ctx, int64_t* perm_out)
     return BH_OK;
 }
 
+int bh_set_keys(bh_context* ctx, const uint64_t* keys)
+{
+    int rc = check_ctx(ctx, "bh_set_keys");
+    if (rc) return rc;
+    if (ctx->n == 0) return BH_OK;
+    if (!keys) return bh_fail(BH_ERR_INVALID_ARGUMENT, "bh_set_keys: null keys");
+    BH_CUDA_TRY(cudaMemcpyAsync(ctx->key, keys, sizeof(uint64_t) * ctx->n, cudaMemcpyHostToDevice, ctx->stream));
+    if ((rc = bh::launch_hist(ctx))) return rc;
+    rc = finish(ctx, "bh_set_keys");
+    ctx->keys_valid = rc == BH_OK;
+    ctx->tree_valid = ctx->sorted_valid = false;
+    return rc;
+}
+
+int bh_set_bbox(bh_context* ctx, const double bbox[6])
+{
+    int rc = check_ctx(ctx, "bh_set_bbox");
+    if (rc) return rc;
+    if (!bbox) return bh_fail(BH_ERR_INVALID_ARGUMENT, "bh_set_bbox: null bbox");
+    BH_CUDA_TRY(cudaMemcpyAsync(ctx->bbox, bbox, 6 * sizeof(double), cudaMemcpyHostToDevice, ctx->stream));
+    rc = finish(ctx, "bh_set_bbox");
+    ctx->bbox_valid = rc == BH_OK;
+    return rc;
+}
+
+int bh_build_tree_options(bh_context* ctx, int merge)
+{
+    int rc = check_ctx(ctx, "bh_build_tree_options");
+    if (rc) return rc;
+    ctx->build_merge = merge != 0;
+    rc = bh_build_tree(ctx);
+    ctx->build_merge = true;
+    return rc;
+}
+
 int bh_build_tree(bh_context* ctx)
 {
     int rc = check_ctx(ctx, "bh_build_tree");
@@ -584,6 +619,42 @@ int bh_export_tree(bh_context* ctx, uint64_t* prefix, uint8_t* depth, double* ma
         com[3 * i + 2] = r.cz;
     }
     return BH_OK;
+}
+
+int bh_tree_slots(bh_context* ctx, uint64_t* prefix, uint8_t* depth)
+{
+    int rc = check_ctx(ctx, "bh_tree_slots");
+    if (rc) return rc;
+    if (!ctx->tree_valid) return ctx->n == 0 ? BH_OK : bh_fail(BH_ERR_STATE, "bh_tree_slots: no tree built");
+    if (!prefix || !depth) return bh_fail(BH_ERR_INVALID_ARGUMENT, "bh_tree_slots: null array");
+    HostTree h;
+    if ((rc = fetch_tree(ctx, h))) return rc;
+    for (int32_t s = 0; s < h.S; ++s) {
+        const int32_t ref = h.slot_ref[s];
+        const int32_t first = ref >= 0 ? ref : h.node_a[~ref];
+        depth[s] = h.rec[s].depth;
+        prefix[s] = h.leaf_key[first] & bh::prefix_mask(h.rec[s].depth);
+    }
+    return BH_OK;
+}
+
+int bh_tree_set_slot_values(bh_context* ctx, const double* mass, const double* com)
+{
+    int rc = check_ctx(ctx, "bh_tree_set_slot_values");
+    if (rc) return rc;
+    if (!ctx->tree_valid) return ctx->n == 0 ? BH_OK : bh_fail(BH_ERR_STATE, "bh_tree_set_slot_values: no tree");
+    if (!mass || !com) return bh_fail(BH_ERR_INVALID_ARGUMENT, "bh_tree_set_slot_values: null array");
+    HostTree h;
+    if ((rc = fetch_tree(ctx, h))) return rc;
+    for (int32_t s = 0; s < h.S; ++s) {
+        h.rec[s].m = mass[s];
+        h.rec[s].cx = com[3 * s];
+        h.rec[s].cy = com[3 * s + 1];
+        h.rec[s].cz = com[3 * s + 2];
+    }
+    BH_CUDA_TRY(cudaMemcpyAsync(ctx->rec, h.rec.data(), sizeof(bh::TreeRec) * h.S, cudaMemcpyHostToDevice, ctx->stream));
+    ctx->tree_far = ctx->tree_moments = false;
+    return finish(ctx, "bh_tree_set_slot_values");
 }
 
 int bh_compute_accelerations(bh_context* ctx, double theta, double G, double soft2, int mode, double* acc_out)

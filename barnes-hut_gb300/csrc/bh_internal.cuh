@@ -137,6 +137,7 @@ struct bh_context {
 
     bool tree_far = false;      // the tree holds far-field masses (FP32 modes)
     bool tree_moments = false;  // the tree's second moments are current
+    bool build_merge = true;    // apply the single-rank exchange merge in builds
     int num_direct = BH_NUM_MASSIVE;  // bodies with id < num_direct: FP64 direct terms in FP32 modes
 
     // Traversal.

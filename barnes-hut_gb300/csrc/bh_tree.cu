@@ -352,10 +352,14 @@ __global__ void monopole_level_kernel(int depth, const int32_t* __restrict__ dep
 
 // com = w/m when m > 0 (linear_octree.cpp:95-104), then the merge of
 // linear_octree.cpp:194-202 with m0 = com0 = 0.
-__device__ inline void finish_com(double m, double wx, double wy, double wz, TreeRec& r)
+__device__ inline void finish_com(double m, double wx, double wy, double wz, TreeRec& r, int merge)
 {
     double cx = wx, cy = wy, cz = wz;
     if (m > 0) { cx = __ddiv_rn(wx, m); cy = __ddiv_rn(wy, m); cz = __ddiv_rn(wz, m); }
+    if (!merge) {  // buildOctreeBottomUp's own output, before any exchange
+        r.cx = cx; r.cy = cy; r.cz = cz; r.m = m;
+        return;
+    }
     const double tot = __dadd_rn(0.0, m);
     if (tot == 0) {
         r.cx = r.cy = r.cz = r.m = 0.0;
@@ -376,7 +380,7 @@ __global__ void finalize_kernel(const int32_t* __restrict__ counts, const int32_
                                 const double* __restrict__ nwz, const int32_t* __restrict__ node_cs,
                                 const int32_t* __restrict__ node_nchild, const uint8_t* __restrict__ node_depth,
                                 TreeRec* __restrict__ rec, const double* __restrict__ lq,
-                                const double* __restrict__ nq, float* __restrict__ spread)
+                                const double* __restrict__ nq, float* __restrict__ spread, int merge)
 {
     const int S = counts[2];
     for (int s = blockIdx.x * blockDim.x + threadIdx.x; s < S; s += gridDim.x * blockDim.x) {
@@ -386,14 +390,14 @@ __global__ void finalize_kernel(const int32_t* __restrict__ counts, const int32_
         o.pad0 = 0;
         o.pad1 = 0;
         if (r >= 0) {
-            finish_com(lm[r], lwx[r], lwy[r], lwz[r], o);
+            finish_com(lm[r], lwx[r], lwy[r], lwz[r], o, merge);
             o.child = -1;
             o.leaf = r;
             o.nchild = 0;
             o.depth = (uint8_t)kMaxDepth;
         } else {
             const int b = ~r;
-            finish_com(nm[b], nwx[b], nwy[b], nwz[b], o);
+            finish_com(nm[b], nwx[b], nwy[b], nwz[b], o, merge);
             o.child = node_cs[b] + 1;
             o.leaf = -1;
             o.nchild = (uint8_t)node_nchild[b];
@@ -492,13 +496,13 @@ int launch_build(bh_context* ctx, const double* mass, bool moments)
                                                        ctx->leaf_wx, ctx->leaf_wy, ctx->leaf_wz, ctx->node_m,
                                                        ctx->node_wx, ctx->node_wy, ctx->node_wz, ctx->node_cs,
                                                        ctx->node_nchild, ctx->node_depth, ctx->rec, ctx->leaf_q,
-                                                       ctx->node_q, ctx->fspread);
+                                                       ctx->node_q, ctx->fspread, ctx->build_merge ? 1 : 0);
     else
         finalize_kernel<false><<<gs, kThreads, 0, st>>>(ctx->counts, ctx->slot_ref, ctx->slot_top, ctx->leaf_m,
                                                         ctx->leaf_wx, ctx->leaf_wy, ctx->leaf_wz, ctx->node_m,
                                                         ctx->node_wx, ctx->node_wy, ctx->node_wz, ctx->node_cs,
                                                         ctx->node_nchild, ctx->node_depth, ctx->rec, ctx->leaf_q,
-                                                        ctx->node_q, ctx->fspread);
+                                                        ctx->node_q, ctx->fspread, ctx->build_merge ? 1 : 0);
     BH_LAUNCH_CHECK(ctx);
     return BH_OK;
 }

@@ -1,0 +1,180 @@
+// simulate: the reference's single-rank `--fc tree` driver (src/main.cpp)
+// on libbh_gpu.so.  Same flags and printed lines, so the reference's
+// benchmark scripts can drive it:
+//
+//   simulate -f bodies.csv --dt 1h --tend 10d --theta 1.05 [-b N] [-r]
+//            [--fc tree] [--steps K] [--mode plain|fp64_list|fp32]
+//            [--generate N --seed S] [--dump FILE]
+//
+// --tend uses the reference's loop (`for (t = 0; t < t_end; t += dt)`, so
+// 10d at 1h runs 241 steps); --steps overrides it.  -r writes the final
+// positions to reference/final_ref.csv (io.cpp:716-722 layout); without -r
+// an existing reference file is compared by body id and SUMMED_DIST_ERROR
+// printed (io.cpp:759-780).  TOTAL_TIME covers the step loop (main.cpp:185,323).
+// --dump writes the final state at full precision in the state-vector CSV
+// layout (what -f reads), bodies in the engine's final (key-sorted) order.
+#include <chrono>
+#include <cmath>
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <filesystem>
+#include <fstream>
+#include <iomanip>
+#include <iostream>
+#include <sstream>
+#include <stdexcept>
+#include <string>
+#include <vector>
+
+#include "bh_gpu.h"
+
+namespace {
+
+// parseTime (include/parse_time.h:6-16): "1h", "2.5d", "1y" -> days.
+double parse_time(const std::string& s)
+{
+    if (s.empty()) throw std::invalid_argument("empty time");
+    const double v = std::stod(s.substr(0, s.size() - 1));
+    switch (s.back()) {
+    case 'h': return v / 24.0;
+    case 'd': return v;
+    case 'y': return v * 365.25;
+    default: throw std::invalid_argument("unknown time unit: " + s);
+    }
+}
+
+void die(const std::string& msg)
+{
+    std::cerr << "Error: " << msg << std::endl;
+    std::exit(1);
+}
+
+void check(int rc, const char* what)
+{
+    if (rc != BH_OK) die(std::string(what) + ": " + bh_last_error());
+}
+
+}  // namespace
+
+int main(int argc, char** argv)
+{
+    std::string file, fc = "tree", mode_s = "plain", dt_s = "1d", tend_s = "1y", dump;
+    double theta = 1.05;
+    long long bodies = -1, steps = -1, generate = 0;
+    unsigned long long seed = 1;
+    bool reference = false;
+    for (int a = 1; a < argc; ++a) {
+        const std::string k = argv[a];
+        auto val = [&]() -> std::string {
+            if (a + 1 >= argc) die("missing value for " + k);
+            return argv[++a];
+        };
+        if (k == "-f" || k == "--file") file = val();
+        else if (k == "--dt") dt_s = val();
+        else if (k == "--tend") tend_s = val();
+        else if (k == "--vs" || k == "-o" || k == "--outdir" || k == "--max-depth" || k == "--bucket-bits" ||
+                 k == "--rebalance-interval") val();  // visualisation / multi-rank options: accepted, unused
+        else if (k == "-b" || k == "--bodies") bodies = std::stoll(val());
+        else if (k == "--fc") fc = val();
+        else if (k == "--theta") theta = std::stod(val());
+        else if (k == "-r" || k == "--reference") reference = true;
+        else if (k == "--steps") steps = std::stoll(val());
+        else if (k == "--mode") mode_s = val();
+        else if (k == "--generate") generate = std::stoll(val());
+        else if (k == "--seed") seed = std::stoull(val());
+        else if (k == "--dump") dump = val();
+        else if (k == "-h" || k == "--help") {
+            std::cout << "simulate -f FILE [--dt 1h] [--tend 1y] [--theta 1.05] [-b N] [-r] [--steps K]\n"
+                         "         [--mode plain|fp64_list|fp32] [--generate N --seed S] [--dump FILE]\n";
+            return 0;
+        } else die("unknown option " + k);
+    }
+    if (reference) fc = "tree";
+    if (fc != "tree") die("only --fc tree (the single-rank path) is provided");
+    int mode = BH_MODE_PLAIN_FP64;
+    if (mode_s == "fp64_list") mode = BH_MODE_FP64_LIST;
+    else if (mode_s == "fp32") mode = BH_MODE_FP32_FAR;
+    else if (mode_s != "plain") die("unknown --mode " + mode_s);
+    const double dt = parse_time(dt_s), t_end = parse_time(tend_s);
+
+    std::vector<uint64_t> ids;
+    std::vector<double> mass, pos, vel;
+    int64_t n = 0;
+    if (generate > 0) {
+        n = generate;
+        ids.resize(n); mass.resize(n); pos.resize(3 * n); vel.resize(3 * n);
+        check(bh_generate_system(seed, n, 0.10, 0.0, pos.data(), vel.data(), mass.data(), ids.data()),
+              "bh_generate_system");
+    } else {
+        if (file.empty()) die("input file required (-f)");
+        check(bh_read_csv(file.c_str(), bodies, &n, nullptr, nullptr, nullptr, nullptr), "bh_read_csv");
+        ids.resize(n); mass.resize(n); pos.resize(3 * n); vel.resize(3 * n);
+        check(bh_read_csv(file.c_str(), bodies, &n, ids.data(), mass.data(), pos.data(), vel.data()), "bh_read_csv");
+    }
+    std::cout << "Loaded " << n << " bodies\n";
+    int64_t nsteps = steps;
+    if (nsteps < 0) {
+        nsteps = 0;
+        for (double t = 0.0; t < t_end; t += dt) ++nsteps;
+    }
+    std::cout << "Starting simulation (dt=" << dt << ", tend=" << t_end << ")\n";
+
+    bh_context* ctx = nullptr;
+    check(bh_context_create(n > 0 ? n : 1, 0, &ctx), "bh_context_create");
+    check(bh_set_bodies(ctx, n, pos.data(), vel.data(), mass.data(), ids.data()), "bh_set_bodies");
+    const double G = 1.48812e-34;
+    double t = 0.0;
+    const auto t0 = std::chrono::high_resolution_clock::now();
+    check(bh_step(ctx, dt, theta, G, nsteps, mode, &t), "bh_step");
+    const auto t1 = std::chrono::high_resolution_clock::now();
+    check(bh_get_bodies(ctx, pos.data(), vel.data(), mass.data(), ids.data(), nullptr), "bh_get_bodies");
+    bh_context_destroy(ctx);
+    if (!dump.empty())
+        check(bh_write_csv(dump.c_str(), n, ids.data(), mass.data(), pos.data(), vel.data()), "bh_write_csv");
+
+    double summed = 0.0;
+    const std::filesystem::path ref = std::filesystem::path("reference") / "final_ref.csv";
+    if (reference) {
+        std::filesystem::create_directories("reference");
+        std::ofstream os(ref);
+        os << "id,x,y,z\n";
+        for (int64_t i = 0; i < n; ++i)
+            os << ids[i] << "," << pos[3 * i] << "," << pos[3 * i + 1] << "," << pos[3 * i + 2] << "\n";
+        std::cout << "Reference positions saved to reference/final_ref.csv" << std::endl;
+    } else if (std::filesystem::exists(ref)) {
+        std::vector<double> rp(3 * (size_t)n, 0.0);
+        std::ifstream is(ref);
+        std::string line;
+        std::getline(is, line);
+        while (std::getline(is, line)) {
+            std::stringstream ss(line);
+            std::string f;
+            std::getline(ss, f, ',');
+            const uint64_t id = std::stoull(f);
+            double v[3];
+            for (double& x : v) {
+                std::getline(ss, f, ',');
+                x = std::stod(f);
+            }
+            if (id < (uint64_t)n)
+                for (int a = 0; a < 3; ++a) rp[3 * id + a] = v[a];
+        }
+        for (int64_t i = 0; i < n; ++i) {
+            const uint64_t id = ids[i];
+            if (id >= (uint64_t)n) continue;
+            const double dx = pos[3 * i] - rp[3 * id], dy = pos[3 * i + 1] - rp[3 * id + 1],
+                         dz = pos[3 * i + 2] - rp[3 * id + 2];
+            summed += std::sqrt(dx * dx + dy * dy + dz * dz);
+        }
+    } else {
+        std::cout << "Reference file not found at reference/final_ref.csv, skipping error analysis." << std::endl;
+    }
+    const double secs = std::chrono::duration<double>(t1 - t0).count();
+    std::cout << std::fixed << std::setprecision(4);
+    std::cout << "TOTAL_TIME          " << secs << std::endl;
+    std::cout << "SUMMED_DIST_ERROR   " << summed << std::endl;
+    std::cout << "BODY_STEPS_PER_S    " << std::setprecision(1) << (secs > 0 ? n * (double)nsteps / secs : 0.0)
+              << std::endl;
+    return 0;
+}

@@ -115,6 +115,17 @@ int bh_compute_keys(bh_context *ctx, uint64_t *keys_out);
  * the keys, then permutes pos, vel, mass, ids (and keys).  perm_out (may be
  * NULL) receives, for each new position, the body's previous position. */
 int bh_sort_bodies(bh_context *ctx, int64_t *perm_out);
+/* The caller's own keys (n) in place of bh_compute_keys, e.g. keys made by
+ * generateMortonCodes elsewhere; bh_sort_bodies may follow. */
+int bh_set_keys(bh_context *ctx, const uint64_t *keys);
+/* The caller's global bounding box (the `global_bb` argument of
+ * computeAccelerations, include/traversal.h:21-30) in place of
+ * bh_compute_bbox. */
+int bh_set_bbox(bh_context *ctx, const double bbox[6]);
+/* buildOctreeBottomUp alone (merge == 0: centres of mass sum/mass, as the
+ * function returns them, src/linear_octree.cpp:95-104) or followed by the
+ * single-rank exchange merge (merge != 0, what bh_build_tree does). */
+int bh_build_tree_options(bh_context *ctx, int merge);
 /* buildOctreeBottomUp (src/linear_octree.cpp:13-107) followed by the
  * single-rank exchangeFullTrees re-merge (src/exchange.cpp:9-29 ->
  * src/linear_octree.cpp:178-204).  Requires sorted keys. */
@@ -127,6 +138,15 @@ int bh_tree_info(bh_context *ctx, int64_t *n_records, int64_t *n_nodes, int64_t 
  * src/linear_octree.cpp:169-176, NodeRecord linear_octree.h:60-65) sorted by
  * (depth, prefix): each array holds n_records entries (com: 3 per node). */
 int bh_export_tree(bh_context *ctx, uint64_t *prefix, uint8_t *depth, double *mass, double *com);
+/* The compressed device tree's nodes (n_nodes of bh_tree_info): the depth
+ * and prefix of the reference cell each node stands for (the deepest cell
+ * of its single-child chain).  No reference counterpart. */
+int bh_tree_slots(bh_context *ctx, uint64_t *prefix, uint8_t *depth);
+/* Overrides the mass and centre of mass (com: 3 per node) of every node of
+ * the compressed device tree, e.g. with the values of an OctreeMap that the
+ * caller changed (the reference's computeAccelerations reads the map it is
+ * given).  No reference counterpart. */
+int bh_tree_set_slot_values(bh_context *ctx, const double *mass, const double *com);
 /* computeAccelerations (src/traversal.cpp:13-103, include/traversal.h:21-30)
  * over the last tree; `mode` is a bh_mode.  acc_out (may be NULL) receives
  * the accelerations in the current body order. */

@@ -13,7 +13,8 @@ Outputs (all produced by the compiled reference, strict IEEE build):
                              every stage's full output.
 * ``synthetic_1000.npz``  -- seeded synthetic system (seed 7, 1,000 bodies,
                              10 % outer belt, 5 % trojans): inputs, every
-                             stage's full output and 5 steps of the loop.
+                             stage's full output (the tree also without the
+                             single-rank merge) and 5 steps of the loop.
 * ``synthetic_19054.npz`` -- the CPU-runnable workload (seed 1, 19,054 bodies:
                              Sun, 8 planets, 19,045 inner-belt asteroids):
                              inputs, keys, permutation, SHA-256 digests of the
@@ -108,6 +109,11 @@ def main() -> None:
     out.update(stages(ref, pos, vel, mass, ids))
     for th in (0.5, 0.8):
         out[f"acc_theta_{th}"] = stages(ref, pos, vel, mass, ids, theta=th)["acc"]
+    # buildOctreeBottomUp alone (no single-rank exchange merge)
+    t_nm = ref.tree(out["sorted_keys"], out["sorted_pos"], out["sorted_mass"], merge=False)
+    for k, v in zip(("prefix", "depth", "mass", "com"), t_nm.records()):
+        out[f"tree_nomerge_{k}"] = v
+    t_nm.close()
     p, v, m, i, a, t, _ = ref.simulate(pos, vel, mass, ids, DT, THETA, G, 5)
     out.update(sim5_pos=p, sim5_vel=v, sim5_mass=m, sim5_ids=i, sim5_acc=a, sim5_t=np.array([t]))
     np.savez_compressed(HERE / "synthetic_1000.npz", **out)
