@@ -323,6 +323,8 @@ class Context:
         return out
 
     def invariants(self, G=G_DEFAULT, theta=THETA_DEFAULT) -> dict:
+        """E, K, U, L (3), P (3).  theta = 0: exact pair potential (N <= 131072);
+        theta > 0: massive-body pairs exact, the rest through the tree."""
         out = np.empty(9)
         _check(library().bh_invariants(self._h, G, theta, _ptr(out)))
         return dict(E=out[0], K=out[1], U=out[2], L=out[3:6].copy(), P=out[6:9].copy())

@@ -143,8 +143,10 @@ int check_ctx(bh_context* ctx, const char* fn)
 
 void collect_phases(bh_context* ctx);
 
+}  // namespace
+
 // Waits for the stream and turns a raised device error word into a status.
-int finish(bh_context* ctx, const char* fn)
+int bh::finish(bh_context* ctx, const char* fn)
 {
     BH_CUDA_TRY(cudaMemcpyAsync(ctx->h_err, ctx->err, sizeof(unsigned), cudaMemcpyDeviceToHost, ctx->stream));
     BH_CUDA_TRY(cudaStreamSynchronize(ctx->stream));
@@ -158,6 +160,9 @@ int finish(bh_context* ctx, const char* fn)
     if (e & bh::kErrOverflow) return bh_fail(BH_ERR_OVERFLOW, std::string(fn) + ": traversal stack overflow");
     return bh_fail(BH_ERR_CUDA, std::string(fn) + ": device error word set");
 }
+
+namespace {
+using bh::finish;
 
 int upload_vec3(bh_context* ctx, const double* host_aos, double* stage, double* x, double* y, double* z, int64_t n)
 {

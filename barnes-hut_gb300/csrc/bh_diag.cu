@@ -108,6 +108,88 @@ __global__ void __launch_bounds__(kDirThreads) potential_pairs_kernel(int64_t n,
 
 constexpr int64_t kExactPotentialMax = 1 << 17;
 
+// Potential of the pairs that involve a massive body (id < nd), exact FP64.
+// Each such pair counts once: a pair of two massive bodies by its higher id.
+__global__ void __launch_bounds__(kDirThreads) potential_massive_kernel(
+    int64_t n, const double* __restrict__ px, const double* __restrict__ py, const double* __restrict__ pz,
+    const double* __restrict__ m, const uint64_t* __restrict__ id, int nd, const double* __restrict__ direct,
+    const int32_t* __restrict__ present, double* __restrict__ part)
+{
+    __shared__ double sh[kDirThreads / 32];
+    double u = 0.0;
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+        const uint64_t idi = id[i];
+        const double xi = px[i], yi = py[i], zi = pz[i], mi = m[i];
+        for (int k = 0; k < nd; ++k) {
+            if (!present[k] || idi == (uint64_t)k || (idi < (uint64_t)nd && idi < (uint64_t)k)) continue;
+            const double dx = direct[4 * k] - xi, dy = direct[4 * k + 1] - yi, dz = direct[4 * k + 2] - zi;
+            const double r = sqrt(dx * dx + dy * dy + dz * dz);
+            if (r > 0) u -= direct[4 * k + 3] * mi / r;
+        }
+    }
+    const double t = block_sum(u, sh);
+    if (threadIdx.x == 0) part[blockIdx.x] = t;
+}
+
+// Potential of all other pairs through the tree of far-field masses (the
+// massive bodies zeroed): U = 1/2 sum_i m_i phi_i over the non-massive
+// bodies, phi_i from the monopoles the theta criterion of the force walk
+// accepts (side(depth)^2 < theta^2 r^2; leaves always, the own leaf never).
+// One thread per body, depth-first with a private stack; a stack that would
+// overflow raises the overflow bit of the error word and drops that subtree.
+constexpr int kPotStack = 8 * bh::kMaxDepth + 8;
+
+__global__ void __launch_bounds__(kDirThreads) potential_tree_kernel(
+    int64_t n, const double* __restrict__ px, const double* __restrict__ py, const double* __restrict__ pz,
+    const double* __restrict__ m, const uint64_t* __restrict__ id, int nd, const int32_t* __restrict__ body_leaf,
+    const bh::TreeRec* __restrict__ rec, const double* __restrict__ bbox, double theta, double G,
+    unsigned* __restrict__ err, double* __restrict__ part)
+{
+    __shared__ double sh[kDirThreads / 32];
+    __shared__ double side2[bh::kMaxDepth + 1];
+    if (threadIdx.x <= bh::kMaxDepth) {
+        double L = bbox[3] - bbox[0];
+        L = fmax(L, bbox[4] - bbox[1]);
+        L = fmax(L, bbox[5] - bbox[2]);
+        const double side = L / (double)(1ull << threadIdx.x);
+        side2[threadIdx.x] = side * side;
+    }
+    __syncthreads();
+    const double t2 = theta * theta;
+    double u = 0.0;
+    int32_t stack[kPotStack];
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+        if (id[i] < (uint64_t)nd) continue;
+        const double x = px[i], y = py[i], z = pz[i];
+        const int32_t own = body_leaf[i];
+        double phi = 0.0;
+        int sp = 0;
+        stack[sp++] = 0;
+        while (sp > 0) {
+            const bh::TreeRec r = rec[stack[--sp]];
+            if (!(r.m > 0.0)) continue;
+            const double dx = r.cx - x, dy = r.cy - y, dz = r.cz - z;
+            const double r2 = dx * dx + dy * dy + dz * dz;
+            if (r.nchild == 0) {
+                if (r.leaf != own && r2 > 0.0) phi -= r.m / sqrt(r2);
+                continue;
+            }
+            if (side2[r.depth] < t2 * r2) {
+                phi -= r.m / sqrt(r2);
+                continue;
+            }
+            if (sp + r.nchild > kPotStack) {
+                atomicOr(err, bh::kErrOverflow);
+                continue;
+            }
+            for (int c = r.nchild - 1; c >= 0; --c) stack[sp++] = r.child + c;
+        }
+        u += 0.5 * G * m[i] * phi;
+    }
+    const double t = block_sum(u, sh);
+    if (threadIdx.x == 0) part[blockIdx.x] = t;
+}
+
 // Eight independent FMA chains per thread; the result is stored so the
 // chains are live.
 template <class T>
@@ -189,31 +271,59 @@ int bh_measure_fma_peak(bh_context* ctx, int fp64, double* tflops_out)
 
 int bh_invariants(bh_context* ctx, double G, double theta, double out[9])
 {
-    (void)theta;
-    if (!ctx || !out) return bh_fail(BH_ERR_INVALID_ARGUMENT, "bh_invariants: bad arguments");
+    if (!ctx || !out || !(theta >= 0.0)) return bh_fail(BH_ERR_INVALID_ARGUMENT, "bh_invariants: bad arguments");
     BH_CUDA_TRY(cudaSetDevice(ctx->device));
     const int64_t n = ctx->n;
     for (int k = 0; k < 9; ++k) out[k] = 0.0;
     if (n == 0) return BH_OK;
-    if (n > kExactPotentialMax)
+    const bool exact = theta == 0.0;
+    if (exact && n > kExactPotentialMax)
         return bh_fail(BH_ERR_INVALID_ARGUMENT, "bh_invariants: exact pair potential limited to 131072 bodies");
-    const int blocks = 4 * bh::kNumSMs;
+    int rc = BH_OK;
+    if (!exact) {
+        // The tree part needs the tree of the current positions with the
+        // massive bodies' masses zeroed.
+        if (!ctx->tree_valid) {
+            if ((rc = bh_compute_bbox(ctx, nullptr)) || (rc = bh_compute_keys(ctx, nullptr)) ||
+                (rc = bh_sort_bodies(ctx, nullptr)) || (rc = bh_build_tree(ctx)))
+                return rc;
+        }
+        if (!ctx->tree_far) {
+            if ((rc = bh::launch_far_mass(ctx)) || (rc = bh::launch_build(ctx, ctx->m2, ctx->tree_moments))) return rc;
+            ctx->tree_far = true;
+        }
+        if ((rc = bh::launch_direct_extract(ctx, G))) return rc;
+    }
+    // Every kernel below writes one partial per block into its own column.
+    const int blocks = 8 * bh::kNumSMs;
     double* part = nullptr;
-    BH_CUDA_TRY(cudaMallocAsync(&part, sizeof(double) * blocks * 8, ctx->stream));
+    BH_CUDA_TRY(cudaMallocAsync(&part, sizeof(double) * blocks * 9, ctx->stream));
+    BH_CUDA_TRY(cudaMemsetAsync(part, 0, sizeof(double) * blocks * 9, ctx->stream));
     moments_kernel<<<blocks, kDirThreads, 0, ctx->stream>>>(n, ctx->px, ctx->py, ctx->pz, ctx->vx, ctx->vy, ctx->vz,
                                                             ctx->m, part);
     BH_LAUNCH_CHECK(ctx);
-    potential_pairs_kernel<<<blocks, kDirThreads, 0, ctx->stream>>>(n, ctx->px, ctx->py, ctx->pz, ctx->m, G,
-                                                                    part + blocks * 7);
-    BH_LAUNCH_CHECK(ctx);
-    std::vector<double> h((size_t)blocks * 8);
-    BH_CUDA_TRY(cudaMemcpyAsync(h.data(), part, sizeof(double) * blocks * 8, cudaMemcpyDeviceToHost, ctx->stream));
+    if (exact) {
+        potential_pairs_kernel<<<blocks, kDirThreads, 0, ctx->stream>>>(n, ctx->px, ctx->py, ctx->pz, ctx->m, G,
+                                                                        part + blocks * 7);
+        BH_LAUNCH_CHECK(ctx);
+    } else {
+        const int nd = ctx->num_direct < 64 ? (ctx->num_direct > 0 ? ctx->num_direct : 0) : 64;
+        potential_massive_kernel<<<blocks, kDirThreads, 0, ctx->stream>>>(
+            n, ctx->px, ctx->py, ctx->pz, ctx->m, ctx->id, nd, ctx->direct, ctx->direct_present, part + blocks * 7);
+        BH_LAUNCH_CHECK(ctx);
+        potential_tree_kernel<<<blocks, kDirThreads, 0, ctx->stream>>>(
+            n, ctx->px, ctx->py, ctx->pz, ctx->m, ctx->id, nd, ctx->body_leaf, ctx->rec, ctx->bbox, theta, G, ctx->err,
+            part + blocks * 8);
+        BH_LAUNCH_CHECK(ctx);
+    }
+    std::vector<double> h((size_t)blocks * 9);
+    BH_CUDA_TRY(cudaMemcpyAsync(h.data(), part, sizeof(double) * blocks * 9, cudaMemcpyDeviceToHost, ctx->stream));
     BH_CUDA_TRY(cudaFreeAsync(part, ctx->stream));
-    BH_CUDA_TRY(cudaStreamSynchronize(ctx->stream));
+    if ((rc = bh::finish(ctx, "bh_invariants"))) return rc;
     double q[7] = {0, 0, 0, 0, 0, 0, 0}, U = 0.0;
     for (int b = 0; b < blocks; ++b) {
         for (int k = 0; k < 7; ++k) q[k] += h[(size_t)b * 7 + k];
-        U += h[(size_t)blocks * 7 + b];
+        U += h[(size_t)blocks * 7 + b] + h[(size_t)blocks * 8 + b];
     }
     out[0] = q[0] + U;
     out[1] = q[0];

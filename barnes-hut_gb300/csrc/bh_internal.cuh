@@ -53,6 +53,24 @@ __device__ inline int common_depth(uint64_t a, uint64_t b)
     return (62 - hb) / 3;
 }
 
+// 1/sqrt(x) in FP64 from the FP32 hardware estimate y0 (relative error below
+// 2^-22) and one third-order Householder step for f(y) = 1/y^2 - x:
+//   e = 1 - x y0^2,   y1 = y0 (1 + e/2 + 3 e^2 / 8),
+// whose truncation error is 5/16 e^3 (below 2^-66); with the roundings of
+// the FP64 steps the result is within about one ulp.  Outside [2^-100, 2^100]
+// (and for 0, inf, NaN), where the FP32 estimate cannot represent the value,
+// the library's rsqrt.  The non-bit-exact FP64 walk and the direct terms use
+// it: 5 FP64 operations instead of a full-precision square root sequence.
+__device__ __forceinline__ double rsqrt_hh(double x)
+{
+    if (!(x >= 0x1p-100 && x <= 0x1p100)) return rsqrt(x);
+    const double y0 = (double)rsqrtf(__double2float_rn(x));
+    const double h = x * y0;
+    const double e = fma(-h, y0, 1.0);
+    const double t = e * fma(e, 0.375, 0.5);
+    return fma(y0, t, y0);
+}
+
 // One node of the compressed octree as the traversal reads it (48 bytes).
 // A node stands for the reference's chain of single-child nodes from depth
 // `top` down to `depth` (all with identical mass and centre of mass), so it
@@ -195,6 +213,11 @@ int sort_passes_raw(int64_t n, const uint64_t* keys_in, uint64_t* keys_out, uint
 int launch_build(bh_context* ctx, const double* mass, bool moments = false);
 // FP32 modes: far-field masses (direct bodies zeroed) into ctx->m2.
 int launch_far_mass(bh_context* ctx);
+// Waits for the context's stream and turns a raised device error word into
+// a status (clearing the word).
+int finish(bh_context* ctx, const char* fn);
+// Positions and G m of the bodies with id < num_direct (ctx->direct, by id).
+int launch_direct_extract(bh_context* ctx, double G);
 
 int launch_traverse(bh_context* ctx, double theta, double G, double soft2, int mode, double kick_h);
 int launch_traverse_masked(bh_context* ctx, double theta, double G, double soft2, double kick_h, bool fp64);

@@ -19,7 +19,7 @@
 // walk at theta accepts.
 //
 // BH_MODE_FP64_LIST: per-lane tests in FP64 with the reference's rounding,
-//   interactions in FP64 (rsqrt + FMA) from the FP64 node records, on the
+//   interactions in FP64 (rsqrt_hh + FMA) from the FP64 node records, on the
 //   reference's tree.
 // BH_MODE_FP32_FAR: precision form.  The bodies with id < num_direct (Sun and
 //   planets) are taken out of the tree (masses zeroed before the build) and
@@ -227,7 +227,7 @@ __global__ void __launch_bounds__(kThreads) traverse_masked_kernel(FParams p)
             if (!p.present[kk] || my_id == (uint64_t)kk) continue;
             const double dx = p.direct[4 * kk] - x, dy = p.direct[4 * kk + 1] - y, dz = p.direct[4 * kk + 2] - z;
             const double r2 = fma(dx, dx, fma(dy, dy, fma(dz, dz, soft2)));
-            const double inv = rsqrt(r2);
+            const double inv = rsqrt_hh(r2);
             const double sc = p.direct[4 * kk + 3] * (inv * inv * inv);
             adx = fma(sc, dx, adx);
             ady = fma(sc, dy, ady);
@@ -292,7 +292,7 @@ __global__ void __launch_bounds__(kThreads) traverse_masked_kernel(FParams p)
             unsigned M = 0, A = 0;
             int nc = 0, ref = 0, depth = 0;
             bool leaf = false, mixed = false, cand = false;
-            float dmin2 = 0.f, dmax2 = 0.f, s2 = 0.f;
+            float dmin2 = 0.f, dmax2 = 0.f, s2 = 0.f, nerr = 0.f;
             float4 e = make_float4(0.f, 0.f, 0.f, 0.f);
             if (lane < k) {
                 node = f_r + (lane - s_r);
@@ -322,6 +322,7 @@ __global__ void __launch_bounds__(kThreads) traverse_masked_kernel(FParams p)
                     nc = (int)(mt & 0xFF);
                     // Absolute error of the FP32 group-relative distances.
                     const float err = kAbsErr * (fmaxf(fabsf(cx), fmaxf(fabsf(cy), fabsf(cz))) + bmag);
+                    nerr = err;
                     const float dlo = fmaxf(sqrtf(dmin2) - err, 0.0f), dhi = sqrtf(dmax2) + err;
                     if (s2 * (1.0f + kMargin) < theta2f * dlo * dlo) {
                         A = M;
@@ -407,12 +408,28 @@ __global__ void __launch_bounds__(kThreads) traverse_masked_kernel(FParams p)
                 const int dj = __shfl_sync(0xffffffffu, depth, j);
                 bool acc = false;
                 if (kFP64) {
+                    // Each lane's FP64 test (the reference's rounding) decides
+                    // only where the FP32 distance, with the same error
+                    // allowance as the group tests, cannot.
                     const int nj = __shfl_sync(0xffffffffu, node, j);
-                    const TreeRec r = p.rec[nj];
-                    const double dx = __dsub_rn(r.cx, x), dy = __dsub_rn(r.cy, y), dz = __dsub_rn(r.cz, z);
-                    const double r2 = __dadd_rn(
-                        __dadd_rn(__dadd_rn(__dmul_rn(dx, dx), __dmul_rn(dy, dy)), __dmul_rn(dz, dz)), soft2);
-                    acc = sm.side2d[dj] < __dmul_rn(theta2, r2);
+                    const float cx = __shfl_sync(0xffffffffu, e.x, j);
+                    const float cy = __shfl_sync(0xffffffffu, e.y, j);
+                    const float cz = __shfl_sync(0xffffffffu, e.z, j);
+                    const float ej = 2.0f * __shfl_sync(0xffffffffu, nerr, j);
+                    const float dxf = cx - rx, dyf = cy - ry, dzf = cz - rz;
+                    const float df = sqrtf(dxf * dxf + dyf * dyf + dzf * dzf);
+                    const float lo = fmaxf(df - ej, 0.0f), hi = df + ej;
+                    const float s2j = sm.side2f[dj], sf = (float)soft2;
+                    const bool sure_acc = s2j * (1.0f + kMargin) < theta2f * (lo * lo + sf);
+                    const bool sure_rej = s2j * (1.0f - kMargin) > theta2f * (hi * hi + sf * (1.0f + kMargin));
+                    acc = sure_acc;
+                    if (((Mj >> lane) & 1u) && !sure_acc && !sure_rej) {
+                        const TreeRec r = p.rec[nj];
+                        const double dx = __dsub_rn(r.cx, x), dy = __dsub_rn(r.cy, y), dz = __dsub_rn(r.cz, z);
+                        const double r2 = __dadd_rn(
+                            __dadd_rn(__dadd_rn(__dmul_rn(dx, dx), __dmul_rn(dy, dy)), __dmul_rn(dz, dz)), soft2);
+                        acc = sm.side2d[dj] < __dmul_rn(theta2, r2);
+                    }
                 } else {
                     const float cx = __shfl_sync(0xffffffffu, e.x, j);
                     const float cy = __shfl_sync(0xffffffffu, e.y, j);
@@ -475,7 +492,7 @@ __global__ void __launch_bounds__(kThreads) traverse_masked_kernel(FParams p)
                         take = r.top <= kMaxDepth - 1 && sm.side2d[kMaxDepth - 1] < __dmul_rn(theta2, r2e);
                     }
                     const double r2 = fma(dx, dx, fma(dy, dy, fma(dz, dz, soft2)));
-                    const double inv = rsqrt(r2);
+                    const double inv = rsqrt_hh(r2);
                     double sc = (G * r.m) * (inv * inv * inv);
                     if (!take) sc = 0.0;
                     adx = fma(sc, dx, adx);
@@ -582,6 +599,17 @@ int launch_far_mass(bh_context* ctx)
     return BH_OK;
 }
 
+int launch_direct_extract(bh_context* ctx, double G)
+{
+    const int nd = ctx->num_direct < 64 ? ctx->num_direct : 64;
+    if (ctx->n == 0 || nd <= 0) return BH_OK;
+    BH_CUDA_TRY(cudaMemsetAsync(ctx->direct_present, 0, sizeof(int32_t) * 64, ctx->stream));
+    direct_extract_kernel<<<grid_n(ctx->n), 256, 0, ctx->stream>>>(ctx->n, ctx->px, ctx->py, ctx->pz, ctx->m, ctx->id,
+                                                                   nd, G, ctx->direct, ctx->direct_present);
+    BH_LAUNCH_CHECK(ctx);
+    return BH_OK;
+}
+
 // Prepares the FP32 node records and the direct bodies and fills the walk's
 // parameters (kick_h and the learned/collection fields are the caller's).
 int prepare_walk(bh_context* ctx, double theta, double G, double soft2, bool fp64, FParams& p)
@@ -591,10 +619,8 @@ int prepare_walk(bh_context* ctx, double theta, double G, double soft2, bool fp6
     fp32_nodes_kernel<<<grid_n(2 * n), 256, 0, ctx->stream>>>(ctx->counts, ctx->rec, G, ctx->fA, ctx->fB, ctx->fmeta);
     BH_LAUNCH_CHECK(ctx);
     if (nd > 0) {
-        BH_CUDA_TRY(cudaMemsetAsync(ctx->direct_present, 0, sizeof(int32_t) * 64, ctx->stream));
-        direct_extract_kernel<<<grid_n(n), 256, 0, ctx->stream>>>(n, ctx->px, ctx->py, ctx->pz, ctx->m, ctx->id, nd, G,
-                                                                  ctx->direct, ctx->direct_present);
-        BH_LAUNCH_CHECK(ctx);
+        int rc = launch_direct_extract(ctx, G);
+        if (rc) return rc;
     }
     p = FParams{};
     p.n = n;

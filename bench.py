@@ -21,6 +21,16 @@ and seeded (the reference's 300k CSV is not part of its repository).
   device.
 * cpu_baseline: the oracle (C restatement of the reference's path, OpenMP,
   every host core) on the same workload, a bounded number of steps.
+* hbm_phases: achieved GB/s of the data-movement phases (algorithmic bytes
+  per body / phase time) against the measured HBM copy bandwidth.
+* the benchmark spec: 4M bodies (85/10/5 with trojans), plain FP64 theta = 1.05
+  against FP32 far field and FP32 + learned criterion (network trained first
+  on 20 seeded 1M-body systems, ~10M pairs, by the engine's GPU kernels).
+* learned_eval: the learned criterion on 5 unseen 1M-body systems at budgets
+  {1e-4, 1e-5, 1e-6} with its fallback rate.
+* precision_run: the FP32 far-field form on 1M bodies at theta {0.5, 0.8,
+  1.05}, then 1,000 steps with error, energy and angular-momentum drift every
+  100 steps.  --no-north-star skips these three blocks.
 
 Multi-GPU: the path does not shard on one GPU per rank; ranks run replicas
 (weak scaling) and value is the sum of their body-steps over the slowest
@@ -38,6 +48,7 @@ import subprocess
 import sys
 import threading
 import time
+from pathlib import Path
 from pathlib import Path
 
 import numpy as np
@@ -81,9 +92,12 @@ def parse():
     ap.add_argument("--cpu-seconds", type=float, default=15.0, help="budget of the CPU-baseline sample")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-north-star", action="store_true",
-                    help="skip the 4M-body comparison of the FP32+learned form against plain FP64")
+                    help="skip the 4M-body comparison, the learned evaluation and the 1M precision run")
     ap.add_argument("--ns-bodies", type=int, default=4_000_000)
     ap.add_argument("--ns-steps", type=int, default=3)
+    ap.add_argument("--train-pairs", type=int, default=10_000_000, help="learned criterion: training pairs")
+    ap.add_argument("--pr-bodies", type=int, default=1_000_000, help="precision run: bodies")
+    ap.add_argument("--pr-steps", type=int, default=1000, help="precision run: steps at theta=1.05")
     ap.add_argument("--theta-max", type=float, default=3.0, help="learned criterion: candidate range")
     ap.add_argument("--budget", type=float, default=1e-7, help="learned criterion: per-node error threshold")
     return ap.parse_args()
@@ -240,7 +254,133 @@ def time_steps(ctx, ext, flush, mode, theta, steps, warmup, t=0.0):
     return sum(ms) / len(ms), ctx.interaction_count() / ctx.n
 
 
-def north_star(args, dev):
+def train_model(args):
+    """The learned criterion's network, trained by the engine's own GPU
+    kernels on pairs labelled by the plain walk at theta = 0.5: 20 seeded
+    1M-body systems (10 with the 90/10 inner/outer belt mix, 10 with the
+    85/10/5 mix that adds trojans), about 10M pairs."""
+    learned = importlib.import_module("barnes-hut_gb300.learned")
+    t0 = time.perf_counter()
+    nb = min(args.ns_bodies, 1_000_000)
+    half = args.train_pairs // 2
+    F1, L1 = learned.collect_pairs(range(9001, 9011), nb, 0.10, 0.0, theta_max=args.theta_max, max_pairs=half)
+    F2, L2 = learned.collect_pairs(range(9011, 9021), nb, 0.10, 0.05, theta_max=args.theta_max, max_pairs=half)
+    F = np.concatenate([F1, F2]); L = np.concatenate([L1, L2])
+    bh = importlib.import_module("barnes-hut_gb300")
+    params, scale, losses = bh.mlp_train(F, L, epochs=6, batch=4096, lr=2e-3, seed=0)
+    info = {"pairs": int(len(L)), "systems": 20, "system_bodies": nb, "epochs": 6,
+            "final_loss": float(losses[-1]), "seconds": time.perf_counter() - t0, "label_theta": 0.5,
+            "theta_max": args.theta_max, "seeds": "9001-9020"}
+    return params, scale, info
+
+
+def _sample_error(ctx, n, G_):
+    rng = np.random.default_rng(0)
+    sample = np.sort(rng.choice(n, min(n, 4096), replace=False))
+    ref = ctx.direct_sum(sample, G_)
+
+    def err(a):
+        e = np.linalg.norm(a[sample] - ref, axis=1) / np.linalg.norm(ref, axis=1)
+        return float(np.median(e)), float(np.quantile(e, 0.99))
+    return err
+
+
+def _fresh(ctx, pos, vel, mass, ids):
+    ctx.set_bodies(pos, vel, mass, ids)
+    ctx.compute_bbox(); ctx.compute_keys(); ctx.sort_bodies(); ctx.build_tree()
+
+
+def precision_run(args, dev):
+    """The precision form on 1M bodies (90/10 inner/outer belt): FP32 far field
+    with FP64 displacements, direct terms and state.  Error against the FP64
+    direct sum at theta in {0.5, 0.8, 1.05}; then a run of --pr-steps steps at
+    theta = 1.05 with the error on the 4,096-body sample and the energy and
+    angular momentum every 100 steps."""
+    import torch
+    bh = importlib.import_module("barnes-hut_gb300")
+    n = args.pr_bodies
+    pos, vel, mass, ids = bh.generate_system(SEED + 2, n, 0.10, 0.0)
+    out = {"workload": f"{n:,} bodies (Sun, 8 planets, 90% inner belt, 10% outer belt), fp32 far field, dt=1h"}
+    with bh.Context(n, dev) as ctx:
+        ext = torch.cuda.ExternalStream(ctx.stream(), device=dev)
+        flush = torch.empty(L2_FLUSH_BYTES // 4, dtype=torch.float32, device=f"cuda:{dev}")
+        _fresh(ctx, pos, vel, mass, ids)
+        err = _sample_error(ctx, n, G)
+        thetas = {}
+        for th in (0.5, 0.8, 1.05):
+            _fresh(ctx, pos, vel, mass, ids)
+            med, p99 = err(ctx.compute_accelerations(th, G, 0.0, bh.MODE_FP32_FAR))
+            ctx.set_bodies(pos, vel, mass, ids)
+            ms, ipb = time_steps(ctx, ext, flush, bh.MODE_FP32_FAR, th, 3, 2)
+            thetas[f"{th:g}"] = {"median_rel_err": med, "p99_rel_err": p99, "ms_per_step": ms,
+                                 "body_steps_per_s": n / (ms * 1e-3), "interactions_per_body": ipb}
+        out["theta"] = thetas
+        ctx.set_bodies(pos, vel, mass, ids)
+        inv0 = ctx.invariants(G, THETA)
+        series = []
+        t, done = 0.0, 0
+        t0 = time.perf_counter()
+        while done < args.pr_steps:
+            k = min(100, args.pr_steps - done)
+            t = ctx.step(DT, THETA, G, k, bh.MODE_FP32_FAR, t=t)
+            done += k
+            inv = ctx.invariants(G, THETA)
+            rng = np.random.default_rng(done)
+            sample = np.sort(rng.choice(n, 4096, replace=False))
+            ref = ctx.direct_sum(sample, G)
+            a = ctx.compute_accelerations(THETA, G, 0.0, bh.MODE_FP32_FAR)
+            e = np.linalg.norm(a[sample] - ref, axis=1) / np.linalg.norm(ref, axis=1)
+            series.append({"step": done, "median_rel_err": float(np.median(e)),
+                           "p99_rel_err": float(np.quantile(e, 0.99)),
+                           "rel_energy_drift": float((inv["E"] - inv0["E"]) / abs(inv0["E"])),
+                           "rel_angular_momentum_drift": float(np.linalg.norm(inv["L"] - inv0["L"]) /
+                                                               np.linalg.norm(inv0["L"]))})
+        out["run"] = {"steps": done, "seconds": time.perf_counter() - t0, "every_100_steps": series,
+                      "energy": "K exact; U: pairs with the Sun or a planet exact in FP64, the rest through the tree"}
+    return out
+
+
+def learned_eval(args, dev, params, scale):
+    """The learned criterion on 5 unseen 1M-body systems (90/10 mix) at
+    per-node error budgets {1e-4, 1e-5, 1e-6}, theta = 1.05 the fallback,
+    against the FP32 walk with the theta criterion alone on the same state."""
+    import torch
+    bh = importlib.import_module("barnes-hut_gb300")
+    n = min(args.ns_bodies, 1_000_000)
+    rows = []
+    with bh.Context(n, dev) as ctx:
+        ext = torch.cuda.ExternalStream(ctx.stream(), device=dev)
+        flush = torch.empty(L2_FLUSH_BYTES // 4, dtype=torch.float32, device=f"cuda:{dev}")
+        for seed in range(9101, 9106):
+            pos, vel, mass, ids = bh.generate_system(seed, n, 0.10, 0.0)
+            _fresh(ctx, pos, vel, mass, ids)
+            err = _sample_error(ctx, n, G)
+            row = {"seed": seed}
+            cases = [("theta_only", bh.MODE_FP32_FAR, None)]
+            cases += [(f"budget_{b:g}", bh.MODE_LEARNED, b) for b in (1e-4, 1e-5, 1e-6)]
+            for name, mode, budget in cases:
+                if budget is not None:
+                    ctx.learned_set_model(params, scale, budget=budget, theta_max=args.theta_max)
+                _fresh(ctx, pos, vel, mass, ids)
+                med, p99 = err(ctx.compute_accelerations(THETA, G, 0.0, mode))
+                r = {"median_rel_err": med, "p99_rel_err": p99}
+                if budget is not None:
+                    st = ctx.learned_stats()
+                    r["fallback_rate"] = st["fallback"] / max(1, st["candidates"])
+                ctx.set_bodies(pos, vel, mass, ids)
+                ms, ipb = time_steps(ctx, ext, flush, mode, THETA, 2, 1)
+                r.update({"ms_per_step": ms, "interactions_per_body": ipb})
+                row[name] = r
+            rows.append(row)
+    summary = {}
+    for name in ("theta_only", "budget_0.0001", "budget_1e-05", "budget_1e-06"):
+        summary[name] = {k: float(np.mean([r[name][k] for r in rows]))
+                         for k in rows[0][name] if k != "seed"}
+    return {"workload": f"{n:,} bodies (90/10), 5 unseen seeds 9101-9105, theta=1.05 fallback",
+            "mean_over_seeds": summary, "per_seed": rows}
+
+
+def north_star(args, dev, params, scale, info):
     """The 4M-body combined-scale system (85 % inner belt, 10 % outer belt, 5 %
     trojans): plain FP64 theta=1.05 (fp64_list: the reference's interaction
     set in FP64) against FP32 far field and FP32 + learned criterion, each
@@ -248,40 +388,25 @@ def north_star(args, dev):
     sample (evaluated on the same initial state)."""
     import torch
     bh = importlib.import_module("barnes-hut_gb300")
-    from importlib import import_module
-    learned = import_module("barnes-hut_gb300.learned")
     n = args.ns_bodies
-    t0 = time.perf_counter()
-    params, scale, losses, npairs = learned.train(seeds=range(9001, 9005), n_bodies=min(n, 1_000_000), epochs=6,
-                                                  theta_max=args.theta_max, max_pairs=4_000_000)
-    train_s = time.perf_counter() - t0
     pos, vel, mass, ids = bh.generate_system(SEED + 1, n, 0.10, 0.05)
     out = {"workload": f"{n:,} bodies (Sun, 8 planets, 85% inner belt, 10% outer belt, 5% trojans), theta=1.05, dt=1h",
-           "training": {"pairs": npairs, "systems": 4, "system_bodies": min(n, 1_000_000), "epochs": 6,
-                        "final_loss": float(losses[-1]), "seconds": train_s, "label_theta": 0.5,
-                        "theta_max": args.theta_max}}
+           "training": info}
     with bh.Context(n, dev) as ctx:
         ext = torch.cuda.ExternalStream(ctx.stream(), device=dev)
         flush = torch.empty(L2_FLUSH_BYTES // 4, dtype=torch.float32, device=f"cuda:{dev}")
-        ctx.set_bodies(pos, vel, mass, ids)
-        ctx.compute_bbox(); ctx.compute_keys(); ctx.sort_bodies(); ctx.build_tree()
-        rng = np.random.default_rng(0)
-        sample = np.sort(rng.choice(n, 4096, replace=False))
-        ref = ctx.direct_sum(sample, G)
-
-        def err(a):
-            e = np.linalg.norm(a[sample] - ref, axis=1) / np.linalg.norm(ref, axis=1)
-            return float(np.median(e)), float(np.quantile(e, 0.99))
-
+        _fresh(ctx, pos, vel, mass, ids)
+        err = _sample_error(ctx, n, G)
         rows = {}
         cases = [("plain_fp64", bh.MODE_FP64_LIST, None), ("fp32_far", bh.MODE_FP32_FAR, None)]
         cases += [(f"fp32_learned_budget_{b:g}", bh.MODE_LEARNED, b) for b in (1e-4, 1e-5, 1e-6, 1e-7)]
         for name, mode, budget in cases:
             if budget is not None:
                 ctx.learned_set_model(params, scale, budget=budget, theta_max=args.theta_max)
-            ctx.set_bodies(pos, vel, mass, ids)
-            ctx.compute_bbox(); ctx.compute_keys(); ctx.sort_bodies(); ctx.build_tree()
+            _fresh(ctx, pos, vel, mass, ids)
+            ctx.set_profiling(True)
             a = ctx.compute_accelerations(THETA, G, 0.0, mode)
+            ctx.set_profiling(False)
             med, p99 = err(a)
             row = {"median_rel_err": med, "p99_rel_err": p99}
             if budget is not None:
@@ -289,9 +414,16 @@ def north_star(args, dev):
                 row["fallback_rate"] = st["fallback"] / max(1, st["candidates"])
                 row["network_accept_rate"] = st["accepted"] / max(1, st["candidates"])
             ctx.set_bodies(pos, vel, mass, ids)
+            ctx.set_profiling(True)
             ms, ipb = time_steps(ctx, ext, flush, mode, THETA, args.ns_steps, 2)
-            row.update({"ms_per_step": ms, "body_steps_per_s": n / (ms * 1e-3), "interactions_per_body": ipb})
+            phases, _ = ctx.phase_times()
+            ctx.set_profiling(False)
+            steps = args.ns_steps + 2
+            row.update({"ms_per_step": ms, "body_steps_per_s": n / (ms * 1e-3), "interactions_per_body": ipb,
+                        "phases_ms_per_step": {k: v / steps for k, v in phases.items()}})
             rows[name] = row
+        # HBM figures of the data-movement phases at this size (fp32 step)
+        out["hbm_phases"] = hbm_phases(rows["fp32_far"]["phases_ms_per_step"], n)
     base = rows["plain_fp64"]
     out["forms"] = rows
     eligible = [k for k, r in rows.items() if k.startswith("fp32_learned") and
@@ -299,6 +431,33 @@ def north_star(args, dev):
     best = max(eligible, key=lambda k: rows[k]["body_steps_per_s"]) if eligible else None
     out["best_learned_at_equal_or_lower_error"] = best
     out["speedup_vs_plain_fp64"] = (rows[best]["body_steps_per_s"] / base["body_steps_per_s"]) if best else None
+    return out
+
+
+# DRAM traffic per launch of the force kernel (dram__bytes_read.sum +
+# dram__bytes_write.sum) from one ncu --set full capture of that kernel on
+# that workload, keyed by (mode, bodies).
+TRAFFIC_BYTES = {("fp64_list", 300_149): 51.66e6 + 1.15e6}
+
+# Algorithmic bytes per body of the HBM-bound phases: the minimum traffic of
+# each phase's work (reads + writes of its inputs and outputs once).
+PHASE_BYTES = {"kick_drift_bbox": 120, "keys": 32, "sort": 200, "permute": 128, "build": 136}
+
+
+def hbm_peak_gbs():
+    try:
+        return float(json.loads((Path(__file__).resolve().parent / "MEASURED_PEAKS.json").read_text())["hbm_gbs"])
+    except (OSError, KeyError, ValueError):
+        return 6800.0
+
+
+def hbm_phases(phases_ms, n):
+    peak = hbm_peak_gbs()
+    out = {}
+    for k, b in PHASE_BYTES.items():
+        if k in phases_ms and phases_ms[k] > 0:
+            gbs = b * n / (phases_ms[k] * 1e-3) / 1e9
+            out[k] = {"bytes_per_body": b, "ms": phases_ms[k], "achieved_gbs": gbs, "frac_of_measured_hbm": gbs / peak}
     return out
 
 
@@ -315,9 +474,7 @@ def run_ours(args, rank, ws, local):
     ext = torch.cuda.ExternalStream(ctx.stream(), device=dev)
     flush = torch.empty(L2_FLUSH_BYTES // 4, dtype=torch.float32, device=f"cuda:{dev}")
     if mode == bh.MODE_LEARNED:
-        learned = importlib.import_module("barnes-hut_gb300.learned")
-        params, scale, _, _ = learned.train(seeds=range(9001, 9005), n_bodies=min(n, 1_000_000), epochs=6,
-                                            theta_max=args.theta_max, max_pairs=4_000_000)
+        params, scale, _ = train_model(args)
         ctx.learned_set_model(params, scale, budget=args.budget, theta_max=args.theta_max)
     ctx.set_bodies(pos, vel, mass, ids)
     t = 0.0
@@ -375,9 +532,12 @@ def run_ours(args, rank, ws, local):
     accuracy = {"median_rel_err": float(np.median(err)), "p99_rel_err": float(np.quantile(err, 0.99)),
                 "sample": int(len(sample)), "judge": "FP64 direct sum"}
 
-    ns = None
+    ns = pr = le = None
     if rank == 0 and ws == 1 and not args.no_north_star:
-        ns = north_star(args, dev)
+        params, scale, info = train_model(args)
+        ns = north_star(args, dev, params, scale, info)
+        le = learned_eval(args, dev, params, scale)
+        pr = precision_run(args, dev)
 
     cpu = None
     if rank == 0 and not args.no_cpu_baseline:
@@ -403,8 +563,10 @@ def run_ours(args, rank, ws, local):
                      "peak": peak, "unit": "TFLOP/s", "frac": achieved / peak,
                      "peak_source": f"measured in-process: {fp.upper()} FMA chains (bh_measure_fma_peak)",
                      "work": f"{FLOPS_PER_INTERACTION} flops x {inter_per_step:.4g} interactions per launch",
-                     "traffic": None},
+                     "traffic": TRAFFIC_BYTES.get((args.mode, n)),
+                     "traffic_unit": "bytes per launch (ncu)"},
         "phases_ms_per_step": {kk: v / k for kk, v in phases.items()},
+        "hbm_phases": hbm_phases({kk: v / k for kk, v in phases.items()}, n),
         "interactions_per_body": inter_per_step / n,
         "accuracy": accuracy,
         "e2e": {"value": ws * n * e2e_steps / e2e_s, "unit": "body-steps/s", "h2d_bytes_per_step": h2d,
@@ -413,6 +575,8 @@ def run_ours(args, rank, ws, local):
         "clocks": clk.summary(),
         "cpu_baseline": cpu,
         "north_star": ns,
+        "learned_eval": le,
+        "precision_run": pr,
     }
     print(json.dumps(line), flush=True)
 

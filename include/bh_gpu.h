@@ -181,10 +181,13 @@ int bh_measure_fma_peak(bh_context *ctx, int fp64, double *tflops_out);
 /* FP64 direct sum over all bodies for the bodies at positions targets[k]
  * of the current order; acc_out: ns*3. */
 int bh_direct_sum(bh_context *ctx, int64_t ns, const int64_t *targets, double G, double *acc_out);
-/* Kinetic energy, potential energy (pairs with at least one of the first
- * BH_NUM_MASSIVE bodies by id exact in FP64, all other pairs through the
- * tree monopoles at theta), total linear and angular momentum.
- * out = {E, K, U, Lx, Ly, Lz, Px, Py, Pz}. */
+/* Kinetic energy, potential energy, total angular and linear momentum,
+ * out = {E, K, U, Lx, Ly, Lz, Px, Py, Pz}.  theta = 0: U is the exact FP64
+ * pair sum (at most 131,072 bodies).  theta > 0: pairs with at least one of
+ * the massive bodies (id < BH_NUM_MASSIVE) are exact in FP64 and all other
+ * pairs go through the monopoles of the tree of the current positions that
+ * the force walk's criterion at theta accepts (any N; the tree is built when
+ * none is current, which re-sorts the bodies). */
 int bh_invariants(bh_context *ctx, double G, double theta, double out[9]);
 
 /* ---- learned acceptance (no reference counterpart) ------------------- */
