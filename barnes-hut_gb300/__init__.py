@@ -93,6 +93,8 @@ def _sig(lib):
     f["bh_measure_fma_peak"] = (C.c_int, [_P, C.c_int, C.POINTER(_D)])
     f["bh_direct_sum"] = (C.c_int, [_P, _I64, _P, _D, _P])
     f["bh_invariants"] = (C.c_int, [_P, _D, _D, _P])
+    f["bh_tree_spread"] = (C.c_int, [_P, _P])
+    f["bh_tree_slots"] = (C.c_int, [_P, _P, _P])
     f["bh_mlp_gradient"] = (C.c_int, [_P, _P, _P, _I64, _P, _P])
     f["bh_mlp_train"] = (C.c_int, [_P, _P, _I64, C.c_int, C.c_int, C.c_float, C.c_uint64, _P, _P, _P])
     f["bh_mlp_predict"] = (C.c_int, [_P, _P, _P, _I64, _P, _P])
@@ -267,6 +269,20 @@ class Context:
         r, nn, nl = _I64(0), _I64(0), _I64(0)
         _check(library().bh_tree_info(self._h, C.byref(r), C.byref(nn), C.byref(nl)))
         return {"records": r.value, "nodes": nn.value, "leaves": nl.value}
+
+    def tree_slots(self):
+        """(prefix u64, depth u8) of the reference cell each device node
+        stands for (the deepest cell of its single-child chain)."""
+        k = self.tree_info()["nodes"]
+        p = np.empty(k, np.uint64); d = np.empty(k, np.uint8)
+        _check(library().bh_tree_slots(self._h, _ptr(p), _ptr(d)))
+        return p, d
+
+    def tree_spread(self) -> np.ndarray:
+        """sqrt(Q/m) of the far-field masses per node (bh_tree_slots order)."""
+        out = np.empty(self.tree_info()["nodes"], np.float32)
+        _check(library().bh_tree_spread(self._h, _ptr(out)))
+        return out
 
     def export_tree(self):
         """The reference's node set sorted by (depth, prefix):

@@ -643,6 +643,25 @@ int bh_tree_slots(bh_context* ctx, uint64_t* prefix, uint8_t* depth)
     return BH_OK;
 }
 
+int bh_tree_spread(bh_context* ctx, float* spread)
+{
+    int rc = check_ctx(ctx, "bh_tree_spread");
+    if (rc) return rc;
+    if (!ctx->tree_valid) return ctx->n == 0 ? BH_OK : bh_fail(BH_ERR_STATE, "bh_tree_spread: no tree built");
+    if (!spread) return bh_fail(BH_ERR_INVALID_ARGUMENT, "bh_tree_spread: null array");
+    if (!ctx->tree_far || !ctx->tree_moments) {
+        if ((rc = bh::launch_far_mass(ctx)) || (rc = bh::launch_build(ctx, ctx->m2, true))) return rc;
+        ctx->tree_far = ctx->tree_moments = true;
+    }
+    int32_t S = 0;
+    BH_CUDA_TRY(cudaMemcpyAsync(ctx->h_small, ctx->counts + 2, sizeof(int32_t), cudaMemcpyDeviceToHost, ctx->stream));
+    BH_CUDA_TRY(cudaStreamSynchronize(ctx->stream));
+    std::memcpy(&S, ctx->h_small, sizeof(int32_t));
+    if (S > 0)
+        BH_CUDA_TRY(cudaMemcpyAsync(spread, ctx->fspread, sizeof(float) * S, cudaMemcpyDeviceToHost, ctx->stream));
+    return finish(ctx, "bh_tree_spread");
+}
+
 int bh_tree_set_slot_values(bh_context* ctx, const double* mass, const double* com)
 {
     int rc = check_ctx(ctx, "bh_tree_set_slot_values");

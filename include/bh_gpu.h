@@ -147,6 +147,12 @@ int bh_tree_slots(bh_context *ctx, uint64_t *prefix, uint8_t *depth);
  * caller changed (the reference's computeAccelerations reads the map it is
  * given).  No reference counterpart. */
 int bh_tree_set_slot_values(bh_context *ctx, const double *mass, const double *com);
+/* The learned criterion's spread feature per node (n_nodes floats, in the
+ * order of bh_tree_slots): sqrt(Q / m) with Q = sum m_i |x_i - com|^2 over
+ * the node's bodies, for the far-field masses (bodies with id <
+ * BH_NUM_MASSIVE zeroed); 0 for a massless node.  Computes the second-moment
+ * pass when the tree in place lacks it.  No reference counterpart. */
+int bh_tree_spread(bh_context *ctx, float *spread);
 /* computeAccelerations (src/traversal.cpp:13-103, include/traversal.h:21-30)
  * over the last tree; `mode` is a bh_mode.  acc_out (may be NULL) receives
  * the accelerations in the current body order. */

@@ -90,3 +90,36 @@ def test_fp32_far_interaction_set_tracks_per_body_theta(bh, system, port):
     c32 = ctx.interaction_counts().astype(np.int64)
     assert np.all(c32 > 0)
     assert abs(c32.sum() / c64.sum() - 1) < 0.15
+
+
+def test_second_moment_spread_matches_fp64(bh):
+    """The second-moment pass (learned features): per device node,
+    sqrt(Q/m) of the far-field masses, Q = sum m |x - com|^2 over the
+    node's bodies, against an FP64 sum over the same bodies (the FP32
+    result: 1e-5 relative)."""
+    pos, vel, mass, ids = bh.generate_system(31, 3000, 0.1, 0.05)
+    with bh.Context(3000) as c:
+        c.set_bodies(pos, vel, mass, ids)
+        c.compute_bbox(); keys = c.compute_keys(); c.sort_bodies(); c.build_tree()
+        prefix, depth = c.tree_slots()
+        spread = c.tree_spread()
+        p, _, m, i, _ = c.get_bodies()
+    sk = np.sort(keys, kind="stable")
+    mf = np.where(i < 9, 0.0, m)
+    checked = 0
+    for s in range(len(prefix)):
+        d = int(depth[s])
+        lo = np.searchsorted(sk, prefix[s], side="left")
+        hi = np.searchsorted(sk, prefix[s] + (np.uint64(1) << np.uint64(63 - 3 * d)), side="left") \
+            if d > 0 else len(sk)
+        w = mf[lo:hi]
+        M = w.sum()
+        if M == 0:
+            assert spread[s] == 0.0
+            continue
+        com = (w[:, None] * p[lo:hi]).sum(axis=0) / M
+        q = (w * ((p[lo:hi] - com) ** 2).sum(axis=1)).sum()
+        ref = np.sqrt(q / M)
+        assert abs(spread[s] - ref) <= 1e-5 * ref + 1e-12 * np.abs(com).max(), (s, d, spread[s], ref)
+        checked += 1
+    assert checked > 2000
