@@ -94,6 +94,7 @@ def _sig(lib):
     f["bh_direct_sum"] = (C.c_int, [_P, _I64, _P, _D, _P])
     f["bh_invariants"] = (C.c_int, [_P, _D, _D, _P])
     f["bh_tree_spread"] = (C.c_int, [_P, _P])
+    f["bh_selftest"] = (C.c_int, [C.c_int, _I64, C.c_uint64, C.POINTER(_I64)])
     f["bh_tree_slots"] = (C.c_int, [_P, _P, _P])
     f["bh_mlp_gradient"] = (C.c_int, [_P, _P, _P, _I64, _P, _P])
     f["bh_mlp_train"] = (C.c_int, [_P, _P, _I64, C.c_int, C.c_int, C.c_float, C.c_uint64, _P, _P, _P])
@@ -162,6 +163,13 @@ def generate_system(seed: int, n: int, frac_outer: float = 0.1, frac_trojan: flo
     _check(library().bh_generate_system(seed, n, frac_outer, frac_trojan, _ptr(pos), _ptr(vel), _ptr(mass),
                                         _ptr(ids)))
     return pos, vel, mass, ids
+
+
+def selftest(which: int, n: int, seed: int = 1) -> int:
+    """Mismatches of a hot-path arithmetic helper against IEEE (bh_selftest)."""
+    f = _I64(0)
+    _check(library().bh_selftest(int(which), int(n), int(seed), C.byref(f)))
+    return f.value
 
 
 def read_csv(path, body_count: int = -1):

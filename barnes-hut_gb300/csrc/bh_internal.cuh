@@ -71,6 +71,84 @@ __device__ __forceinline__ double rsqrt_hh(double x)
     return fma(y0, t, y0);
 }
 
+// norm + quantise of generateMortonCodes (src/morton_keys.cpp:77-94):
+// t = (v - lo)/span clamped to [0, 1 - 2^-53], then (uint32)(t * 2^21).
+__device__ inline uint32_t quantise_exact(double v, double lo, double span)
+{
+    double t = __ddiv_rn(__dsub_rn(v, lo), span);
+    if (t <= 0.0) t = 0.0;
+    else if (t >= 1.0) t = __longlong_as_double(0x3FEFFFFFFFFFFFFFll);  // nextafter(1, 0)
+    return __double2uint_rz(__dmul_rn(t, 2097152.0));
+}
+
+// The same integer with two FP64 operations in nearly every case (FP64 runs
+// at 1/64 of the FP32 rate here, comparisons included).  inv21 is
+// RN(1/span) 2^21, so u = RN(d inv21) = RN(d RN(1/span)) 2^21 exactly, within
+// 3 ulps (relative 3 2^-53) of t 2^21 with t = RN(d/span): the two differ by
+// less than 2^-30.  The integer and fractional parts of u come from its bits
+// (integer operations); where u lies in [2, 2^21 - 2] (no clamp) and its
+// fractional part is farther than 2^-24 from an integer, both truncate to the
+// same integer.  Elsewhere the IEEE division decides.
+__device__ inline uint32_t quantise(double v, double lo, double span, double inv21)
+{
+    const double u = __dmul_rn(__dsub_rn(v, lo), inv21);
+    const long long ub = __double_as_longlong(u);
+    const int ue = (int)(ub >> 52);  // the biased exponent for u > 0 (negative u: < 0)
+    if (ue >= 1024 && ue <= 1043) {  // 2 <= u < 2^21
+        const int sh = 1075 - ue;    // fraction bits of u: 32 .. 51
+        const unsigned long long mant = ((unsigned long long)ub & 0x000FFFFFFFFFFFFFull) | (1ull << 52);
+        const unsigned long long ip = mant >> sh;
+        const unsigned long long fr = mant & ((1ull << sh) - 1ull);
+        const unsigned long long lim = 1ull << (sh - 24);
+        if (ip <= (1ull << 21) - 3ull && fr > lim && fr < (1ull << sh) - lim) return (uint32_t)ip;
+    }
+    return quantise_exact(v, lo, span);
+}
+
+// RN((0 + RN(m c)) / m) for m > 0 with two FP64 operations in nearly every
+// case: the centre of mass after the single-rank merge
+// (linear_octree.cpp:194-202 with m0 = com0 = 0), and the centre of mass of a
+// one-body leaf ((0 + x m) / m, linear_octree.cpp:28-38,95-104).
+// p = RN(m c) and the product's rounding error e = p - m c are exact (the
+// error of a floating-point product is a double, and one FMA computes it:
+// the TwoProduct of Ogita, Rump and Oishi), so p / m = c + e / m with
+// |e / m| <= ulp(c).  The correctly rounded quotient is therefore c, or the
+// neighbour of c on the side of e, whichever is within ulp(c) / 2 of p / m:
+// |e| against m ulp(c) / 2, compared exactly on the bit patterns after
+// scaling |e| by a power of two (integer operations).  Powers of two
+// (uneven spacing below), exact ties and exponents outside 2^+-200 take the
+// IEEE division.
+__device__ inline double merge_div(double m, double c)
+{
+    const double p = __dmul_rn(m, c);
+    const long long cb = __double_as_longlong(c), mb = __double_as_longlong(m);
+    const int ce = (int)((cb >> 52) & 0x7FF), me = (int)((mb >> 52) & 0x7FF);
+    if (mb <= 0 || ce < 823 || ce > 1223 || me < 823 || me > 1223 || (cb & 0x000FFFFFFFFFFFFFll) == 0)
+        return __ddiv_rn(__dadd_rn(0.0, p), m);
+    const double e = fma(-c, m, p);
+    const long long eb = __double_as_longlong(e);
+    const long long ea = eb & 0x7FFFFFFFFFFFFFFFll;
+    if (ea == 0) return c;
+    // |e| 2^(1076 - ce) against m: |e| < m 2^(ce - 1076) = m ulp(c) / 2
+    const long long es = ea + ((long long)(1076 - ce) << 52);
+    if (es < mb) return c;
+    if (es > mb) return __longlong_as_double(((eb ^ cb) >= 0) ? cb + 1 : cb - 1);
+    return __ddiv_rn(__dadd_rn(0.0, p), m);
+}
+
+// 1/x to about 2^-60 relative (not correctly rounded): the FP32 estimate
+// refined by one second-order Newton step, y1 = y0 (1 + e + e^2) with
+// e = 1 - x y0.  For quantities that need no bit-exactness (the second
+// moments of the learned features).  Outside [2^-120, 2^120] the IEEE one.
+__device__ __forceinline__ double rcp_nr(double x)
+{
+    const double ax = fabs(x);
+    if (!(ax >= 0x1p-120 && ax <= 0x1p120)) return 1.0 / x;
+    const double y0 = (double)__frcp_rn(__double2float_rn(x));
+    const double e = fma(-x, y0, 1.0);
+    return fma(y0, fma(e, e, e), y0);
+}
+
 // One node of the compressed octree as the traversal reads it (48 bytes).
 // A node stands for the reference's chain of single-child nodes from depth
 // `top` down to `depth` (all with identical mass and centre of mass), so it

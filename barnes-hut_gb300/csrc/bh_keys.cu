@@ -132,15 +132,6 @@ __device__ inline uint64_t spread21(uint32_t v)
     return x;
 }
 
-// norm + quantise of generateMortonCodes (src/morton_keys.cpp:77-94):
-// t = (v - lo)/span clamped to [0, 1 - 2^-53], then (uint32)(t * 2^21).
-__device__ inline uint32_t quantise(double v, double lo, double span)
-{
-    double t = __ddiv_rn(__dsub_rn(v, lo), span);
-    if (t <= 0.0) t = 0.0;
-    else if (t >= 1.0) t = __longlong_as_double(0x3FEFFFFFFFFFFFFFll);  // nextafter(1, 0)
-    return __double2uint_rz(__dmul_rn(t, 2097152.0));
-}
 
 constexpr int kKeyThreads = 512;
 
@@ -158,11 +149,12 @@ __global__ void __launch_bounds__(kKeyThreads) keys_kernel(int64_t n, const doub
     const double s0 = (bbox[3] == lo0) ? 1.0 : __dsub_rn(bbox[3], lo0);
     const double s1 = (bbox[4] == lo1) ? 1.0 : __dsub_rn(bbox[4], lo1);
     const double s2 = (bbox[5] == lo2) ? 1.0 : __dsub_rn(bbox[5], lo2);
+    const double i0 = __drcp_rn(s0) * 2097152.0, i1 = __drcp_rn(s1) * 2097152.0, i2 = __drcp_rn(s2) * 2097152.0;
     __syncthreads();
     for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
-        const uint32_t xi = quantise(px[i], lo0, s0);
-        const uint32_t yi = quantise(py[i], lo1, s1);
-        const uint32_t zi = quantise(pz[i], lo2, s2);
+        const uint32_t xi = quantise(px[i], lo0, s0, i0);
+        const uint32_t yi = quantise(py[i], lo1, s1, i1);
+        const uint32_t zi = quantise(pz[i], lo2, s2, i2);
         const uint64_t k = spread21(xi) | (spread21(yi) << 1) | (spread21(zi) << 2);
         key[i] = k;
         if (with_hist) {

@@ -135,7 +135,8 @@ __global__ void leaf_sum_kernel(const int32_t* __restrict__ counts, const int32_
         if (kMoments) {
             double q = 0.0;
             if (b1 - b0 > 1 && sm > 0) {
-                const double cx = sx / sm, cy = sy / sm, cz = sz / sm;
+                const double is = rcp_nr(sm);
+                const double cx = sx * is, cy = sy * is, cz = sz * is;
                 for (int b = b0; b < b1; ++b) {
                     const double dx = px[b] - cx, dy = py[b] - cy, dz = pz[b] - cz;
                     q += m[b] * (dx * dx + dy * dy + dz * dz);
@@ -333,14 +334,16 @@ __global__ void monopole_level_kernel(int depth, const int32_t* __restrict__ dep
         if (kMoments) {
             double q = 0.0;
             if (sm > 0) {
-                const double gx = sx / sm, gy = sy / sm, gz = sz / sm;
+                const double is = rcp_nr(sm);
+                const double gx = sx * is, gy = sy * is, gz = sz * is;
                 for (int s = s0; s < s1; ++s) {
                     const int r = slot_ref[s];
                     double cm, wx, wy, wz, cq;
                     if (r >= 0) { cm = lm[r]; wx = lwx[r]; wy = lwy[r]; wz = lwz[r]; cq = lq[r]; }
                     else { const int c = ~r; cm = nm[c]; wx = nwx[c]; wy = nwy[c]; wz = nwz[c]; cq = nq[c]; }
                     if (cm > 0) {
-                        const double dx = wx / cm - gx, dy = wy / cm - gy, dz = wz / cm - gz;
+                        const double ic = rcp_nr(cm);
+                        const double dx = wx * ic - gx, dy = wy * ic - gy, dz = wz * ic - gz;
                         q += cq + cm * (dx * dx + dy * dy + dz * dz);
                     }
                 }
@@ -351,11 +354,16 @@ __global__ void monopole_level_kernel(int depth, const int32_t* __restrict__ dep
 }
 
 // com = w/m when m > 0 (linear_octree.cpp:95-104), then the merge of
-// linear_octree.cpp:194-202 with m0 = com0 = 0.
-__device__ inline void finish_com(double m, double wx, double wy, double wz, TreeRec& r, int merge)
+// linear_octree.cpp:194-202 with m0 = com0 = 0.  A one-body leaf passes its
+// body's position (one = true): its w is 0 + x m, so w/m is merge_div(m, x).
+__device__ inline void finish_com(double m, double wx, double wy, double wz, TreeRec& r, int merge, bool one,
+                                  double x, double y, double z)
 {
     double cx = wx, cy = wy, cz = wz;
-    if (m > 0) { cx = __ddiv_rn(wx, m); cy = __ddiv_rn(wy, m); cz = __ddiv_rn(wz, m); }
+    if (m > 0) {
+        if (one) { cx = merge_div(m, x); cy = merge_div(m, y); cz = merge_div(m, z); }
+        else { cx = __ddiv_rn(wx, m); cy = __ddiv_rn(wy, m); cz = __ddiv_rn(wz, m); }
+    }
     if (!merge) {  // buildOctreeBottomUp's own output, before any exchange
         r.cx = cx; r.cy = cy; r.cz = cz; r.m = m;
         return;
@@ -365,9 +373,9 @@ __device__ inline void finish_com(double m, double wx, double wy, double wz, Tre
         r.cx = r.cy = r.cz = r.m = 0.0;
         return;
     }
-    r.cx = __ddiv_rn(__dadd_rn(0.0, __dmul_rn(m, cx)), tot);
-    r.cy = __ddiv_rn(__dadd_rn(0.0, __dmul_rn(m, cy)), tot);
-    r.cz = __ddiv_rn(__dadd_rn(0.0, __dmul_rn(m, cz)), tot);
+    r.cx = merge_div(tot, cx);
+    r.cy = merge_div(tot, cy);
+    r.cz = merge_div(tot, cz);
     r.m = tot;
 }
 
@@ -380,7 +388,9 @@ __global__ void finalize_kernel(const int32_t* __restrict__ counts, const int32_
                                 const double* __restrict__ nwz, const int32_t* __restrict__ node_cs,
                                 const int32_t* __restrict__ node_nchild, const uint8_t* __restrict__ node_depth,
                                 TreeRec* __restrict__ rec, const double* __restrict__ lq,
-                                const double* __restrict__ nq, float* __restrict__ spread, int merge)
+                                const double* __restrict__ nq, float* __restrict__ spread, int merge,
+                                const int32_t* __restrict__ leaf_first, const double* __restrict__ px,
+                                const double* __restrict__ py, const double* __restrict__ pz)
 {
     const int S = counts[2];
     for (int s = blockIdx.x * blockDim.x + threadIdx.x; s < S; s += gridDim.x * blockDim.x) {
@@ -390,14 +400,17 @@ __global__ void finalize_kernel(const int32_t* __restrict__ counts, const int32_
         o.pad0 = 0;
         o.pad1 = 0;
         if (r >= 0) {
-            finish_com(lm[r], lwx[r], lwy[r], lwz[r], o, merge);
+            const int b = leaf_first[r];
+            const bool one = leaf_first[r + 1] == b + 1;
+            finish_com(lm[r], lwx[r], lwy[r], lwz[r], o, merge, one, one ? px[b] : 0.0, one ? py[b] : 0.0,
+                       one ? pz[b] : 0.0);
             o.child = -1;
             o.leaf = r;
             o.nchild = 0;
             o.depth = (uint8_t)kMaxDepth;
         } else {
             const int b = ~r;
-            finish_com(nm[b], nwx[b], nwy[b], nwz[b], o, merge);
+            finish_com(nm[b], nwx[b], nwy[b], nwz[b], o, merge, false, 0.0, 0.0, 0.0);
             o.child = node_cs[b] + 1;
             o.leaf = -1;
             o.nchild = (uint8_t)node_nchild[b];
@@ -407,7 +420,7 @@ __global__ void finalize_kernel(const int32_t* __restrict__ counts, const int32_
         if (kMoments) {
             const double m = r >= 0 ? lm[r] : nm[~r];
             const double q = r >= 0 ? lq[r] : nq[~r];
-            spread[s] = m > 0 ? (float)sqrt(q / m) : 0.0f;
+            spread[s] = m > 0 ? (float)sqrt(q * rcp_nr(m)) : 0.0f;
         }
     }
 }
@@ -496,13 +509,15 @@ int launch_build(bh_context* ctx, const double* mass, bool moments)
                                                        ctx->leaf_wx, ctx->leaf_wy, ctx->leaf_wz, ctx->node_m,
                                                        ctx->node_wx, ctx->node_wy, ctx->node_wz, ctx->node_cs,
                                                        ctx->node_nchild, ctx->node_depth, ctx->rec, ctx->leaf_q,
-                                                       ctx->node_q, ctx->fspread, ctx->build_merge ? 1 : 0);
+                                                       ctx->node_q, ctx->fspread, ctx->build_merge ? 1 : 0,
+                                                       ctx->leaf_first, ctx->px, ctx->py, ctx->pz);
     else
         finalize_kernel<false><<<gs, kThreads, 0, st>>>(ctx->counts, ctx->slot_ref, ctx->slot_top, ctx->leaf_m,
                                                         ctx->leaf_wx, ctx->leaf_wy, ctx->leaf_wz, ctx->node_m,
                                                         ctx->node_wx, ctx->node_wy, ctx->node_wz, ctx->node_cs,
                                                         ctx->node_nchild, ctx->node_depth, ctx->rec, ctx->leaf_q,
-                                                        ctx->node_q, ctx->fspread, ctx->build_merge ? 1 : 0);
+                                                        ctx->node_q, ctx->fspread, ctx->build_merge ? 1 : 0,
+                                                       ctx->leaf_first, ctx->px, ctx->py, ctx->pz);
     BH_LAUNCH_CHECK(ctx);
     return BH_OK;
 }

@@ -195,6 +195,14 @@ int bh_direct_sum(bh_context *ctx, int64_t ns, const int64_t *targets, double G,
  * the force walk's criterion at theta accepts (any N; the tree is built when
  * none is current, which re-sorts the bodies). */
 int bh_invariants(bh_context *ctx, double G, double theta, double out[9]);
+/* Checks on the current device of the arithmetic that replaces IEEE
+ * divisions and square roots on the hot path, over n seeded inputs;
+ * *failures = the number of mismatches.  which = 0: the division-free
+ * single-rank merge quotient against RN((0 + RN(m c)) / m); 1: the
+ * division-free key quantisation against the IEEE one; 2: the refined
+ * reciprocal square root against RN(1 / RN(sqrt x)) (more than 2 ulps
+ * apart counts).  No reference counterpart. */
+int bh_selftest(int which, int64_t n, uint64_t seed, int64_t *failures);
 
 /* ---- learned acceptance (no reference counterpart) ------------------- */
 /* The network 8 -> 64 -> 64 -> 1 (ReLU; BF16 weights, FP32 accumulation)
