@@ -124,6 +124,7 @@ void layout(bh_context* ctx, Carver& c)
     ctx->fA = c.take<float4>(2 * n);
     ctx->fB = c.take<float4>(2 * n);
     ctx->fmeta = c.take<uint32_t>(2 * n);
+    ctx->d4 = c.take<double4_32a>(2 * n);
     ctx->fspread = c.take<float>(2 * n);
     ctx->leaf_q = c.take<double>(n);
     ctx->node_q = c.take<double>(n);

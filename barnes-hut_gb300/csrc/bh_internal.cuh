@@ -63,7 +63,8 @@ __device__ inline int common_depth(uint64_t a, uint64_t b)
 // it: 5 FP64 operations instead of a full-precision square root sequence.
 __device__ __forceinline__ double rsqrt_hh(double x)
 {
-    if (!(x >= 0x1p-100 && x <= 0x1p100)) return rsqrt(x);
+    const int xe = (int)(__double_as_longlong(x) >> 52);  // biased exponent for x >= 0; < 0 for x < 0
+    if (xe < 923 || xe > 1122) return rsqrt(x);           // outside [2^-100, 2^100): also 0, inf, NaN
     const double y0 = (double)rsqrtf(__double2float_rn(x));
     const double h = x * y0;
     const double e = fma(-h, y0, 1.0);
@@ -244,6 +245,7 @@ struct bh_context {
     float4* fA = nullptr;   // {hi.x, hi.y, hi.z, G m}
     float4* fB = nullptr;   // {lo.x, lo.y, lo.z, bits of ref (child or leaf id)}
     uint32_t* fmeta = nullptr;  // nchild | depth << 8 | leaf << 16
+    double4_32a* d4 = nullptr;  // FP64 walk: {cx, cy, cz, G m} per slot
     float* fspread = nullptr;   // sqrt(Q / m) per slot (second moment about the centre of mass)
     double* leaf_q = nullptr;   // second moments of leaves and branching nodes
     double* node_q = nullptr;

@@ -64,12 +64,16 @@ __global__ void far_mass_kernel(int64_t n, const double* __restrict__ m, const u
 }
 
 // FP32 node records from the FP64 ones.
+// d4 (FP64 walk only): {cx, cy, cz, G m} per slot, the FP64 evaluation's
+// 32-byte record.
 __global__ void fp32_nodes_kernel(const int32_t* __restrict__ counts, const TreeRec* __restrict__ rec, double G,
-                                  float4* __restrict__ A, float4* __restrict__ B, uint32_t* __restrict__ meta)
+                                  float4* __restrict__ A, float4* __restrict__ B, uint32_t* __restrict__ meta,
+                                  double4_32a* __restrict__ d4)
 {
     const int S = counts[2];
     for (int s = blockIdx.x * blockDim.x + threadIdx.x; s < S; s += gridDim.x * blockDim.x) {
         const TreeRec r = rec[s];
+        if (d4) d4[s] = double4_32a{r.cx, r.cy, r.cz, G * r.m};
         const float hx = __double2float_rn(r.cx), hy = __double2float_rn(r.cy), hz = __double2float_rn(r.cz);
         const float lx = __double2float_rn(r.cx - (double)hx);
         const float ly = __double2float_rn(r.cy - (double)hy);
@@ -113,6 +117,7 @@ struct FParams {
     const float4* B;
     const uint32_t* meta;
     const TreeRec* rec;
+    const double4_32a* d4;
     const float* spread;
     const double* bbox;
     double theta2;
@@ -159,6 +164,12 @@ struct WalkSmem {
     double side2d[kMaxDepth + 1];
     float feat[kLearn ? kWarps : 1][32][9];
     uint8_t plist[kFP64 ? kWarps : 1][kList][32];  // FP64: each lane's own entries, in order
+    // FP64: the balanced evaluation's per-warp tables (see the flush).
+    int poff[kFP64 ? kWarps : 1][33];       // first pair of each lane, then the total
+    double bpos[kFP64 ? kWarps : 1][3][32]; // the bodies' positions
+    int bleaf[kFP64 ? kWarps : 1][32];      // the bodies' leaf ids
+    double bacc[kFP64 ? kWarps : 1][3][32]; // the bodies' accumulated list terms
+    unsigned bcnt[kFP64 ? kWarps : 1][32];  // and their interaction counts
 };
 
 template <bool kFP64, int kLearn>
@@ -206,7 +217,18 @@ __global__ void __launch_bounds__(kThreads) traverse_masked_kernel(FParams p)
     const unsigned full = __ballot_sync(0xffffffffu, valid);
     const int my_leaf = valid ? p.body_leaf[i] : -2;
     const float theta2f = (float)p.theta2;
-    const double theta2 = p.theta2, soft2 = p.soft2, G = p.G;
+    const double theta2 = p.theta2, soft2 = p.soft2;
+    if (kFP64) {
+        sm.bpos[w][0][lane] = x;
+        sm.bpos[w][1][lane] = y;
+        sm.bpos[w][2][lane] = z;
+        sm.bleaf[w][lane] = my_leaf;
+        sm.bacc[w][0][lane] = 0.0;
+        sm.bacc[w][1][lane] = 0.0;
+        sm.bacc[w][2][lane] = 0.0;
+        sm.bcnt[w][lane] = 0u;
+        __syncwarp();
+    }
     int2* stk = sm.stack[w];
     float4* L = sm.lst[w];
     int* LN = sm.lst_node[w];
@@ -467,39 +489,78 @@ __global__ void __launch_bounds__(kThreads) traverse_masked_kernel(FParams p)
                 continue;
             }
             if (kFP64) {
-                // Each lane compacts the entries it takes into its own list,
-                // then all lanes walk their lists in lockstep: the FP64 pipe
-                // then serves (nearly) only lanes with work, instead of every
-                // lane for every partly-accepted entry.
+                // The (entry, body) pairs of the staged list, grouped by body,
+                // are split evenly over the 32 threads: the FP64 pipe then
+                // evaluates only pairs that count, however unevenly the
+                // bodies' shares of the list are spread.  A thread sums its
+                // consecutive pairs in registers while they belong to one
+                // body and adds the partial sum to that body's shared
+                // accumulator when the body changes.
                 uint8_t (*PL)[32] = sm.plist[w];
+                int* OFF = sm.poff[w];
                 int mine = 0;
                 for (int j = 0; j < nlist; ++j)
                     if (LM[j] & me) PL[mine++][lane] = (uint8_t)j;
-                int most = mine;
+                int incl = mine;
 #pragma unroll
-                for (int off = 16; off > 0; off >>= 1) most = max(most, __shfl_xor_sync(0xffffffffu, most, off));
-                for (int q = 0; q < most; ++q) {
-                    const bool on = q < mine;
-                    const int j = on ? PL[q][lane] : 0;
-                    const TreeRec r = p.rec[LN[j]];
-                    const double dx = r.cx - x, dy = r.cy - y, dz = r.cz - z;
+                for (int off = 1; off < 32; off <<= 1) {
+                    const int t = __shfl_up_sync(0xffffffffu, incl, off);
+                    if (lane >= off) incl += t;
+                }
+                OFF[lane] = incl - mine;
+                if (lane == 31) OFF[32] = incl;
+                __syncwarp();
+                const int P = OFF[32];
+                const int per = (P + 31) >> 5;
+                const int k0 = min(lane * per, P), k1 = min(k0 + per, P);
+                int b = 0;  // the body of pair k0: the last lane whose first pair is <= k0
+#pragma unroll
+                for (int step = 16; step > 0; step >>= 1)
+                    if (b + step < 32 && OFF[b + step] <= k0) b += step;
+                double sx = 0.0, sy = 0.0, sz = 0.0;
+                unsigned sn = 0;
+                for (int t = 0; t < per; ++t) {
+                    const int k = k0 + t;
+                    const bool on = k < k1;
+                    if (on) {
+                        while (k >= OFF[b + 1]) {  // the next body: hand over the partial sum
+                            atomicAdd(&sm.bacc[w][0][b], sx);
+                            atomicAdd(&sm.bacc[w][1][b], sy);
+                            atomicAdd(&sm.bacc[w][2][b], sz);
+                            atomicAdd(&sm.bcnt[w][b], sn);
+                            sx = sy = sz = 0.0;
+                            sn = 0;
+                            ++b;
+                        }
+                    }
+                    const int j = on ? PL[k - OFF[b]][b] : 0;
+                    const double4_32a r = p.d4[LN[j]];
+                    const double dx = r.x - sm.bpos[w][0][b], dy = r.y - sm.bpos[w][1][b],
+                                 dz = r.z - sm.bpos[w][2][b];
                     bool take = on;
-                    if (on && LL[j] == my_leaf) {
+                    if (on && LL[j] == sm.bleaf[w][b]) {
                         // Own leaf: skipped at depth 21 unless a chain cell above
                         // it (depths top..20) accepts (traversal.cpp:70,78).
                         const double r2e = __dadd_rn(__dadd_rn(__dadd_rn(__dmul_rn(dx, dx), __dmul_rn(dy, dy)),
                                                                __dmul_rn(dz, dz)), soft2);
-                        take = r.top <= kMaxDepth - 1 && sm.side2d[kMaxDepth - 1] < __dmul_rn(theta2, r2e);
+                        take = p.rec[LN[j]].top <= kMaxDepth - 1 && sm.side2d[kMaxDepth - 1] < __dmul_rn(theta2, r2e);
                     }
                     const double r2 = fma(dx, dx, fma(dy, dy, fma(dz, dz, soft2)));
                     const double inv = rsqrt_hh(r2);
-                    double sc = (G * r.m) * (inv * inv * inv);
+                    double sc = r.w * (inv * inv * inv);
                     if (!take) sc = 0.0;
-                    adx = fma(sc, dx, adx);
-                    ady = fma(sc, dy, ady);
-                    adz = fma(sc, dz, adz);
-                    cnt += take ? 1u : 0u;
+                    sx = fma(sc, dx, sx);
+                    sy = fma(sc, dy, sy);
+                    sz = fma(sc, dz, sz);
+                    sn += take ? 1u : 0u;
                 }
+                if (k0 < k1) {
+                    atomicAdd(&sm.bacc[w][0][b], sx);
+                    atomicAdd(&sm.bacc[w][1][b], sy);
+                    atomicAdd(&sm.bacc[w][2][b], sz);
+                    atomicAdd(&sm.bcnt[w][b], sn);
+                }
+                __syncwarp();
             } else {
                 float fx = 0.f, fy = 0.f, fz = 0.f;
                 for (int j = 0; j < nlist; ++j) {
@@ -526,6 +587,13 @@ __global__ void __launch_bounds__(kThreads) traverse_masked_kernel(FParams p)
     }
     if (overflow && lane == 0) atomicOr(p.err, kErrOverflow);
     if (kLearn == kLearnCollect) return;
+    if (kFP64) {
+        __syncwarp();
+        adx += sm.bacc[w][0][lane];
+        ady += sm.bacc[w][1][lane];
+        adz += sm.bacc[w][2][lane];
+        cnt += sm.bcnt[w][lane];
+    }
 
     if (valid) {
         p.ax[i] = adx;
@@ -585,7 +653,7 @@ int launch_fp32_nodes(bh_context* ctx, double G)
 {
     if (ctx->n == 0) return BH_OK;
     fp32_nodes_kernel<<<grid_n(2 * ctx->n), 256, 0, ctx->stream>>>(ctx->counts, ctx->rec, G, ctx->fA, ctx->fB,
-                                                                    ctx->fmeta);
+                                                                    ctx->fmeta, nullptr);
     BH_LAUNCH_CHECK(ctx);
     return BH_OK;
 }
@@ -616,7 +684,8 @@ int prepare_walk(bh_context* ctx, double theta, double G, double soft2, bool fp6
 {
     const int64_t n = ctx->n;
     const int nd = fp64 ? 0 : (ctx->num_direct < 64 ? ctx->num_direct : 64);
-    fp32_nodes_kernel<<<grid_n(2 * n), 256, 0, ctx->stream>>>(ctx->counts, ctx->rec, G, ctx->fA, ctx->fB, ctx->fmeta);
+    fp32_nodes_kernel<<<grid_n(2 * n), 256, 0, ctx->stream>>>(ctx->counts, ctx->rec, G, ctx->fA, ctx->fB, ctx->fmeta,
+                                                              fp64 ? ctx->d4 : nullptr);
     BH_LAUNCH_CHECK(ctx);
     if (nd > 0) {
         int rc = launch_direct_extract(ctx, G);
@@ -629,6 +698,7 @@ int prepare_walk(bh_context* ctx, double theta, double G, double soft2, bool fp6
     p.body_leaf = ctx->body_leaf;
     p.A = ctx->fA; p.B = ctx->fB; p.meta = ctx->fmeta;
     p.rec = ctx->rec;
+    p.d4 = ctx->d4;
     p.spread = ctx->fspread;
     p.bbox = ctx->bbox;
     p.theta2 = theta * theta;
