@@ -54,18 +54,26 @@ __device__ inline int common_depth(uint64_t a, uint64_t b)
 }
 
 // 1/sqrt(x) in FP64 from the FP32 hardware estimate y0 (relative error below
-// 2^-22) and one third-order Householder step for f(y) = 1/y^2 - x:
+// 2^-21 with the truncation below) and one third-order Householder step for
+// f(y) = 1/y^2 - x:
 //   e = 1 - x y0^2,   y1 = y0 (1 + e/2 + 3 e^2 / 8),
-// whose truncation error is 5/16 e^3 (below 2^-66); with the roundings of
+// whose truncation error is 5/16 e^3 (below 2^-61); with the roundings of
 // the FP64 steps the result is within about one ulp.  Outside [2^-100, 2^100]
 // (and for 0, inf, NaN), where the FP32 estimate cannot represent the value,
 // the library's rsqrt.  The non-bit-exact FP64 walk and the direct terms use
 // it: 5 FP64 operations instead of a full-precision square root sequence.
 __device__ __forceinline__ double rsqrt_hh(double x)
 {
-    const int xe = (int)(__double_as_longlong(x) >> 52);  // biased exponent for x >= 0; < 0 for x < 0
-    if (xe < 923 || xe > 1122) return rsqrt(x);           // outside [2^-100, 2^100): also 0, inf, NaN
-    const double y0 = (double)rsqrtf(__double2float_rn(x));
+    const long long xb = __double_as_longlong(x);
+    const int xe = (int)(xb >> 52);             // biased exponent for x >= 0; < 0 for x < 0
+    if (xe < 923 || xe > 1122) return rsqrt(x);  // outside [2^-100, 2^100): also 0, inf, NaN
+    // x truncated to FP32 and the estimate widened back, on the bit patterns
+    // (integer operations: the FP64 pipe, at 1/64 of the FP32 rate, is the
+    // walk's bound).  Truncation adds at most 2^-23 to the estimate's error.
+    const float xf = __int_as_float(((xe - 896) << 23) | (int)((xb >> 29) & 0x7FFFFF));
+    const int yb = __float_as_int(rsqrtf(xf));
+    const double y0 = __longlong_as_double(((long long)(((yb >> 23) & 0xFF) + 896) << 52) |
+                                           ((long long)(yb & 0x7FFFFF) << 29));
     const double h = x * y0;
     const double e = fma(-h, y0, 1.0);
     const double t = e * fma(e, 0.375, 0.5);
