@@ -268,6 +268,9 @@ __global__ void __launch_bounds__(kThreads) traverse_masked_kernel(FParams p)
     const float gextent = sqrtf((bmaxx - bminx) * (bmaxx - bminx) + (bmaxy - bminy) * (bmaxy - bminy) +
                                 (bmaxz - bminz) * (bmaxz - bminz));
     const float bcx = 0.5f * (bminx + bmaxx), bcy = 0.5f * (bminy + bmaxy), bcz = 0.5f * (bminz + bmaxz);
+    // Per-walk logarithms of the learned features (base 2).
+    const float lext = kLearn ? __log2f(fmaxf(gextent, 1e-30f)) : 0.0f;
+    const float lascale = kLearn ? __log2f(ascale) : 0.0f;
     unsigned long long ncand = 0, nacc = 0, nfall = 0;
 
     int nlist = 0;
@@ -364,17 +367,24 @@ __global__ void __launch_bounds__(kThreads) traverse_masked_kernel(FParams p)
 #pragma unroll
                     for (int q = 0; q < kFeat; ++q) f[q] = 0.0f;
                     if (cand) {
-                        const float dmin = sqrtf(dmin2), side = sqrtf(s2);
-                        const float spr = fmaxf(__ldg(p.spread + node), 1e-8f * side);
+                        // log10 of ratios as differences of base-2 logarithms
+                        // of the (squared) lengths: hardware log2 estimates,
+                        // no divisions and no square roots.  Training pairs
+                        // are collected by this same code, so the network
+                        // sees the same feature arithmetic it was trained on.
+                        constexpr float kL = 0.30102999566f;  // log10(2)
+                        const float l2dmin = __log2f(dmin2), l2s = __log2f(s2);
+                        const float lspr = __log2f(fmaxf(__ldg(p.spread + node), 1e-8f * sqrtf(s2)));
                         const float dcx = e.x - bcx, dcy = e.y - bcy, dcz = e.z - bcz;
-                        f[0] = log10f(side / dmin);
-                        f[1] = log10f(spr / dmin);
-                        f[2] = log10f(fmaxf(gextent, 1e-30f) / dmin);
-                        f[3] = log10f(e.w / (dmin2 * ascale));
-                        f[4] = log10f(sqrtf(dmax2) / dmin);
+                        const float ldmin = 0.5f * l2dmin;
+                        f[0] = kL * (0.5f * l2s - ldmin);
+                        f[1] = kL * (lspr - ldmin);
+                        f[2] = kL * (lext - ldmin);
+                        f[3] = kL * (__log2f(e.w) - l2dmin - lascale);
+                        f[4] = kL * 0.5f * (__log2f(dmax2) - l2dmin);
                         f[5] = (float)depth * (1.0f / kMaxDepth);
-                        f[6] = log10f(spr / side);
-                        f[7] = log10f(fmaxf(sqrtf(dcx * dcx + dcy * dcy + dcz * dcz), 1e-30f) / dmin);
+                        f[6] = kL * (lspr - 0.5f * l2s);
+                        f[7] = kL * (0.5f * __log2f(fmaxf(dcx * dcx + dcy * dcy + dcz * dcz, 1e-36f)) - ldmin);
                     }
                     if (kLearn == kLearnCollect) {
                         const int leader = __ffs(cb) - 1;

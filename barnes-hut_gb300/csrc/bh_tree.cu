@@ -420,7 +420,7 @@ __global__ void finalize_kernel(const int32_t* __restrict__ counts, const int32_
         if (kMoments) {
             const double m = r >= 0 ? lm[r] : nm[~r];
             const double q = r >= 0 ? lq[r] : nq[~r];
-            spread[s] = m > 0 ? (float)sqrt(q * rcp_nr(m)) : 0.0f;
+            spread[s] = m > 0 ? sqrtf((float)(q * rcp_nr(m))) : 0.0f;
         }
     }
 }
