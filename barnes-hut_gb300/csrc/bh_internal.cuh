@@ -145,17 +145,76 @@ __device__ inline double merge_div(double m, double c)
     return __ddiv_rn(__dadd_rn(0.0, p), m);
 }
 
-// 1/x to about 2^-60 relative (not correctly rounded): the FP32 estimate
-// refined by one second-order Newton step, y1 = y0 (1 + e + e^2) with
-// e = 1 - x y0.  For quantities that need no bit-exactness (the second
-// moments of the learned features).  Outside [2^-120, 2^120] the IEEE one.
+// 1/x to within about one ulp (not correctly rounded): the FP32 hardware
+// estimate (x narrowed and the estimate widened on the bit patterns, integer
+// operations) refined by one third-order Newton step, y1 = y0 (1 + e + e^2)
+// with e = 1 - x y0, whose truncation error e^3 is below 2^-60.  Outside
+// [2^-100, 2^100] (and for 0, negative, inf, NaN) the IEEE reciprocal.
 __device__ __forceinline__ double rcp_nr(double x)
 {
-    const double ax = fabs(x);
-    if (!(ax >= 0x1p-120 && ax <= 0x1p120)) return 1.0 / x;
-    const double y0 = (double)__frcp_rn(__double2float_rn(x));
+    const long long xb = __double_as_longlong(x);
+    const int xe = (int)(xb >> 52);
+    if (xe < 923 || xe > 1122) return __drcp_rn(x);
+    const float xf = __int_as_float(((xe - 896) << 23) | (int)((xb >> 29) & 0x7FFFFF));
+    const int yb = __float_as_int(__frcp_rn(xf));
+    const double y0 = __longlong_as_double(((long long)(((yb >> 23) & 0xFF) + 896) << 52) |
+                                           ((long long)(yb & 0x7FFFFF) << 29));
     const double e = fma(-x, y0, 1.0);
     return fma(y0, fma(e, e, e), y0);
+}
+
+// x truncated to FP32 on the bit patterns (integer operations; the FP64
+// conversion instructions run on the slow FP64 pipe): relative error below
+// 2^-23; magnitudes below 2^-126 give a signed zero, above 2^127 the
+// converted value.  widen() is the exact inverse direction.
+__device__ __forceinline__ float narrow_trunc(double x)
+{
+    const long long xb = __double_as_longlong(x);
+    const int e = (int)((xb >> 52) & 0x7FF);
+    const int sign = (int)((unsigned long long)xb >> 63) << 31;
+    if (e <= 896) return __int_as_float(sign);
+    if (e >= 1151) return __double2float_rn(x);
+    return __int_as_float(sign | ((e - 896) << 23) | (int)((xb >> 29) & 0x7FFFFF));
+}
+
+__device__ __forceinline__ double widen(float f)
+{
+    const int b = __float_as_int(f);
+    const int e = (b >> 23) & 0xFF;
+    const long long sign = (long long)((unsigned)b >> 31) << 63;
+    if (e == 0 || e == 0xFF) return (double)f;
+    return __longlong_as_double(sign | ((long long)(e + 896) << 52) | ((long long)(b & 0x7FFFFF) << 29));
+}
+
+// RN(w / m) for m > 0 with four FP64 operations in nearly every case, given
+// r = rcp_nr(m).  q0 = RN(w r) is within a few ulps of w/m; one correction
+// q1 = q0 + (w - q0 m) r (Markstein's) brings it within one ulp, where the
+// residual w - q1 m is exact (the remainder of a faithful quotient is a
+// double).  RN(w/m) is then q1 or its neighbour on the residual's side,
+// decided exactly on the bit patterns as in merge_div; a residual of an ulp
+// times m or more (q1 not faithful), a power-of-two q1, a tie or exponents
+// outside 2^+-200 take the IEEE division.
+__device__ inline double div_exact(double w, double m, double r)
+{
+    const long long mb = __double_as_longlong(m);
+    const int me = (int)((mb >> 52) & 0x7FF);
+    const double q0 = w * r;
+    const double rho = fma(-q0, m, w);
+    const double q1 = fma(rho, r, q0);
+    const double rho1 = fma(-q1, m, w);
+    const long long qb = __double_as_longlong(q1);
+    const int eq = (int)((qb >> 52) & 0x7FF);
+    if (mb <= 0 || me < 823 || me > 1223 || eq < 823 || eq > 1223 || (qb & 0x000FFFFFFFFFFFFFll) == 0)
+        return __ddiv_rn(w, m);
+    const long long rb = __double_as_longlong(rho1);
+    const long long ra = rb & 0x7FFFFFFFFFFFFFFFll;
+    if (ra == 0) return q1;
+    const long long es = ra + ((long long)(1076 - eq) << 52);  // |rho1| / (ulp(q1) / 2)
+    if (es < mb) return q1;
+    const long long es2 = ra + ((long long)(1075 - eq) << 52);  // |rho1| / ulp(q1)
+    if (es2 >= mb) return __ddiv_rn(w, m);
+    if (es > mb) return __longlong_as_double(((rb ^ qb) >= 0) ? qb + 1 : qb - 1);
+    return __ddiv_rn(w, m);
 }
 
 // One node of the compressed octree as the traversal reads it (48 bytes).

@@ -13,20 +13,34 @@ constexpr int kBoxThreads = 256;
 // Order-aware extremum: the reference keeps the FIRST body holding the
 // extreme value (compute_local_bbox, src/bounding_box.cpp:33-41, replaces
 // only on a strict comparison), so ties are broken towards the lower index.
+// Values are compared as order-preserving integer images of their bit
+// patterns (FP64 comparisons run on the slow FP64 pipe): for finite doubles
+// ord(a) < ord(b) exactly when a < b, with -0 mapped to +0 so that the two
+// zeros tie as they do in the reference's comparison.
 struct Ext {
-    double v;
+    long long k;  // ord(value)
     long long i;
 };
-__device__ inline bool better_min(const Ext& a, const Ext& b) { return a.v < b.v || (a.v == b.v && a.i < b.i); }
-__device__ inline bool better_max(const Ext& a, const Ext& b) { return b.v < a.v || (a.v == b.v && a.i < b.i); }
+__device__ inline long long ord(double v)
+{
+    long long b = __double_as_longlong(v);
+    if (b == (long long)0x8000000000000000ull) b = 0;
+    return b >= 0 ? b : (b ^ 0x7FFFFFFFFFFFFFFFll);
+}
+__device__ inline double unord(long long k) { return __longlong_as_double(k >= 0 ? k : (k ^ 0x7FFFFFFFFFFFFFFFll)); }
+__device__ inline bool better_min(const Ext& a, const Ext& b) { return a.k < b.k || (a.k == b.k && a.i < b.i); }
+__device__ inline bool better_max(const Ext& a, const Ext& b) { return b.k < a.k || (a.k == b.k && a.i < b.i); }
 
 __device__ inline Ext shfl_ext(const Ext& e, int off)
 {
     Ext r;
-    r.v = __shfl_down_sync(0xffffffffu, e.v, off);
+    r.k = __shfl_down_sync(0xffffffffu, e.k, off);
     r.i = __shfl_down_sync(0xffffffffu, e.i, off);
     return r;
 }
+
+// Finite: the exponent field is not all ones.
+__device__ inline bool finite_bits(double v) { return ((__double_as_longlong(v) >> 52) & 0x7FF) != 0x7FF; }
 
 // Block-wide reduction of the six extrema (min x,y,z then max x,y,z) into
 // thread 0's `e`.
@@ -63,7 +77,7 @@ __global__ void __launch_bounds__(kBoxThreads) drift_bbox_kernel(
     Ext* __restrict__ part, double* __restrict__ bbox, unsigned* __restrict__ ticket, unsigned* __restrict__ err)
 {
     Ext e[6];
-    for (int a = 0; a < 3; ++a) { e[a] = {DBL_MAX, LLONG_MAX}; e[3 + a] = {-DBL_MAX, LLONG_MAX}; }
+    for (int a = 0; a < 3; ++a) { e[a] = {ord(DBL_MAX), LLONG_MAX}; e[3 + a] = {ord(-DBL_MAX), LLONG_MAX}; }
     // +-DBL_MAX with an index past every body loses every comparison with a
     // real (finite) coordinate; infinities and NaN are flagged below.
     bool bad = false;
@@ -84,11 +98,11 @@ __global__ void __launch_bounds__(kBoxThreads) drift_bbox_kernel(
                 px[i] = x; py[i] = y; pz[i] = z;
             }
         }
-        bad |= !(isfinite(x) && isfinite(y) && isfinite(z));
+        bad |= !(finite_bits(x) && finite_bits(y) && finite_bits(z));
         const double c[3] = {x, y, z};
 #pragma unroll
         for (int a = 0; a < 3; ++a) {
-            Ext o{c[a], (long long)i};
+            Ext o{ord(c[a]), (long long)i};
             if (better_min(o, e[a])) e[a] = o;
             if (better_max(o, e[3 + a])) e[3 + a] = o;
         }
@@ -105,7 +119,7 @@ __global__ void __launch_bounds__(kBoxThreads) drift_bbox_kernel(
     if (!last) return;
     __threadfence();
     // Last block: reduce the partials (block count <= a few thousand).
-    for (int a = 0; a < 3; ++a) { e[a] = {DBL_MAX, LLONG_MAX}; e[3 + a] = {-DBL_MAX, LLONG_MAX}; }
+    for (int a = 0; a < 3; ++a) { e[a] = {ord(DBL_MAX), LLONG_MAX}; e[3 + a] = {ord(-DBL_MAX), LLONG_MAX}; }
     for (int b = threadIdx.x; b < (int)gridDim.x; b += blockDim.x) {
         for (int a = 0; a < 6; ++a) {
             Ext o = part[b * 6 + a];
@@ -115,7 +129,13 @@ __global__ void __launch_bounds__(kBoxThreads) drift_bbox_kernel(
     __syncthreads();
     block_reduce_box(e);
     if (threadIdx.x == 0) {
-        for (int a = 0; a < 6; ++a) bbox[a] = e[a].v;
+        // The extreme body's own value (keeps the sign of a zero, which the
+        // integer image folds).
+        for (int a = 0; a < 6; ++a) {
+            const long long bi = e[a].i;
+            const double* src = (a % 3 == 0) ? px : (a % 3 == 1) ? py : pz;
+            bbox[a] = (bi >= 0 && bi < n) ? src[bi] : unord(e[a].k);
+        }
         *ticket = 0u;
     }
 }

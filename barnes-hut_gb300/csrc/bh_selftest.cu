@@ -26,6 +26,7 @@ __device__ inline double with_exp(uint64_t r, int e)
 // which = 0: merge_div(m, c) == RN((0 + RN(m c)) / m)
 // which = 1: quantise(...) == quantise_exact(...)
 // which = 2: rsqrt_hh(x) within 2 ulps of RN(1 / RN(sqrt(x)))
+// which = 3: div_exact(w, m, rcp_nr(m)) == RN(w / m)
 __global__ void selftest_kernel(int which, int64_t n, uint64_t seed, unsigned long long* fails)
 {
     unsigned long long bad = 0;
@@ -57,6 +58,16 @@ __global__ void selftest_kernel(int which, int64_t n, uint64_t seed, unsigned lo
             }
             const double inv = __drcp_rn(span) * 2097152.0;
             bad += bh::quantise(v, lo, span, inv) != bh::quantise_exact(v, lo, span);
+        } else if (which == 3) {
+            // sums over 2^-50 .. 2^120 of either sign (one in 8 a rounded
+            // product m c, as a one-body sum is) over masses 2^-10 .. 2^110
+            const double m = with_exp(r0, -10 + (int)(r1 % 120));
+            double w = with_exp(r2, -50 + (int)(r3 % 170));
+            if ((r3 >> 30) & 1) w = -w;
+            if (((r3 >> 31) & 7) == 0) w = __dmul_rn(m, with_exp(r2, -20 + (int)(r3 % 40)));
+            const double want = __ddiv_rn(w, m);
+            const double got = bh::div_exact(w, m, bh::rcp_nr(m));
+            bad += __double_as_longlong(want) != __double_as_longlong(got);
         } else {
             const double x = with_exp(r0, -90 + (int)(r1 % 180));
             const double want = __drcp_rn(__dsqrt_rn(x));
@@ -72,7 +83,7 @@ __global__ void selftest_kernel(int which, int64_t n, uint64_t seed, unsigned lo
 
 extern "C" int bh_selftest(int which, int64_t n, uint64_t seed, int64_t* failures)
 {
-    if (which < 0 || which > 2 || n < 0 || !failures) return bh_fail(BH_ERR_INVALID_ARGUMENT, "bh_selftest: bad arguments");
+    if (which < 0 || which > 3 || n < 0 || !failures) return bh_fail(BH_ERR_INVALID_ARGUMENT, "bh_selftest: bad arguments");
     int dev = 0;
     BH_CUDA_TRY(cudaGetDevice(&dev));
     unsigned long long* d = nullptr;

@@ -74,12 +74,14 @@ __global__ void fp32_nodes_kernel(const int32_t* __restrict__ counts, const Tree
     for (int s = blockIdx.x * blockDim.x + threadIdx.x; s < S; s += gridDim.x * blockDim.x) {
         const TreeRec r = rec[s];
         if (d4) d4[s] = double4_32a{r.cx, r.cy, r.cz, G * r.m};
-        const float hx = __double2float_rn(r.cx), hy = __double2float_rn(r.cy), hz = __double2float_rn(r.cz);
-        const float lx = __double2float_rn(r.cx - (double)hx);
-        const float ly = __double2float_rn(r.cy - (double)hy);
-        const float lz = __double2float_rn(r.cz - (double)hz);
+        // hi + lo splits by truncation on the bit patterns: c - hi is exact,
+        // and hi + lo represents c to about 2^-46 relative.
+        const float hx = narrow_trunc(r.cx), hy = narrow_trunc(r.cy), hz = narrow_trunc(r.cz);
+        const float lx = narrow_trunc(r.cx - widen(hx));
+        const float ly = narrow_trunc(r.cy - widen(hy));
+        const float lz = narrow_trunc(r.cz - widen(hz));
         const bool leaf = r.child < 0;
-        A[s] = make_float4(hx, hy, hz, __double2float_rn(G * r.m));
+        A[s] = make_float4(hx, hy, hz, narrow_trunc(G * r.m));
         B[s] = make_float4(lx, ly, lz, __int_as_float(leaf ? r.leaf : r.child));
         meta[s] = (uint32_t)r.nchild | ((uint32_t)r.depth << 8) | ((leaf ? 1u : 0u) << 16) |
                   ((r.m == 0.0 ? 1u : 0u) << 17);

@@ -362,7 +362,10 @@ __device__ inline void finish_com(double m, double wx, double wy, double wz, Tre
     double cx = wx, cy = wy, cz = wz;
     if (m > 0) {
         if (one) { cx = merge_div(m, x); cy = merge_div(m, y); cz = merge_div(m, z); }
-        else { cx = __ddiv_rn(wx, m); cy = __ddiv_rn(wy, m); cz = __ddiv_rn(wz, m); }
+        else {
+            const double r = rcp_nr(m);
+            cx = div_exact(wx, m, r); cy = div_exact(wy, m, r); cz = div_exact(wz, m, r);
+        }
     }
     if (!merge) {  // buildOctreeBottomUp's own output, before any exchange
         r.cx = cx; r.cy = cy; r.cz = cz; r.m = m;

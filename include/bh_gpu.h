@@ -201,7 +201,8 @@ int bh_invariants(bh_context *ctx, double G, double theta, double out[9]);
  * single-rank merge quotient against RN((0 + RN(m c)) / m); 1: the
  * division-free key quantisation against the IEEE one; 2: the refined
  * reciprocal square root against RN(1 / RN(sqrt x)) (more than 2 ulps
- * apart counts).  No reference counterpart. */
+ * apart counts); 3: the division-free centre-of-mass quotient against
+ * RN(w / m).  No reference counterpart. */
 int bh_selftest(int which, int64_t n, uint64_t seed, int64_t *failures);
 
 /* ---- learned acceptance (no reference counterpart) ------------------- */
