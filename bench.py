@@ -104,6 +104,9 @@ def parse():
 
 
 def dist_init():
+    """Rank, world size and local rank from the launcher's environment; one
+    process per GPU over NCCL (gloo where no GPU is present, for the host-side
+    replica logic)."""
     ws = int(os.environ.get("WORLD_SIZE", "1"))
     if ws <= 1:
         return 0, 1, 0
@@ -111,8 +114,11 @@ def dist_init():
     import torch.distributed as dist
     rank = int(os.environ["RANK"])
     local = int(os.environ.get("LOCAL_RANK", rank))
-    torch.cuda.set_device(local)
-    dist.init_process_group("nccl")
+    if torch.cuda.is_available():
+        torch.cuda.set_device(local)
+        dist.init_process_group("nccl")
+    else:
+        dist.init_process_group("gloo")
     return rank, ws, local
 
 
@@ -550,7 +556,7 @@ def run_ours(args, rank, ws, local):
     inter_per_step = inter / k
     achieved = inter_per_step * FLOPS_PER_INTERACTION / (force_ms * 1e-3) / 1e12
     fp = "fp64" if mode <= 1 else "fp32"
-    value = ws * n * k / (total_ms * 1e-3)
+    value = replica_value(ws, n, k, total_ms)
     line = {
         "metric": "body-steps/s", "value": value, "unit": "body-steps/s", "n_gpus": ws, "steps": k,
         "warmup": args.warmup, "ms_per_step": total_ms / k, "higher_is_better": True, "scaling": "weak",
@@ -592,9 +598,16 @@ def reduce_max(x: float, ws: int) -> float:
         return x
     import torch
     import torch.distributed as dist
-    t = torch.tensor([x], dtype=torch.float64, device="cuda")
+    dev = "cuda" if dist.get_backend() == "nccl" else "cpu"
+    t = torch.tensor([x], dtype=torch.float64, device=dev)
     dist.all_reduce(t, op=dist.ReduceOp.MAX)
     return float(t.item())
+
+
+def replica_value(ws: int, n: int, k: int, slowest_ms: float) -> float:
+    """Whole-job body-steps/s of ws replicas that each ran k steps of n
+    bodies, over the slowest rank's time (weak scaling)."""
+    return ws * n * k / (slowest_ms * 1e-3)
 
 
 def main():
