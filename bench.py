@@ -362,24 +362,24 @@ def learned_eval(args, dev, params, scale):
             _fresh(ctx, pos, vel, mass, ids)
             err = _sample_error(ctx, n, G)
             row = {"seed": seed}
-            cases = [("theta_only", bh.MODE_FP32_FAR, None)]
-            cases += [(f"budget_{b:g}", bh.MODE_LEARNED, b) for b in (1e-4, 1e-5, 1e-6)]
-            for name, mode, budget in cases:
+            cases = [("theta_only", bh.MODE_FP32_FAR, None, THETA), ("theta_1.6_only", bh.MODE_FP32_FAR, None, 1.6)]
+            cases += [(f"budget_{b:g}", bh.MODE_LEARNED, b, THETA) for b in (1e-4, 1e-5, 1e-6)]
+            for name, mode, budget, theta in cases:
                 if budget is not None:
                     ctx.learned_set_model(params, scale, budget=budget, theta_max=args.theta_max)
                 _fresh(ctx, pos, vel, mass, ids)
-                med, p99 = err(ctx.compute_accelerations(THETA, G, 0.0, mode))
+                med, p99 = err(ctx.compute_accelerations(theta, G, 0.0, mode))
                 r = {"median_rel_err": med, "p99_rel_err": p99}
                 if budget is not None:
                     st = ctx.learned_stats()
                     r["fallback_rate"] = st["fallback"] / max(1, st["candidates"])
                 ctx.set_bodies(pos, vel, mass, ids)
-                ms, ipb = time_steps(ctx, ext, flush, mode, THETA, 2, 1)
+                ms, ipb = time_steps(ctx, ext, flush, mode, theta, 2, 1)
                 r.update({"ms_per_step": ms, "interactions_per_body": ipb})
                 row[name] = r
             rows.append(row)
     summary = {}
-    for name in ("theta_only", "budget_0.0001", "budget_1e-05", "budget_1e-06"):
+    for name in ("theta_only", "theta_1.6_only", "budget_0.0001", "budget_1e-05", "budget_1e-06"):
         summary[name] = {k: float(np.mean([r[name][k] for r in rows]))
                          for k in rows[0][name] if k != "seed"}
     return {"workload": f"{n:,} bodies (90/10), 5 unseen seeds 9101-9105, theta=1.05 fallback",
@@ -404,24 +404,27 @@ def north_star(args, dev, params, scale, info):
         _fresh(ctx, pos, vel, mass, ids)
         err = _sample_error(ctx, n, G)
         rows = {}
-        cases = [("plain_fp64", bh.MODE_FP64_LIST, None), ("fp32_far", bh.MODE_FP32_FAR, None)]
-        cases += [(f"fp32_learned_budget_{b:g}", bh.MODE_LEARNED, b) for b in (1e-4, 1e-5, 1e-6, 1e-7)]
-        for name, mode, budget in cases:
+        cases = [("plain_fp64", bh.MODE_FP64_LIST, None, THETA), ("fp32_far", bh.MODE_FP32_FAR, None, THETA)]
+        cases += [(f"fp32_learned_budget_{b:g}", bh.MODE_LEARNED, b, THETA) for b in (1e-4, 1e-5, 1e-6, 1e-7)]
+        # the FP32 form with a wider opening angle instead of the network: the
+        # baseline the learned criterion has to beat at equal error
+        cases += [(f"fp32_far_theta_{th:g}", bh.MODE_FP32_FAR, None, th) for th in (1.3, 1.6)]
+        for name, mode, budget, theta in cases:
             if budget is not None:
                 ctx.learned_set_model(params, scale, budget=budget, theta_max=args.theta_max)
             _fresh(ctx, pos, vel, mass, ids)
             ctx.set_profiling(True)
-            a = ctx.compute_accelerations(THETA, G, 0.0, mode)
+            a = ctx.compute_accelerations(theta, G, 0.0, mode)
             ctx.set_profiling(False)
             med, p99 = err(a)
-            row = {"median_rel_err": med, "p99_rel_err": p99}
+            row = {"theta": theta, "median_rel_err": med, "p99_rel_err": p99}
             if budget is not None:
                 st = ctx.learned_stats()
                 row["fallback_rate"] = st["fallback"] / max(1, st["candidates"])
                 row["network_accept_rate"] = st["accepted"] / max(1, st["candidates"])
             ctx.set_bodies(pos, vel, mass, ids)
             ctx.set_profiling(True)
-            ms, ipb = time_steps(ctx, ext, flush, mode, THETA, args.ns_steps, 2)
+            ms, ipb = time_steps(ctx, ext, flush, mode, theta, args.ns_steps, 2)
             phases, _ = ctx.phase_times()
             ctx.set_profiling(False)
             steps = args.ns_steps + 2
@@ -443,7 +446,7 @@ def north_star(args, dev, params, scale, info):
 # DRAM traffic per launch of the force kernel (dram__bytes_read.sum +
 # dram__bytes_write.sum) from one ncu --set full capture of that kernel on
 # that workload, keyed by (mode, bodies).
-TRAFFIC_BYTES = {("fp64_list", 300_149): 51.66e6 + 1.15e6}
+TRAFFIC_BYTES = {("fp64_list", 300_149): 62.50e6 + 2.27e6, ("fp32", 4_000_000): 482.06e6 + 184.12e6}
 
 # Algorithmic bytes per body of the HBM-bound phases: the minimum traffic of
 # each phase's work (reads + writes of its inputs and outputs once).
