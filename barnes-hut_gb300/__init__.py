@@ -94,6 +94,7 @@ def _sig(lib):
     f["bh_direct_sum"] = (C.c_int, [_P, _I64, _P, _D, _P])
     f["bh_invariants"] = (C.c_int, [_P, _D, _D, _P])
     f["bh_tree_spread"] = (C.c_int, [_P, _P])
+    f["bh_write_vtp"] = (C.c_int, [C.c_char_p, C.c_int, _I64, _P, _P, _P, _P, _P])
     f["bh_selftest"] = (C.c_int, [C.c_int, _I64, C.c_uint64, C.POINTER(_I64)])
     f["bh_tree_slots"] = (C.c_int, [_P, _P, _P])
     f["bh_mlp_gradient"] = (C.c_int, [_P, _P, _P, _I64, _P, _P])
@@ -187,6 +188,13 @@ def read_csv(path, body_count: int = -1):
 def write_csv(path, ids, mass, pos, vel) -> None:
     ids = _u64(ids); mass = _f64(mass); pos = _f64(pos); vel = _f64(vel)
     _check(library().bh_write_csv(str(path).encode(), len(mass), _ptr(ids), _ptr(mass), _ptr(pos), _ptr(vel)))
+
+
+def write_vtp(path, ids, mass, pos, vel, acc, rank: int = 0) -> None:
+    """writeSnapshot: one VTK XML PolyData snapshot (ParaView)."""
+    ids = _u64(ids); mass = _f64(mass); pos = _f64(pos); vel = _f64(vel); acc = _f64(acc)
+    _check(library().bh_write_vtp(str(path).encode(), int(rank), len(mass), _ptr(ids), _ptr(mass), _ptr(pos),
+                                  _ptr(vel), _ptr(acc)))
 
 
 # ---------------------------------------------------------------- device context

@@ -76,7 +76,7 @@ def build(verbose: bool = False, force: bool = False) -> Path:
     # The reference's C++ call surface over the library, and the
     # reference-compatible driver.
     _host_link(SHIM_LIB, [SHIM / "bh_reference_api.cpp"], ["-shared"], force)
-    _host_link(OUT / "simulate", [SHIM / "simulate.cpp"], [], force)
+    _host_link(OUT / "simulate", [SHIM / "simulate.cpp"], ["-pthread"], force)
     return LIB
 
 

@@ -1,6 +1,7 @@
 // Host-side input: Kepler conversion, the seeded synthetic solar system and
 // the reference's CSV format.  Plain C++; no GPU is touched here.
 #include <cerrno>
+#include <cstdint>
 #include <cmath>
 #include <cstdio>
 #include <cstdlib>
@@ -217,4 +218,57 @@ extern "C" int bh_write_csv(const char* path, int64_t n, const uint64_t* ids, co
     const bool bad = std::ferror(f) != 0;
     std::fclose(f);
     return bad ? bh_fail(BH_ERR_IO, "bh_write_csv: write failed") : BH_OK;
+}
+
+// writeSnapshot (src/io.cpp:84-232): one VTK XML PolyData file per snapshot
+// with the same elements, array names, types and number formatting (the
+// default stream formatting, 6 significant digits): Points "position";
+// PointData "rank", "body_id", "velocity", "mass", "acceleration" (the
+// magnitude); Verts "offsets" / "connectivity", one vertex per body.
+extern "C" int bh_write_vtp(const char* path, int rank, int64_t n, const uint64_t* ids, const double* mass,
+                            const double* pos, const double* vel, const double* acc)
+{
+    if (!path || n < 0 || n > INT32_MAX || (n > 0 && (!ids || !mass || !pos || !vel || !acc)))
+        return bh_fail(BH_ERR_INVALID_ARGUMENT, "bh_write_vtp: bad arguments");
+    std::ofstream os(path);
+    if (!os) return bh_fail(BH_ERR_IO, std::string("bh_write_vtp: cannot open ") + path);
+    const std::string I1 = "    ", I2 = I1 + I1, I3 = I2 + I1, I4 = I3 + I1;
+    auto open_array = [&](const std::string& ind, const char* type, const char* name, int comps, bool tuples) {
+        os << ind << "<DataArray type=\"" << type << "\" Name=\"" << name << "\"";
+        if (comps > 0) os << " NumberOfComponents=\"" << comps << "\"";
+        if (tuples) os << " NumberOfTuples=\"" << n << "\"";
+        os << " format=\"ascii\">";
+    };
+    os << "<VTKFile type=\"PolyData\" version=\"0.1\">\n" << I1 << "<PolyData>\n";
+    os << I2 << "<Piece NumberOfPoints=\"" << n << "\" NumberOfVerts=\"" << n << "\">\n";
+    os << I3 << "<Points>\n";
+    open_array(I4, "Float64", "position", 3, true);
+    for (int64_t i = 0; i < n; ++i) os << pos[3 * i] << " " << pos[3 * i + 1] << " " << pos[3 * i + 2] << "\n";
+    os << "</DataArray>\n" << I3 << "</Points>\n" << I3 << "<PointData>\n";
+    open_array(I4, "Int32", "rank", 1, true);
+    for (int64_t i = 0; i < n; ++i) os << rank << "\n";
+    os << "</DataArray>\n";
+    open_array(I4, "UInt64", "body_id", 1, true);
+    for (int64_t i = 0; i < n; ++i) os << ids[i] << "\n";
+    os << "</DataArray>\n";
+    open_array(I4, "Float64", "velocity", 3, true);
+    for (int64_t i = 0; i < n; ++i) os << vel[3 * i] << " " << vel[3 * i + 1] << " " << vel[3 * i + 2] << "\n";
+    os << "</DataArray>\n";
+    open_array(I4, "Float64", "mass", 1, true);
+    for (int64_t i = 0; i < n; ++i) os << mass[i] << "\n";
+    os << "</DataArray>\n";
+    open_array(I4, "Float64", "acceleration", 1, true);
+    for (int64_t i = 0; i < n; ++i) {
+        const double ax = acc[3 * i], ay = acc[3 * i + 1], az = acc[3 * i + 2];
+        os << std::sqrt(ax * ax + ay * ay + az * az) << "\n";
+    }
+    os << "</DataArray>\n" << I3 << "</PointData>\n" << I3 << "<Verts>\n";
+    open_array(I4, "Int64", "offsets", 0, false);
+    for (int64_t i = 1; i <= n; ++i) os << i << " ";
+    os << "</DataArray>\n";
+    open_array(I4, "Int64", "connectivity", 0, false);
+    for (int64_t i = 0; i < n; ++i) os << i << " ";
+    os << "</DataArray>\n" << I3 << "</Verts>\n" << I2 << "</Piece>\n" << I1 << "</PolyData>\n</VTKFile>\n";
+    os.flush();
+    return os ? BH_OK : bh_fail(BH_ERR_IO, "bh_write_vtp: write failed");
 }

@@ -3,8 +3,8 @@
 // benchmark scripts can drive it:
 //
 //   simulate -f bodies.csv --dt 1h --tend 10d --theta 1.05 [-b N] [-r]
-//            [--fc tree] [--steps K] [--mode plain|fp64_list|fp32]
-//            [--generate N --seed S] [--dump FILE]
+//            [--fc tree] [--steps K] [--vs 10d|none] [-o sim_out]
+//            [--mode plain|fp64_list|fp32] [--generate N --seed S] [--dump FILE]
 //
 // --tend uses the reference's loop (`for (t = 0; t < t_end; t += dt)`, so
 // 10d at 1h runs 241 steps); --steps overrides it.  -r writes the final
@@ -13,12 +13,22 @@
 // printed (io.cpp:759-780).  TOTAL_TIME covers the step loop (main.cpp:185,323).
 // --dump writes the final state at full precision in the state-vector CSV
 // layout (what -f reads), bodies in the engine's final (key-sorted) order.
+//
+// Snapshots follow main.cpp:176-177,283-320: after a step whose time t
+// (before the step's t += dt) reaches the next visualisation time, and after
+// the first step, the state goes to <outdir>/0/sim.<k>.vtp (writeSnapshot,
+// io.cpp:84-232) and <outdir>/<stem>_dt.._tend.._theta.._bodies.._fc...pvd
+// lists the frames (updatePVDFile, io.cpp:235-298); -o/--outdir defaults to
+// sim_out and --vs to 10d, as in the reference.  --vs none turns them off.
+// The download of a frame waits for the GPU; its file is written by a host
+// thread while the next steps run.
 #include <chrono>
 #include <cmath>
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
 #include <filesystem>
+#include <future>
 #include <fstream>
 #include <iomanip>
 #include <iostream>
@@ -59,7 +69,8 @@ void check(int rc, const char* what)
 
 int main(int argc, char** argv)
 {
-    std::string file, fc = "tree", mode_s = "plain", dt_s = "1d", tend_s = "1y", dump;
+    std::string file, fc = "tree", mode_s = "plain", dt_s = "1d", tend_s = "1y", dump, vs_s = "10d",
+                out_dir = "sim_out";
     double theta = 1.05;
     long long bodies = -1, steps = -1, generate = 0;
     unsigned long long seed = 1;
@@ -73,7 +84,9 @@ int main(int argc, char** argv)
         if (k == "-f" || k == "--file") file = val();
         else if (k == "--dt") dt_s = val();
         else if (k == "--tend") tend_s = val();
-        else if (k == "--vs" || k == "-o" || k == "--outdir" || k == "--max-depth" || k == "--bucket-bits" ||
+        else if (k == "--vs") vs_s = val();
+        else if (k == "-o" || k == "--outdir") out_dir = val();
+        else if (k == "--max-depth" || k == "--bucket-bits" ||
                  k == "--rebalance-interval") val();  // visualisation / multi-rank options: accepted, unused
         else if (k == "-b" || k == "--bodies") bodies = std::stoll(val());
         else if (k == "--fc") fc = val();
@@ -86,7 +99,8 @@ int main(int argc, char** argv)
         else if (k == "--dump") dump = val();
         else if (k == "-h" || k == "--help") {
             std::cout << "simulate -f FILE [--dt 1h] [--tend 1y] [--theta 1.05] [-b N] [-r] [--steps K]\n"
-                         "         [--mode plain|fp64_list|fp32] [--generate N --seed S] [--dump FILE]\n";
+                         "         [--vs 10d|none] [-o sim_out] [--mode plain|fp64_list|fp32]\n"
+                         "         [--generate N --seed S] [--dump FILE]\n";
             return 0;
         } else die("unknown option " + k);
     }
@@ -125,8 +139,51 @@ int main(int argc, char** argv)
     check(bh_set_bodies(ctx, n, pos.data(), vel.data(), mass.data(), ids.data()), "bh_set_bodies");
     const double G = 1.48812e-34;
     double t = 0.0;
+    const bool frames = vs_s != "none";
+    const double vs_interval = frames ? parse_time(vs_s) : 0.0;
+    std::ostringstream pvd_name;  // updatePVDFile's file name (io.cpp:242-254)
+    pvd_name << (file.empty() ? std::string("generated") : std::filesystem::path(file).stem().string()) << "_dt"
+             << dt_s << "_tend" << tend_s << "_theta" << theta << "_bodies" << bodies << "_fc" << fc << ".pvd";
+    const std::filesystem::path vs_dir(out_dir);
+    if (frames) std::filesystem::create_directories(vs_dir / "0");
+    std::vector<double> fpos, fvel, facc, fmass, frame_t;
+    std::vector<uint64_t> fids;
+    std::future<int> writer;
+    double next_vis = 0.0;
     const auto t0 = std::chrono::high_resolution_clock::now();
-    check(bh_step(ctx, dt, theta, G, nsteps, mode, &t), "bh_step");
+    for (int64_t s = 0; s < nsteps;) {
+        // Steps up to and including the next one that writes a frame.
+        double tq = t;
+        int64_t q = s;
+        while (q < nsteps && !(frames && (tq >= next_vis || q == 0))) {
+            tq += dt;
+            ++q;
+        }
+        const int64_t run = q < nsteps ? q - s + 1 : nsteps - s;
+        check(bh_step(ctx, dt, theta, G, run, mode, &t), "bh_step");
+        s += run;
+        if (q >= nsteps) break;
+        if (writer.valid()) check(writer.get(), "bh_write_vtp");
+        fpos.resize(3 * n); fvel.resize(3 * n); facc.resize(3 * n); fmass.resize(n); fids.resize(n);
+        check(bh_get_bodies(ctx, fpos.data(), fvel.data(), fmass.data(), fids.data(), facc.data()), "bh_get_bodies");
+        const int k = (int)frame_t.size();
+        const std::string path = (vs_dir / "0" / ("sim." + std::to_string(k) + ".vtp")).string();
+        writer = std::async(std::launch::async, [&, path]() {
+            return bh_write_vtp(path.c_str(), 0, n, fids.data(), fmass.data(), fpos.data(), fvel.data(), facc.data());
+        });
+        frame_t.push_back(tq);
+        std::ofstream pvd(vs_dir / pvd_name.str());
+        pvd << "<VTKFile type=\"Collection\">\n    <Collection>\n";
+        char ts[64];
+        for (int f = 0; f < (int)frame_t.size(); ++f) {
+            std::snprintf(ts, sizeof ts, "%.17g", frame_t[f]);
+            pvd << "        <DataSet timestep=\"" << ts << "\" part=\"0\" file=\"0/sim." << f << ".vtp\"/>\n";
+        }
+        pvd << "    </Collection>\n</VTKFile>\n";
+        std::cout << "Saved frame " << k << " at t=" << tq << std::endl;
+        next_vis += vs_interval;
+    }
+    if (writer.valid()) check(writer.get(), "bh_write_vtp");
     const auto t1 = std::chrono::high_resolution_clock::now();
     check(bh_get_bodies(ctx, pos.data(), vel.data(), mass.data(), ids.data(), nullptr), "bh_get_bodies");
     bh_context_destroy(ctx);

@@ -301,6 +301,12 @@ int bh_read_csv(const char *path, int64_t body_count, int64_t *n_out, uint64_t *
  * id,name,class,mass,pos_x,pos_y,pos_z,vel_x,vel_y,vel_z). */
 int bh_write_csv(const char *path, int64_t n, const uint64_t *ids, const double *mass, const double *pos,
                  const double *vel);
+/* writeSnapshot (src/io.cpp:84-232): one VTK XML PolyData snapshot of n
+ * bodies (pos, vel, acc: 3 per body) in the reference's layout and number
+ * formatting, for ParaView; rank is the value of the "rank" array (0 for the
+ * single-rank path).  Host function: no device work. */
+int bh_write_vtp(const char *path, int rank, int64_t n, const uint64_t *ids, const double *mass, const double *pos,
+                 const double *vel, const double *acc);
 
 #ifdef __cplusplus
 }

@@ -118,3 +118,37 @@ def test_csv_round_trip_and_reader_rules(bh, tmp_path):
     assert rmass[0] == 5.0 and rvel[0].tolist() == [4.0, 5.0, 5.0]
     with pytest.raises(bh.BhError):
         bh.read_csv(tmp_path / "missing.csv")
+
+
+def test_vtp_snapshot_layout(bh, tmp_path):
+    """bh_write_vtp follows writeSnapshot (io.cpp:84-232): PolyData with the
+    position points, rank/body_id/velocity/mass/acceleration-magnitude point
+    arrays and one vertex per body, numbers in the default stream format."""
+    import xml.etree.ElementTree as ET
+    rng = np.random.default_rng(5)
+    n = 7
+    pos = rng.normal(0, 3, (n, 3)); vel = rng.normal(0, 1e-2, (n, 3)); acc = rng.normal(0, 1e-5, (n, 3))
+    mass = rng.uniform(1e15, 1e25, n); ids = np.arange(100, 100 + n, dtype=np.uint64)
+    path = tmp_path / "sim.0.vtp"
+    bh.write_vtp(path, ids, mass, pos, vel, acc)
+    root = ET.parse(path).getroot()
+    assert root.tag == "VTKFile" and root.get("type") == "PolyData" and root.get("version") == "0.1"
+    piece = root.find("PolyData/Piece")
+    assert piece.get("NumberOfPoints") == str(n) and piece.get("NumberOfVerts") == str(n)
+
+    def arr(where, name):
+        for da in piece.find(where).findall("DataArray"):
+            if da.get("Name") == name:
+                return da
+        raise AssertionError(name)
+    g = lambda v: "%g" % v  # noqa: E731  (the default ostream format: 6 significant digits)
+    p = arr("Points", "position")
+    assert p.get("type") == "Float64" and p.get("NumberOfComponents") == "3"
+    assert p.text.split() == [g(v) for v in pos.ravel()]
+    assert arr("PointData", "rank").text.split() == ["0"] * n
+    assert arr("PointData", "body_id").text.split() == [str(i) for i in ids]
+    assert arr("PointData", "velocity").text.split() == [g(v) for v in vel.ravel()]
+    assert arr("PointData", "mass").text.split() == [g(v) for v in mass]
+    assert arr("PointData", "acceleration").text.split() == [g(v) for v in np.sqrt((acc ** 2).sum(axis=1))]
+    assert arr("Verts", "offsets").text.split() == [str(i) for i in range(1, n + 1)]
+    assert arr("Verts", "connectivity").text.split() == [str(i) for i in range(n)]

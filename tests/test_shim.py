@@ -163,3 +163,43 @@ def test_simulate_driver_matches_reference_loop(bh, tmp_path):
     r = subprocess.run([str(BUILD / "simulate"), "--generate", "2000", "--seed", "3", "--steps", "2",
                         "--mode", "fp32"], capture_output=True, text=True, cwd=tmp_path)
     assert r.returncode == 0 and "Loaded 2000 bodies" in r.stdout
+
+
+@pytest.mark.gpu
+def test_simulate_snapshots_follow_reference_schedule(bh, tmp_path):
+    """Frames as main.cpp:283-320 writes them: after the first step and after
+    every step whose time (before t += dt) reaches the next visualisation
+    time; one .vtp per frame under <outdir>/0 and a .pvd collection of them.
+    The last frame holds the final state (6 significant digits)."""
+    import xml.etree.ElementTree as ET
+    _built()
+    g = np.load(GOLDEN / "synthetic_1000.npz")
+    csv = tmp_path / "bodies.csv"
+    bh.write_csv(csv, g["ids"], g["mass"], g["pos"], g["vel"])
+    steps, dt, vs = 5, 1.0 / 24.0, 2.0 / 24.0
+    out = tmp_path / "frames"
+    r = subprocess.run([str(BUILD / "simulate"), "-f", str(csv), "--dt", "1h", "--steps", str(steps), "--vs", "2h",
+                        "-o", str(out), "--dump", str(tmp_path / "final.csv")], capture_output=True, text=True,
+                       cwd=tmp_path)
+    assert r.returncode == 0, r.stderr
+    # the reference's schedule, in the same floating-point arithmetic
+    want, t, nxt = [], 0.0, 0.0
+    for s in range(steps):
+        if t >= nxt or s == 0:
+            want.append((s, t))
+            nxt += vs
+        t += dt
+    pvd = out / f"bodies_dt1h_tend1y_theta{THETA:g}_bodies-1_fctree.pvd"
+    sets = ET.parse(pvd).getroot().findall("Collection/DataSet")
+    assert [float(d.get("timestep")) for d in sets] == [w[1] for w in want]
+    assert [d.get("file") for d in sets] == [f"0/sim.{k}.vtp" for k in range(len(want))]
+    assert r.stdout.count("Saved frame") == len(want)
+    last = ET.parse(out / "0" / f"sim.{len(want) - 1}.vtp").getroot()
+    if want[-1][0] == steps - 1:
+        _, mass, pos, vel = bh.read_csv(tmp_path / "final.csv")
+        da = [d for d in last.iter("DataArray") if d.get("Name") == "position"][0]
+        got = np.array(da.text.split(), dtype=float).reshape(-1, 3)
+        assert np.allclose(got, pos, rtol=1e-5, atol=1e-9)
+    r = subprocess.run([str(BUILD / "simulate"), "-f", str(csv), "--steps", "2", "--vs", "none", "-o",
+                        str(tmp_path / "none")], capture_output=True, text=True, cwd=tmp_path)
+    assert r.returncode == 0 and not (tmp_path / "none").exists()
