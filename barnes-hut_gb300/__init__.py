@@ -94,6 +94,7 @@ def _sig(lib):
     f["bh_direct_sum"] = (C.c_int, [_P, _I64, _P, _D, _P])
     f["bh_invariants"] = (C.c_int, [_P, _D, _D, _P])
     f["bh_tree_spread"] = (C.c_int, [_P, _P])
+    f["bh_kepler_to_cartesian_gpu"] = (C.c_int, [_P, _I64, _P])
     f["bh_write_vtp"] = (C.c_int, [C.c_char_p, C.c_int, _I64, _P, _P, _P, _P, _P])
     f["bh_selftest"] = (C.c_int, [C.c_int, _I64, C.c_uint64, C.POINTER(_I64)])
     f["bh_tree_slots"] = (C.c_int, [_P, _P, _P])
@@ -155,6 +156,14 @@ def kepler_to_cartesian(elements) -> np.ndarray:
     el = _f64(elements).reshape(-1, 8)
     out = np.empty((el.shape[0], 6))
     _check(library().bh_kepler_to_cartesian(_ptr(el), el.shape[0], _ptr(out)))
+    return out
+
+
+def kepler_to_cartesian_gpu(elements) -> np.ndarray:
+    """The same conversion, batched on the GPU (agrees to rounding)."""
+    el = _f64(elements).reshape(-1, 8)
+    out = np.empty((el.shape[0], 6))
+    _check(library().bh_kepler_to_cartesian_gpu(_ptr(el), el.shape[0], _ptr(out)))
     return out
 
 

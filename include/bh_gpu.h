@@ -283,6 +283,11 @@ int bh_sort_keys_noalloc(const uint64_t *keys_in, uint64_t *keys_out, uint32_t *
  * el: n*8 = {e, a, i, arg. periapsis, long. asc. node, M, epoch, mu}
  * (radians, AU, days); out: n*6 = {x, y, z, vx, vy, vz}. */
 int bh_kepler_to_cartesian(const double *el, int64_t n, double *out);
+/* The same conversion for many bodies at once on the current CUDA device
+ * (one thread per body; host arrays in and out).  Agrees with
+ * bh_kepler_to_cartesian to rounding: the device math functions differ from
+ * the host's in their last bits. */
+int bh_kepler_to_cartesian_gpu(const double *el, int64_t n, double *out);
 /* Seeded synthetic solar system (std::mt19937_64): the Sun (1.989e30 kg at
  * rest at the origin), the 8 planets on circular coplanar orbits, and
  * n - 9 asteroids: an inner belt, a fraction frac_outer in an outer belt

@@ -123,3 +123,25 @@ def test_second_moment_spread_matches_fp64(bh):
         assert abs(spread[s] - ref) <= 1e-5 * ref + 1e-12 * np.abs(com).max(), (s, d, spread[s], ref)
         checked += 1
     assert checked > 2000
+
+
+def test_kepler_batch_on_gpu_matches_host(bh):
+    """The batched GPU conversion of orbital elements agrees with the host
+    restatement of convertKeplerToCartesian to 1e-12 relative (the two math
+    libraries round sin, cos and atan2 differently in the last bits), on
+    asteroid-belt elements, and is faster than the host at 1M bodies."""
+    import time
+    rng = np.random.default_rng(9)
+    n = 1_000_000
+    mu = 1.48812e-34 * 1.989e30
+    el = np.stack([rng.uniform(0, 0.3, n), rng.uniform(2.1, 3.3, n), rng.uniform(0, 0.35, n),
+                   rng.uniform(0, 2 * np.pi, n), rng.uniform(0, 2 * np.pi, n), rng.uniform(0, 2 * np.pi, n),
+                   np.full(n, 2451544.5), np.full(n, mu)], axis=1)
+    t0 = time.perf_counter(); host = bh.kepler_to_cartesian(el); t1 = time.perf_counter()
+    bh.kepler_to_cartesian_gpu(el[:1000])  # context set-up outside the timing
+    t2 = time.perf_counter(); dev = bh.kepler_to_cartesian_gpu(el); t3 = time.perf_counter()
+    print(f"host {t1 - t0:.3f} s, gpu {t3 - t2:.3f} s for {n} bodies")
+    for sl in (slice(0, 3), slice(3, 6)):
+        d = np.linalg.norm(dev[:, sl] - host[:, sl], axis=1) / np.linalg.norm(host[:, sl], axis=1)
+        assert d.max() < 1e-12
+    assert t3 - t2 < t1 - t0
