@@ -94,6 +94,7 @@ def _sig(lib):
     f["bh_direct_sum"] = (C.c_int, [_P, _I64, _P, _D, _P])
     f["bh_invariants"] = (C.c_int, [_P, _D, _D, _P])
     f["bh_tree_spread"] = (C.c_int, [_P, _P])
+    f["bh_set_step_graphs"] = (C.c_int, [_P, C.c_int])
     f["bh_kepler_to_cartesian_gpu"] = (C.c_int, [_P, _I64, _P])
     f["bh_write_vtp"] = (C.c_int, [C.c_char_p, C.c_int, _I64, _P, _P, _P, _P, _P])
     f["bh_selftest"] = (C.c_int, [C.c_int, _I64, C.c_uint64, C.POINTER(_I64)])
@@ -334,6 +335,10 @@ class Context:
         v = _I64(0)
         _check(library().bh_interaction_count(self._h, C.byref(v)))
         return v.value
+
+    def set_step_graphs(self, on: bool) -> None:
+        """Replay kicked steps through a captured CUDA graph (default on)."""
+        _check(library().bh_set_step_graphs(self._h, 1 if on else 0))
 
     def set_profiling(self, on: bool = True) -> None:
         _check(library().bh_set_profiling(self._h, 1 if on else 0))

@@ -253,6 +253,61 @@ int step_once(bh_context* ctx, double dt, double theta, double G, int mode)
     return rc;
 }
 
+// A step with the kick (every step of a run after its first) through a CUDA
+// graph: captured from step_once on first use for this (bodies, mode, dt,
+// theta, G, merge, direct-body count) configuration, then replayed, which
+// enqueues the step's ~50 kernels with one call.  The step reads one body set
+// and leaves the state in the other, so there is one graph per starting set;
+// after a replay the host pointers trade places as step_once's permutation
+// would make them.  The kernels read no host state that the key leaves out:
+// buffers live in the context's single allocation and the learned model in a
+// fixed device block.
+int step_graph(bh_context* ctx, double dt, double theta, double G, int mode)
+{
+    const int merge = ctx->build_merge ? 1 : 0;
+    bh_context::StepGraph& g = ctx->sg[ctx->px < ctx->px2 ? 0 : 1];
+    if (!(g.exec && g.n == ctx->n && g.mode == mode && g.dt == dt && g.theta == theta && g.G == G &&
+          g.merge == merge && g.nd == ctx->num_direct)) {
+        if (g.exec) {
+            cudaGraphExecDestroy(g.exec);
+            g.exec = nullptr;
+        }
+        const int64_t l0 = ctx->launches;
+        BH_CUDA_TRY(cudaStreamBeginCapture(ctx->stream, cudaStreamCaptureModeRelaxed));
+        const int rc = step_once(ctx, dt, theta, G, mode);
+        bh::swap_body_sets(ctx);  // capturing ran no kernel: back to the starting set
+        const int64_t captured = ctx->launches - l0;
+        ctx->launches = l0;
+        cudaGraph_t graph = nullptr;
+        cudaError_t e = cudaStreamEndCapture(ctx->stream, &graph);
+        if (rc || e != cudaSuccess) {
+            if (graph) cudaGraphDestroy(graph);
+            cudaGetLastError();
+            return rc ? rc : bh_fail(BH_ERR_CUDA, std::string("bh_step: graph capture: ") + cudaGetErrorString(e));
+        }
+        e = cudaGraphInstantiate(&g.exec, graph, 0);
+        cudaGraphDestroy(graph);
+        if (e != cudaSuccess) {
+            g.exec = nullptr;
+            return bh_fail(BH_ERR_CUDA, std::string("bh_step: graph instantiation: ") + cudaGetErrorString(e));
+        }
+        g.launches = captured;
+        g.n = ctx->n;
+        g.mode = mode;
+        g.dt = dt;
+        g.theta = theta;
+        g.G = G;
+        g.merge = merge;
+        g.nd = ctx->num_direct;
+    }
+    BH_CUDA_TRY(cudaGraphLaunch(g.exec, ctx->stream));
+    bh::swap_body_sets(ctx);
+    ctx->launches += g.launches;
+    ctx->tree_far = mode >= BH_MODE_FP32_FAR;
+    ctx->tree_moments = mode == BH_MODE_LEARNED;
+    return BH_OK;
+}
+
 }  // namespace
 
 int bh_fail(int status, const std::string& msg)
@@ -342,7 +397,16 @@ int bh_context_destroy(bh_context* ctx)
     if (ctx->h_small) cudaFreeHost(ctx->h_small);
     for (cudaEvent_t e : ctx->ev_pool) cudaEventDestroy(e);
     if (ctx->mlp_dev) cudaFree(ctx->mlp_dev);
+    for (auto& g : ctx->sg)
+        if (g.exec) cudaGraphExecDestroy(g.exec);
     delete ctx;
+    return BH_OK;
+}
+
+int bh_set_step_graphs(bh_context* ctx, int on)
+{
+    if (!ctx) return bh_fail(BH_ERR_INVALID_ARGUMENT, "bh_set_step_graphs: null context");
+    ctx->graphs = on != 0;
     return BH_OK;
 }
 
@@ -734,7 +798,10 @@ int bh_step(bh_context* ctx, double dt, double theta, double G, int64_t nsteps, 
     if (nsteps < 0 || !(theta >= 0.0)) return bh_fail(BH_ERR_INVALID_ARGUMENT, "bh_step: bad nsteps or theta");
     if (t_io) ctx->t = *t_io;
     for (int64_t s = 0; s < nsteps; ++s) {
-        if (ctx->n > 0 && (rc = step_once(ctx, dt, theta, G, mode))) return rc;
+        if (ctx->n > 0) {
+            const bool graph = ctx->graphs && !ctx->prof && ctx->t > 0;
+            if ((rc = graph ? step_graph(ctx, dt, theta, G, mode) : step_once(ctx, dt, theta, G, mode))) return rc;
+        }
         ctx->t += dt;
     }
     rc = finish(ctx, "bh_step");

@@ -331,6 +331,15 @@ struct bh_context {
     std::vector<Mark> marks;
     double phase_ms[8] = {0, 0, 0, 0, 0, 0, 0, 0};
     int64_t launches = 0;  // kernels of this library enqueued so far
+    // CUDA graphs of one kicked step, replayed while their configuration
+    // holds; one per body set the step starts from (the sets alternate).
+    bool graphs = true;
+    struct StepGraph {
+        cudaGraphExec_t exec = nullptr;
+        int64_t n = -1, launches = 0;
+        int mode = -1, merge = -1, nd = -1;
+        double dt = 0.0, theta = 0.0, G = 0.0;
+    } sg[2];
 
     // Error word raised by kernels and a pinned mirror for readback.
     unsigned* err = nullptr;
@@ -350,6 +359,9 @@ size_t sort_smem_bytes();
 int64_t scan_tmp_ints(int64_t n_max);
 int launch_sort(bh_context* ctx);
 int launch_permute(bh_context* ctx);
+// The permutation gathers into the second body set; the two sets then trade
+// places (host pointers only).
+void swap_body_sets(bh_context* ctx);
 // The onesweep passes over raw buffers (the allocation-free sort entry).
 int sort_passes_raw(int64_t n, const uint64_t* keys_in, uint64_t* keys_out, uint32_t* vals_out, uint64_t* key_alt,
                     uint32_t* val_alt, uint32_t* hist, uint32_t* lookback, uint32_t* tile_ctr, unsigned* err,

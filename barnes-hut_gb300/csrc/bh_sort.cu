@@ -293,6 +293,12 @@ int launch_permute(bh_context* ctx)
                                                              ctx->vz, ctx->m, ctx->id, ctx->px2, ctx->py2, ctx->pz2,
                                                              ctx->vx2, ctx->vy2, ctx->vz2, ctx->m2, ctx->id2);
     BH_LAUNCH_CHECK(ctx);
+    swap_body_sets(ctx);
+    return BH_OK;
+}
+
+void swap_body_sets(bh_context* ctx)
+{
     std::swap(ctx->px, ctx->px2);
     std::swap(ctx->py, ctx->py2);
     std::swap(ctx->pz, ctx->pz2);
@@ -301,7 +307,6 @@ int launch_permute(bh_context* ctx)
     std::swap(ctx->vz, ctx->vz2);
     std::swap(ctx->m, ctx->m2);
     std::swap(ctx->id, ctx->id2);
-    return BH_OK;
 }
 
 }  // namespace bh

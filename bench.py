@@ -423,11 +423,16 @@ def north_star(args, dev, params, scale, info):
                 row["fallback_rate"] = st["fallback"] / max(1, st["candidates"])
                 row["network_accept_rate"] = st["accepted"] / max(1, st["candidates"])
             ctx.set_bodies(pos, vel, mass, ids)
-            ctx.set_profiling(True)
             ms, ipb = time_steps(ctx, ext, flush, mode, theta, args.ns_steps, 2)
+            # phase split from a separate profiled pass (kernels one by one)
+            ctx.set_profiling(True)
+            for _ in range(2):
+                flush.fill_(1.0)
+                ctx.step(DT, theta, G, 1, mode, t=1.0)
+            torch.cuda.synchronize()
             phases, _ = ctx.phase_times()
             ctx.set_profiling(False)
-            steps = args.ns_steps + 2
+            steps = 2
             row.update({"ms_per_step": ms, "body_steps_per_s": n / (ms * 1e-3), "interactions_per_body": ipb,
                         "phases_ms_per_step": {k: v / steps for k, v in phases.items()}})
             rows[name] = row
@@ -491,7 +496,6 @@ def run_ours(args, rank, ws, local):
         t = ctx.step(DT, theta, G, 1, mode, t=t)
     peak = ctx.measure_fma_peak(mode <= 1)
 
-    ctx.set_profiling(True)
     l0 = ctx.launches()
     times, inter = [], 0
     barrier(ws)
@@ -509,10 +513,17 @@ def run_ours(args, rank, ws, local):
             inter += ctx.interaction_count()
     torch.cuda.synchronize(dev)
     launches = ctx.launches() - l0
-    phases, _ = ctx.phase_times()
-    ctx.set_profiling(False)
     total_ms = sum(times)
     total_ms = reduce_max(total_ms, ws)
+    # Per-phase device times: the same number of steps again with CUDA events
+    # around each phase (kernels launched one by one), outside the timed run.
+    ctx.set_profiling(True)
+    for _ in range(args.steps):
+        flush.fill_(1.0)
+        t = ctx.step(DT, theta, G, 1, mode, t=t)
+    torch.cuda.synchronize(dev)
+    phases, _ = ctx.phase_times()
+    ctx.set_profiling(False)
 
     # End to end through the C ABI with host-resident state (pinned memory).
     pin = lambda shape, dt: torch.empty(shape, dtype=dt, pin_memory=True).numpy()  # noqa: E731

@@ -170,6 +170,12 @@ int bh_interaction_counts(bh_context *ctx, int32_t *per_body);
 int bh_step(bh_context *ctx, double dt, double theta, double G, int64_t nsteps, int mode, double *t_io);
 
 /* ---- measurement (no reference counterpart) -------------------------- */
+/* Steps with the kick (all but the first of a run) go through a CUDA graph
+ * of the whole step, captured on first use and replayed while the bodies
+ * count, mode, dt, theta, G, merge option and direct-body count stay the
+ * same (not while profiling).  on = 0 launches every kernel one by one.
+ * No reference counterpart. */
+int bh_set_step_graphs(bh_context *ctx, int on);
 /* Enables (on != 0) or disables CUDA-event timing of the phases of bh_step
  * and clears the accumulated times. */
 int bh_set_profiling(bh_context *ctx, int on);
