@@ -30,7 +30,11 @@ and seeded (the reference's 300k CSV is not part of its repository).
   {1e-4, 1e-5, 1e-6} with its fallback rate.
 * precision_run: the FP32 far-field form on 1M bodies at theta {0.5, 0.8,
   1.05}, then 1,000 steps with error, energy and angular-momentum drift every
-  100 steps.  --no-north-star skips these three blocks.
+  100 steps.
+* long_runs: the configurations' own run lengths, 2,000 steps of the 300k
+  FP64 list workload and 500 steps of the 4M FP32 + learned form, each timed
+  as one span, with the final error and the energy/angular-momentum drift.
+  --no-north-star skips these four blocks.
 
 Multi-GPU: the path does not shard on one GPU per rank; ranks run replicas
 (weak scaling) and value is the sum of their body-steps over the slowest
@@ -296,6 +300,44 @@ def _fresh(ctx, pos, vel, mass, ids):
     ctx.compute_bbox(); ctx.compute_keys(); ctx.sort_bodies(); ctx.build_tree()
 
 
+def long_run(dev, n, frac_outer, frac_trojan, seed, mode_name, steps, params=None, scale=None, budget=None,
+             theta_max=3.0):
+    """A run of the configuration's own length: `steps` steps through the
+    step loop (graph replay after the first) timed as one span of CUDA events
+    on the engine's stream, then the error against the FP64 direct sum on a
+    4,096-body sample and the drift of energy and angular momentum."""
+    import torch
+    bh = importlib.import_module("barnes-hut_gb300")
+    mode = MODES[mode_name]
+    pos, vel, mass, ids = bh.generate_system(seed, n, frac_outer, frac_trojan)
+    with bh.Context(n, dev) as ctx:
+        ext = torch.cuda.ExternalStream(ctx.stream(), device=dev)
+        if budget is not None:
+            ctx.learned_set_model(params, scale, budget=budget, theta_max=theta_max)
+        ctx.set_bodies(pos, vel, mass, ids)
+        inv0 = ctx.invariants(G, THETA)
+        ctx.set_bodies(pos, vel, mass, ids)
+        torch.cuda.synchronize(dev)
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record(ext)
+        t = ctx.step(DT, THETA, G, steps, mode, t=0.0)
+        e1.record(ext)
+        e1.synchronize()
+        ms = e0.elapsed_time(e1)
+        inv = ctx.invariants(G, THETA)
+        rng = np.random.default_rng(7)
+        sample = np.sort(rng.choice(n, min(n, 4096), replace=False))
+        ref = ctx.direct_sum(sample, G)
+        a = ctx.compute_accelerations(THETA, G, 0.0, mode)
+        e = np.linalg.norm(a[sample] - ref, axis=1) / np.linalg.norm(ref, axis=1)
+    return {"bodies": n, "mode": mode_name, "budget": budget, "steps": steps, "simulated_days": t,
+            "ms_total": ms, "body_steps_per_s": n * steps / (ms * 1e-3),
+            "final_median_rel_err": float(np.median(e)), "final_p99_rel_err": float(np.quantile(e, 0.99)),
+            "rel_energy_drift": float((inv["E"] - inv0["E"]) / abs(inv0["E"])),
+            "rel_angular_momentum_drift": float(np.linalg.norm(inv["L"] - inv0["L"]) / np.linalg.norm(inv0["L"]))}
+
+
 def precision_run(args, dev):
     """The precision form on 1M bodies (90/10 inner/outer belt): FP32 far field
     with FP64 displacements, direct terms and state.  Error against the FP64
@@ -552,12 +594,15 @@ def run_ours(args, rank, ws, local):
     accuracy = {"median_rel_err": float(np.median(err)), "p99_rel_err": float(np.quantile(err, 0.99)),
                 "sample": int(len(sample)), "judge": "FP64 direct sum"}
 
-    ns = pr = le = None
+    ns = pr = le = runs = None
     if rank == 0 and ws == 1 and not args.no_north_star:
         params, scale, info = train_model(args)
         ns = north_star(args, dev, params, scale, info)
         le = learned_eval(args, dev, params, scale)
         pr = precision_run(args, dev)
+        runs = {"config2_300k_fp64_list_2000_steps": long_run(dev, N_BODIES, 0.10, 0.0, SEED, "fp64_list", 2000),
+                "config5_4m_fp32_learned_500_steps": long_run(dev, args.ns_bodies, 0.10, 0.05, SEED + 1, "learned",
+                                                              500, params, scale, 1e-6, args.theta_max)}
 
     cpu = None
     if rank == 0 and not args.no_cpu_baseline:
@@ -597,6 +642,7 @@ def run_ours(args, rank, ws, local):
         "north_star": ns,
         "learned_eval": le,
         "precision_run": pr,
+        "long_runs": runs,
     }
     print(json.dumps(line), flush=True)
 
