@@ -40,6 +40,8 @@
 //   training range use the theta test (the fallback), and are counted.
 // Collection (bh_learned_collect): the FP32 walk with the theta test only,
 //   recording every candidate's group, slot, lane mask and raw features.
+#include <climits>
+
 #include "bh_internal.cuh"
 #include "bh_mlp.cuh"
 
@@ -218,6 +220,13 @@ __global__ void __launch_bounds__(kThreads) traverse_masked_kernel(FParams p)
     }
     const unsigned full = __ballot_sync(0xffffffffu, valid);
     const int my_leaf = valid ? p.body_leaf[i] : -2;
+    // The group's leaf ids span [leaf_lo, leaf_hi] (bodies in key order).
+    int leaf_lo = valid ? my_leaf : INT_MAX, leaf_hi = valid ? my_leaf : INT_MIN;
+#pragma unroll
+    for (int off = 16; off > 0; off >>= 1) {
+        leaf_lo = min(leaf_lo, __shfl_xor_sync(0xffffffffu, leaf_lo, off));
+        leaf_hi = max(leaf_hi, __shfl_xor_sync(0xffffffffu, leaf_hi, off));
+    }
     const float theta2f = (float)p.theta2;
     const double theta2 = p.theta2, soft2 = p.soft2;
     if (kFP64) {
@@ -474,6 +483,22 @@ __global__ void __launch_bounds__(kThreads) traverse_masked_kernel(FParams p)
                 const unsigned Aj = __ballot_sync(0xffffffffu, acc) & Mj;
                 if (lane == j) A = Aj;
             }
+            if (!kFP64 && kLearn == kLearnNone) {
+                // A body never interacts with its own leaf (traversal.cpp:70,
+                // the FP32 form has no chain rule for it): its lanes leave
+                // the leaf's mask here, so the evaluation needs no leaf test.
+                // (The learned walk keeps the test: the extra registers cost
+                // it more occupancy than the test costs.)
+                const bool own_cand = A != 0 && leaf && ref >= leaf_lo && ref <= leaf_hi;
+                unsigned oc = __ballot_sync(0xffffffffu, own_cand);
+                while (oc) {
+                    const int j = __ffs(oc) - 1;
+                    oc &= oc - 1u;
+                    const int lj = __shfl_sync(0xffffffffu, ref, j);
+                    const unsigned own = __ballot_sync(0xffffffffu, my_leaf == lj);
+                    if (lane == j) A &= ~own;
+                }
+            }
             // Stage the accepted (node, lanes) entries.
             const bool stage = A != 0;
             const unsigned am = __ballot_sync(0xffffffffu, stage);
@@ -578,7 +603,7 @@ __global__ void __launch_bounds__(kThreads) traverse_masked_kernel(FParams p)
                 for (int j = 0; j < nlist; ++j) {
                     const float4 q = L[j];
                     const unsigned mj = LM[j];
-                    const bool take = (mj & me) && LL[j] != my_leaf;
+                    const bool take = (mj & me) != 0u && (kLearn == kLearnNone || LL[j] != my_leaf);
                     const float dx = q.x - rx, dy = q.y - ry, dz = q.z - rz;
                     const float r2 = fmaf(dx, dx, fmaf(dy, dy, fmaf(dz, dz, (float)soft2)));
                     const float inv = rsqrtf(r2);

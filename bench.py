@@ -633,6 +633,7 @@ def run_ours(args, rank, ws, local):
         "phases_ms_per_step": {kk: v / k for kk, v in phases.items()},
         "hbm_phases": hbm_phases({kk: v / k for kk, v in phases.items()}, n),
         "interactions_per_body": inter_per_step / n,
+        "interactions_per_s": inter_per_step / (force_ms * 1e-3),
         "accuracy": accuracy,
         "e2e": {"value": ws * n * e2e_steps / e2e_s, "unit": "body-steps/s", "h2d_bytes_per_step": h2d,
                 "d2h_bytes_per_step": d2h},
