@@ -252,16 +252,23 @@ def test_division_free_helpers_match_ieee(bh, which, n):
     assert bh.selftest(which, n, seed=12345) == 0
 
 
-@pytest.mark.parametrize("mode", ["MODE_PLAIN_FP64", "MODE_FP64_LIST", "MODE_FP32_FAR"])
+@pytest.mark.parametrize("mode", ["MODE_PLAIN_FP64", "MODE_FP64_LIST", "MODE_FP32_FAR", "MODE_LEARNED"])
 def test_step_graphs_replay_the_same_kernels(bh, mode):
     """Kicked steps replayed through the captured CUDA graph give the same
     state bit for bit as launching the kernels one by one, with the same
-    count of kernels; a change of theta re-captures."""
+    count of kernels; a change of theta re-captures.  The learned form runs
+    with a fixed (untrained) network: its decisions only need to repeat."""
     pos, vel, mass, ids = bh.generate_system(41, 20_000, 0.1, 0.05)
+    rng = np.random.default_rng(3)
+    params = (rng.normal(0, 0.2, bh.MLP_PARAMS)).astype(np.float32)
+    scale = np.concatenate([np.zeros(8), np.ones(8), np.full(8, -50.0), np.full(8, 50.0),
+                            [0.0, 1.0]]).astype(np.float32)
     out = []
     for graphs in (False, True):
         with bh.Context(len(mass)) as c:
             c.set_step_graphs(graphs)
+            if mode == "MODE_LEARNED":
+                c.learned_set_model(params, scale, budget=1e-6, theta_max=3.0)
             c.set_bodies(pos, vel, mass, ids)
             l0 = c.launches()
             t = c.step(DT, THETA, G, nsteps=4, mode=getattr(bh, mode), t=0.0)
