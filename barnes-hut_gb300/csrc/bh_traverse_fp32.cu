@@ -260,6 +260,9 @@ __global__ void __launch_bounds__(kThreads) traverse_masked_kernel(FParams p)
             if (!p.present[kk] || my_id == (uint64_t)kk) continue;
             const double dx = p.direct[4 * kk] - x, dy = p.direct[4 * kk + 1] - y, dz = p.direct[4 * kk + 2] - z;
             const double r2 = fma(dx, dx, fma(dy, dy, fma(dz, dz, soft2)));
+            // A body at the very position of a direct body shares its leaf,
+            // which the reference skips (traversal.cpp:70): no term.
+            if (__double_as_longlong(r2) == 0) continue;
             const double inv = rsqrt_hh(r2);
             const double sc = p.direct[4 * kk + 3] * (inv * inv * inv);
             adx = fma(sc, dx, adx);
