@@ -287,11 +287,16 @@ def test_edge_systems_step_in_every_form(bh, golden, port, name):
     the oracle's loop bit for bit."""
     g = golden("edge_cases.npz")
     pos, vel, mass, ids = (g[f"{name}/{k}"] for k in ("pos", "vel", "mass", "ids"))
-    for mode in ("MODE_PLAIN_FP64", "MODE_FP64_LIST", "MODE_FP32_FAR"):
+    rng = np.random.default_rng(3)
+    params = (rng.normal(0, 0.2, bh.MLP_PARAMS)).astype(np.float32)
+    scale = np.concatenate([np.zeros(8), np.ones(8), np.full(8, -50.0), np.full(8, 50.0),
+                            [0.0, 1.0]]).astype(np.float32)
+    for mode in ("MODE_PLAIN_FP64", "MODE_FP64_LIST", "MODE_FP32_FAR", "MODE_LEARNED"):
         res = []
         for graphs in (False, True):
             with bh.Context(max(len(mass), 16)) as c:  # capacity above the bodies count
                 c.set_step_graphs(graphs)
+                c.learned_set_model(params, scale, budget=1e-6, theta_max=3.0)
                 c.set_bodies(pos, vel, mass, ids)
                 c.step(DT, THETA, G, nsteps=3, mode=getattr(bh, mode), t=0.0)
                 res.append(c.get_bodies())
