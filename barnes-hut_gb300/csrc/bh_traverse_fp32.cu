@@ -157,23 +157,28 @@ struct FParams {
 
 namespace {
 
+// Per-block shared memory of the walk.  Tables a variant does not use shrink
+// to one element, so that the FP32 walk fits 8 blocks (32 warps) per SM.
 template <bool kFP64, int kLearn>
 struct WalkSmem {
+    static constexpr int kW64 = kFP64 ? kWarps : 1;      // FP64-only tables
+    static constexpr bool kLL = kFP64 || kLearn == 1;     // leaf ids kept for the evaluation's own-leaf test
+    static constexpr bool kF = kLearn == 1;              // network input rows
     int2 stack[kWarps][kStack];  // sibling ranges: {first | (count - 1) << 28, lane mask}
     float4 lst[kWarps][kList];
     int lst_node[kWarps][kList];
-    int lst_leaf[kWarps][kList];
+    int lst_leaf[kLL ? kWarps : 1][kLL ? kList : 1];
     unsigned lst_mask[kWarps][kList];
     float side2f[kMaxDepth + 1];
     double side2d[kMaxDepth + 1];
-    float feat[kLearn ? kWarps : 1][32][9];
-    uint8_t plist[kFP64 ? kWarps : 1][kList][32];  // FP64: each lane's own entries, in order
+    float feat[kF ? kWarps : 1][kF ? 32 : 1][9];
+    uint8_t plist[kW64][kFP64 ? kList : 1][32];  // FP64: each lane's own entries, in order
     // FP64: the balanced evaluation's per-warp tables (see the flush).
-    int poff[kFP64 ? kWarps : 1][33];       // first pair of each lane, then the total
-    double bpos[kFP64 ? kWarps : 1][3][32]; // the bodies' positions
-    int bleaf[kFP64 ? kWarps : 1][32];      // the bodies' leaf ids
-    double bacc[kFP64 ? kWarps : 1][3][32]; // the bodies' accumulated list terms
-    unsigned bcnt[kFP64 ? kWarps : 1][32];  // and their interaction counts
+    int poff[kW64][33];                     // first pair of each lane, then the total
+    double bpos[kW64][3][kFP64 ? 32 : 1];   // the bodies' positions
+    int bleaf[kW64][kFP64 ? 32 : 1];        // the bodies' leaf ids
+    double bacc[kW64][3][kFP64 ? 32 : 1];   // the bodies' accumulated list terms
+    unsigned bcnt[kW64][kFP64 ? 32 : 1];    // and their interaction counts
 };
 
 template <bool kFP64, int kLearn>
@@ -243,7 +248,7 @@ __global__ void __launch_bounds__(kThreads) traverse_masked_kernel(FParams p)
     int2* stk = sm.stack[w];
     float4* L = sm.lst[w];
     int* LN = sm.lst_node[w];
-    int* LL = sm.lst_leaf[w];
+    int* LL = WalkSmem<kFP64, kLearn>::kLL ? sm.lst_leaf[w] : nullptr;
     unsigned* LM = sm.lst_mask[w];
     const unsigned me = 1u << lane;
     const unsigned lt = me - 1u;
@@ -509,7 +514,7 @@ __global__ void __launch_bounds__(kThreads) traverse_masked_kernel(FParams p)
                 const int pos = nlist + __popc(am & lt);
                 L[pos] = e;
                 LN[pos] = node;
-                LL[pos] = leaf ? ref : -1;  // leaf id for the own-leaf test
+                if (WalkSmem<kFP64, kLearn>::kLL) LL[pos] = leaf ? ref : -1;  // for the own-leaf test
                 LM[pos] = A;
             }
             nlist += __popc(am);
@@ -680,6 +685,14 @@ int launch_walk(bh_context* ctx, const FParams& p)
     const size_t smem = sizeof(WalkSmem<kFP64, kLearn>);
     BH_CUDA_TRY(cudaFuncSetAttribute(traverse_masked_kernel<kFP64, kLearn>,
                                      cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    // The plain walks keep their working set in shared memory and L2 (L1
+    // hit rates are low): shared memory takes the whole carveout, for more
+    // resident blocks.  The learned walk reads the network's weights through
+    // L1 and keeps the default split.
+    if (kLearn == kLearnNone)
+        BH_CUDA_TRY(cudaFuncSetAttribute(traverse_masked_kernel<kFP64, kLearn>,
+                                         cudaFuncAttributePreferredSharedMemoryCarveout,
+                                         (int)cudaSharedmemCarveoutMaxShared));
     const int64_t groups = (p.n + 31) / 32;
     const int64_t blocks = (groups + kWarps - 1) / kWarps;
     traverse_masked_kernel<kFP64, kLearn><<<(unsigned)blocks, kThreads, smem, ctx->stream>>>(p);
