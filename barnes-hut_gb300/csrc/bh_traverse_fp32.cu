@@ -165,7 +165,7 @@ struct WalkSmem {
     static constexpr bool kLL = kFP64 || kLearn == 1;     // leaf ids kept for the evaluation's own-leaf test
     static constexpr bool kF = kLearn == 1;              // network input rows
     int2 stack[kWarps][kStack];  // sibling ranges: {first | (count - 1) << 28, lane mask}
-    float4 lst[kWarps][kList];
+    float4 lst[kFP64 ? 1 : kWarps][kFP64 ? 1 : kList];  // FP32 node data of the staged entries
     int lst_node[kWarps][kList];
     int lst_leaf[kLL ? kWarps : 1][kLL ? kList : 1];
     unsigned lst_mask[kWarps][kList];
@@ -246,7 +246,7 @@ __global__ void __launch_bounds__(kThreads) traverse_masked_kernel(FParams p)
         __syncwarp();
     }
     int2* stk = sm.stack[w];
-    float4* L = sm.lst[w];
+    float4* L = kFP64 ? nullptr : sm.lst[w];
     int* LN = sm.lst_node[w];
     int* LL = WalkSmem<kFP64, kLearn>::kLL ? sm.lst_leaf[w] : nullptr;
     unsigned* LM = sm.lst_mask[w];
@@ -512,7 +512,7 @@ __global__ void __launch_bounds__(kThreads) traverse_masked_kernel(FParams p)
             const unsigned am = __ballot_sync(0xffffffffu, stage);
             if (stage) {
                 const int pos = nlist + __popc(am & lt);
-                L[pos] = e;
+                if (!kFP64) L[pos] = e;
                 LN[pos] = node;
                 if (WalkSmem<kFP64, kLearn>::kLL) LL[pos] = leaf ? ref : -1;  // for the own-leaf test
                 LM[pos] = A;
