@@ -80,8 +80,10 @@ def _sig(lib):
     f["bh_num_bodies"] = (C.c_int, [_P, C.POINTER(_I64)])
     f["bh_compute_bbox"] = (C.c_int, [_P, _P])
     f["bh_compute_keys"] = (C.c_int, [_P, _P])
+    f["bh_set_bbox"] = (C.c_int, [_P, _P])
     f["bh_sort_bodies"] = (C.c_int, [_P, _P])
     f["bh_build_tree"] = (C.c_int, [_P])
+    f["bh_build_tree_options"] = (C.c_int, [_P, C.c_int])
     f["bh_tree_info"] = (C.c_int, [_P, C.POINTER(_I64), C.POINTER(_I64), C.POINTER(_I64)])
     f["bh_export_tree"] = (C.c_int, [_P, _P, _P, _P, _P])
     f["bh_compute_accelerations"] = (C.c_int, [_P, _D, _D, _D, C.c_int, _P])
@@ -99,6 +101,9 @@ def _sig(lib):
     f["bh_write_vtp"] = (C.c_int, [C.c_char_p, C.c_int, _I64, _P, _P, _P, _P, _P])
     f["bh_selftest"] = (C.c_int, [C.c_int, _I64, C.c_uint64, C.POINTER(_I64)])
     f["bh_tree_slots"] = (C.c_int, [_P, _P, _P])
+    f["bh_let_export"] = (C.c_int, [_P, _P, _I64, _P, _D, C.c_int, _I64, _P, _P, _P, _P, C.POINTER(_I64)])
+    f["bh_let_bucket_boxes"] = (C.c_int, [_P, _I64, C.c_int, _P, _P])
+    f["bh_pseudo_leaf_tree"] = (C.c_int, [_P, _P, _P, _P, _P, _I64, _I64, _P, _P, _P, _P, C.POINTER(_I64)])
     f["bh_mlp_gradient"] = (C.c_int, [_P, _P, _P, _I64, _P, _P])
     f["bh_mlp_train"] = (C.c_int, [_P, _P, _I64, C.c_int, C.c_int, C.c_float, C.c_uint64, _P, _P, _P])
     f["bh_mlp_predict"] = (C.c_int, [_P, _P, _P, _I64, _P, _P])
@@ -207,6 +212,15 @@ def write_vtp(path, ids, mass, pos, vel, acc, rank: int = 0) -> None:
                                   _ptr(vel), _ptr(acc)))
 
 
+def let_bucket_boxes(prefixes, bucket_bits: int, bbox) -> np.ndarray:
+    """The bucket boxes of a remote domain (exchangeEssentialTrees): one
+    (6,) box per bucket prefix, {min.xyz, max.xyz}."""
+    p = _u64(prefixes)
+    out = np.empty((len(p), 6))
+    _check(library().bh_let_bucket_boxes(_ptr(p), len(p), int(bucket_bits), _ptr(_f64(bbox)), _ptr(out)))
+    return out
+
+
 # ---------------------------------------------------------------- device context
 class Context:
     """A device-resident body set on one GPU (bh_context)."""
@@ -278,6 +292,11 @@ class Context:
         _check(library().bh_compute_bbox(self._h, _ptr(out)))
         return out
 
+    def set_bbox(self, bbox) -> None:
+        """The global box (e.g. over all ranks' bodies) in place of
+        compute_bbox."""
+        _check(library().bh_set_bbox(self._h, _ptr(_f64(bbox))))
+
     def compute_keys(self) -> np.ndarray:
         out = np.empty(self.n, np.uint64)
         _check(library().bh_compute_keys(self._h, _ptr(out)))
@@ -288,8 +307,13 @@ class Context:
         _check(library().bh_sort_bodies(self._h, _ptr(perm)))
         return perm
 
-    def build_tree(self) -> None:
-        _check(library().bh_build_tree(self._h))
+    def build_tree(self, merge: bool = True) -> None:
+        """buildOctreeBottomUp, with (default) or without the single-rank
+        exchange merge."""
+        if merge:
+            _check(library().bh_build_tree(self._h))
+        else:
+            _check(library().bh_build_tree_options(self._h, 0))
 
     def tree_info(self):
         r, nn, nl = _I64(0), _I64(0), _I64(0)
@@ -318,6 +342,35 @@ class Context:
         com = np.empty((k, 3))
         _check(library().bh_export_tree(self._h, _ptr(prefix), _ptr(depth), _ptr(mass), _ptr(com)))
         return prefix, depth, mass, com
+
+    def let_export(self, boxes, bbox, theta2: float, max_depth: int = 21):
+        """createInteractionListForRank on the tree in place: the cells a
+        remote domain (boxes, (k, 6)) needs, as (prefix u64, depth u8,
+        mass f64, com (k, 3) f64) in the tree's node order."""
+        bx = _f64(boxes).reshape(-1, 6)
+        cap = self.tree_info()["nodes"]
+        prefix = np.empty(cap, np.uint64); depth = np.empty(cap, np.uint8); mass = np.empty(cap)
+        com = np.empty((cap, 3))
+        k = _I64(0)
+        _check(library().bh_let_export(self._h, _ptr(bx), bx.shape[0], _ptr(_f64(bbox)), float(theta2),
+                                       int(max_depth), cap, _ptr(prefix), _ptr(depth), _ptr(mass), _ptr(com),
+                                       C.byref(k)))
+        k = k.value
+        return prefix[:k], depth[:k], mass[:k], com[:k]
+
+    def pseudo_leaf_tree(self, prefix, depth, mass, com):
+        """buildTreeFromPseudoLeaves over received records on this context's
+        device: the map's cells sorted by (depth, prefix), as (prefix u64,
+        depth u8, mass f64, com (k, 3) f64)."""
+        p = _u64(prefix); d = np.ascontiguousarray(depth, np.uint8); m = _f64(mass)
+        c = _f64(com).reshape(-1, 3)
+        cap = int(np.sum(np.minimum(d.astype(np.int64), 21) + 1)) if len(d) else 0
+        op = np.empty(cap, np.uint64); od = np.empty(cap, np.uint8); om = np.empty(cap); oc = np.empty((cap, 3))
+        k = _I64(0)
+        _check(library().bh_pseudo_leaf_tree(self._h, _ptr(p), _ptr(d), _ptr(m), _ptr(c), len(p), cap, _ptr(op),
+                                             _ptr(od), _ptr(om), _ptr(oc), C.byref(k)))
+        k = k.value
+        return op[:k], od[:k], om[:k], oc[:k]
 
     def compute_accelerations(self, theta=THETA_DEFAULT, G=G_DEFAULT, soft2=0.0, mode=MODE_PLAIN_FP64,
                               download=True):

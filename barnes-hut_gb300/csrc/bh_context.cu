@@ -397,6 +397,9 @@ int bh_context_destroy(bh_context* ctx)
     if (ctx->h_small) cudaFreeHost(ctx->h_small);
     for (cudaEvent_t e : ctx->ev_pool) cudaEventDestroy(e);
     if (ctx->mlp_dev) cudaFree(ctx->mlp_dev);
+    if (ctx->let_buf) cudaFree(ctx->let_buf);
+    if (ctx->imp_buf) cudaFree(ctx->imp_buf);
+    if (ctx->imp_buf2) cudaFree(ctx->imp_buf2);
     for (auto& g : ctx->sg)
         if (g.exec) cudaGraphExecDestroy(g.exec);
     delete ctx;

@@ -272,3 +272,29 @@ extern "C" int bh_write_vtp(const char* path, int rank, int64_t n, const uint64_
     os.flush();
     return os ? BH_OK : bh_fail(BH_ERR_IO, "bh_write_vtp: write failed");
 }
+
+// Bucket boxes of a remote domain (src/exchange.cpp:45-71): the cell of
+// depth bucket_bits / 3 that each bucket prefix names, in the reference's
+// arithmetic (cell size span / 2^d; minimum corner bbox.min + (i 2^-d) span).
+extern "C" int bh_let_bucket_boxes(const uint64_t* prefixes, int64_t n, int bucket_bits, const double bbox[6],
+                                   double* boxes_out)
+{
+    if (n < 0 || !bbox || bucket_bits < 0 || bucket_bits > 63 || (n > 0 && (!prefixes || !boxes_out)))
+        return bh_fail(BH_ERR_INVALID_ARGUMENT, "bh_let_bucket_boxes: bad arguments");
+    const int d = bucket_bits / 3;
+    const double span[3] = {bbox[3] - bbox[0], bbox[4] - bbox[1], bbox[5] - bbox[2]};
+    const double scale = 1.0 / static_cast<double>(1ull << d);
+    double cell[3];
+    for (int a = 0; a < 3; ++a) cell[a] = span[a] / static_cast<double>(1 << d);
+    for (int64_t k = 0; k < n; ++k) {
+        const uint64_t bits = d == 0 ? 0 : prefixes[k] >> (63 - 3 * d);
+        for (int a = 0; a < 3; ++a) {
+            uint32_t v = 0;
+            for (int b = 0; b < d; ++b) v |= static_cast<uint32_t>((bits >> (3 * b + a)) & 1u) << b;
+            const double lo = bbox[a] + (static_cast<double>(v) * scale) * span[a];
+            boxes_out[6 * k + a] = lo;
+            boxes_out[6 * k + 3 + a] = lo + cell[a];
+        }
+    }
+    return BH_OK;
+}

@@ -345,6 +345,12 @@ struct bh_context {
     unsigned* err = nullptr;
     unsigned* h_err = nullptr;
     double* h_small = nullptr;  // pinned host scratch (64 doubles)
+    void* let_buf = nullptr;    // locally essential tree export scratch (bh_let_export)
+    size_t let_bytes = 0;
+    void* imp_buf = nullptr;    // pseudo-leaf tree scratch (bh_pseudo_leaf_tree): records
+    size_t imp_bytes = 0;
+    void* imp_buf2 = nullptr;   // and entries / cells
+    size_t imp_bytes2 = 0;
 };
 
 namespace bh {
@@ -362,6 +368,8 @@ int launch_permute(bh_context* ctx);
 // The permutation gathers into the second body set; the two sets then trade
 // places (host pointers only).
 void swap_body_sets(bh_context* ctx);
+// Digit counts for sort_passes_raw (hist zeroed by the caller).
+int launch_digit_hist(int64_t n, const uint64_t* keys, uint32_t* hist, cudaStream_t st);
 // The onesweep passes over raw buffers (the allocation-free sort entry).
 int sort_passes_raw(int64_t n, const uint64_t* keys_in, uint64_t* keys_out, uint32_t* vals_out, uint64_t* key_alt,
                     uint32_t* val_alt, uint32_t* hist, uint32_t* lookback, uint32_t* tile_ctr, unsigned* err,
@@ -389,5 +397,8 @@ int launch_fp32_nodes(bh_context* ctx, double G);
 // n_dev != nullptr (device-side count, at most n_max), else n_max is used.
 int device_exclusive_scan(bh_context* ctx, const int32_t* in, int32_t* out, int64_t n_max,
                           const int32_t* n_dev, int32_t* total);
+// The same over a caller's block-sum scratch of scan_tmp_ints(n_max) ints.
+int device_exclusive_scan_tmp(bh_context* ctx, const int32_t* in, int32_t* out, int64_t n_max,
+                              const int32_t* n_dev, int32_t* total, int32_t* tmp);
 
 }  // namespace bh

@@ -1,0 +1,594 @@
+// Locally essential tree export on the GPU: the cells of this rank's tree
+// that a remote rank needs, selected as createInteractionListForRank
+// (src/exchange.cpp:117-179) selects them, and the remote domain's bucket
+// boxes of exchangeEssentialTrees (src/exchange.cpp:45-71).
+//
+// The reference walks its hash map depth first from the root.  A cell is
+// opened when s^2 >= theta2 * d^2 for any remote box (s the largest side of
+// the cell's box from getBoundingBoxForCell, src/bounding_box.cpp:55-75; d^2
+// min_distance_sq, :10-18) and its depth is below max_depth; otherwise it is
+// kept.  Which cells are kept does not depend on the visiting order (each
+// cell is reached through its ancestors only), so the GPU walks the
+// compressed tree breadth first instead: one warp per frontier node, lanes
+// over the remote boxes, one launch per chain level (at most 22).  A node
+// stands for the chain of single-child cells from `top` to `depth`; the warp
+// tests the chain's cells from the top down and either keeps one of them,
+// stops (a failing depth-21 leaf below max_depth has no children and is
+// dropped, as in the reference), or appends the node's children to the next
+// frontier.  Every cell box and distance is evaluated with the reference's
+// operation order in round-to-nearest FP64 without contraction, so the kept
+// set is the reference's bit for bit.  The kept cells are compacted in slot
+// order with the device scan.
+#include "bh_internal.cuh"
+
+#include <algorithm>
+#include <cstring>
+
+namespace {
+
+constexpr int kLetThreads = 256;
+constexpr int kLetWarps = kLetThreads / 32;
+constexpr int kLetLevels = bh::kMaxDepth + 1;  // chain tops 0..21
+
+struct LetGeom {
+    double lo[3];    // global box minimum corner
+    double span[3];  // global box extent per axis (max - min)
+};
+
+// std::max(a, b) of the reference: (a < b) ? b : a.
+__device__ __forceinline__ double ref_max(double a, double b) { return (a < b) ? b : a; }
+
+// Integer cell coordinate on one axis from the top 3 d bits of a prefix.
+__device__ __forceinline__ uint32_t cell_axis(uint64_t prefix, int d, int axis)
+{
+    if (d == 0) return 0;
+    const uint64_t bits = prefix >> (63 - 3 * d);
+    uint32_t v = 0;
+    for (int b = 0; b < d; ++b) v |= (uint32_t)((bits >> (3 * b + axis)) & 1ull) << b;
+    return v;
+}
+
+// Whether the cell (prefix, d) fails the opening test against any of the nb
+// remote boxes; warp-uniform result.  Cell box: size = span / 2^d,
+// min = gmin + (ix * 2^-d) * span, max = min + size (all RN).
+__device__ bool cell_opens(uint64_t prefix, int d, const LetGeom& g, const double* __restrict__ boxes, int nb,
+                           double theta2, int lane)
+{
+    const double scale = 1.0 / (double)(1ull << d);  // exact
+    const double div = (double)(1 << d);
+    double lo[3], hi[3];
+#pragma unroll
+    for (int a = 0; a < 3; ++a) {
+        const double size = __ddiv_rn(g.span[a], div);
+        lo[a] = __dadd_rn(g.lo[a], __dmul_rn(__dmul_rn((double)cell_axis(prefix, d, a), scale), g.span[a]));
+        hi[a] = __dadd_rn(lo[a], size);
+    }
+    double s = __dsub_rn(hi[0], lo[0]);
+    s = ref_max(s, __dsub_rn(hi[1], lo[1]));
+    s = ref_max(s, __dsub_rn(hi[2], lo[2]));
+    const double s2 = __dmul_rn(s, s);
+    for (int k0 = 0; k0 < nb; k0 += 32) {
+        const int k = k0 + lane;
+        bool f = false;
+        if (k < nb) {
+            const double* r = boxes + 6 * (int64_t)k;
+            double e[3];
+#pragma unroll
+            for (int a = 0; a < 3; ++a)
+                e[a] = ref_max(0.0, ref_max(__dsub_rn(lo[a], __ldg(r + 3 + a)), __dsub_rn(__ldg(r + a), hi[a])));
+            const double d2 = __dadd_rn(__dadd_rn(__dmul_rn(e[0], e[0]), __dmul_rn(e[1], e[1])), __dmul_rn(e[2], e[2]));
+            f = s2 >= __dmul_rn(theta2, d2);
+        }
+        if (__any_sync(0xffffffffu, f)) return true;
+    }
+    return false;
+}
+
+__global__ void let_seed_kernel(int32_t* __restrict__ q0, int32_t* __restrict__ cnt)
+{
+    q0[0] = 0;  // the root slot
+    cnt[0] = 1;
+}
+
+// One chain level of the frontier: q_in[0 .. cnt_in) -> kept depths and the
+// next level's nodes.
+__global__ void __launch_bounds__(kLetThreads) let_level_kernel(
+    const bh::TreeRec* __restrict__ rec, const int32_t* __restrict__ slot_ref, const int32_t* __restrict__ node_a,
+    const uint64_t* __restrict__ leaf_key, const double* __restrict__ boxes, int nb, LetGeom g, double theta2,
+    int max_depth, const int32_t* __restrict__ q_in, const int32_t* __restrict__ cnt_in, int32_t* __restrict__ q_out,
+    int32_t* __restrict__ cnt_out, int32_t* __restrict__ keep)
+{
+    const int lane = threadIdx.x & 31;
+    const int count = *cnt_in;
+    const int nwarps = gridDim.x * kLetWarps;
+    for (int w = blockIdx.x * kLetWarps + (threadIdx.x >> 5); w < count; w += nwarps) {
+        const int32_t s = q_in[w];
+        const bh::TreeRec r = rec[s];
+        const int32_t ref = slot_ref[s];
+        const uint64_t key = leaf_key[ref >= 0 ? ref : node_a[~ref]];
+        int kept = -1;
+        bool descend = false;
+        for (int d = r.top;; ++d) {
+            const bool opens = cell_opens(key & bh::prefix_mask(d), d, g, boxes, nb, theta2, lane);
+            if (!opens || d >= max_depth) { kept = d; break; }
+            if (d < r.depth) continue;
+            descend = r.nchild > 0;
+            break;
+        }
+        if (lane == 0) {
+            keep[s] = kept;
+            if (descend) {
+                const int32_t base = atomicAdd(cnt_out, (int32_t)r.nchild);
+                for (int c = 0; c < r.nchild; ++c) q_out[base + c] = r.child + c;
+            }
+        }
+    }
+}
+
+__global__ void let_flag_kernel(const int32_t* __restrict__ counts, const int32_t* __restrict__ keep,
+                                int32_t* __restrict__ flag)
+{
+    const int32_t S = counts[2];
+    for (int32_t s = blockIdx.x * blockDim.x + threadIdx.x; s < S; s += gridDim.x * blockDim.x)
+        flag[s] = keep[s] >= 0 ? 1 : 0;
+}
+
+__global__ void let_write_kernel(const int32_t* __restrict__ counts, const int32_t* __restrict__ keep,
+                                 const int32_t* __restrict__ pos, const bh::TreeRec* __restrict__ rec,
+                                 const int32_t* __restrict__ slot_ref, const int32_t* __restrict__ node_a,
+                                 const uint64_t* __restrict__ leaf_key, uint64_t* __restrict__ o_prefix,
+                                 uint8_t* __restrict__ o_depth, double* __restrict__ o_mass, double* __restrict__ o_com)
+{
+    const int32_t S = counts[2];
+    for (int32_t s = blockIdx.x * blockDim.x + threadIdx.x; s < S; s += gridDim.x * blockDim.x) {
+        const int d = keep[s];
+        if (d < 0) continue;
+        const int32_t o = pos[s];
+        const int32_t ref = slot_ref[s];
+        const uint64_t key = leaf_key[ref >= 0 ? ref : node_a[~ref]];
+        const bh::TreeRec r = rec[s];
+        o_prefix[o] = key & bh::prefix_mask(d);
+        o_depth[o] = (uint8_t)d;
+        o_mass[o] = r.m;
+        o_com[3 * (int64_t)o] = r.cx;
+        o_com[3 * (int64_t)o + 1] = r.cy;
+        o_com[3 * (int64_t)o + 2] = r.cz;
+    }
+}
+
+// Scratch for one export: frontier queues, kept depths, scan, outputs,
+// remote boxes and the per-level counts; grown on demand, kept with the
+// context.
+struct LetLayout {
+    size_t q0, q1, keep, flag, prefix, depth, mass, com, boxes, cnt, total;
+};
+
+LetLayout let_layout(int64_t S, int64_t nb)
+{
+    auto up = [](size_t v) { return (v + 255) & ~(size_t)255; };
+    LetLayout L{};
+    size_t o = 0;
+    L.q0 = o; o += up(sizeof(int32_t) * S);
+    L.q1 = o; o += up(sizeof(int32_t) * S);
+    L.keep = o; o += up(sizeof(int32_t) * S);
+    L.flag = o; o += up(sizeof(int32_t) * S);
+    L.prefix = o; o += up(sizeof(uint64_t) * S);
+    L.depth = o; o += up(S);
+    L.mass = o; o += up(sizeof(double) * S);
+    L.com = o; o += up(3 * sizeof(double) * S);
+    L.boxes = o; o += up(6 * sizeof(double) * nb);
+    L.cnt = o; o += up(sizeof(int32_t) * (kLetLevels + 2));
+    L.total = o;
+    return L;
+}
+
+// ---- buildTreeFromPseudoLeaves (src/linear_octree.cpp:242-322) ------------
+//
+// Every valid record (mass > 0 and finite; depth clamped to 21; prefix masked
+// to its depth) contributes its own cell and the cell's ancestors.  A cell is
+// named by its locational code (1 << 3e) | (prefix >> (63 - 3e)); the sort
+// key of an entry is that code shifted left by one with an "ancestor" bit
+// below it (depth-21 entries, always a record's own cell, keep the bare
+// code, which sorts above every shifted one).  One sort thus orders the
+// cells by (depth, prefix), groups each cell's entries, and puts the
+// records' own entries first in record order (the radix sort is stable), so
+// duplicate records are summed in input order, as the reference's insertion
+// loop sums them.  Levels are then aggregated bottom up: a cell's
+// sums are its own records' (mass, mass x com), then its children's, in
+// octant order.  The reference adds children in the iteration order of its
+// hash map, which no other program reproduces; sums over several children
+// can therefore differ from it in the last bits.
+
+__device__ __forceinline__ uint64_t loc_code(uint64_t key, int e)
+{
+    return (1ull << (3 * e)) | (e ? key >> (63 - 3 * e) : 0ull);
+}
+
+__device__ __forceinline__ int code_depth(uint64_t code) { return (63 - __clzll((long long)code)) / 3; }
+
+// Sort key of an entry (see above) and its inverse.
+__device__ __forceinline__ uint64_t entry_key(uint64_t code, int e, bool own)
+{
+    return e == bh::kMaxDepth ? code : (code << 1) | (own ? 0ull : 1ull);
+}
+__device__ __forceinline__ uint64_t key_code(uint64_t k) { return (k >> 63) ? k : (k >> 1); }
+__device__ __forceinline__ bool key_own(uint64_t k) { return (k >> 63) || !(k & 1ull); }
+
+__device__ __forceinline__ int clamp_depth(uint8_t d) { return d > bh::kMaxDepth ? bh::kMaxDepth : (int)d; }
+
+__global__ void imp_count_kernel(int64_t m, const uint8_t* __restrict__ depth, const double* __restrict__ mass,
+                                 int32_t* __restrict__ cnt)
+{
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < m; i += (int64_t)gridDim.x * blockDim.x) {
+        const double w = mass[i];
+        const bool valid = (w > 0.0) && isfinite(w);
+        cnt[i] = valid ? clamp_depth(depth[i]) + 1 : 0;
+    }
+}
+
+__global__ void imp_expand_kernel(int64_t m, const uint64_t* __restrict__ prefix, const uint8_t* __restrict__ depth,
+                                  const int32_t* __restrict__ cnt, const int32_t* __restrict__ off,
+                                  uint64_t* __restrict__ code, int32_t* __restrict__ ent_rec)
+{
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < m; i += (int64_t)gridDim.x * blockDim.x) {
+        if (!cnt[i]) continue;
+        const int d = clamp_depth(depth[i]);
+        const uint64_t key = prefix[i] & bh::prefix_mask(d);
+        const int32_t o = off[i];
+        for (int e = 0; e <= d; ++e) {
+            code[o + e] = entry_key(loc_code(key, e), e, e == d);
+            ent_rec[o + e] = (int32_t)i;
+        }
+    }
+}
+
+__global__ void imp_head_kernel(int64_t t, const uint64_t* __restrict__ code, int32_t* __restrict__ head)
+{
+    for (int64_t j = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; j < t; j += (int64_t)gridDim.x * blockDim.x)
+        head[j] = (j == 0 || key_code(code[j]) != key_code(code[j - 1])) ? 1 : 0;
+}
+
+__global__ void imp_cells_kernel(int64_t t, const uint64_t* __restrict__ code, const int32_t* __restrict__ cidx,
+                                 uint64_t* __restrict__ cell_code, int32_t* __restrict__ cell_start)
+{
+    for (int64_t j = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; j < t; j += (int64_t)gridDim.x * blockDim.x) {
+        if (j == 0 || key_code(code[j]) != key_code(code[j - 1])) {
+            cell_code[cidx[j]] = key_code(code[j]);
+            cell_start[cidx[j]] = (int32_t)j;
+        }
+    }
+}
+
+// level_start[e] = first cell of depth e (e = 0..22; level 22 = the end).
+__global__ void imp_levels_kernel(const uint64_t* __restrict__ cell_code, const int32_t* __restrict__ ncell,
+                                  int32_t* __restrict__ level_start)
+{
+    const int e = threadIdx.x;
+    if (e > bh::kMaxDepth + 1) return;
+    const int32_t c = *ncell;
+    if (e == bh::kMaxDepth + 1) { level_start[e] = c; return; }
+    const uint64_t lo = 1ull << (3 * e);
+    int32_t a = 0, b = c;
+    while (a < b) {
+        const int32_t mid = a + (b - a) / 2;
+        if (cell_code[mid] < lo) a = mid + 1; else b = mid;
+    }
+    level_start[e] = a;
+}
+
+// One level of the bottom-up aggregation: cells [c0, c1) of depth e; the
+// children are the cells of depth e + 1 in [k0, k1).
+__global__ void imp_level_kernel(int e, int32_t c0, int32_t c1, int32_t k0, int32_t k1, int32_t ncell, int64_t t,
+                                 const uint64_t* __restrict__ cell_code, const int32_t* __restrict__ cell_start,
+                                 const uint64_t* __restrict__ skey, const uint32_t* __restrict__ perm,
+                                 const int32_t* __restrict__ ent_rec, const double* __restrict__ mass,
+                                 const double* __restrict__ com, double4_32a* __restrict__ acc)
+{
+    for (int32_t c = c0 + blockIdx.x * blockDim.x + threadIdx.x; c < c1; c += gridDim.x * blockDim.x) {
+        const uint64_t code = cell_code[c];
+        double m = 0.0, wx = 0.0, wy = 0.0, wz = 0.0;
+        const int32_t j1 = (c + 1 < ncell) ? cell_start[c + 1] : (int32_t)t;
+        for (int32_t j = cell_start[c]; j < j1 && key_own(skey[j]); ++j) {  // own entries come first
+            const int32_t r = ent_rec[perm[j]];
+            const double w = mass[r];
+            m = __dadd_rn(m, w);
+            wx = __dadd_rn(wx, __dmul_rn(com[3 * (int64_t)r], w));
+            wy = __dadd_rn(wy, __dmul_rn(com[3 * (int64_t)r + 1], w));
+            wz = __dadd_rn(wz, __dmul_rn(com[3 * (int64_t)r + 2], w));
+        }
+        if (k0 < k1) {
+            const uint64_t first = code << 3;
+            int32_t a = k0, b = k1;
+            while (a < b) {
+                const int32_t mid = a + (b - a) / 2;
+                if (cell_code[mid] < first) a = mid + 1; else b = mid;
+            }
+            for (int32_t k = a; k < k1 && (cell_code[k] >> 3) == code; ++k) {
+                const double4_32a q = acc[k];
+                m = __dadd_rn(m, q.w);
+                wx = __dadd_rn(wx, q.x);
+                wy = __dadd_rn(wy, q.y);
+                wz = __dadd_rn(wz, q.z);
+            }
+        }
+        acc[c] = double4_32a{wx, wy, wz, m};
+    }
+}
+
+__global__ void imp_out_kernel(int32_t ncell, const uint64_t* __restrict__ cell_code, const double4_32a* __restrict__ acc,
+                               uint64_t* __restrict__ o_prefix, uint8_t* __restrict__ o_depth,
+                               double* __restrict__ o_mass, double* __restrict__ o_com)
+{
+    for (int32_t c = blockIdx.x * blockDim.x + threadIdx.x; c < ncell; c += gridDim.x * blockDim.x) {
+        const uint64_t code = cell_code[c];
+        const int e = code_depth(code);
+        o_prefix[c] = e ? (code ^ (1ull << (3 * e))) << (63 - 3 * e) : 0ull;
+        o_depth[c] = (uint8_t)e;
+        const double4_32a q = acc[c];
+        o_mass[c] = q.w;
+        const bool div = q.w > 1e-12;
+        o_com[3 * (int64_t)c] = div ? __ddiv_rn(q.x, q.w) : q.x;
+        o_com[3 * (int64_t)c + 1] = div ? __ddiv_rn(q.y, q.w) : q.y;
+        o_com[3 * (int64_t)c + 2] = div ? __ddiv_rn(q.z, q.w) : q.z;
+    }
+}
+
+struct Arena {
+    char* base;
+    size_t off;
+    template <class T>
+    T* take(int64_t n)
+    {
+        T* p = reinterpret_cast<T*>(base + off);
+        off += ((size_t)std::max<int64_t>(n, 1) * sizeof(T) + 255) & ~(size_t)255;
+        return p;
+    }
+};
+
+int grow(void** buf, size_t* bytes, size_t want)
+{
+    if (*bytes >= want) return BH_OK;
+    if (*buf) BH_CUDA_TRY(cudaFree(*buf));
+    *buf = nullptr;
+    *bytes = 0;
+    if (cudaMalloc(buf, want) != cudaSuccess) {
+        cudaGetLastError();
+        return bh_fail(BH_ERR_OUT_OF_MEMORY, "pseudo-leaf tree: scratch allocation failed");
+    }
+    *bytes = want;
+    return BH_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int bh_let_export(bh_context* ctx, const double* boxes, int64_t nboxes, const double bbox[6], double theta2,
+                  int max_depth, int64_t capacity, uint64_t* prefix, uint8_t* depth, double* mass, double* com,
+                  int64_t* count_out)
+{
+    if (!ctx || !bbox || !count_out || nboxes < 0 || capacity < 0 || (nboxes > 0 && !boxes) ||
+        nboxes > (int64_t)INT32_MAX)
+        return bh_fail(BH_ERR_INVALID_ARGUMENT, "bh_let_export: bad arguments");
+    BH_CUDA_TRY(cudaSetDevice(ctx->device));
+    *count_out = 0;
+    if (ctx->n == 0 || nboxes == 0) return BH_OK;
+    if (!ctx->tree_valid) return bh_fail(BH_ERR_STATE, "bh_let_export: no tree built");
+    int rc;
+    if (ctx->tree_far) {  // the export carries the reference's tree: real masses
+        if ((rc = bh::launch_build(ctx, ctx->m))) return rc;
+        ctx->tree_far = ctx->tree_moments = false;
+    }
+    cudaStream_t st = ctx->stream;
+    int32_t S = 0;
+    BH_CUDA_TRY(cudaMemcpyAsync(ctx->h_small, ctx->counts + 2, sizeof(int32_t), cudaMemcpyDeviceToHost, st));
+    BH_CUDA_TRY(cudaStreamSynchronize(st));
+    std::memcpy(&S, ctx->h_small, sizeof(int32_t));
+    if (S <= 0) return BH_OK;
+
+    const LetLayout L = let_layout(S, nboxes);
+    if (ctx->let_bytes < L.total) {
+        if (ctx->let_buf) BH_CUDA_TRY(cudaFree(ctx->let_buf));
+        ctx->let_buf = nullptr;
+        ctx->let_bytes = 0;
+        if (cudaMalloc(&ctx->let_buf, L.total) != cudaSuccess) {
+            cudaGetLastError();
+            return bh_fail(BH_ERR_OUT_OF_MEMORY, "bh_let_export: scratch allocation failed");
+        }
+        ctx->let_bytes = L.total;
+    }
+    char* base = static_cast<char*>(ctx->let_buf);
+    int32_t* q[2] = {reinterpret_cast<int32_t*>(base + L.q0), reinterpret_cast<int32_t*>(base + L.q1)};
+    int32_t* keep = reinterpret_cast<int32_t*>(base + L.keep);
+    int32_t* flag = reinterpret_cast<int32_t*>(base + L.flag);
+    uint64_t* o_prefix = reinterpret_cast<uint64_t*>(base + L.prefix);
+    uint8_t* o_depth = reinterpret_cast<uint8_t*>(base + L.depth);
+    double* o_mass = reinterpret_cast<double*>(base + L.mass);
+    double* o_com = reinterpret_cast<double*>(base + L.com);
+    double* d_boxes = reinterpret_cast<double*>(base + L.boxes);
+    int32_t* cnt = reinterpret_cast<int32_t*>(base + L.cnt);
+
+    LetGeom g;
+    for (int a = 0; a < 3; ++a) {
+        g.lo[a] = bbox[a];
+        g.span[a] = bbox[3 + a] - bbox[a];
+    }
+    BH_CUDA_TRY(cudaMemcpyAsync(d_boxes, boxes, sizeof(double) * 6 * nboxes, cudaMemcpyHostToDevice, st));
+    BH_CUDA_TRY(cudaMemsetAsync(keep, 0xff, sizeof(int32_t) * S, st));
+    BH_CUDA_TRY(cudaMemsetAsync(cnt, 0, sizeof(int32_t) * (kLetLevels + 2), st));
+    let_seed_kernel<<<1, 1, 0, st>>>(q[0], cnt);
+    BH_LAUNCH_CHECK(ctx);
+    int dev_sms = 0;
+    BH_CUDA_TRY(cudaDeviceGetAttribute(&dev_sms, cudaDevAttrMultiProcessorCount, ctx->device));
+    const int64_t want = (S + kLetWarps - 1) / kLetWarps;
+    const int grid = (int)std::max<int64_t>(1, std::min<int64_t>(want, (int64_t)dev_sms * 8));
+    // Chain tops grow by at least one per level, and no cell is deeper than
+    // 21, so kLetLevels launches drain every frontier.
+    for (int lv = 0; lv < kLetLevels; ++lv) {
+        let_level_kernel<<<grid, kLetThreads, 0, st>>>(ctx->rec, ctx->slot_ref, ctx->node_a, ctx->leaf_key, d_boxes,
+                                                       (int)nboxes, g, theta2, max_depth, q[lv & 1], cnt + lv,
+                                                       q[(lv + 1) & 1], cnt + lv + 1, keep);
+        BH_LAUNCH_CHECK(ctx);
+    }
+    const int sgrid = (int)std::min<int64_t>((S + 255) / 256, (int64_t)dev_sms * 16);
+    let_flag_kernel<<<sgrid, 256, 0, st>>>(ctx->counts, keep, flag);
+    BH_LAUNCH_CHECK(ctx);
+    int32_t* total = cnt + kLetLevels + 1;
+    if ((rc = bh::device_exclusive_scan(ctx, flag, flag, S, ctx->counts + 2, total))) return rc;
+    let_write_kernel<<<sgrid, 256, 0, st>>>(ctx->counts, keep, flag, ctx->rec, ctx->slot_ref, ctx->node_a,
+                                            ctx->leaf_key, o_prefix, o_depth, o_mass, o_com);
+    BH_LAUNCH_CHECK(ctx);
+    BH_CUDA_TRY(cudaMemcpyAsync(ctx->h_small, total, sizeof(int32_t), cudaMemcpyDeviceToHost, st));
+    BH_CUDA_TRY(cudaMemcpyAsync(reinterpret_cast<char*>(ctx->h_small) + 8, cnt + kLetLevels, sizeof(int32_t),
+                                cudaMemcpyDeviceToHost, st));
+    BH_CUDA_TRY(cudaStreamSynchronize(st));
+    int32_t k = 0, spill = 0;
+    std::memcpy(&k, ctx->h_small, sizeof(int32_t));
+    std::memcpy(&spill, reinterpret_cast<char*>(ctx->h_small) + 8, sizeof(int32_t));
+    if (spill != 0) return bh_fail(BH_ERR_OVERFLOW, "bh_let_export: frontier deeper than the tree");
+    *count_out = k;
+    if (k > capacity) return bh_fail(BH_ERR_INVALID_ARGUMENT, "bh_let_export: capacity below the exported count");
+    if (k == 0) return BH_OK;
+    if (!prefix || !depth || !mass || !com) return bh_fail(BH_ERR_INVALID_ARGUMENT, "bh_let_export: null array");
+    BH_CUDA_TRY(cudaMemcpyAsync(prefix, o_prefix, sizeof(uint64_t) * k, cudaMemcpyDeviceToHost, st));
+    BH_CUDA_TRY(cudaMemcpyAsync(depth, o_depth, k, cudaMemcpyDeviceToHost, st));
+    BH_CUDA_TRY(cudaMemcpyAsync(mass, o_mass, sizeof(double) * k, cudaMemcpyDeviceToHost, st));
+    BH_CUDA_TRY(cudaMemcpyAsync(com, o_com, 3 * sizeof(double) * k, cudaMemcpyDeviceToHost, st));
+    BH_CUDA_TRY(cudaStreamSynchronize(st));
+    return BH_OK;
+}
+
+}  // extern "C"
+
+extern "C" int bh_pseudo_leaf_tree(bh_context* ctx, const uint64_t* prefix, const uint8_t* depth, const double* mass,
+                                   const double* com, int64_t m, int64_t capacity, uint64_t* o_prefix,
+                                   uint8_t* o_depth, double* o_mass, double* o_com, int64_t* count_out)
+{
+    if (!ctx || !count_out || m < 0 || capacity < 0 || (m > 0 && (!prefix || !depth || !mass || !com)))
+        return bh_fail(BH_ERR_INVALID_ARGUMENT, "bh_pseudo_leaf_tree: bad arguments");
+    // entries (record cells and their ancestors) are numbered in int32
+    if (m > (int64_t)(INT32_MAX / (bh::kMaxDepth + 1)))
+        return bh_fail(BH_ERR_INVALID_ARGUMENT, "bh_pseudo_leaf_tree: too many records");
+    BH_CUDA_TRY(cudaSetDevice(ctx->device));
+    *count_out = 0;
+    if (m == 0) return BH_OK;
+    cudaStream_t st = ctx->stream;
+    int dev_sms = 0;
+    BH_CUDA_TRY(cudaDeviceGetAttribute(&dev_sms, cudaDevAttrMultiProcessorCount, ctx->device));
+    auto grid_for = [&](int64_t n) {
+        return (int)std::max<int64_t>(1, std::min<int64_t>((n + 255) / 256, 16 * (int64_t)dev_sms));
+    };
+    int rc;
+
+    // Phase 1: the records, their entry counts and offsets.
+    auto layout_a = [&](Arena& a, uint64_t** rp, uint8_t** rd, double** rm, double** rc3, int32_t** cnt,
+                        int32_t** off, int32_t** tmp, int32_t** small) {
+        *rp = a.take<uint64_t>(m); *rd = a.take<uint8_t>(m); *rm = a.take<double>(m); *rc3 = a.take<double>(3 * m);
+        *cnt = a.take<int32_t>(m); *off = a.take<int32_t>(m); *tmp = a.take<int32_t>(bh::scan_tmp_ints(m));
+        *small = a.take<int32_t>(64);  // [0] entries, [1] cells, [8..30] level starts
+    };
+    uint64_t* r_prefix; uint8_t* r_depth; double* r_mass; double* r_com; int32_t *cnt, *off, *tmp_a, *small;
+    {
+        Arena probe{nullptr, 0};
+        layout_a(probe, &r_prefix, &r_depth, &r_mass, &r_com, &cnt, &off, &tmp_a, &small);
+        if ((rc = grow(&ctx->imp_buf, &ctx->imp_bytes, probe.off))) return rc;
+    }
+    Arena a{static_cast<char*>(ctx->imp_buf), 0};
+    layout_a(a, &r_prefix, &r_depth, &r_mass, &r_com, &cnt, &off, &tmp_a, &small);
+    BH_CUDA_TRY(cudaMemcpyAsync(r_prefix, prefix, sizeof(uint64_t) * m, cudaMemcpyHostToDevice, st));
+    BH_CUDA_TRY(cudaMemcpyAsync(r_depth, depth, m, cudaMemcpyHostToDevice, st));
+    BH_CUDA_TRY(cudaMemcpyAsync(r_mass, mass, sizeof(double) * m, cudaMemcpyHostToDevice, st));
+    BH_CUDA_TRY(cudaMemcpyAsync(r_com, com, 3 * sizeof(double) * m, cudaMemcpyHostToDevice, st));
+    imp_count_kernel<<<grid_for(m), 256, 0, st>>>(m, r_depth, r_mass, cnt);
+    BH_LAUNCH_CHECK(ctx);
+    if ((rc = bh::device_exclusive_scan_tmp(ctx, cnt, off, m, nullptr, small, tmp_a))) return rc;
+    BH_CUDA_TRY(cudaMemcpyAsync(ctx->h_small, small, sizeof(int32_t), cudaMemcpyDeviceToHost, st));
+    BH_CUDA_TRY(cudaStreamSynchronize(st));
+    int32_t t = 0;
+    std::memcpy(&t, ctx->h_small, sizeof(int32_t));
+    if (t == 0) return BH_OK;
+
+    // Phase 2: t entries -> sorted codes -> cells -> level sums.
+    const int64_t tiles = (t + bh::kSortTile - 1) / bh::kSortTile;
+    uint64_t *code, *code_s, *key_alt, *cell_code, *d_prefix;
+    uint32_t *val_alt, *perm, *hist, *lookback, *tile_ctr;
+    int32_t *ent_rec, *head, *cell_start, *tmp_b;
+    unsigned* err;
+    double4_32a* acc;
+    uint8_t* d_depth;
+    double *d_mass, *d_com;
+    auto layout_b = [&](Arena& b) {
+        code = b.take<uint64_t>(t); code_s = b.take<uint64_t>(t); key_alt = b.take<uint64_t>(t);
+        val_alt = b.take<uint32_t>(t); perm = b.take<uint32_t>(t); ent_rec = b.take<int32_t>(t);
+        head = b.take<int32_t>(t); tmp_b = b.take<int32_t>(bh::scan_tmp_ints(t));
+        hist = b.take<uint32_t>(bh::kSortPasses * bh::kRadix);
+        lookback = b.take<uint32_t>(bh::kSortPasses * tiles * bh::kRadix);
+        tile_ctr = b.take<uint32_t>(bh::kSortPasses); err = b.take<unsigned>(1);
+        cell_code = b.take<uint64_t>(t); cell_start = b.take<int32_t>(t); acc = b.take<double4_32a>(t);
+        d_prefix = b.take<uint64_t>(t); d_depth = b.take<uint8_t>(t); d_mass = b.take<double>(t);
+        d_com = b.take<double>(3 * (int64_t)t);
+    };
+    {
+        Arena probe{nullptr, 0};
+        layout_b(probe);
+        if ((rc = grow(&ctx->imp_buf2, &ctx->imp_bytes2, probe.off))) return rc;
+    }
+    Arena b{static_cast<char*>(ctx->imp_buf2), 0};
+    layout_b(b);
+    imp_expand_kernel<<<grid_for(m), 256, 0, st>>>(m, r_prefix, r_depth, cnt, off, code, ent_rec);
+    BH_LAUNCH_CHECK(ctx);
+    if (t == 1) {
+        BH_CUDA_TRY(cudaMemcpyAsync(code_s, code, sizeof(uint64_t), cudaMemcpyDeviceToDevice, st));
+        BH_CUDA_TRY(cudaMemsetAsync(perm, 0, sizeof(uint32_t), st));
+        BH_CUDA_TRY(cudaMemsetAsync(err, 0, sizeof(unsigned), st));
+    } else {
+        BH_CUDA_TRY(cudaMemsetAsync(hist, 0, sizeof(uint32_t) * bh::kSortPasses * bh::kRadix, st));
+        BH_CUDA_TRY(cudaMemsetAsync(lookback, 0, sizeof(uint32_t) * bh::kSortPasses * tiles * bh::kRadix, st));
+        BH_CUDA_TRY(cudaMemsetAsync(tile_ctr, 0, sizeof(uint32_t) * bh::kSortPasses, st));
+        BH_CUDA_TRY(cudaMemsetAsync(err, 0, sizeof(unsigned), st));
+        if ((rc = bh::launch_digit_hist(t, code, hist, st))) return rc;
+        if ((rc = bh::sort_passes_raw(t, code, code_s, perm, key_alt, val_alt, hist, lookback, tile_ctr, err, st)))
+            return rc;
+    }
+    imp_head_kernel<<<grid_for(t), 256, 0, st>>>(t, code_s, head);
+    BH_LAUNCH_CHECK(ctx);
+    if ((rc = bh::device_exclusive_scan_tmp(ctx, head, head, t, nullptr, small + 1, tmp_b))) return rc;
+    imp_cells_kernel<<<grid_for(t), 256, 0, st>>>(t, code_s, head, cell_code, cell_start);
+    BH_LAUNCH_CHECK(ctx);
+    imp_levels_kernel<<<1, 32, 0, st>>>(cell_code, small + 1, small + 8);
+    BH_LAUNCH_CHECK(ctx);
+    BH_CUDA_TRY(cudaMemcpyAsync(ctx->h_small, small, 32 * sizeof(int32_t), cudaMemcpyDeviceToHost, st));
+    BH_CUDA_TRY(cudaMemcpyAsync(reinterpret_cast<char*>(ctx->h_small) + 256, err, sizeof(unsigned),
+                                cudaMemcpyDeviceToHost, st));
+    BH_CUDA_TRY(cudaStreamSynchronize(st));
+    int32_t hs[32];
+    unsigned h_err = 0;
+    std::memcpy(hs, ctx->h_small, sizeof(hs));
+    std::memcpy(&h_err, reinterpret_cast<char*>(ctx->h_small) + 256, sizeof(unsigned));
+    if (h_err & bh::kErrTimeout) return bh_fail(BH_ERR_TIMEOUT, "bh_pseudo_leaf_tree: a bounded device wait gave up");
+    const int32_t ncell = hs[1];
+    const int32_t* ls = hs + 8;  // ls[0..22]
+    *count_out = ncell;
+    if (ncell > capacity)
+        return bh_fail(BH_ERR_INVALID_ARGUMENT, "bh_pseudo_leaf_tree: capacity below the cell count");
+    if (!o_prefix || !o_depth || !o_mass || !o_com)
+        return bh_fail(BH_ERR_INVALID_ARGUMENT, "bh_pseudo_leaf_tree: null output array");
+
+    // Bottom-up sums, deepest level first.
+    for (int e = bh::kMaxDepth; e >= 0; --e) {
+        const int32_t c0 = ls[e], c1 = ls[e + 1];
+        if (c0 == c1) continue;
+        const int32_t k1 = e < bh::kMaxDepth ? ls[e + 2] : c1;
+        imp_level_kernel<<<grid_for(c1 - c0), 256, 0, st>>>(e, c0, c1, c1, k1, ncell, t, cell_code, cell_start,
+                                                            code_s, perm, ent_rec, r_mass, r_com, acc);
+        BH_LAUNCH_CHECK(ctx);
+    }
+    imp_out_kernel<<<grid_for(ncell), 256, 0, st>>>(ncell, cell_code, acc, d_prefix, d_depth, d_mass, d_com);
+    BH_LAUNCH_CHECK(ctx);
+    BH_CUDA_TRY(cudaMemcpyAsync(o_prefix, d_prefix, sizeof(uint64_t) * ncell, cudaMemcpyDeviceToHost, st));
+    BH_CUDA_TRY(cudaMemcpyAsync(o_depth, d_depth, ncell, cudaMemcpyDeviceToHost, st));
+    BH_CUDA_TRY(cudaMemcpyAsync(o_mass, d_mass, sizeof(double) * ncell, cudaMemcpyDeviceToHost, st));
+    BH_CUDA_TRY(cudaMemcpyAsync(o_com, d_com, 3 * sizeof(double) * ncell, cudaMemcpyDeviceToHost, st));
+    BH_CUDA_TRY(cudaStreamSynchronize(st));
+    return BH_OK;
+}

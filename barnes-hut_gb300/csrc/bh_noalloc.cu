@@ -82,6 +82,22 @@ __global__ void __launch_bounds__(kHistThreads) noalloc_hist_kernel(int64_t n, c
 
 }  // namespace
 
+namespace bh {
+
+// Digit counts of the eight passes (hist: kSortPasses x kRadix, zeroed by
+// the caller) for sort_passes_raw.
+int launch_digit_hist(int64_t n, const uint64_t* keys, uint32_t* hist, cudaStream_t st)
+{
+    int64_t blocks = (n + kHistThreads * 4 - 1) / (kHistThreads * 4);
+    if (blocks > 4 * bh::kNumSMs) blocks = 4 * bh::kNumSMs;
+    if (blocks < 1) blocks = 1;
+    noalloc_hist_kernel<<<(unsigned)blocks, kHistThreads, 0, st>>>(n, keys, hist);
+    BH_CUDA_TRY(cudaGetLastError());
+    return BH_OK;
+}
+
+}  // namespace bh
+
 extern "C" int bh_sort_keys_noalloc(const uint64_t* keys_in, uint64_t* keys_out, uint32_t* perm_out, int64_t n,
                                     void* stream)
 {
@@ -118,10 +134,7 @@ extern "C" int bh_sort_keys_noalloc(const uint64_t* keys_in, uint64_t* keys_out,
     BH_CUDA_TRY(cudaMemsetAsync(lookback, 0, sizeof(uint32_t) * bh::kSortPasses * tiles * bh::kRadix, st));
     BH_CUDA_TRY(cudaMemsetAsync(tile_ctr, 0, sizeof(uint32_t) * bh::kSortPasses, st));
     BH_CUDA_TRY(cudaMemsetAsync(err, 0, sizeof(unsigned), st));
-    int64_t blocks = (n + kHistThreads * 4 - 1) / (kHistThreads * 4);
-    if (blocks > 4 * bh::kNumSMs) blocks = 4 * bh::kNumSMs;
-    noalloc_hist_kernel<<<(unsigned)blocks, kHistThreads, 0, st>>>(n, keys_in, hist);
-    BH_CUDA_TRY(cudaGetLastError());
+    if ((rc = bh::launch_digit_hist(n, keys_in, hist, st))) return rc;
     if ((rc = bh::sort_passes_raw(n, keys_in, keys_out, perm_out, key_alt, val_alt, hist, lookback, tile_ctr, err,
                                   st)))
         return rc;

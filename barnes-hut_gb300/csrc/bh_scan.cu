@@ -108,16 +108,22 @@ int64_t scan_tmp_ints(int64_t n_max) { return (n_max + kScanBlock - 1) / kScanBl
 int device_exclusive_scan(bh_context* ctx, const int32_t* in, int32_t* out, int64_t n_max, const int32_t* n_dev,
                           int32_t* total)
 {
+    return device_exclusive_scan_tmp(ctx, in, out, n_max, n_dev, total, ctx->scan_tmp);
+}
+
+int device_exclusive_scan_tmp(bh_context* ctx, const int32_t* in, int32_t* out, int64_t n_max, const int32_t* n_dev,
+                              int32_t* total, int32_t* tmp)
+{
     if (n_max <= 0) {
         BH_CUDA_TRY(cudaMemsetAsync(total, 0, sizeof(int32_t), ctx->stream));
         return BH_OK;
     }
     const int nb = (int)((n_max + kScanBlock - 1) / kScanBlock);
-    scan_reduce_kernel<<<nb, kScanThreads, 0, ctx->stream>>>(in, n_max, n_dev, ctx->scan_tmp);
+    scan_reduce_kernel<<<nb, kScanThreads, 0, ctx->stream>>>(in, n_max, n_dev, tmp);
     BH_LAUNCH_CHECK(ctx);
-    scan_bsum_kernel<<<1, 1024, 0, ctx->stream>>>(ctx->scan_tmp, nb, total);
+    scan_bsum_kernel<<<1, 1024, 0, ctx->stream>>>(tmp, nb, total);
     BH_LAUNCH_CHECK(ctx);
-    scan_down_kernel<<<nb, kScanThreads, 0, ctx->stream>>>(in, out, n_max, n_dev, ctx->scan_tmp);
+    scan_down_kernel<<<nb, kScanThreads, 0, ctx->stream>>>(in, out, n_max, n_dev, tmp);
     BH_LAUNCH_CHECK(ctx);
     return BH_OK;
 }

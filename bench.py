@@ -34,7 +34,9 @@ and seeded (the reference's 300k CSV is not part of its repository).
 * long_runs: the configurations' own run lengths, 2,000 steps of the 300k
   FP64 list workload and 500 steps of the 4M FP32 + learned form, each timed
   as one span, with the final error and the energy/angular-momentum drift.
-  --no-north-star skips these four blocks.
+* let_exchange: the locally essential tree export and import at 4M bodies
+  split over 8 ranks, against the oracle on the host cores.
+  --no-north-star skips these five blocks.
 
 Multi-GPU: the path does not shard on one GPU per rank; ranks run replicas
 (weak scaling) and value is the sum of their body-steps over the slowest
@@ -52,7 +54,6 @@ import subprocess
 import sys
 import threading
 import time
-from pathlib import Path
 from pathlib import Path
 
 import numpy as np
@@ -500,6 +501,97 @@ TRAFFIC_BYTES = {("fp64_list", 300_149): 62.50e6 + 2.27e6, ("fp32", 4_000_000): 
 PHASE_BYTES = {"kick_drift_bbox": 120, "keys": 32, "sort": 200, "permute": 128, "build": 136}
 
 
+def bucket_domains(keys, bucket_bits, nranks):
+    """update_rank_domains' split (src/load_balancing.cpp:12-65): the owner
+    rank of each body and each rank's non-empty bucket prefixes."""
+    bidx = (keys >> np.uint64(63 - bucket_bits)).astype(np.int64)
+    hist = np.bincount(bidx, minlength=1 << bucket_bits)
+    ideal = (len(keys) + nranks - 1) // nranks
+    split, run = [], 0
+    for i, h in enumerate(hist.tolist()):
+        run += h
+        if len(split) < nranks - 1 and run >= (len(split) + 1) * ideal:
+            split.append(i)
+    owner = np.searchsorted(np.array(split, np.int64), np.arange(1 << bucket_bits), side="right")
+    doms = [(np.nonzero((hist > 0) & (owner == r))[0].astype(np.uint64)) << np.uint64(63 - bucket_bits)
+            for r in range(nranks)]
+    return owner[bidx], doms
+
+
+def let_exchange(args, dev):
+    """The LET data path at the 4M-body size split over 8 ranks (18-bit
+    buckets, theta = 1.05): rank 0's device tree exports to the 7 other
+    domains (createInteractionListForRank), and the records rank 0 receives
+    from them are built into a map (buildTreeFromPseudoLeaves).  Host clock
+    around the C-ABI calls (records copied back to the host included); the
+    oracle does the same export and import on the host cores."""
+    bh = importlib.import_module("barnes-hut_gb300")
+    from oracle.oracle import Oracle
+    n = args.ns_bodies
+    pos, vel, mass, ids = bh.generate_system(SEED + 3, n, 0.10, 0.05)
+    with bh.Context(n, dev) as full:
+        full.set_bodies(pos, vel, mass, ids)
+        bb = full.compute_bbox()
+        keys = full.compute_keys()
+    owner, doms = bucket_domains(keys, 18, 8)
+    boxes = [bh.let_bucket_boxes(doms[r], 18, bb) for r in range(8)]
+    theta2 = THETA * THETA
+
+    def local(r):
+        sel = np.nonzero(owner == r)[0]
+        c = bh.Context(len(sel), dev)
+        c.set_bodies(pos[sel], vel[sel], mass[sel], ids[sel])
+        c.set_bbox(bb)
+        c.compute_keys()
+        c.sort_bodies()
+        c.build_tree(merge=False)
+        return c, sel
+
+    ctx0, sel0 = local(0)
+    ctx0.let_export(boxes[1], bb, theta2)
+    t0 = time.perf_counter()
+    sent = [ctx0.let_export(boxes[r], bb, theta2) for r in range(1, 8)]
+    t_exp = time.perf_counter() - t0
+    recv = []
+    for r in range(1, 8):
+        c, _ = local(r)
+        recv.append(c.let_export(boxes[0], bb, theta2))
+        c.close()
+    p, d, m, com = (np.concatenate([x[k] for x in recv]) for k in range(4))
+    ctx0.pseudo_leaf_tree(p, d, m, com)
+    reps = 3
+    t0 = time.perf_counter()
+    for _ in range(reps):
+        cells = ctx0.pseudo_leaf_tree(p, d, m, com)
+    t_imp = (time.perf_counter() - t0) / reps
+    ctx0.close()
+
+    o, kind = Oracle("port"), "port"
+    try:
+        o, kind = Oracle("reference"), "reference"
+    except (FileNotFoundError, OSError):
+        pass
+    sk, sp, sm, *_ = o.sort(keys[sel0], pos[sel0], mass[sel0], vel[sel0], ids[sel0])
+    tree = o.tree(sk, sp, sm, merge=False)
+    t0 = time.perf_counter()
+    cpu_sent = o.let_export(tree, boxes[1], bb, theta2)
+    c_exp = time.perf_counter() - t0
+    tree.close()
+    t0 = time.perf_counter()
+    pt = o.pseudo_tree(p, d, m, com)
+    c_imp = time.perf_counter() - t0
+    same_cells = len(pt) == len(cells[0])
+    pt.close()
+    return {"bodies": n, "ranks": 8, "bucket_bits": 18, "theta": THETA, "rank0_bodies": int(len(sel0)),
+            "export": {"destinations": 7, "boxes": [int(len(b)) for b in boxes[1:]],
+                       "records": [int(len(x[0])) for x in sent], "ms_per_export": 1e3 * t_exp / 7,
+                       "cpu_ms_rank1": 1e3 * c_exp, "cpu_records_rank1": int(len(cpu_sent[0])),
+                       "records_equal_rank1": int(len(sent[0][0])) == int(len(cpu_sent[0]))},
+            "import": {"records": int(len(p)), "cells": int(len(cells[0])), "ms": 1e3 * t_imp,
+                       "cpu_ms": 1e3 * c_imp, "cpu_cells_equal": bool(same_cells)},
+            "cpu_kind": kind, "timing": "host clock around the C-ABI call, results copied to the host"}
+
+
 def hbm_peak_gbs():
     try:
         return float(json.loads((Path(__file__).resolve().parent / "MEASURED_PEAKS.json").read_text())["hbm_gbs"])
@@ -594,12 +686,13 @@ def run_ours(args, rank, ws, local):
     accuracy = {"median_rel_err": float(np.median(err)), "p99_rel_err": float(np.quantile(err, 0.99)),
                 "sample": int(len(sample)), "judge": "FP64 direct sum"}
 
-    ns = pr = le = runs = None
+    ns = pr = le = runs = let = None
     if rank == 0 and ws == 1 and not args.no_north_star:
         params, scale, info = train_model(args)
         ns = north_star(args, dev, params, scale, info)
         le = learned_eval(args, dev, params, scale)
         pr = precision_run(args, dev)
+        let = let_exchange(args, dev)
         runs = {"config2_300k_fp64_list_2000_steps": long_run(dev, N_BODIES, 0.10, 0.0, SEED, "fp64_list", 2000),
                 "config5_4m_fp32_learned_500_steps": long_run(dev, args.ns_bodies, 0.10, 0.05, SEED + 1, "learned",
                                                               500, params, scale, 1e-6, args.theta_max)}
@@ -644,6 +737,7 @@ def run_ours(args, rank, ws, local):
         "learned_eval": le,
         "precision_run": pr,
         "long_runs": runs,
+        "let_exchange": let,
     }
     print(json.dumps(line), flush=True)
 

@@ -153,6 +153,46 @@ int bh_tree_set_slot_values(bh_context *ctx, const double *mass, const double *c
  * BH_NUM_MASSIVE zeroed); 0 for a massless node.  Computes the second-moment
  * pass when the tree in place lacks it.  No reference counterpart. */
 int bh_tree_spread(bh_context *ctx, float *spread);
+/* createInteractionListForRank (src/exchange.cpp:117-179, include/exchange.h)
+ * on the device tree in place: the cells a remote rank whose domain is the
+ * union of `boxes` (nboxes x {min.x, min.y, min.z, max.x, max.y, max.z})
+ * needs, for the global box `bbox`, opening criterion s^2 >= theta2 * d^2
+ * and max_depth (the reference's --max-depth, 21 = full depth).  Writes the
+ * NodeRecords (prefix, depth, mass, com: 3 per record) in the tree's node
+ * order (the reference returns them in the iteration order of a hash set)
+ * and their number to *count_out.  At most one cell per node of
+ * bh_tree_info's n_nodes is kept, so that capacity always suffices; a
+ * smaller capacity that the count exceeds returns BH_ERR_INVALID_ARGUMENT
+ * with *count_out set.  main.cpp exports the local tree of
+ * buildOctreeBottomUp, i.e. the tree of bh_build_tree_options(ctx, 0).
+ * The arrays may be NULL when the count is 0. */
+int bh_let_export(bh_context *ctx, const double *boxes, int64_t nboxes, const double bbox[6], double theta2,
+                  int max_depth, int64_t capacity, uint64_t *prefix, uint8_t *depth, double *mass, double *com,
+                  int64_t *count_out);
+/* buildTreeFromPseudoLeaves (src/linear_octree.cpp:242-322,
+ * include/linear_octree.h:85-94) on the device: the map made of m received
+ * NodeRecords (records with mass <= 0 or not finite are skipped; depth is
+ * clamped to 21 and the prefix masked to it) and all their ancestors, each
+ * cell holding the sum of its records' masses and the mass-weighted centre
+ * of everything below it (divided by the mass where it exceeds 1e-12).
+ * Writes the cells sorted by (depth, prefix) and their number to
+ * *count_out; a capacity below the count returns BH_ERR_INVALID_ARGUMENT
+ * with *count_out set (sum over records of min(depth, 21) + 1 always
+ * suffices).  Duplicate records are summed in input order as in the
+ * reference; children are summed in octant order, while the reference sums
+ * them in its hash map's iteration order, so cells with several children
+ * agree with it to rounding (relative 1e-15).  Uses ctx's device and
+ * stream only; the body state is untouched. */
+int bh_pseudo_leaf_tree(bh_context *ctx, const uint64_t *prefix, const uint8_t *depth, const double *mass,
+                        const double *com, int64_t m, int64_t capacity, uint64_t *out_prefix, uint8_t *out_depth,
+                        double *out_mass, double *out_com, int64_t *count_out);
+/* The bucket boxes of a remote rank's domain as exchangeEssentialTrees
+ * builds them (src/exchange.cpp:45-71): bucket prefix p (a key prefix of
+ * depth bucket_bits / 3, as update_rank_domains, src/load_balancing.cpp:12-65,
+ * stores it) -> min = bbox.min + (i * 2^-d) * span, max = min + span / 2^d
+ * per axis.  boxes_out: 6 doubles per prefix.  Host code. */
+int bh_let_bucket_boxes(const uint64_t *prefixes, int64_t n, int bucket_bits, const double bbox[6],
+                        double *boxes_out);
 /* computeAccelerations (src/traversal.cpp:13-103, include/traversal.h:21-30)
  * over the last tree; `mode` is a bh_mode.  acc_out (may be NULL) receives
  * the accelerations in the current body order. */

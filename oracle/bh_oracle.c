@@ -460,6 +460,180 @@ int orc_accelerations(void *h, int64_t n, const uint64_t *key, const double *pos
 }
 
 /* ------------------------------------------------------------------ */
+/* createInteractionListForRank, src/exchange.cpp:117-179: the cells of */
+/* a rank's tree that a remote rank (domain = `nb` boxes, 6 doubles     */
+/* each) needs.  Depth-first from the root; a cell is opened when       */
+/* s^2 >= theta2 * d^2 for any remote box (s the largest side of the    */
+/* cell's box, getBoundingBoxForCell in src/bounding_box.cpp:55-75; d^2 */
+/* min_distance_sq of :10-18) and its depth is below max_depth; it is  */
+/* kept otherwise.  Children are pushed in octant order while the       */
+/* 256-entry stack has room.  A failing cell at depth 21 with           */
+/* max_depth > 21 has no children in the map and is dropped.  Writes up */
+/* to `cap` records in visiting order; returns the count.              */
+/* ------------------------------------------------------------------ */
+static double orc_max2(double a, double b) { return (a < b) ? b : a; }
+
+int64_t orc_let_export(void *h, const double *boxes, int64_t nb, const double bb[6], double theta2, int max_depth,
+                       uint64_t *prefix, uint8_t *depth, double *mass, double *com, int64_t cap)
+{
+    const orc_tree *t = (const orc_tree *)h;
+    if (t->count == 0 || nb <= 0 || !orc_tree_find(t, 0, 0)) return 0;
+    const double span[3] = {bb[3] - bb[0], bb[4] - bb[1], bb[5] - bb[2]};
+    uint64_t sp[ORC_STACK_MAX];
+    int sd[ORC_STACK_MAX];
+    int top = 0;
+    int64_t out = 0;
+    sp[top] = 0;
+    sd[top] = 0;
+    top++;
+    while (top) {
+        --top;
+        const uint64_t pref = sp[top];
+        const int dep = sd[top];
+        /* the cell's box: integer coordinates from the prefix's bits */
+        uint32_t ic[3] = {0, 0, 0};
+        if (dep > 0) {
+            const uint64_t bits = pref >> (63 - 3 * dep);
+            for (int b = 0; b < dep; ++b)
+                for (int a = 0; a < 3; ++a) ic[a] |= (uint32_t)((bits >> (3 * b + a)) & 1u) << b;
+        }
+        const double scale = 1.0 / (double)(1ULL << dep);
+        double lo[3], hi[3];
+        for (int a = 0; a < 3; ++a) {
+            const double size = span[a] / (double)(1 << dep);
+            lo[a] = bb[a] + ((double)ic[a] * scale) * span[a];
+            hi[a] = lo[a] + size;
+        }
+        double s = hi[0] - lo[0];
+        s = orc_max2(s, hi[1] - lo[1]);
+        s = orc_max2(s, hi[2] - lo[2]);
+        const double s2 = s * s;
+        int opens = 0;
+        for (int64_t k = 0; k < nb && !opens; ++k) {
+            const double *r = boxes + 6 * k;
+            double e[3];
+            for (int a = 0; a < 3; ++a) e[a] = orc_max2(0.0, orc_max2(lo[a] - r[3 + a], r[a] - hi[a]));
+            const double d2 = e[0] * e[0] + e[1] * e[1] + e[2] * e[2];
+            opens = s2 >= theta2 * d2;
+        }
+        if (opens && dep < max_depth) {
+            if (dep >= ORC_MAX_DEPTH) continue; /* no deeper cells exist */
+            const int cd = dep + 1;
+            const uint64_t stride = 1ULL << (63 - 3 * cd);
+            for (int oc = 0; oc < 8; ++oc) {
+                const uint64_t c = pref | (uint64_t)oc * stride;
+                if (orc_tree_find(t, c, cd) && top < ORC_STACK_MAX) {
+                    sp[top] = c;
+                    sd[top] = cd;
+                    top++;
+                }
+            }
+        } else {
+            const orc_node *nd = orc_tree_find(t, pref, dep);
+            if (out < cap) {
+                prefix[out] = pref;
+                depth[out] = (uint8_t)dep;
+                mass[out] = nd->mass;
+                com[3 * out] = nd->cx;
+                com[3 * out + 1] = nd->cy;
+                com[3 * out + 2] = nd->cz;
+            }
+            out++;
+        }
+    }
+    return out;
+}
+
+/* ------------------------------------------------------------------ */
+/* buildTreeFromPseudoLeaves, src/linear_octree.cpp:242-322: a map of   */
+/* the given records (mass > 0 and finite; depth clamped to 21; prefix  */
+/* masked to it) and all their ancestors.  A record adds m and c * m to */
+/* its cell, in input order; every cell then adds its children's sums,  */
+/* deepest level first; com = sum / mass where mass > 1e-12.  Children  */
+/* are added in octant order here; the reference adds them in the      */
+/* iteration order of its hash map, so sums over several children agree */
+/* with it to rounding only.  Returns a tree handle (orc_tree_records). */
+/* ------------------------------------------------------------------ */
+typedef struct { uint64_t prefix; int depth; } orc_cell;
+
+static int orc_cell_cmp(const void *a, const void *b)
+{
+    const orc_cell *x = (const orc_cell *)a, *y = (const orc_cell *)b;
+    if (x->depth != y->depth) return (x->depth > y->depth) - (x->depth < y->depth);
+    return (x->prefix > y->prefix) - (x->prefix < y->prefix);
+}
+
+void *orc_pseudo_tree(const uint64_t *prefix, const uint8_t *depth, const double *mass, const double *com, int64_t m)
+{
+    orc_tree *t = (orc_tree *)malloc(sizeof(orc_tree));
+    if (!t || orc_tree_init(t, (uint64_t)(m > 0 ? m : 1) * 4) != ORC_OK) {
+        free(t);
+        return NULL;
+    }
+    for (int64_t k = 0; k < m; ++k) {
+        const double w = mass[k];
+        if (!(w > 0.0) || !isfinite(w)) continue;
+        const int d = depth[k] > ORC_MAX_DEPTH ? ORC_MAX_DEPTH : depth[k];
+        orc_node *nd = orc_tree_get(t, orc_prefix(prefix[k], d), d);
+        if (!nd) goto fail;
+        nd->mass += w;
+        nd->cx += com[3 * k] * w;
+        nd->cy += com[3 * k + 1] * w;
+        nd->cz += com[3 * k + 2] * w;
+    }
+    {
+        /* ancestors */
+        uint64_t nrec = t->count;
+        orc_cell *own = (orc_cell *)malloc(sizeof(orc_cell) * (nrec ? nrec : 1));
+        if (!own) goto fail;
+        uint64_t w = 0;
+        for (uint64_t i = 0; i < t->cap; ++i)
+            if (t->slot[i].depth >= 0) own[w++] = (orc_cell){t->slot[i].prefix, t->slot[i].depth};
+        for (uint64_t i = 0; i < w; ++i)
+            for (int d = own[i].depth - 1; d >= 0; --d)
+                if (!orc_tree_get(t, orc_prefix(own[i].prefix, d), d)) {
+                    free(own);
+                    goto fail;
+                }
+        free(own);
+        /* bottom-up sums in octant order */
+        orc_cell *all = (orc_cell *)malloc(sizeof(orc_cell) * (t->count ? t->count : 1));
+        if (!all) goto fail;
+        w = 0;
+        for (uint64_t i = 0; i < t->cap; ++i)
+            if (t->slot[i].depth >= 0) all[w++] = (orc_cell){t->slot[i].prefix, t->slot[i].depth};
+        qsort(all, (size_t)w, sizeof(orc_cell), orc_cell_cmp);
+        for (int64_t i = (int64_t)w - 1; i >= 0; --i) {
+            const int d = all[i].depth;
+            if (d >= ORC_MAX_DEPTH) continue;
+            orc_node *p = orc_tree_find(t, all[i].prefix, d);
+            const uint64_t stride = 1ULL << (63 - 3 * (d + 1));
+            for (int oc = 0; oc < 8; ++oc) {
+                const orc_node *c = orc_tree_find(t, all[i].prefix | (uint64_t)oc * stride, d + 1);
+                if (!c) continue;
+                p->mass += c->mass;
+                p->cx += c->cx;
+                p->cy += c->cy;
+                p->cz += c->cz;
+            }
+        }
+        free(all);
+    }
+    for (uint64_t i = 0; i < t->cap; ++i) {
+        orc_node *n = &t->slot[i];
+        if (n->depth < 0 || !(n->mass > 1e-12)) continue;
+        n->cx /= n->mass;
+        n->cy /= n->mass;
+        n->cz /= n->mass;
+    }
+    return t;
+fail:
+    free(t->slot);
+    free(t);
+    return NULL;
+}
+
+/* ------------------------------------------------------------------ */
 /* The step loop of src/main.cpp:191-282 for `--fc tree` on one rank.   */
 /* The half kick at :193-200 runs only when t > 0; t is accumulated in  */
 /* double (t += dt), as the reference's loop header does.  The MPI      */

@@ -84,6 +84,8 @@ class Oracle:
             self._direct = f("direct_sum", None, [_I64, _P, _P, _I64, _P, _D, _P])
             self._inv = f("invariants", None, [_I64, _P, _P, _P, _D, _P])
             self._threads = f("num_threads", C.c_int, [])
+            self._let = f("let_export", _I64, [_P, _P, _I64, _P, _D, C.c_int, _P, _P, _P, _P, _I64])
+            self._pseudo = f("pseudo_tree", _P, [_P, _P, _P, _P, _I64])
         else:
             self._bbox = f("compute_local_bbox", None, [_P, _I64, _P])
             self._keys = f("generate_morton_codes", None, [_P, _I64, _P, _P])
@@ -95,6 +97,8 @@ class Oracle:
             self._accel = f("compute_accelerations", None, [_P, _I64, _P, _P, _D, _D, _D, _P, _P])
             self._sim = f("simulate", None, [_I64, _P, _P, _P, _P, _P, _D, _D, _D, _I64, _P, _P])
             self._kepler = f("kepler_to_cartesian", None, [_P, _I64, _P])
+            self._let = f("let_export", _I64, [_P, _P, _I64, _P, _D, C.c_int, _P, _P, _P, _P, _I64])
+            self._pseudo = f("pseudo_tree", _P, [_P, _P, _P, _P, _I64])
 
     # -- stages ---------------------------------------------------------
     def bbox(self, pos) -> np.ndarray:
@@ -144,6 +148,28 @@ class Oracle:
             return (acc, cnt) if count else acc
         self._accel(tree.h, len(k), _ptr(k), _ptr(p), theta, G, soft2, _ptr(bb), _ptr(acc))
         return acc
+
+    def let_export(self, tree, boxes, bbox, theta2, max_depth=21):
+        """createInteractionListForRank (src/exchange.cpp:117-179) on `tree`:
+        the exported cells (prefix, depth, mass, com) sorted by (depth, prefix)."""
+        bx = np.ascontiguousarray(boxes, np.float64).reshape(-1, 6)
+        bb = np.ascontiguousarray(bbox, np.float64)
+        cap = len(tree)
+        p = np.empty(cap, np.uint64); d = np.empty(cap, np.uint8); m = np.empty(cap); c = np.empty((cap, 3))
+        k = int(self._let(tree.h, _ptr(bx), len(bx), _ptr(bb), theta2, int(max_depth), _ptr(p), _ptr(d), _ptr(m),
+                          _ptr(c), cap))
+        o = np.lexsort((p[:k], d[:k]))
+        return p[:k][o], d[:k][o], m[:k][o], c[:k][o]
+
+    def pseudo_tree(self, prefix, depth, mass, com) -> "OracleTree":
+        """buildTreeFromPseudoLeaves (src/linear_octree.cpp:242-322) over
+        NodeRecords; read the map back with .records()."""
+        p = np.ascontiguousarray(prefix, np.uint64); d = np.ascontiguousarray(depth, np.uint8)
+        m = np.ascontiguousarray(mass, np.float64); c = np.ascontiguousarray(com, np.float64).reshape(-1, 3)
+        h = self._pseudo(_ptr(p), _ptr(d), _ptr(m), _ptr(c), len(p))
+        if not h:
+            raise MemoryError("pseudo_tree")
+        return OracleTree(self, h)
 
     def simulate(self, pos, vel, mass, ids, dt, theta, G, nsteps, t=0.0, acc=None):
         """Runs the step loop; returns (pos, vel, mass, ids, acc, t, phase_s)."""

@@ -18,6 +18,7 @@
 
 #include "body.h"
 #include "bounding_box.h"
+#include "exchange.h"
 #include "kepler_to_cartesian.h"
 #include "linear_octree.h"
 #include "morton_keys.h"
@@ -239,6 +240,38 @@ void ref_kepler_to_cartesian(const double* el, int64_t n, double* out)
         o[3] = b->vx; o[4] = b->vy; o[5] = b->vz;
         delete b;
     }
+}
+
+// createInteractionListForRank (src/exchange.cpp:117-179): the cells of the
+// tree a remote rank whose domain is covered by `boxes` (nb x {min, max})
+// needs, as NodeRecords; up to `cap` are written, the count is returned.
+int64_t ref_let_export(TreeHandle* t, const double* boxes, int64_t nb, const double bb[6], double theta2,
+                       int max_depth, uint64_t* prefix, uint8_t* depth, double* mass, double* com, int64_t cap)
+{
+    std::vector<BoundingBox> rb((size_t)nb);
+    for (int64_t k = 0; k < nb; ++k) rb[(size_t)k] = to_bbox(boxes + 6 * k);
+    const std::vector<NodeRecord> recs = createInteractionListForRank(t->map, rb, to_bbox(bb), theta2, max_depth);
+    for (size_t k = 0; k < recs.size() && (int64_t)k < cap; ++k) {
+        prefix[k] = recs[k].prefix;
+        depth[k] = recs[k].depth;
+        mass[k] = recs[k].mass;
+        com[3 * k] = recs[k].comX;
+        com[3 * k + 1] = recs[k].comY;
+        com[3 * k + 2] = recs[k].comZ;
+    }
+    return (int64_t)recs.size();
+}
+
+// buildTreeFromPseudoLeaves (src/linear_octree.cpp:242-322) over m
+// NodeRecords; the map is read back with ref_tree_size / ref_tree_records.
+void* ref_pseudo_tree(const uint64_t* prefix, const uint8_t* depth, const double* mass, const double* com, int64_t m)
+{
+    std::vector<NodeRecord> recs((size_t)m);
+    for (int64_t k = 0; k < m; ++k)
+        recs[(size_t)k] = {prefix[k], depth[k], mass[k], com[3 * k], com[3 * k + 1], com[3 * k + 2]};
+    auto* h = new TreeHandle();
+    h->map = buildTreeFromPseudoLeaves(recs);
+    return h;
 }
 
 }  // extern "C"

@@ -3,7 +3,9 @@ sources, compiled unmodified by ``make -C oracle ref`` (oracle/_ref).
 
 Run in a checkout where the reference is present:
 
-    python tests/golden/make_golden.py
+    python tests/golden/make_golden.py [edge synthetic let pseudo scenario]
+
+(no arguments: every fixture).
 
 Outputs (all produced by the compiled reference, strict IEEE build):
 
@@ -20,6 +22,20 @@ Outputs (all produced by the compiled reference, strict IEEE build):
                              inputs, keys, permutation, SHA-256 digests of the
                              tree and of the accelerations, and the first 512
                              accelerations in full.
+* ``let_export.npz``      -- createInteractionListForRank on the tree of
+                             buildOctreeBottomUp (no merge) of the two
+                             synthetic systems above (their inputs are read
+                             from those files): remote domains of bucket boxes
+                             (key-range splits as update_rank_domains makes
+                             them) and of random boxes, several theta and
+                             max_depth values; the kept cells sorted by
+                             (depth, prefix).
+* ``pseudo_tree.npz``     -- buildTreeFromPseudoLeaves over the records rank 0
+                             of a 4-way split of synthetic_1000 receives
+                             (the other ranks' exports to its bucket boxes),
+                             plus duplicate, massless, non-finite, negative,
+                             unmasked and too-deep records: inputs and the
+                             map, sorted by (depth, prefix).
 * ``scenario1.json``      -- digests of the same stages on the reference's own
                              data/state_vectors_csvs/scenario1_19054.csv (the
                              file itself is not copied here).
@@ -84,13 +100,99 @@ def edge_systems():
     return cases
 
 
+def bucket_boxes(prefixes, bucket_bits, bb):
+    """exchangeEssentialTrees' bucket boxes (src/exchange.cpp:45-71) in the
+    same float64 operation order (numpy rounds each operation, no FMA)."""
+    d = bucket_bits // 3
+    bits = np.asarray(prefixes, np.uint64) >> np.uint64(63 - 3 * d) if d else np.zeros(len(prefixes), np.uint64)
+    out = np.empty((len(prefixes), 6))
+    scale = 1.0 / float(1 << d)
+    for a in range(3):
+        v = np.zeros(len(prefixes), np.uint64)
+        for b in range(d):
+            v |= ((bits >> np.uint64(3 * b + a)) & np.uint64(1)) << np.uint64(b)
+        span = bb[3 + a] - bb[a]
+        lo = bb[a] + (v.astype(np.float64) * scale) * span
+        out[:, a] = lo
+        out[:, 3 + a] = lo + span / float(1 << d)
+    return out
+
+
+def let_cases(ref: Oracle, pos, vel, mass, ids, rng, full: bool):
+    """LET exports of one system for a few remote domains.  Bucket cases:
+    the bodies are split into contiguous bucket ranges of about n / nranks
+    bodies (as update_rank_domains, src/load_balancing.cpp:12-65, splits
+    them); rank 0's bodies form the local tree (keys in the global box) and
+    each other rank's non-empty buckets its domain.  Random cases: all bodies
+    are local, the domain is a few random boxes.  With `full` the kept cells
+    are stored, otherwise their count, depth histogram and SHA-256 digest."""
+    n = len(mass)
+    bb = ref.bbox(pos)
+    keys = ref.keys(pos, bb)
+    out = {"bbox": bb}
+    cases = []
+    for bucket_bits, nranks in ((6, 2), (9, 4), (12, 3)):
+        bidx = (keys >> np.uint64(63 - bucket_bits)).astype(np.int64)
+        hist = np.bincount(bidx, minlength=1 << bucket_bits)
+        ideal = (n + nranks - 1) // nranks
+        split, run = [], 0
+        for i, h in enumerate(hist):
+            run += int(h)
+            if len(split) < nranks - 1 and run >= (len(split) + 1) * ideal:
+                split.append(i)
+        owner = np.searchsorted(np.array(split, np.int64), np.arange(1 << bucket_bits), side="right")
+        local = owner[bidx] == 0
+        for r in range(1, nranks):
+            pref = (np.nonzero((hist > 0) & (owner == r))[0].astype(np.uint64)) << np.uint64(63 - bucket_bits)
+            cases.append((bucket_boxes(pref, bucket_bits, bb), local, pref, bucket_bits))
+    for _ in range(4):
+        k = int(rng.integers(1, 6))
+        c = rng.uniform(bb[:3], bb[3:], (k, 3)); h = rng.uniform(0.2, 15.0, (k, 3))
+        cases.append((np.concatenate([c - h, c + h], axis=1), np.ones(n, bool), None, -1))
+    params = ((1.05, 21), (0.5, 21), (1.05, 4), (0.3, 0), (1.5, 25), (0.7, 21))
+    for ci, (boxes, local, pref, bits) in enumerate(cases):
+        theta, max_depth = params[ci % len(params)]
+        sel = np.nonzero(local)[0]
+        sk, sp, sm, _, _, _ = ref.sort(keys[sel], pos[sel], mass[sel], vel[sel], ids[sel])
+        tree = ref.tree(sk, sp, sm, merge=False)
+        p, d, m, c = ref.let_export(tree, boxes, bb, theta * theta, max_depth)
+        tree.close()
+        out[f"c{ci}/local"] = np.packbits(local)
+        out[f"c{ci}/boxes"] = boxes
+        out[f"c{ci}/theta2"] = np.array([theta * theta])
+        out[f"c{ci}/max_depth"] = np.array([max_depth])
+        if pref is not None:
+            out[f"c{ci}/bucket_prefixes"] = pref
+            out[f"c{ci}/bucket_bits"] = np.array([bits])
+        out[f"c{ci}/count"] = np.array([len(p)])
+        out[f"c{ci}/depth_hist"] = np.bincount(d, minlength=22)
+        out[f"c{ci}/digest"] = np.array([digest(p, d, m, c)])
+        if full:
+            out[f"c{ci}/prefix"] = p; out[f"c{ci}/depth"] = d; out[f"c{ci}/mass"] = m; out[f"c{ci}/com"] = c
+    out["n_cases"] = np.array([len(cases)])
+    return out
+
+
 def main() -> None:
     if build_reference() is None:
         raise SystemExit("the reference checkout is needed to regenerate the fixtures")
     ref = Oracle("reference")
     bh = importlib.import_module("barnes-hut_gb300")
+    want = set(sys.argv[1:]) or {"edge", "synthetic", "let", "pseudo", "scenario"}
+    if "edge" in want:
+        edge_fixtures(ref, bh)
+    if "synthetic" in want:
+        synthetic_fixtures(ref, bh)
+    if "let" in want:
+        let_fixtures(ref, bh)
+    if "pseudo" in want:
+        pseudo_fixtures(ref)
+    if "scenario" in want:
+        scenario_fixture(ref, bh)
+    print("fixtures written to", HERE)
 
-    # Edge cases
+
+def edge_fixtures(ref, bh):
     out = {}
     for name, (pos, vel, mass) in edge_systems().items():
         ids = np.arange(len(mass), dtype=np.uint64)
@@ -103,6 +205,8 @@ def main() -> None:
         out[f"massive/{k}"] = v
     np.savez_compressed(HERE / "edge_cases.npz", **out)
 
+
+def synthetic_fixtures(ref, bh):
     # Synthetic 1,000
     pos, vel, mass, ids = bh.generate_system(7, 1000, 0.1, 0.05)
     out = dict(pos=pos, vel=vel, mass=mass, ids=ids)
@@ -131,6 +235,59 @@ def main() -> None:
     out.update(sim3_digest=np.array([digest(p, v, m, i, a)]), sim3_t=np.array([t]))
     np.savez_compressed(HERE / "synthetic_19054.npz", **out)
 
+
+def let_fixtures(ref, bh):
+    # Locally essential tree exports
+    rng = np.random.default_rng(2024)
+    out = {}
+    for tag in ("synthetic_1000", "synthetic_19054"):
+        g = np.load(HERE / f"{tag}.npz")
+        for k, v in let_cases(ref, g["pos"], g["vel"], g["mass"], g["ids"], rng, tag == "synthetic_1000").items():
+            out[f"{tag}/{k}"] = v
+    np.savez_compressed(HERE / "let_export.npz", **out)
+
+
+def pseudo_fixtures(ref):
+    g = np.load(HERE / "synthetic_1000.npz")
+    pos, vel, mass, ids = g["pos"], g["vel"], g["mass"], g["ids"]
+    bb = ref.bbox(pos)
+    keys = ref.keys(pos, bb)
+    bits, nranks = 6, 4
+    bidx = (keys >> np.uint64(63 - bits)).astype(np.int64)
+    hist = np.bincount(bidx, minlength=1 << bits)
+    ideal = (len(keys) + nranks - 1) // nranks
+    split, run = [], 0
+    for i, h in enumerate(hist):
+        run += int(h)
+        if len(split) < nranks - 1 and run >= (len(split) + 1) * ideal:
+            split.append(i)
+    owner = np.searchsorted(np.array(split, np.int64), np.arange(1 << bits), side="right")
+    pref0 = (np.nonzero((hist > 0) & (owner == 0))[0].astype(np.uint64)) << np.uint64(63 - bits)
+    boxes0 = bucket_boxes(pref0, bits, bb)
+    parts = []
+    for r in range(1, nranks):
+        sel = np.nonzero(owner[bidx] == r)[0]
+        sk, sp, sm, _, _, _ = ref.sort(keys[sel], pos[sel], mass[sel], vel[sel], ids[sel])
+        tree = ref.tree(sk, sp, sm, merge=False)
+        parts.append(ref.let_export(tree, boxes0, bb, 0.5 ** 2, 21))
+        tree.close()
+    p = np.concatenate([x[0] for x in parts]); d = np.concatenate([x[1] for x in parts])
+    m = np.concatenate([x[2] for x in parts]); c = np.concatenate([x[3] for x in parts])
+    # edge records: a duplicate key (summed in input order), massless,
+    # non-finite and negative masses (skipped), an unmasked prefix, depth 30
+    p = np.concatenate([p, p[:3], p[3:6], [p[6] | np.uint64(0x5555)], [p[7]]])
+    d = np.concatenate([d, d[:3], d[3:6], [d[6]], [30]]).astype(np.uint8)
+    m = np.concatenate([m, m[:3] * 0.25, [0.0, np.nan, -m[5]], [m[6]], [m[7]]])
+    c = np.concatenate([c, c[:3] * 0.5, c[3:6], c[6:7], c[7:8]])
+    out = dict(prefix=p, depth=d, mass=m, com=c)
+    t = ref.pseudo_tree(p, d, m, c)
+    for k, v in zip(("prefix", "depth", "mass", "com"), t.records()):
+        out[f"tree_{k}"] = v
+    t.close()
+    np.savez_compressed(HERE / "pseudo_tree.npz", **out)
+
+
+def scenario_fixture(ref, bh):
     # The reference's own scenario-1 CSV: digests only.
     csv = Path("/root/reference/data/state_vectors_csvs/scenario1_19054.csv")
     if csv.exists():
@@ -144,7 +301,6 @@ def main() -> None:
                     tree_digest=digest(s["tree_prefix"], s["tree_depth"], s["tree_mass"], s["tree_com"]),
                     acc_digest=digest(s["acc"]))
         (HERE / "scenario1.json").write_text(json.dumps(info, indent=1) + "\n")
-    print("fixtures written to", HERE)
 
 
 if __name__ == "__main__":

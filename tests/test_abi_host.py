@@ -152,3 +152,20 @@ def test_vtp_snapshot_layout(bh, tmp_path):
     assert arr("PointData", "acceleration").text.split() == [g(v) for v in np.sqrt((acc ** 2).sum(axis=1))]
     assert arr("Verts", "offsets").text.split() == [str(i) for i in range(1, n + 1)]
     assert arr("Verts", "connectivity").text.split() == [str(i) for i in range(n)]
+
+
+def test_let_bucket_boxes_match_fixture(bh, golden):
+    """bh_let_bucket_boxes reproduces the bucket boxes of the LET fixtures
+    (exchangeEssentialTrees' arithmetic) bit for bit."""
+    from conftest import assert_bits_equal
+    f = golden("let_export.npz")
+    seen = 0
+    for system in ("synthetic_1000", "synthetic_19054"):
+        for ci in range(int(f[f"{system}/n_cases"][0])):
+            key = f"{system}/c{ci}/bucket_prefixes"
+            if key not in f:
+                continue
+            got = bh.let_bucket_boxes(f[key], int(f[f"{system}/c{ci}/bucket_bits"][0]), f[f"{system}/bbox"])
+            assert_bits_equal(got, f[f"{system}/c{ci}/boxes"], f"{system} case {ci}")
+            seen += 1
+    assert seen >= 10

@@ -162,3 +162,53 @@ def test_port_equals_compiled_reference_random(port):
                           rng.uniform(0, 6.3, 50), rng.uniform(0, 6.3, 50), rng.uniform(-7, 7, 50),
                           rng.uniform(2451000, 2452000, 50), np.full(50, 2.96e-4)])
     assert_bits_equal(port.kepler(el), ref.kepler(el), "kepler")
+
+
+def _let_tree(o, g, local, bb):
+    """The local tree of buildOctreeBottomUp (no merge) over the bodies in
+    `local`, keys in the global box `bb`."""
+    sel = np.nonzero(local)[0]
+    keys = o.keys(g["pos"][sel], bb)
+    sk, sp, sm, _, _, _ = o.sort(keys, g["pos"][sel], g["mass"][sel], g["vel"][sel], g["ids"][sel])
+    return o.tree(sk, sp, sm, merge=False)
+
+
+@pytest.mark.parametrize("system", ["synthetic_1000", "synthetic_19054"])
+def test_let_export_matches_reference(port, golden, system):
+    """createInteractionListForRank restated in the oracle against the
+    compiled reference's exports (bucket domains of other ranks and random
+    boxes; theta 0.3-1.5; max_depth 0, 4, 21, 25)."""
+    g = golden(f"{system}.npz")
+    f = golden("let_export.npz")
+    bb = f[f"{system}/bbox"]
+    for ci in range(int(f[f"{system}/n_cases"][0])):
+        c = f"{system}/c{ci}/"
+        local = np.unpackbits(f[c + "local"])[:len(g["mass"])].astype(bool)
+        tree = _let_tree(port, g, local, bb)
+        p, d, m, com = port.let_export(tree, f[c + "boxes"], bb, float(f[c + "theta2"][0]), int(f[c + "max_depth"][0]))
+        tree.close()
+        assert len(p) == int(f[c + "count"][0]), ci
+        h = hashlib.sha256()
+        for a in (p, d, m, com):
+            h.update(np.ascontiguousarray(a).tobytes())
+        assert h.hexdigest() == str(f[c + "digest"][0]), ci
+        if c + "prefix" in f:
+            assert_bits_equal(p, f[c + "prefix"], f"case {ci} prefixes")
+            assert_bits_equal(com, f[c + "com"], f"case {ci} centres of mass")
+
+
+def test_pseudo_tree_matches_reference(port, golden):
+    """buildTreeFromPseudoLeaves restated in the oracle (children summed in
+    octant order) against the compiled reference (hash-map order): the same
+    cells; masses and centres of mass within 1e-14 relative."""
+    f = golden("pseudo_tree.npz")
+    t = port.pseudo_tree(f["prefix"], f["depth"], f["mass"], f["com"])
+    p, d, m, c = t.records()
+    t.close()
+    assert_bits_equal(p, f["tree_prefix"], "prefixes")
+    assert_bits_equal(d, f["tree_depth"], "depths")
+    assert np.all(np.abs(m - f["tree_mass"]) <= 1e-14 * np.abs(f["tree_mass"]))
+    scale = np.abs(f["tree_com"]).max(axis=1, keepdims=True)
+    assert np.all(np.abs(c - f["tree_com"]) <= 1e-14 * scale)
+    # cells whose sums involve no reordering agree bit for bit
+    assert np.mean(m == f["tree_mass"]) > 0.8
