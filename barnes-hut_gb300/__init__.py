@@ -104,6 +104,8 @@ def _sig(lib):
     f["bh_let_export"] = (C.c_int, [_P, _P, _I64, _P, _D, C.c_int, _I64, _P, _P, _P, _P, C.POINTER(_I64)])
     f["bh_let_bucket_boxes"] = (C.c_int, [_P, _I64, C.c_int, _P, _P])
     f["bh_pseudo_leaf_tree"] = (C.c_int, [_P, _P, _P, _P, _P, _I64, _I64, _P, _P, _P, _P, C.POINTER(_I64)])
+    f["bh_let_accelerations"] = (C.c_int, [_P, _P, _P, _P, _P, _I64, _D, _D, _D, _P])
+    f["bh_let_direct_accelerations"] = (C.c_int, [_P, _P, _P, _P, _P, _I64, _D, _D, _D, _P])
     f["bh_mlp_gradient"] = (C.c_int, [_P, _P, _P, _I64, _P, _P])
     f["bh_mlp_train"] = (C.c_int, [_P, _P, _I64, C.c_int, C.c_int, C.c_float, C.c_uint64, _P, _P, _P])
     f["bh_mlp_predict"] = (C.c_int, [_P, _P, _P, _I64, _P, _P])
@@ -371,6 +373,19 @@ class Context:
                                              _ptr(od), _ptr(om), _ptr(oc), C.byref(k)))
         k = k.value
         return op[:k], od[:k], om[:k], oc[:k]
+
+    def let_accelerations(self, prefix, depth, mass, com, theta=THETA_DEFAULT, G=G_DEFAULT, soft2=0.0,
+                          direct=False) -> np.ndarray:
+        """computeAccelerationsWithLET (direct=False) or
+        computeAccelerationsWithRemoteDirectSum (direct=True) for the local
+        bodies (current order) with the received records."""
+        p = _u64(prefix); d = np.ascontiguousarray(depth, np.uint8); m = _f64(mass)
+        c = _f64(com).reshape(-1, 3)
+        out = np.empty((self.n, 3))
+        fn = library().bh_let_direct_accelerations if direct else library().bh_let_accelerations
+        _check(fn(self._h, _ptr(p), _ptr(d), _ptr(m), _ptr(c), len(m), float(theta), float(G), float(soft2),
+                  _ptr(out)))
+        return out
 
     def compute_accelerations(self, theta=THETA_DEFAULT, G=G_DEFAULT, soft2=0.0, mode=MODE_PLAIN_FP64,
                               download=True):

@@ -400,6 +400,7 @@ int bh_context_destroy(bh_context* ctx)
     if (ctx->let_buf) cudaFree(ctx->let_buf);
     if (ctx->imp_buf) cudaFree(ctx->imp_buf);
     if (ctx->imp_buf2) cudaFree(ctx->imp_buf2);
+    if (ctx->letf_buf) cudaFree(ctx->letf_buf);
     for (auto& g : ctx->sg)
         if (g.exec) cudaGraphExecDestroy(g.exec);
     delete ctx;

@@ -351,6 +351,8 @@ struct bh_context {
     size_t imp_bytes = 0;
     void* imp_buf2 = nullptr;   // and entries / cells
     size_t imp_bytes2 = 0;
+    void* letf_buf = nullptr;   // merged map of the LET force paths
+    size_t letf_bytes = 0;
 };
 
 namespace bh {

@@ -460,17 +460,26 @@ int bh_let_export(bh_context* ctx, const double* boxes, int64_t nboxes, const do
 
 }  // extern "C"
 
-extern "C" int bh_pseudo_leaf_tree(bh_context* ctx, const uint64_t* prefix, const uint8_t* depth, const double* mass,
-                                   const double* com, int64_t m, int64_t capacity, uint64_t* o_prefix,
-                                   uint8_t* o_depth, double* o_mass, double* o_com, int64_t* count_out)
+namespace {
+
+// The device map of buildTreeFromPseudoLeaves: n cells sorted by
+// locational code, in ctx->imp_buf2.
+struct PseudoCells {
+    int32_t n = 0;
+    const uint64_t* code = nullptr;
+    const uint64_t* prefix = nullptr;
+    const uint8_t* depth = nullptr;
+    const double* mass = nullptr;
+    const double* com = nullptr;  // 3 per cell
+};
+
+int pseudo_tree_device(bh_context* ctx, const uint64_t* prefix, const uint8_t* depth, const double* mass,
+                       const double* com, int64_t m, PseudoCells* out)
 {
-    if (!ctx || !count_out || m < 0 || capacity < 0 || (m > 0 && (!prefix || !depth || !mass || !com)))
-        return bh_fail(BH_ERR_INVALID_ARGUMENT, "bh_pseudo_leaf_tree: bad arguments");
+    *out = PseudoCells{};
     // entries (record cells and their ancestors) are numbered in int32
     if (m > (int64_t)(INT32_MAX / (bh::kMaxDepth + 1)))
-        return bh_fail(BH_ERR_INVALID_ARGUMENT, "bh_pseudo_leaf_tree: too many records");
-    BH_CUDA_TRY(cudaSetDevice(ctx->device));
-    *count_out = 0;
+        return bh_fail(BH_ERR_INVALID_ARGUMENT, "pseudo-leaf tree: too many records");
     if (m == 0) return BH_OK;
     cudaStream_t st = ctx->stream;
     int dev_sms = 0;
@@ -565,14 +574,9 @@ extern "C" int bh_pseudo_leaf_tree(bh_context* ctx, const uint64_t* prefix, cons
     unsigned h_err = 0;
     std::memcpy(hs, ctx->h_small, sizeof(hs));
     std::memcpy(&h_err, reinterpret_cast<char*>(ctx->h_small) + 256, sizeof(unsigned));
-    if (h_err & bh::kErrTimeout) return bh_fail(BH_ERR_TIMEOUT, "bh_pseudo_leaf_tree: a bounded device wait gave up");
+    if (h_err & bh::kErrTimeout) return bh_fail(BH_ERR_TIMEOUT, "pseudo-leaf tree: a bounded device wait gave up");
     const int32_t ncell = hs[1];
     const int32_t* ls = hs + 8;  // ls[0..22]
-    *count_out = ncell;
-    if (ncell > capacity)
-        return bh_fail(BH_ERR_INVALID_ARGUMENT, "bh_pseudo_leaf_tree: capacity below the cell count");
-    if (!o_prefix || !o_depth || !o_mass || !o_com)
-        return bh_fail(BH_ERR_INVALID_ARGUMENT, "bh_pseudo_leaf_tree: null output array");
 
     // Bottom-up sums, deepest level first.
     for (int e = bh::kMaxDepth; e >= 0; --e) {
@@ -585,10 +589,453 @@ extern "C" int bh_pseudo_leaf_tree(bh_context* ctx, const uint64_t* prefix, cons
     }
     imp_out_kernel<<<grid_for(ncell), 256, 0, st>>>(ncell, cell_code, acc, d_prefix, d_depth, d_mass, d_com);
     BH_LAUNCH_CHECK(ctx);
-    BH_CUDA_TRY(cudaMemcpyAsync(o_prefix, d_prefix, sizeof(uint64_t) * ncell, cudaMemcpyDeviceToHost, st));
-    BH_CUDA_TRY(cudaMemcpyAsync(o_depth, d_depth, ncell, cudaMemcpyDeviceToHost, st));
-    BH_CUDA_TRY(cudaMemcpyAsync(o_mass, d_mass, sizeof(double) * ncell, cudaMemcpyDeviceToHost, st));
-    BH_CUDA_TRY(cudaMemcpyAsync(o_com, d_com, 3 * sizeof(double) * ncell, cudaMemcpyDeviceToHost, st));
+    out->n = ncell;
+    out->code = cell_code;
+    out->prefix = d_prefix;
+    out->depth = d_depth;
+    out->mass = d_mass;
+    out->com = d_com;
+    return BH_OK;
+}
+
+}  // namespace
+
+extern "C" int bh_pseudo_leaf_tree(bh_context* ctx, const uint64_t* prefix, const uint8_t* depth, const double* mass,
+                                   const double* com, int64_t m, int64_t capacity, uint64_t* o_prefix,
+                                   uint8_t* o_depth, double* o_mass, double* o_com, int64_t* count_out)
+{
+    if (!ctx || !count_out || m < 0 || capacity < 0 || (m > 0 && (!prefix || !depth || !mass || !com)))
+        return bh_fail(BH_ERR_INVALID_ARGUMENT, "bh_pseudo_leaf_tree: bad arguments");
+    BH_CUDA_TRY(cudaSetDevice(ctx->device));
+    *count_out = 0;
+    PseudoCells pc;
+    int rc = pseudo_tree_device(ctx, prefix, depth, mass, com, m, &pc);
+    if (rc) return rc;
+    *count_out = pc.n;
+    if (pc.n == 0) return BH_OK;
+    if (pc.n > capacity)
+        return bh_fail(BH_ERR_INVALID_ARGUMENT, "bh_pseudo_leaf_tree: capacity below the cell count");
+    if (!o_prefix || !o_depth || !o_mass || !o_com)
+        return bh_fail(BH_ERR_INVALID_ARGUMENT, "bh_pseudo_leaf_tree: null output array");
+    cudaStream_t st = ctx->stream;
+    BH_CUDA_TRY(cudaMemcpyAsync(o_prefix, pc.prefix, sizeof(uint64_t) * pc.n, cudaMemcpyDeviceToHost, st));
+    BH_CUDA_TRY(cudaMemcpyAsync(o_depth, pc.depth, pc.n, cudaMemcpyDeviceToHost, st));
+    BH_CUDA_TRY(cudaMemcpyAsync(o_mass, pc.mass, sizeof(double) * pc.n, cudaMemcpyDeviceToHost, st));
+    BH_CUDA_TRY(cudaMemcpyAsync(o_com, pc.com, 3 * sizeof(double) * pc.n, cudaMemcpyDeviceToHost, st));
+    BH_CUDA_TRY(cudaStreamSynchronize(st));
+    return BH_OK;
+}
+
+// ---- Forces with imported LET records --------------------------------------
+//
+// computeAccelerationsWithLET (src/traversal.cpp:107-127): the received
+// records become a pseudo-leaf map, which mergeRecordsIntoTree
+// (src/linear_octree.cpp:178-204) folds into the local map (a cell in both:
+// com = (m0 c0 + m1 c1) / (m0 + m1), skipped when that mass is 0; a cell
+// only in the pseudo map enters with m0 = 0), and computeAccelerations
+// (src/traversal.cpp:13-103) walks the merged map.  The merged map is not
+// the compressed tree of any body set, so it is built here as an explicit
+// cell array: the local chains expanded into their cells, the pseudo cells
+// appended, one stable sort of the locational codes, and a merge of equal
+// codes.  Each body then walks it depth first with the reference's visiting
+// order (children pushed in octant order, popped last first) and its IEEE
+// operation sequence, so the result is the reference's on the same merged
+// map.  computeAccelerationsWithRemoteDirectSum (:149-221) is the exact
+// traversal of the local tree plus a direct sum over the records, in record
+// order.
+namespace {
+
+constexpr int kLetStack = 192;  // DFS depth <= 7 * 21 + 1 entries
+
+struct Side2 {
+    double v[bh::kMaxDepth + 1];
+};
+
+__global__ void chain_count_kernel(const int32_t* __restrict__ counts, const bh::TreeRec* __restrict__ rec,
+                                   int32_t* __restrict__ cnt)
+{
+    const int32_t S = counts[2];
+    for (int32_t s = blockIdx.x * blockDim.x + threadIdx.x; s < S; s += gridDim.x * blockDim.x)
+        cnt[s] = (int32_t)rec[s].depth - (int32_t)rec[s].top + 1;
+}
+
+// Local cells (codes at [0, L)) and the pseudo cells appended at [L, L + R).
+__global__ void chain_cells_kernel(const int32_t* __restrict__ counts, const bh::TreeRec* __restrict__ rec,
+                                   const int32_t* __restrict__ slot_ref, const int32_t* __restrict__ node_a,
+                                   const uint64_t* __restrict__ leaf_key, const int32_t* __restrict__ off,
+                                   uint64_t* __restrict__ code, int32_t* __restrict__ cell_slot)
+{
+    const int32_t S = counts[2];
+    for (int32_t s = blockIdx.x * blockDim.x + threadIdx.x; s < S; s += gridDim.x * blockDim.x) {
+        const bh::TreeRec r = rec[s];
+        const int32_t ref = slot_ref[s];
+        const uint64_t key = leaf_key[ref >= 0 ? ref : node_a[~ref]];
+        const int32_t o = off[s];
+        for (int d = r.top; d <= r.depth; ++d) {
+            code[o + d - r.top] = loc_code(key & bh::prefix_mask(d), d);
+            cell_slot[o + d - r.top] = s;
+        }
+    }
+}
+
+__global__ void merge_head_kernel(int64_t t, const uint64_t* __restrict__ code, int32_t* __restrict__ head)
+{
+    for (int64_t j = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; j < t; j += (int64_t)gridDim.x * blockDim.x)
+        head[j] = (j == 0 || code[j] != code[j - 1]) ? 1 : 0;
+}
+
+// One merged cell per distinct code.  Sorted entries of one code: the local
+// cell (entry index < L) first, then the pseudo cell.
+__global__ void merge_cells_kernel(int64_t t, int32_t L, const uint64_t* __restrict__ code,
+                                   const uint32_t* __restrict__ perm, const int32_t* __restrict__ midx,
+                                   const int32_t* __restrict__ cell_slot, const bh::TreeRec* __restrict__ rec,
+                                   const double* __restrict__ p_mass, const double* __restrict__ p_com,
+                                   uint64_t* __restrict__ m_code, double4_32a* __restrict__ m_val)
+{
+    for (int64_t j = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; j < t; j += (int64_t)gridDim.x * blockDim.x) {
+        if (j > 0 && code[j] == code[j - 1]) continue;
+        const uint32_t e0 = perm[j];
+        double m0 = 0.0, x0 = 0.0, y0 = 0.0, z0 = 0.0;
+        int32_t remote = -1;
+        if ((int32_t)e0 < L) {
+            const bh::TreeRec r = rec[cell_slot[e0]];
+            m0 = r.m; x0 = r.cx; y0 = r.cy; z0 = r.cz;
+            if (j + 1 < t && code[j + 1] == code[j]) remote = (int32_t)perm[j + 1] - L;
+        } else {
+            remote = (int32_t)e0 - L;
+        }
+        if (remote >= 0) {
+            const double m1 = p_mass[remote];
+            const double tot = __dadd_rn(m0, m1);
+            if (tot != 0.0) {
+                x0 = __ddiv_rn(__dadd_rn(__dmul_rn(m0, x0), __dmul_rn(m1, p_com[3 * (int64_t)remote])), tot);
+                y0 = __ddiv_rn(__dadd_rn(__dmul_rn(m0, y0), __dmul_rn(m1, p_com[3 * (int64_t)remote + 1])), tot);
+                z0 = __ddiv_rn(__dadd_rn(__dmul_rn(m0, z0), __dmul_rn(m1, p_com[3 * (int64_t)remote + 2])), tot);
+                m0 = tot;
+            }
+        }
+        const int32_t k = midx[j];
+        m_code[k] = code[j];
+        m_val[k] = double4_32a{x0, y0, z0, m0};
+    }
+}
+
+// First child (index into the merged cells) and the octants present.
+__global__ void merge_children_kernel(int32_t M, const uint64_t* __restrict__ m_code, int32_t* __restrict__ first,
+                                      uint8_t* __restrict__ mask)
+{
+    for (int32_t c = blockIdx.x * blockDim.x + threadIdx.x; c < M; c += gridDim.x * blockDim.x) {
+        const uint64_t code = m_code[c];
+        uint8_t bits = 0;
+        int32_t a = M;
+        if (!(code >> 63)) {  // depth < 21
+            const uint64_t lo = code << 3;
+            int32_t b = M;
+            a = c + 1;
+            while (a < b) {
+                const int32_t mid = a + (b - a) / 2;
+                if (m_code[mid] < lo) a = mid + 1; else b = mid;
+            }
+            for (int32_t k = a; k < M && (m_code[k] >> 3) == code; ++k) bits |= (uint8_t)(1u << (m_code[k] & 7u));
+        }
+        first[c] = a;
+        mask[c] = bits;
+    }
+}
+
+__global__ void __launch_bounds__(128) merged_walk_kernel(
+    int64_t n, const double* __restrict__ px, const double* __restrict__ py, const double* __restrict__ pz,
+    const uint64_t* __restrict__ key, int32_t M, const uint64_t* __restrict__ m_code,
+    const double4_32a* __restrict__ m_val, const int32_t* __restrict__ first, const uint8_t* __restrict__ mask,
+    Side2 side2, double theta2, double G, double soft2, double* __restrict__ ax, double* __restrict__ ay,
+    double* __restrict__ az, unsigned* __restrict__ err)
+{
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+        const double x = px[i], y = py[i], z = pz[i];
+        const uint64_t ki = key[i];
+        double sx = 0.0, sy = 0.0, sz = 0.0;
+        int32_t stack[kLetStack];
+        int top = 0;
+        if (M > 0 && m_code[0] == 1ull) stack[top++] = 0;
+        while (top) {
+            const int32_t c = stack[--top];
+            const double4_32a v = m_val[c];
+            if (v.w == 0.0) continue;
+            const uint64_t code = m_code[c];
+            const int dep = code_depth(code);
+            if (dep == bh::kMaxDepth && ((code ^ (1ull << 63)) == ki)) continue;  // the body's own leaf
+            const double dx = __dsub_rn(v.x, x), dy = __dsub_rn(v.y, y), dz = __dsub_rn(v.z, z);
+            const double r2 = __dadd_rn(
+                __dadd_rn(__dadd_rn(__dmul_rn(dx, dx), __dmul_rn(dy, dy)), __dmul_rn(dz, dz)), soft2);
+            if (dep == bh::kMaxDepth || side2.v[dep] < __dmul_rn(theta2, r2)) {
+                const double inv = __ddiv_rn(1.0, __dsqrt_rn(r2));
+                const double inv3 = __dmul_rn(__dmul_rn(inv, inv), inv);
+                const double s = __dmul_rn(__dmul_rn(G, v.w), inv3);
+                sx = __dadd_rn(sx, __dmul_rn(s, dx));
+                sy = __dadd_rn(sy, __dmul_rn(s, dy));
+                sz = __dadd_rn(sz, __dmul_rn(s, dz));
+            } else {
+                const uint8_t bits = mask[c];
+                int32_t k = first[c];
+                for (int oc = 0; oc < 8; ++oc) {
+                    if (!((bits >> oc) & 1u)) continue;
+                    if (top == kLetStack) {  // cannot happen below depth 22; flagged, never written past
+                        atomicOr(err, bh::kErrOverflow);
+                        top = 0;
+                        break;
+                    }
+                    stack[top++] = k++;
+                }
+            }
+        }
+        ax[i] = sx;
+        ay[i] = sy;
+        az[i] = sz;
+    }
+}
+
+// out += sum over records in record order (rm = mass * G).
+constexpr int kDirectTile = 128;
+
+__global__ void __launch_bounds__(kDirectTile) remote_direct_kernel(
+    int64_t n, const double* __restrict__ px, const double* __restrict__ py, const double* __restrict__ pz, int64_t M,
+    const double* __restrict__ rcom, const double* __restrict__ rmass, double G, double soft2,
+    double* __restrict__ ax, double* __restrict__ ay, double* __restrict__ az)
+{
+    __shared__ double4_32a tile[kDirectTile];
+    const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    const bool live = i < n;
+    const double x = live ? px[i] : 0.0, y = live ? py[i] : 0.0, z = live ? pz[i] : 0.0;
+    double sx = 0.0, sy = 0.0, sz = 0.0;
+    for (int64_t j0 = 0; j0 < M; j0 += kDirectTile) {
+        const int64_t j = j0 + threadIdx.x;
+        if (j < M)
+            tile[threadIdx.x] = double4_32a{rcom[3 * j], rcom[3 * j + 1], rcom[3 * j + 2], __dmul_rn(rmass[j], G)};
+        __syncthreads();
+        const int cnt = (int)(M - j0 < kDirectTile ? M - j0 : kDirectTile);
+        for (int k = 0; k < cnt; ++k) {
+            const double4_32a q = tile[k];
+            const double dx = __dsub_rn(q.x, x), dy = __dsub_rn(q.y, y), dz = __dsub_rn(q.z, z);
+            const double r2 = __dadd_rn(
+                __dadd_rn(__dadd_rn(__dmul_rn(dx, dx), __dmul_rn(dy, dy)), __dmul_rn(dz, dz)), soft2);
+            if (r2 <= 1e-12) continue;
+            const double inv = __ddiv_rn(1.0, __dsqrt_rn(r2));
+            const double inv3 = __dmul_rn(__dmul_rn(inv, inv), inv);
+            const double s = __dmul_rn(q.w, inv3);
+            sx = __dadd_rn(sx, __dmul_rn(s, dx));
+            sy = __dadd_rn(sy, __dmul_rn(s, dy));
+            sz = __dadd_rn(sz, __dmul_rn(s, dz));
+        }
+        __syncthreads();
+    }
+    if (live) {
+        ax[i] = __dadd_rn(ax[i], sx);
+        ay[i] = __dadd_rn(ay[i], sy);
+        az[i] = __dadd_rn(az[i], sz);
+    }
+}
+
+int download_acc(bh_context* ctx, double* acc_out)
+{
+    const int64_t n = ctx->n;
+    std::vector<double> h(3 * (size_t)n);
+    BH_CUDA_TRY(cudaMemcpyAsync(h.data(), ctx->ax, sizeof(double) * n, cudaMemcpyDeviceToHost, ctx->stream));
+    BH_CUDA_TRY(cudaMemcpyAsync(h.data() + n, ctx->ay, sizeof(double) * n, cudaMemcpyDeviceToHost, ctx->stream));
+    BH_CUDA_TRY(cudaMemcpyAsync(h.data() + 2 * n, ctx->az, sizeof(double) * n, cudaMemcpyDeviceToHost, ctx->stream));
+    BH_CUDA_TRY(cudaStreamSynchronize(ctx->stream));
+    for (int64_t i = 0; i < n; ++i) {
+        acc_out[3 * i] = h[(size_t)i];
+        acc_out[3 * i + 1] = h[(size_t)(n + i)];
+        acc_out[3 * i + 2] = h[(size_t)(2 * n + i)];
+    }
+    return BH_OK;
+}
+
+int let_check(bh_context* ctx, const uint64_t* prefix, const uint8_t* depth, const double* mass, const double* com,
+              int64_t m, double theta, double soft2, bool need_keys, const char* fn)
+{
+    if (!ctx || m < 0 || (m > 0 && (!mass || !com || (need_keys && (!prefix || !depth)))) || !(theta >= 0.0) ||
+        !(soft2 >= 0.0))
+        return bh_fail(BH_ERR_INVALID_ARGUMENT, std::string(fn) + ": bad arguments");
+    BH_CUDA_TRY(cudaSetDevice(ctx->device));
+    if (ctx->n > 0 && !ctx->tree_valid) return bh_fail(BH_ERR_STATE, std::string(fn) + ": no tree built");
+    if (ctx->tree_far) {  // the reference's local tree: real masses
+        int rc = bh::launch_build(ctx, ctx->m);
+        if (rc) return rc;
+        ctx->tree_far = ctx->tree_moments = false;
+    }
+    return BH_OK;
+}
+
+}  // namespace
+
+extern "C" int bh_let_accelerations(bh_context* ctx, const uint64_t* prefix, const uint8_t* depth,
+                                    const double* mass, const double* com, int64_t m, double theta, double G,
+                                    double soft2, double* acc_out)
+{
+    int rc = let_check(ctx, prefix, depth, mass, com, m, theta, soft2, true, "bh_let_accelerations");
+    if (rc) return rc;
+    const int64_t n = ctx->n;
+    if (n == 0) return BH_OK;
+    cudaStream_t st = ctx->stream;
+    int dev_sms = 0;
+    BH_CUDA_TRY(cudaDeviceGetAttribute(&dev_sms, cudaDevAttrMultiProcessorCount, ctx->device));
+    auto grid_for = [&](int64_t k) {
+        return (int)std::max<int64_t>(1, std::min<int64_t>((k + 255) / 256, 16 * (int64_t)dev_sms));
+    };
+
+    // The pseudo-leaf map (in imp_buf2) and the local cell count.
+    PseudoCells pc;
+    if ((rc = pseudo_tree_device(ctx, prefix, depth, mass, com, m, &pc))) return rc;
+    int32_t S = 0;
+    BH_CUDA_TRY(cudaMemcpyAsync(ctx->h_small, ctx->counts + 2, sizeof(int32_t), cudaMemcpyDeviceToHost, st));
+    BH_CUDA_TRY(cudaStreamSynchronize(st));
+    std::memcpy(&S, ctx->h_small, sizeof(int32_t));
+    const int64_t lmax = (int64_t)S * (bh::kMaxDepth + 1);
+    if (lmax + pc.n > (int64_t)INT32_MAX) return bh_fail(BH_ERR_INVALID_ARGUMENT, "bh_let_accelerations: map too large");
+
+    auto layout1 = [&](Arena& a, int32_t** cnt, int32_t** off, int32_t** tmp, int32_t** small) {
+        *cnt = a.take<int32_t>(S); *off = a.take<int32_t>(S); *tmp = a.take<int32_t>(bh::scan_tmp_ints(S));
+        *small = a.take<int32_t>(64);
+    };
+    int32_t *cnt, *off, *tmp1, *small;
+    {
+        Arena probe{nullptr, 0};
+        layout1(probe, &cnt, &off, &tmp1, &small);
+        if ((rc = grow(&ctx->letf_buf, &ctx->letf_bytes, probe.off))) return rc;
+    }
+    Arena a1{static_cast<char*>(ctx->letf_buf), 0};
+    layout1(a1, &cnt, &off, &tmp1, &small);
+    chain_count_kernel<<<grid_for(S), 256, 0, st>>>(ctx->counts, ctx->rec, cnt);
+    BH_LAUNCH_CHECK(ctx);
+    if ((rc = bh::device_exclusive_scan_tmp(ctx, cnt, off, S, nullptr, small, tmp1))) return rc;
+    BH_CUDA_TRY(cudaMemcpyAsync(ctx->h_small, small, sizeof(int32_t), cudaMemcpyDeviceToHost, st));
+    BH_CUDA_TRY(cudaStreamSynchronize(st));
+    int32_t L = 0;
+    std::memcpy(&L, ctx->h_small, sizeof(int32_t));
+    const int64_t t = (int64_t)L + pc.n;
+
+    // Local cells + pseudo cells -> one stable sort -> merged cells.
+    const int64_t tiles = (t + bh::kSortTile - 1) / bh::kSortTile;
+    uint64_t *code, *code_s, *key_alt, *m_code;
+    uint32_t *val_alt, *perm, *hist, *lookback, *tile_ctr;
+    int32_t *cell_slot, *head, *tmp2, *first;
+    unsigned* err;
+    double4_32a* m_val;
+    uint8_t* mask;
+    auto layout2 = [&](Arena& b) {
+        code = b.take<uint64_t>(t); code_s = b.take<uint64_t>(t); key_alt = b.take<uint64_t>(t);
+        val_alt = b.take<uint32_t>(t); perm = b.take<uint32_t>(t); cell_slot = b.take<int32_t>(L);
+        head = b.take<int32_t>(t); tmp2 = b.take<int32_t>(bh::scan_tmp_ints(t));
+        hist = b.take<uint32_t>(bh::kSortPasses * bh::kRadix);
+        lookback = b.take<uint32_t>(bh::kSortPasses * tiles * bh::kRadix);
+        tile_ctr = b.take<uint32_t>(bh::kSortPasses); err = b.take<unsigned>(1);
+        m_code = b.take<uint64_t>(t); m_val = b.take<double4_32a>(t); first = b.take<int32_t>(t);
+        mask = b.take<uint8_t>(t);
+    };
+    {
+        Arena probe{nullptr, 0};
+        layout2(probe);
+        size_t need = a1.off + probe.off;
+        if (ctx->letf_bytes < need) {
+            // grow keeps nothing: redo the local cell count after growing
+            if ((rc = grow(&ctx->letf_buf, &ctx->letf_bytes, need))) return rc;
+            Arena again{static_cast<char*>(ctx->letf_buf), 0};
+            layout1(again, &cnt, &off, &tmp1, &small);
+            chain_count_kernel<<<grid_for(S), 256, 0, st>>>(ctx->counts, ctx->rec, cnt);
+            BH_LAUNCH_CHECK(ctx);
+            if ((rc = bh::device_exclusive_scan_tmp(ctx, cnt, off, S, nullptr, small, tmp1))) return rc;
+        }
+    }
+    Arena a2{static_cast<char*>(ctx->letf_buf), a1.off};
+    layout2(a2);
+    chain_cells_kernel<<<grid_for(S), 256, 0, st>>>(ctx->counts, ctx->rec, ctx->slot_ref, ctx->node_a, ctx->leaf_key,
+                                                    off, code, cell_slot);
+    BH_LAUNCH_CHECK(ctx);
+    if (pc.n)
+        BH_CUDA_TRY(cudaMemcpyAsync(code + L, pc.code, sizeof(uint64_t) * pc.n, cudaMemcpyDeviceToDevice, st));
+    BH_CUDA_TRY(cudaMemsetAsync(err, 0, sizeof(unsigned), st));
+    if (t == 1) {
+        BH_CUDA_TRY(cudaMemcpyAsync(code_s, code, sizeof(uint64_t), cudaMemcpyDeviceToDevice, st));
+        BH_CUDA_TRY(cudaMemsetAsync(perm, 0, sizeof(uint32_t), st));
+    } else {
+        BH_CUDA_TRY(cudaMemsetAsync(hist, 0, sizeof(uint32_t) * bh::kSortPasses * bh::kRadix, st));
+        BH_CUDA_TRY(cudaMemsetAsync(lookback, 0, sizeof(uint32_t) * bh::kSortPasses * tiles * bh::kRadix, st));
+        BH_CUDA_TRY(cudaMemsetAsync(tile_ctr, 0, sizeof(uint32_t) * bh::kSortPasses, st));
+        if ((rc = bh::launch_digit_hist(t, code, hist, st))) return rc;
+        if ((rc = bh::sort_passes_raw(t, code, code_s, perm, key_alt, val_alt, hist, lookback, tile_ctr, err, st)))
+            return rc;
+    }
+    merge_head_kernel<<<grid_for(t), 256, 0, st>>>(t, code_s, head);
+    BH_LAUNCH_CHECK(ctx);
+    if ((rc = bh::device_exclusive_scan_tmp(ctx, head, head, t, nullptr, small + 1, tmp2))) return rc;
+    merge_cells_kernel<<<grid_for(t), 256, 0, st>>>(t, L, code_s, perm, head, cell_slot, ctx->rec, pc.mass, pc.com,
+                                                    m_code, m_val);
+    BH_LAUNCH_CHECK(ctx);
+    BH_CUDA_TRY(cudaMemcpyAsync(ctx->h_small, small, 2 * sizeof(int32_t), cudaMemcpyDeviceToHost, st));
+    BH_CUDA_TRY(cudaStreamSynchronize(st));
+    int32_t hs[2];
+    std::memcpy(hs, ctx->h_small, sizeof(hs));
+    const int32_t M = hs[1];
+    merge_children_kernel<<<grid_for(M), 256, 0, st>>>(M, m_code, first, mask);
+    BH_LAUNCH_CHECK(ctx);
+
+    // The walk: the reference's side^2 table over the global box.
+    double bb[6];
+    BH_CUDA_TRY(cudaMemcpyAsync(bb, ctx->bbox, sizeof(bb), cudaMemcpyDeviceToHost, st));
+    BH_CUDA_TRY(cudaStreamSynchronize(st));
+    double Lside = bb[3] - bb[0];
+    if (Lside < bb[4] - bb[1]) Lside = bb[4] - bb[1];
+    if (Lside < bb[5] - bb[2]) Lside = bb[5] - bb[2];
+    Side2 side2;
+    for (int d = 0; d <= bh::kMaxDepth; ++d) {
+        const double side = Lside / (double)(1ull << d);
+        side2.v[d] = side * side;
+    }
+    const int wgrid = (int)std::max<int64_t>(1, std::min<int64_t>((n + 127) / 128, 64 * (int64_t)dev_sms));
+    merged_walk_kernel<<<wgrid, 128, 0, st>>>(n, ctx->px, ctx->py, ctx->pz, ctx->key, M, m_code, m_val, first, mask,
+                                              side2, theta * theta, G, soft2, ctx->ax, ctx->ay, ctx->az, err);
+    BH_LAUNCH_CHECK(ctx);
+    unsigned h_err = 0;
+    BH_CUDA_TRY(cudaMemcpyAsync(ctx->h_small, err, sizeof(unsigned), cudaMemcpyDeviceToHost, st));
+    BH_CUDA_TRY(cudaStreamSynchronize(st));
+    std::memcpy(&h_err, ctx->h_small, sizeof(unsigned));
+    if (h_err & bh::kErrTimeout) return bh_fail(BH_ERR_TIMEOUT, "bh_let_accelerations: a bounded device wait gave up");
+    if (h_err & bh::kErrOverflow) return bh_fail(BH_ERR_OVERFLOW, "bh_let_accelerations: walk stack overflow");
+    return acc_out ? download_acc(ctx, acc_out) : BH_OK;
+}
+
+extern "C" int bh_let_direct_accelerations(bh_context* ctx, const uint64_t* prefix, const uint8_t* depth,
+                                           const double* mass, const double* com, int64_t m, double theta, double G,
+                                           double soft2, double* acc_out)
+{
+    int rc = let_check(ctx, prefix, depth, mass, com, m, theta, soft2, false, "bh_let_direct_accelerations");
+    if (rc) return rc;
+    const int64_t n = ctx->n;
+    if (n == 0) return BH_OK;
+    cudaStream_t st = ctx->stream;
+    if ((rc = bh::launch_traverse(ctx, theta, G, soft2, BH_MODE_PLAIN_FP64, 0.0))) return rc;
+    if (m > 0) {
+        auto layout = [&](Arena& a, double** rc3, double** rm) {
+            *rc3 = a.take<double>(3 * m);
+            *rm = a.take<double>(m);
+        };
+        double *rcom, *rmass;
+        {
+            Arena probe{nullptr, 0};
+            layout(probe, &rcom, &rmass);
+            if ((rc = grow(&ctx->letf_buf, &ctx->letf_bytes, probe.off))) return rc;
+        }
+        Arena a{static_cast<char*>(ctx->letf_buf), 0};
+        layout(a, &rcom, &rmass);
+        BH_CUDA_TRY(cudaMemcpyAsync(rcom, com, 3 * sizeof(double) * m, cudaMemcpyHostToDevice, st));
+        BH_CUDA_TRY(cudaMemcpyAsync(rmass, mass, sizeof(double) * m, cudaMemcpyHostToDevice, st));
+        const int64_t blocks = (n + kDirectTile - 1) / kDirectTile;
+        remote_direct_kernel<<<(unsigned)blocks, kDirectTile, 0, st>>>(n, ctx->px, ctx->py, ctx->pz, m, rcom, rmass, G,
+                                                                      soft2, ctx->ax, ctx->ay, ctx->az);
+        BH_LAUNCH_CHECK(ctx);
+    }
+    if (acc_out) return download_acc(ctx, acc_out);
     BH_CUDA_TRY(cudaStreamSynchronize(st));
     return BH_OK;
 }

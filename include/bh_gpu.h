@@ -186,6 +186,28 @@ int bh_let_export(bh_context *ctx, const double *boxes, int64_t nboxes, const do
 int bh_pseudo_leaf_tree(bh_context *ctx, const uint64_t *prefix, const uint8_t *depth, const double *mass,
                         const double *com, int64_t m, int64_t capacity, uint64_t *out_prefix, uint8_t *out_depth,
                         double *out_mass, double *out_com, int64_t *count_out);
+/* computeAccelerationsWithLET (src/traversal.cpp:107-127,
+ * include/traversal.h): the m received records become a pseudo-leaf map
+ * (as bh_pseudo_leaf_tree), mergeRecordsIntoTree (src/linear_octree.cpp:
+ * 178-204) folds it into the local tree in place (built by
+ * bh_build_tree_options(ctx, 0) over keys in the global box of bh_set_bbox),
+ * and computeAccelerations walks the merged map for the local bodies.
+ * The walk repeats the reference's visiting order and IEEE operations, so
+ * the result is the reference's on the same merged map; the pseudo-leaf
+ * sums (see bh_pseudo_leaf_tree) make it agree with the reference to
+ * rounding.  The accelerations replace the context's (acc_out, current
+ * body order, may be NULL); the local tree is left as it was. */
+int bh_let_accelerations(bh_context *ctx, const uint64_t *prefix, const uint8_t *depth, const double *mass,
+                         const double *com, int64_t m, double theta, double G, double soft2, double *acc_out);
+/* computeAccelerationsWithRemoteDirectSum (src/traversal.cpp:149-221): the
+ * reference's traversal of the local tree (bit-exact, BH_MODE_PLAIN_FP64)
+ * plus, per body, a direct sum over the m records (pairs with r^2 <= 1e-12
+ * skipped) added to it.  The records are summed in order; the reference's
+ * `omp simd` reduction leaves its order to the compiler, so the sum agrees
+ * with it to rounding.  prefix and depth are not read (may be NULL). */
+int bh_let_direct_accelerations(bh_context *ctx, const uint64_t *prefix, const uint8_t *depth, const double *mass,
+                                const double *com, int64_t m, double theta, double G, double soft2,
+                                double *acc_out);
 /* The bucket boxes of a remote rank's domain as exchangeEssentialTrees
  * builds them (src/exchange.cpp:45-71): bucket prefix p (a key prefix of
  * depth bucket_bits / 3, as update_rank_domains, src/load_balancing.cpp:12-65,

@@ -634,6 +634,90 @@ fail:
 }
 
 /* ------------------------------------------------------------------ */
+/* computeAccelerationsWithLET, src/traversal.cpp:107-127: the records'  */
+/* pseudo-leaf map (orc_pseudo_tree) merged into a copy of the local map */
+/* as mergeRecordsIntoTree (src/linear_octree.cpp:178-204) merges -- a   */
+/* cell in both gets com = (m0 c0 + m1 c1) / (m0 + m1), nothing when   */
+/* that mass is 0; a new cell enters with m0 = c0 = 0 -- then the       */
+/* ordinary traversal over the merged map.  `direct` selects            */
+/* computeAccelerationsWithRemoteDirectSum (:149-221): the traversal of */
+/* the local map plus, per body, the records summed in order (rm =     */
+/* mass * G; pairs with r^2 <= 1e-12 skipped).                          */
+/* ------------------------------------------------------------------ */
+static orc_tree *orc_tree_clone(const orc_tree *t)
+{
+    orc_tree *c = (orc_tree *)malloc(sizeof(orc_tree));
+    if (!c) return NULL;
+    c->slot = (orc_node *)malloc(sizeof(orc_node) * t->cap);
+    if (!c->slot) {
+        free(c);
+        return NULL;
+    }
+    memcpy(c->slot, t->slot, sizeof(orc_node) * t->cap);
+    c->cap = t->cap;
+    c->count = t->count;
+    return c;
+}
+
+int orc_let_accelerations(void *h, const uint64_t *prefix, const uint8_t *depth, const double *mass,
+                          const double *com, int64_t m, int64_t n, const uint64_t *key, const double *pos,
+                          double theta, double G, double soft2, const double bb[6], int direct, double *acc)
+{
+    const orc_tree *local = (const orc_tree *)h;
+    if (direct) {
+        int rc = orc_accelerations(h, n, key, pos, theta, G, soft2, bb, acc, NULL);
+        if (rc) return rc;
+#pragma omp parallel for schedule(static)
+        for (int64_t i = 0; i < n; ++i) {
+            double ax = 0.0, ay = 0.0, az = 0.0;
+            const double px = pos[3 * i], py = pos[3 * i + 1], pz = pos[3 * i + 2];
+            for (int64_t j = 0; j < m; ++j) {
+                const double dx = com[3 * j] - px, dy = com[3 * j + 1] - py, dz = com[3 * j + 2] - pz;
+                const double r2 = dx * dx + dy * dy + dz * dz + soft2;
+                if (r2 <= 1e-12) continue;
+                const double inv = 1.0 / sqrt(r2);
+                const double inv3 = inv * inv * inv;
+                const double s = (mass[j] * G) * inv3;
+                ax += s * dx;
+                ay += s * dy;
+                az += s * dz;
+            }
+            acc[3 * i] += ax;
+            acc[3 * i + 1] += ay;
+            acc[3 * i + 2] += az;
+        }
+        return ORC_OK;
+    }
+    orc_tree *merged = orc_tree_clone(local);
+    orc_tree *pt = (orc_tree *)orc_pseudo_tree(prefix, depth, mass, com, m);
+    if (!merged || !pt) {
+        if (merged) orc_tree_free(merged);
+        if (pt) orc_tree_free(pt);
+        return ORC_ERR_OOM;
+    }
+    for (uint64_t i = 0; i < pt->cap; ++i) {
+        const orc_node *r = &pt->slot[i];
+        if (r->depth < 0) continue;
+        orc_node *nd = orc_tree_get(merged, r->prefix, r->depth);
+        if (!nd) {
+            orc_tree_free(merged);
+            orc_tree_free(pt);
+            return ORC_ERR_OOM;
+        }
+        const double m0 = nd->mass, tot = m0 + r->mass;
+        if (tot == 0) continue;
+        nd->cx = (m0 * nd->cx + r->mass * r->cx) / tot;
+        nd->cy = (m0 * nd->cy + r->mass * r->cy) / tot;
+        nd->cz = (m0 * nd->cz + r->mass * r->cz) / tot;
+        nd->mass = tot;
+    }
+    int rc = orc_accelerations(merged, n, key, pos, theta, G, soft2, bb, acc, NULL);
+    orc_tree_free(merged);
+    orc_tree_free(pt);
+    return rc;
+}
+
+/* ------------------------------------------------------------------ */
 /* The step loop of src/main.cpp:191-282 for `--fc tree` on one rank.   */
 /* The half kick at :193-200 runs only when t > 0; t is accumulated in  */
 /* double (t += dt), as the reference's loop header does.  The MPI      */

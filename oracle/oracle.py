@@ -86,6 +86,8 @@ class Oracle:
             self._threads = f("num_threads", C.c_int, [])
             self._let = f("let_export", _I64, [_P, _P, _I64, _P, _D, C.c_int, _P, _P, _P, _P, _I64])
             self._pseudo = f("pseudo_tree", _P, [_P, _P, _P, _P, _I64])
+            self._letacc = f("let_accelerations", C.c_int, [_P, _P, _P, _P, _P, _I64, _I64, _P, _P, _D, _D, _D, _P,
+                                                             C.c_int, _P])
         else:
             self._bbox = f("compute_local_bbox", None, [_P, _I64, _P])
             self._keys = f("generate_morton_codes", None, [_P, _I64, _P, _P])
@@ -99,6 +101,8 @@ class Oracle:
             self._kepler = f("kepler_to_cartesian", None, [_P, _I64, _P])
             self._let = f("let_export", _I64, [_P, _P, _I64, _P, _D, C.c_int, _P, _P, _P, _P, _I64])
             self._pseudo = f("pseudo_tree", _P, [_P, _P, _P, _P, _I64])
+            self._letacc = f("let_accelerations", None, [_P, _P, _P, _P, _P, _I64, _I64, _P, _P, _D, _D, _D, _P,
+                                                          C.c_int, _P])
 
     # -- stages ---------------------------------------------------------
     def bbox(self, pos) -> np.ndarray:
@@ -170,6 +174,23 @@ class Oracle:
         if not h:
             raise MemoryError("pseudo_tree")
         return OracleTree(self, h)
+
+    def let_accelerations(self, tree, records, keys, pos, theta, G, bbox, soft2=0.0, direct=False):
+        """computeAccelerationsWithLET (direct=False) or
+        computeAccelerationsWithRemoteDirectSum (direct=True): local `tree`
+        (unchanged), received `records` = (prefix, depth, mass, com), bodies
+        with `keys` and `pos`."""
+        p = np.ascontiguousarray(records[0], np.uint64); d = np.ascontiguousarray(records[1], np.uint8)
+        m = np.ascontiguousarray(records[2], np.float64)
+        c = np.ascontiguousarray(records[3], np.float64).reshape(-1, 3)
+        k = np.ascontiguousarray(keys, np.uint64); x = np.ascontiguousarray(pos, np.float64).reshape(-1, 3)
+        bb = np.ascontiguousarray(bbox, np.float64)
+        out = np.empty((len(k), 3))
+        rc = self._letacc(tree.h, _ptr(p), _ptr(d), _ptr(m), _ptr(c), len(m), len(k), _ptr(k), _ptr(x), theta, G,
+                          soft2, _ptr(bb), int(direct), _ptr(out))
+        if rc:
+            raise RuntimeError(f"oracle let_accelerations failed ({rc})")
+        return out
 
     def simulate(self, pos, vel, mass, ids, dt, theta, G, nsteps, t=0.0, acc=None):
         """Runs the step loop; returns (pos, vel, mass, ids, acc, t, phase_s)."""

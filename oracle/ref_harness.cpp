@@ -274,4 +274,29 @@ void* ref_pseudo_tree(const uint64_t* prefix, const uint8_t* depth, const double
     return h;
 }
 
+// computeAccelerationsWithLET (src/traversal.cpp:107-127) on a copy of the
+// tree `t` (the function merges the records into the map it is given) and
+// computeAccelerationsWithRemoteDirectSum (:149-221), for n bodies with
+// keys and positions; `direct` picks the second.
+void ref_let_accelerations(void* handle, const uint64_t* prefix, const uint8_t* depth, const double* mass,
+                           const double* com, int64_t m, int64_t n, const uint64_t* keys, const double* pos,
+                           double theta, double G, double soft2, const double bb[6], int direct, double* acc)
+{
+    std::vector<NodeRecord> recs((size_t)m);
+    for (int64_t k = 0; k < m; ++k)
+        recs[(size_t)k] = {prefix[k], depth[k], mass[k], com[3 * k], com[3 * k + 1], com[3 * k + 2]};
+    OctreeMap map = static_cast<TreeHandle*>(handle)->map;
+    std::vector<uint64_t> key(keys, keys + n);
+    std::vector<Acceleration> out;
+    if (direct)
+        computeAccelerationsWithRemoteDirectSum(map, recs, key, to_vec3(pos, n), theta, G, soft2, to_bbox(bb), out, 0);
+    else
+        computeAccelerationsWithLET(map, recs, key, to_vec3(pos, n), theta, G, soft2, to_bbox(bb), out, 0);
+    for (int64_t i = 0; i < n; ++i) {
+        acc[3 * i] = out[(size_t)i].x;
+        acc[3 * i + 1] = out[(size_t)i].y;
+        acc[3 * i + 2] = out[(size_t)i].z;
+    }
+}
+
 }  // extern "C"

@@ -3,7 +3,7 @@ sources, compiled unmodified by ``make -C oracle ref`` (oracle/_ref).
 
 Run in a checkout where the reference is present:
 
-    python tests/golden/make_golden.py [edge synthetic let pseudo scenario]
+    python tests/golden/make_golden.py [edge synthetic let pseudo config1 scenario]
 
 (no arguments: every fixture).
 
@@ -35,7 +35,15 @@ Outputs (all produced by the compiled reference, strict IEEE build):
                              (the other ranks' exports to its bucket boxes),
                              plus duplicate, massless, non-finite, negative,
                              unmasked and too-deep records: inputs and the
-                             map, sorted by (depth, prefix).
+                             map, sorted by (depth, prefix); rank 0's forces
+                             from computeAccelerationsWithLET (with and without
+                             the edge records) and
+                             computeAccelerationsWithRemoteDirectSum.
+* ``config1_240_steps.json`` -- the CPU-runnable configuration's full run:
+                             240 steps of 1 h at theta 1.05 from the inputs of
+                             synthetic_19054.npz; SHA-256 of the final state
+                             (pos, vel, mass, ids, acc in the final sorted
+                             order) and the final time.
 * ``scenario1.json``      -- digests of the same stages on the reference's own
                              data/state_vectors_csvs/scenario1_19054.csv (the
                              file itself is not copied here).
@@ -178,7 +186,7 @@ def main() -> None:
         raise SystemExit("the reference checkout is needed to regenerate the fixtures")
     ref = Oracle("reference")
     bh = importlib.import_module("barnes-hut_gb300")
-    want = set(sys.argv[1:]) or {"edge", "synthetic", "let", "pseudo", "scenario"}
+    want = set(sys.argv[1:]) or {"edge", "synthetic", "let", "pseudo", "config1", "scenario"}
     if "edge" in want:
         edge_fixtures(ref, bh)
     if "synthetic" in want:
@@ -187,6 +195,8 @@ def main() -> None:
         let_fixtures(ref, bh)
     if "pseudo" in want:
         pseudo_fixtures(ref)
+    if "config1" in want:
+        config1_fixture(ref)
     if "scenario" in want:
         scenario_fixture(ref, bh)
     print("fixtures written to", HERE)
@@ -273,18 +283,44 @@ def pseudo_fixtures(ref):
         tree.close()
     p = np.concatenate([x[0] for x in parts]); d = np.concatenate([x[1] for x in parts])
     m = np.concatenate([x[2] for x in parts]); c = np.concatenate([x[3] for x in parts])
+    n_valid = len(p)
+    # rank 0's forces with these records: computeAccelerationsWithLET and
+    # computeAccelerationsWithRemoteDirectSum over its local tree (bodies in
+    # sorted key order)
+    local = owner[bidx] == 0
+    sel = np.nonzero(local)[0]
+    sk, sp, sm, _, _, _ = ref.sort(keys[sel], pos[sel], mass[sel], vel[sel], ids[sel])
+    tree = ref.tree(sk, sp, sm, merge=False)
+    let_acc = ref.let_accelerations(tree, (p, d, m, c), sk, sp, THETA, G, bb)
+    letds_acc = ref.let_accelerations(tree, (p, d, m, c), sk, sp, THETA, G, bb, direct=True)
+    tree.close()
     # edge records: a duplicate key (summed in input order), massless,
     # non-finite and negative masses (skipped), an unmasked prefix, depth 30
     p = np.concatenate([p, p[:3], p[3:6], [p[6] | np.uint64(0x5555)], [p[7]]])
     d = np.concatenate([d, d[:3], d[3:6], [d[6]], [30]]).astype(np.uint8)
     m = np.concatenate([m, m[:3] * 0.25, [0.0, np.nan, -m[5]], [m[6]], [m[7]]])
     c = np.concatenate([c, c[:3] * 0.5, c[3:6], c[6:7], c[7:8]])
-    out = dict(prefix=p, depth=d, mass=m, com=c)
+    out = dict(prefix=p, depth=d, mass=m, com=c, n_valid=np.array([n_valid]), local=np.packbits(local), bbox=bb)
+    # the forces again with the edge records (the pseudo-leaf map skips them)
+    sk, sp, sm, _, _, _ = ref.sort(keys[sel], pos[sel], mass[sel], vel[sel], ids[sel])
+    tree = ref.tree(sk, sp, sm, merge=False)
+    out["let_acc_all"] = ref.let_accelerations(tree, (p, d, m, c), sk, sp, THETA, G, bb)
+    tree.close()
+    out["let_acc"] = let_acc
+    out["letds_acc"] = letds_acc
     t = ref.pseudo_tree(p, d, m, c)
     for k, v in zip(("prefix", "depth", "mass", "com"), t.records()):
         out[f"tree_{k}"] = v
     t.close()
     np.savez_compressed(HERE / "pseudo_tree.npz", **out)
+
+
+def config1_fixture(ref):
+    g = np.load(HERE / "synthetic_19054.npz")
+    p, v, m, i, a, t, _ = ref.simulate(g["pos"], g["vel"], g["mass"], g["ids"], DT, THETA, G, 240)
+    info = dict(steps=240, dt=DT, theta=THETA, G=G, t=t, digest=digest(p, v, m, i, a),
+                pos_head=p[:4].tolist())
+    (HERE / "config1_240_steps.json").write_text(json.dumps(info, indent=1) + "\n")
 
 
 def scenario_fixture(ref, bh):

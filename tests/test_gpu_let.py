@@ -221,3 +221,60 @@ def test_pseudo_leaf_tree_matches_oracle_bits(bh, port):
     for a, b, what in zip(got, want, ("prefix", "depth", "mass", "com")):
         assert_bits_equal(a, b, what)
     assert len(empty[0]) == 0 and len(bad[0]) == 0
+
+
+def test_let_forces_match_reference_golden(bh, golden):
+    """computeAccelerationsWithLET and ...WithRemoteDirectSum on the device
+    against the compiled reference (rank 0 of a 4-way split of the 1,000-body
+    system): within 1e-13 relative."""
+    f = golden("pseudo_tree.npz")
+    g = golden("synthetic_1000.npz")
+    nv = int(f["n_valid"][0])
+    sel = np.nonzero(np.unpackbits(f["local"])[:len(g["mass"])].astype(bool))[0]
+    with _local_ctx(bh, g["pos"][sel], g["vel"][sel], g["mass"][sel], g["ids"][sel], f["bbox"]) as ctx:
+        rec = (f["prefix"], f["depth"], f["mass"], f["com"])
+        valid = tuple(a[:nv] for a in rec)
+        got = {"let_acc": ctx.let_accelerations(*valid, theta=1.05),
+               "let_acc_all": ctx.let_accelerations(*rec, theta=1.05),
+               "letds_acc": ctx.let_accelerations(*valid, theta=1.05, direct=True)}
+    for k, a in got.items():
+        want = f[k]
+        rel = np.linalg.norm(a - want, axis=1) / np.linalg.norm(want, axis=1)
+        assert rel.max() <= 1e-13, k
+
+
+def test_let_forces_match_oracle_bits(bh, port):
+    """300,000 bodies over 4 ranks (9-bit buckets): rank 0's forces with the
+    records the other ranks export to it, on the device and in the oracle
+    (which builds the pseudo-leaf map in the same octant order and sums the
+    records in the same order): bit for bit, both LET forms; the local tree
+    is unchanged afterwards."""
+    n = 300_000
+    pos, vel, mass, ids = bh.generate_system(34, n, 0.1, 0.05)
+    bb = port.bbox(pos)
+    keys = port.keys(pos, bb)
+    owner, doms = _bucket_domains(keys, 9, 4)
+    boxes0 = bh.let_bucket_boxes(doms[0], 9, bb)
+    parts = []
+    for r in range(1, 4):
+        sel = np.nonzero(owner == r)[0]
+        with _local_ctx(bh, pos[sel], vel[sel], mass[sel], ids[sel], bb) as ctx:
+            parts.append(ctx.let_export(boxes0, bb, 1.05 ** 2, 21))
+    rec = tuple(np.concatenate([x[k] for x in parts]) for k in range(4))
+    sel = np.nonzero(owner == 0)[0]
+    sk, sp, sm, _, _, _ = port.sort(keys[sel], pos[sel], mass[sel], vel[sel], ids[sel])
+    tree = port.tree(sk, sp, sm, merge=False)
+    want = [port.let_accelerations(tree, rec, sk, sp, 1.05, 1.48812e-34, bb, direct=d) for d in (False, True)]
+    tree.close()
+    with _local_ctx(bh, pos[sel], vel[sel], mass[sel], ids[sel], bb) as ctx:
+        before = ctx.export_tree()
+        got = [ctx.let_accelerations(*rec, theta=1.05, direct=d) for d in (False, True)]
+        after = ctx.export_tree()
+        plain = ctx.compute_accelerations(1.05)
+    assert len(rec[0]) > 1000
+    assert_bits_equal(got[0], want[0], "LET forces")
+    assert_bits_equal(got[1], want[1], "LET remote direct sum forces")
+    for a, b in zip(before, after):
+        assert_bits_equal(a, b, "local tree")
+    # the imported records move the forces by about the remote share
+    assert np.median(np.linalg.norm(got[0] - plain, axis=1) / np.linalg.norm(plain, axis=1)) > 1e-9

@@ -9,7 +9,7 @@ import hashlib
 import numpy as np
 import pytest
 
-from conftest import DT, G, THETA, assert_bits_equal
+from conftest import DT, G, GOLDEN, THETA, assert_bits_equal
 
 pytestmark = pytest.mark.gpu
 
@@ -112,6 +112,24 @@ def test_synthetic_19054(ctx, golden):
     p, v, m, i, a = ctx.get_bodies()
     assert digest(p, v, m, i, a) == str(g["sim3_digest"][0])
     assert t == g["sim3_t"][0]
+
+
+def test_config1_full_run_240_steps(ctx, golden):
+    """The CPU-runnable configuration's whole run: 240 steps of 1 h at
+    theta 1.05 on the 19,054-body system, bit for bit against the compiled
+    reference's own loop (state and time after the last step); with and
+    without the step-graph replay."""
+    import json
+    g = golden("synthetic_19054.npz")
+    want = json.loads((GOLDEN / "config1_240_steps.json").read_text())
+    for graphs in (True, False):
+        ctx.set_step_graphs(graphs)
+        ctx.set_bodies(g["pos"], g["vel"], g["mass"], g["ids"])
+        t = ctx.step(DT, THETA, G, nsteps=240, t=0.0)
+        p, v, m, i, a = ctx.get_bodies()
+        assert digest(p, v, m, i, a) == want["digest"], graphs
+        assert t == want["t"]
+    ctx.set_step_graphs(True)
 
 
 def test_300k_against_oracle(bh, ctx, port):

@@ -212,3 +212,33 @@ def test_pseudo_tree_matches_reference(port, golden):
     assert np.all(np.abs(c - f["tree_com"]) <= 1e-14 * scale)
     # cells whose sums involve no reordering agree bit for bit
     assert np.mean(m == f["tree_mass"]) > 0.8
+
+
+def _rank0_tree(o, f, g):
+    local = np.unpackbits(f["local"])[:len(g["mass"])].astype(bool)
+    sel = np.nonzero(local)[0]
+    bb = f["bbox"]
+    keys = o.keys(g["pos"][sel], bb)
+    sk, sp, sm, _, _, _ = o.sort(keys, g["pos"][sel], g["mass"][sel], g["vel"][sel], g["ids"][sel])
+    return o.tree(sk, sp, sm, merge=False), sk, sp
+
+
+def test_let_forces_match_reference(port, golden):
+    """computeAccelerationsWithLET and ...WithRemoteDirectSum restated in the
+    oracle against the compiled reference (rank 0 of a 4-way split of the
+    1,000-body system): within 1e-13 relative (the pseudo-leaf map's child
+    sums are the only order difference)."""
+    f = golden("pseudo_tree.npz")
+    g = golden("synthetic_1000.npz")
+    nv = int(f["n_valid"][0])
+    rec = (f["prefix"], f["depth"], f["mass"], f["com"])
+    valid = tuple(a[:nv] for a in rec)
+    tree, sk, sp = _rank0_tree(port, f, g)
+    got = {"let_acc": port.let_accelerations(tree, valid, sk, sp, THETA, G, f["bbox"]),
+           "let_acc_all": port.let_accelerations(tree, rec, sk, sp, THETA, G, f["bbox"]),
+           "letds_acc": port.let_accelerations(tree, valid, sk, sp, THETA, G, f["bbox"], direct=True)}
+    tree.close()
+    for k, a in got.items():
+        want = f[k]
+        rel = np.linalg.norm(a - want, axis=1) / np.linalg.norm(want, axis=1)
+        assert rel.max() <= 1e-13, k
