@@ -1,9 +1,9 @@
-// simulate: the reference's single-rank `--fc tree` driver (src/main.cpp)
+// simulate: the reference's single-rank driver (src/main.cpp)
 // on libbh_gpu.so.  Same flags and printed lines, so the reference's
 // benchmark scripts can drive it:
 //
 //   simulate -f bodies.csv --dt 1h --tend 10d --theta 1.05 [-b N] [-r]
-//            [--fc tree] [--steps K] [--vs 10d|none] [-o sim_out]
+//            [--fc let|tree|let_direct] [--steps K] [--vs 10d|none] [-o sim_out]
 //            [--mode plain|fp64_list|fp32] [--generate N --seed S] [--dump FILE]
 //
 // --tend uses the reference's loop (`for (t = 0; t < t_end; t += dt)`, so
@@ -69,7 +69,7 @@ void check(int rc, const char* what)
 
 int main(int argc, char** argv)
 {
-    std::string file, fc = "tree", mode_s = "plain", dt_s = "1d", tend_s = "1y", dump, vs_s = "10d",
+    std::string file, fc = "let", mode_s = "plain", dt_s = "1d", tend_s = "1y", dump, vs_s = "10d",
                 out_dir = "sim_out";
     double theta = 1.05;
     long long bodies = -1, steps = -1, generate = 0;
@@ -99,13 +99,18 @@ int main(int argc, char** argv)
         else if (k == "--dump") dump = val();
         else if (k == "-h" || k == "--help") {
             std::cout << "simulate -f FILE [--dt 1h] [--tend 1y] [--theta 1.05] [-b N] [-r] [--steps K]\n"
+                         "         [--fc let|tree|let_direct] (one rank: the same step)\n"
                          "         [--vs 10d|none] [-o sim_out] [--mode plain|fp64_list|fp32]\n"
                          "         [--generate N --seed S] [--dump FILE]\n";
             return 0;
         } else die("unknown option " + k);
     }
-    if (reference) fc = "tree";
-    if (fc != "tree") die("only --fc tree (the single-rank path) is provided");
+    if (reference) std::cout << "Running in reference mode. Force calculation method will be 'tree'." << std::endl;
+    // main.cpp:93-109: -r forces the "tree" policy; "tree" and "let_direct"
+    // name their policies and any other value is "let" (the default).  On
+    // one rank the exchange sends nothing, so all three compute
+    // computeAccelerations over the local tree: the same step.  File names
+    // carry the --fc string as given (io.cpp:247-254).
     int mode = BH_MODE_PLAIN_FP64;
     if (mode_s == "fp64_list") mode = BH_MODE_FP64_LIST;
     else if (mode_s == "fp32") mode = BH_MODE_FP32_FAR;

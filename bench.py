@@ -564,6 +564,11 @@ def let_exchange(args, dev):
     for _ in range(reps):
         cells = ctx0.pseudo_leaf_tree(p, d, m, com)
     t_imp = (time.perf_counter() - t0) / reps
+    ctx0.let_accelerations(p, d, m, com, THETA, G)
+    t0 = time.perf_counter()
+    for _ in range(reps):
+        acc_let = ctx0.let_accelerations(p, d, m, com, THETA, G)
+    t_acc = (time.perf_counter() - t0) / reps
     ctx0.close()
 
     o, kind = Oracle("port"), "port"
@@ -582,6 +587,12 @@ def let_exchange(args, dev):
     c_imp = time.perf_counter() - t0
     same_cells = len(pt) == len(cells[0])
     pt.close()
+    tree = o.tree(sk, sp, sm, merge=False)
+    t0 = time.perf_counter()
+    cpu_acc = o.let_accelerations(tree, (p, d, m, com), sk, sp, THETA, G, bb)
+    c_acc = time.perf_counter() - t0
+    tree.close()
+    acc_equal = bool(np.array_equal(cpu_acc.view(np.uint64), acc_let.view(np.uint64)))
     return {"bodies": n, "ranks": 8, "bucket_bits": 18, "theta": THETA, "rank0_bodies": int(len(sel0)),
             "export": {"destinations": 7, "boxes": [int(len(b)) for b in boxes[1:]],
                        "records": [int(len(x[0])) for x in sent], "ms_per_export": 1e3 * t_exp / 7,
@@ -589,6 +600,10 @@ def let_exchange(args, dev):
                        "records_equal_rank1": int(len(sent[0][0])) == int(len(cpu_sent[0]))},
             "import": {"records": int(len(p)), "cells": int(len(cells[0])), "ms": 1e3 * t_imp,
                        "cpu_ms": 1e3 * c_imp, "cpu_cells_equal": bool(same_cells)},
+            "let_forces": {"bodies": int(len(sel0)), "ms": 1e3 * t_acc, "cpu_ms": 1e3 * c_acc,
+                           "bits_equal_oracle": acc_equal,
+                           "form": "computeAccelerationsWithLET: pseudo-leaf map merged into the local map, "
+                                   "exact FP64 walk per body"},
             "cpu_kind": kind, "timing": "host clock around the C-ABI call, results copied to the host"}
 
 

@@ -52,8 +52,8 @@ def test_simulate_help_and_bad_flags():
     _built()
     r = subprocess.run([str(BUILD / "simulate"), "--help"], capture_output=True, text=True)
     assert r.returncode == 0 and "--theta" in r.stdout
-    r = subprocess.run([str(BUILD / "simulate"), "--fc", "direct"], capture_output=True, text=True)
-    assert r.returncode == 1 and "--fc tree" in r.stderr
+    r = subprocess.run([str(BUILD / "simulate"), "--nonsense"], capture_output=True, text=True)
+    assert r.returncode == 1 and "unknown option" in r.stderr
 
 
 def _compile_check(tmp_path):
@@ -189,7 +189,8 @@ def test_simulate_snapshots_follow_reference_schedule(bh, tmp_path):
             want.append((s, t))
             nxt += vs
         t += dt
-    pvd = out / f"bodies_dt1h_tend1y_theta{THETA:g}_bodies-1_fctree.pvd"
+    # the reference's default policy string, "let", names the files
+    pvd = out / f"bodies_dt1h_tend1y_theta{THETA:g}_bodies-1_fclet.pvd"
     sets = ET.parse(pvd).getroot().findall("Collection/DataSet")
     assert [float(d.get("timestep")) for d in sets] == [w[1] for w in want]
     assert [d.get("file") for d in sets] == [f"0/sim.{k}.vtp" for k in range(len(want))]
