@@ -21,6 +21,7 @@
 #ifdef BH_SHIM_USE_REFERENCE_HEADERS
 #include "body.h"
 #include "bounding_box.h"
+#include "exchange.h"
 #include "linear_octree.h"
 #include "morton_keys.h"
 #include "traversal.h"
@@ -73,6 +74,14 @@ struct OctreeNode {
 };
 using OctreeMap = std::unordered_map<OctreeKey, OctreeNode, OctreeKeyHash>;
 
+// include/linear_octree.h:60-65: one cell as the exchange sends it.
+struct NodeRecord {
+    uint64_t prefix;
+    uint8_t depth;
+    double mass;
+    double comX, comY, comZ;
+};
+
 BoundingBox compute_local_bbox(const std::vector<Position>& points);
 
 // include/utility.h:23-52 (in place; equal keys keep their input order)
@@ -95,4 +104,32 @@ OctreeMap buildOctreeBottomUp(const std::vector<uint64_t>& mortonCodes, const st
 void computeAccelerations(const OctreeMap& tree, const std::vector<uint64_t>& key, const std::vector<Position>& pos,
                           double theta, double G, double soft2, const BoundingBox& global_bb,
                           std::vector<Acceleration>& out, int rank = 0);
+#endif
+
+// The LET data path (`--fc let` / `--fc let_direct` beyond one rank).
+#ifndef BH_SHIM_USE_REFERENCE_HEADERS
+// src/exchange.cpp:117-179, bit for bit.  `tree` must be a local tree of
+// buildOctreeBottomUp (its depth-21 cells name its bodies' keys).
+std::vector<NodeRecord> createInteractionListForRank(const OctreeMap& tree, const std::vector<BoundingBox>& remote_boxes,
+                                                     const BoundingBox& global_bb, double theta2,
+                                                     int max_traversal_depth);
+
+// src/linear_octree.cpp:242-322; the records' own cells are marked
+// is_pseudo.  Children are summed in octant order (the reference: in its
+// hash map's order), so sums over several children agree to rounding.
+OctreeMap buildTreeFromPseudoLeaves(const std::vector<NodeRecord>& remote_nodes);
+
+// src/traversal.cpp:107-127.  Like the reference, merges the records'
+// pseudo-leaf map into local_tree (mergeRecordsIntoTree), then walks it.
+void computeAccelerationsWithLET(OctreeMap& local_tree, const std::vector<NodeRecord>& remote_nodes,
+                                 const std::vector<uint64_t>& bodyKey, const std::vector<Position>& pos, double theta,
+                                 double G, double soft2, const BoundingBox& global_bb, std::vector<Acceleration>& out,
+                                 int rank);
+
+// src/traversal.cpp:149-221: the local walk (bit for bit) plus the records
+// summed directly in record order.
+void computeAccelerationsWithRemoteDirectSum(const OctreeMap& local_tree, const std::vector<NodeRecord>& remote_nodes,
+                                             const std::vector<uint64_t>& key, const std::vector<Position>& pos,
+                                             double theta, double G, double soft2, const BoundingBox& global_bb,
+                                             std::vector<Acceleration>& out, int rank = 0);
 #endif

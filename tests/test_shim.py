@@ -16,7 +16,8 @@ PKG = ROOT / "barnes-hut_gb300"
 BUILD = PKG / "_build"
 SHIM = PKG / "shim"
 SHIM_FUNCS = ("compute_local_bbox", "generateMortonCodes", "sortBodiesByMortonKey", "buildOctreeBottomUp",
-              "computeAccelerations")
+              "computeAccelerations", "createInteractionListForRank", "buildTreeFromPseudoLeaves",
+              "computeAccelerationsWithLET", "computeAccelerationsWithRemoteDirectSum")
 
 
 def _built():
@@ -204,3 +205,83 @@ def test_simulate_snapshots_follow_reference_schedule(bh, tmp_path):
     r = subprocess.run([str(BUILD / "simulate"), "-f", str(csv), "--steps", "2", "--vs", "none", "-o",
                         str(tmp_path / "none")], capture_output=True, text=True, cwd=tmp_path)
     assert r.returncode == 0 and not (tmp_path / "none").exists()
+
+
+def _read_records(buf, o):
+    k = int(np.frombuffer(buf, np.int64, 1, o)[0]); o += 8
+    rec = np.dtype([("prefix", "<u8"), ("depth", "u1"), ("v", "<f8", 4)])
+    r = np.frombuffer(buf, rec, k, o)
+    return r, o + r.nbytes
+
+
+@pytest.mark.gpu
+def test_shim_let_functions(tmp_path, port, golden):
+    """The shim's LET functions on rank 0 of the 4-way split of the
+    1,000-body system with the records it receives: the export equals the
+    oracle's bit for bit, the pseudo-leaf map equals the oracle's (same
+    octant order) with the records' cells marked pseudo, and both force
+    forms match the compiled reference's fixtures to 1e-13; the local map
+    holds the merge afterwards, as in the reference."""
+    _built()
+    f = golden("pseudo_tree.npz")
+    g = golden("synthetic_1000.npz")
+    nv = int(f["n_valid"][0])
+    bb = f["bbox"]
+    sel = np.nonzero(np.unpackbits(f["local"])[:len(g["mass"])].astype(bool))[0]
+    keys = port.keys(g["pos"][sel], bb)
+    sk, sp, sm, _, _, _ = port.sort(keys, g["pos"][sel], g["mass"][sel], g["vel"][sel], g["ids"][sel])
+    rec = (f["prefix"][:nv], f["depth"][:nv], f["mass"][:nv], f["com"][:nv])
+    lf = golden("let_export.npz")
+    boxes = lf["synthetic_1000/c0/boxes"]
+    exe = tmp_path / "shim_let_check"
+    cmd = ["g++", "-O2", "-std=c++17", f"-I{ROOT / 'include'}", f"-I{SHIM}", str(ROOT / "tests" / "shim_let_check.cpp"),
+           "-o", str(exe), f"-L{BUILD}", "-lbh_reference_api", "-lbh_gpu", f"-Wl,-rpath,{BUILD}"]
+    subprocess.run(cmd, check=True, capture_output=True, text=True)
+    inp = tmp_path / "in.bin"
+    with open(inp, "wb") as fh:
+        fh.write(np.array([len(sk)], np.int64).tobytes()); fh.write(np.array([THETA]).tobytes())
+        fh.write(np.ascontiguousarray(bb).tobytes())
+        for a in (sk, sp, sm):
+            fh.write(np.ascontiguousarray(a).tobytes())
+        fh.write(np.array([nv], np.int64).tobytes())
+        for k in range(nv):
+            fh.write(np.uint64(rec[0][k]).tobytes()); fh.write(np.uint8(rec[1][k]).tobytes())
+            fh.write(np.float64(rec[2][k]).tobytes()); fh.write(np.ascontiguousarray(rec[3][k]).tobytes())
+        fh.write(np.array([len(boxes)], np.int64).tobytes()); fh.write(np.ascontiguousarray(boxes).tobytes())
+        fh.write(np.array([0.7 ** 2]).tobytes()); fh.write(np.array([21], np.int64).tobytes())
+    out = tmp_path / "out.bin"
+    r = subprocess.run([str(exe), str(inp), str(out)], capture_output=True, text=True)
+    assert r.returncode == 0, r.stdout + r.stderr
+    buf = out.read_bytes()
+    exp, o = _read_records(buf, 0)
+    pm, o = _read_records(buf, o)
+    npseudo = int(np.frombuffer(buf, np.int64, 1, o)[0]); o += 8
+    n = len(sk)
+    ds = np.frombuffer(buf, np.float64, 3 * n, o).reshape(n, 3); o += 24 * n
+    let = np.frombuffer(buf, np.float64, 3 * n, o).reshape(n, 3); o += 24 * n
+    merged = int(np.frombuffer(buf, np.int64, 1, o)[0]); o += 8
+    assert o == len(buf)
+
+    tree = port.tree(sk, sp, sm, merge=False)
+    local_cells = set(zip(*[a.tolist() for a in tree.records()[:2]]))
+    p, d, m, c = port.let_export(tree, boxes, bb, 0.7 ** 2, 21)
+    tree.close()
+    assert_bits_equal(exp["prefix"], p, "export prefixes")
+    assert_bits_equal(exp["depth"], d, "export depths")
+    assert_bits_equal(np.ascontiguousarray(exp["v"][:, 0]), m, "export masses")
+    assert_bits_equal(np.ascontiguousarray(exp["v"][:, 1:]), c, "export centres of mass")
+    t = port.pseudo_tree(*rec)
+    want = t.records()
+    t.close()
+    assert_bits_equal(pm["prefix"], want[0], "pseudo prefixes")
+    assert_bits_equal(pm["depth"], want[1], "pseudo depths")
+    assert_bits_equal(np.ascontiguousarray(pm["v"][:, 0]), want[2], "pseudo masses")
+    assert_bits_equal(np.ascontiguousarray(pm["v"][:, 1:]), want[3], "pseudo centres of mass")
+    own = {(int(pp) & (0 if dd == 0 else ((1 << 64) - 1) << (63 - 3 * min(int(dd), 21)) & ((1 << 64) - 1)),
+            min(int(dd), 21)) for pp, dd, mm in zip(*rec[:3]) if mm > 0 and np.isfinite(mm)}
+    assert npseudo == len(own)
+    for got, key in ((let, "let_acc"), (ds, "letds_acc")):
+        rel = np.linalg.norm(got - f[key], axis=1) / np.linalg.norm(f[key], axis=1)
+        assert rel.max() <= 1e-13, key
+    pseudo_cells = set(zip(want[0].tolist(), want[1].tolist()))
+    assert merged == len(local_cells | pseudo_cells)
