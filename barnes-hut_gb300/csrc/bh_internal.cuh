@@ -80,6 +80,31 @@ __device__ __forceinline__ double rsqrt_hh(double x)
     return fma(y0, t, y0);
 }
 
+// x^(-3/2), the r^-3 of a monopole term from r^2, for the non-bit-exact
+// FP64 walk and the direct terms: the FP32 estimate y0 of x^-1/2 as in
+// rsqrt_hh (a 24-bit value, so y0^2 is exact in FP64), e = 1 - x y0^2, and
+// x^-3/2 = y0^3 (1 - e)^-3/2 = y0^3 (1 + 3/2 e + 15/8 e^2 + ...): with
+// |e| < 2^-20 the next term is below 2^-58 relative.  Five FP64 operations
+// where rsqrt_hh and two products take seven.  Within 4 ulps of
+// RN(1 / RN(x RN(sqrt(x)))) (checked by bh_selftest).
+__device__ __forceinline__ double rcube_hh(double x)
+{
+    const long long xb = __double_as_longlong(x);
+    const int xe = (int)(xb >> 52);
+    if (xe < 923 || xe > 1122) {  // outside [2^-100, 2^100): also 0, inf, NaN
+        const double r = rsqrt(x);
+        return r * r * r;
+    }
+    const float xf = __int_as_float(((xe - 896) << 23) | (int)((xb >> 29) & 0x7FFFFF));
+    const int yb = __float_as_int(rsqrtf(xf));
+    const double y0 = __longlong_as_double(((long long)(((yb >> 23) & 0xFF) + 896) << 52) |
+                                           ((long long)(yb & 0x7FFFFF) << 29));
+    const double y2 = y0 * y0;
+    const double e = fma(-x, y2, 1.0);
+    const double f = fma(e, fma(e, 1.875, 1.5), 1.0);
+    return (y2 * y0) * f;
+}
+
 // norm + quantise of generateMortonCodes (src/morton_keys.cpp:77-94):
 // t = (v - lo)/span clamped to [0, 1 - 2^-53], then (uint32)(t * 2^21).
 __device__ inline uint32_t quantise_exact(double v, double lo, double span)

@@ -27,6 +27,7 @@ __device__ inline double with_exp(uint64_t r, int e)
 // which = 1: quantise(...) == quantise_exact(...)
 // which = 2: rsqrt_hh(x) within 2 ulps of RN(1 / RN(sqrt(x)))
 // which = 3: div_exact(w, m, rcp_nr(m)) == RN(w / m)
+// which = 4: rcube_hh(x) within 4 ulps of RN(1 / RN(x RN(sqrt(x))))
 __global__ void selftest_kernel(int which, int64_t n, uint64_t seed, unsigned long long* fails)
 {
     unsigned long long bad = 0;
@@ -68,6 +69,12 @@ __global__ void selftest_kernel(int which, int64_t n, uint64_t seed, unsigned lo
             const double want = __ddiv_rn(w, m);
             const double got = bh::div_exact(w, m, bh::rcp_nr(m));
             bad += __double_as_longlong(want) != __double_as_longlong(got);
+        } else if (which == 4) {
+            const double x = with_exp(r0, -90 + (int)(r1 % 180));
+            const double want = __drcp_rn(__dmul_rn(x, __dsqrt_rn(x)));
+            const double got = bh::rcube_hh(x);
+            const long long d = __double_as_longlong(want) - __double_as_longlong(got);
+            bad += (d > 4 || d < -4);
         } else {
             const double x = with_exp(r0, -90 + (int)(r1 % 180));
             const double want = __drcp_rn(__dsqrt_rn(x));
@@ -83,7 +90,7 @@ __global__ void selftest_kernel(int which, int64_t n, uint64_t seed, unsigned lo
 
 extern "C" int bh_selftest(int which, int64_t n, uint64_t seed, int64_t* failures)
 {
-    if (which < 0 || which > 3 || n < 0 || !failures) return bh_fail(BH_ERR_INVALID_ARGUMENT, "bh_selftest: bad arguments");
+    if (which < 0 || which > 4 || n < 0 || !failures) return bh_fail(BH_ERR_INVALID_ARGUMENT, "bh_selftest: bad arguments");
     int dev = 0;
     BH_CUDA_TRY(cudaGetDevice(&dev));
     unsigned long long* d = nullptr;

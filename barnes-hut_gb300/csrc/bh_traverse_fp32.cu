@@ -19,7 +19,7 @@
 // walk at theta accepts.
 //
 // BH_MODE_FP64_LIST: per-lane tests in FP64 with the reference's rounding,
-//   interactions in FP64 (rsqrt_hh + FMA) from the FP64 node records, on the
+//   interactions in FP64 (rcube_hh + FMA) from the FP64 node records, on the
 //   reference's tree.
 // BH_MODE_FP32_FAR: precision form.  The bodies with id < num_direct (Sun and
 //   planets) are taken out of the tree (masses zeroed before the build) and
@@ -268,8 +268,7 @@ __global__ void __launch_bounds__(kThreads) traverse_masked_kernel(FParams p)
             // A body at the very position of a direct body shares its leaf,
             // which the reference skips (traversal.cpp:70): no term.
             if (__double_as_longlong(r2) == 0) continue;
-            const double inv = rsqrt_hh(r2);
-            const double sc = p.direct[4 * kk + 3] * (inv * inv * inv);
+            const double sc = p.direct[4 * kk + 3] * rcube_hh(r2);
             adx = fma(sc, dx, adx);
             ady = fma(sc, dy, ady);
             adz = fma(sc, dz, adz);
@@ -591,8 +590,7 @@ __global__ void __launch_bounds__(kThreads) traverse_masked_kernel(FParams p)
                         take = p.rec[LN[j]].top <= kMaxDepth - 1 && sm.side2d[kMaxDepth - 1] < __dmul_rn(theta2, r2e);
                     }
                     const double r2 = fma(dx, dx, fma(dy, dy, fma(dz, dz, soft2)));
-                    const double inv = rsqrt_hh(r2);
-                    double sc = r.w * (inv * inv * inv);
+                    double sc = r.w * rcube_hh(r2);
                     if (!take) sc = 0.0;
                     sx = fma(sc, dx, sx);
                     sy = fma(sc, dy, sy);

@@ -270,7 +270,9 @@ int bh_invariants(bh_context *ctx, double G, double theta, double out[9]);
  * division-free key quantisation against the IEEE one; 2: the refined
  * reciprocal square root against RN(1 / RN(sqrt x)) (more than 2 ulps
  * apart counts); 3: the division-free centre-of-mass quotient against
- * RN(w / m).  No reference counterpart. */
+ * RN(w / m); 4: the fused r^-3 of the FP64 list form and the direct terms
+ * against RN(1 / RN(x RN(sqrt x))) (more than 4 ulps apart counts).  No
+ * reference counterpart. */
 int bh_selftest(int which, int64_t n, uint64_t seed, int64_t *failures);
 
 /* ---- learned acceptance (no reference counterpart) ------------------- */
