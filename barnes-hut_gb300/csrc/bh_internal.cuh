@@ -84,8 +84,8 @@ __device__ __forceinline__ double rsqrt_hh(double x)
 // FP64 walk and the direct terms: the FP32 estimate y0 of x^-1/2 as in
 // rsqrt_hh (a 24-bit value, so y0^2 is exact in FP64), e = 1 - x y0^2, and
 // x^-3/2 = y0^3 (1 - e)^-3/2 = y0^3 (1 + 3/2 e + 15/8 e^2 + ...): with
-// |e| < 2^-20 the next term is below 2^-58 relative.  Five FP64 operations
-// where rsqrt_hh and two products take seven.  Within 4 ulps of
+// |e| < 2^-20 the next term is below 2^-58 relative.  Six FP64 operations
+// where rsqrt_hh and the cube take seven.  Within 4 ulps of
 // RN(1 / RN(x RN(sqrt(x)))) (checked by bh_selftest).
 __device__ __forceinline__ double rcube_hh(double x)
 {
