@@ -243,7 +243,7 @@ int step_once(bh_context* ctx, double dt, double theta, double G, int mode)
     e = phase_begin(ctx);
     if (!rc && far) rc = bh::launch_far_mass(ctx);
     const bool moments = mode == BH_MODE_LEARNED;
-    if (!rc) rc = bh::launch_build(ctx, far ? ctx->m2 : ctx->m, moments);
+    if (!rc) rc = bh::launch_build(ctx, far ? ctx->m2 : ctx->m, moments, far, G);
     ctx->tree_far = far;
     ctx->tree_moments = moments;
     phase_end(ctx, 4, e);
@@ -747,6 +747,7 @@ int bh_tree_set_slot_values(bh_context* ctx, const double* mass, const double* c
     }
     BH_CUDA_TRY(cudaMemcpyAsync(ctx->rec, h.rec.data(), sizeof(bh::TreeRec) * h.S, cudaMemcpyHostToDevice, ctx->stream));
     ctx->tree_far = ctx->tree_moments = false;
+    ctx->fnodes_fused = false;
     return finish(ctx, "bh_tree_set_slot_values");
 }
 

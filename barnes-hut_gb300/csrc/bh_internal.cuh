@@ -338,6 +338,8 @@ struct bh_context {
     float4* fB = nullptr;   // {lo.x, lo.y, lo.z, bits of ref (child or leaf id)}
     uint32_t* fmeta = nullptr;  // nchild | depth << 8 | leaf << 16
     double4_32a* d4 = nullptr;  // FP64 walk: {cx, cy, cz, G m} per slot
+    bool fnodes_fused = false;  // fA / fB / fmeta are current for rec and fnodes_G
+    double fnodes_G = 0.0;
     float* fspread = nullptr;   // sqrt(Q / m) per slot (second moment about the centre of mass)
     double* leaf_q = nullptr;   // second moments of leaves and branching nodes
     double* node_q = nullptr;
@@ -404,7 +406,9 @@ int sort_passes_raw(int64_t n, const uint64_t* keys_in, uint64_t* keys_out, uint
 // Builds the octree over the sorted bodies with the given masses (ctx->m
 // for the reference's tree; the far-field masses for the FP32 modes);
 // `moments` also computes the second moments (spread per slot).
-int launch_build(bh_context* ctx, const double* mass, bool moments = false);
+// far_fused: the far-field tree of an FP32 form, whose centres of mass need
+// no bit-exact quotient; the FP32 node records for G are written too.
+int launch_build(bh_context* ctx, const double* mass, bool moments = false, bool far_fused = false, double G = 0.0);
 // FP32 modes: far-field masses (direct bodies zeroed) into ctx->m2.
 int launch_far_mass(bh_context* ctx);
 // Waits for the context's stream and turns a raised device error word into

@@ -706,6 +706,8 @@ int launch_fp32_nodes(bh_context* ctx, double G)
     fp32_nodes_kernel<<<grid_n(2 * ctx->n), 256, 0, ctx->stream>>>(ctx->counts, ctx->rec, G, ctx->fA, ctx->fB,
                                                                     ctx->fmeta, nullptr);
     BH_LAUNCH_CHECK(ctx);
+    ctx->fnodes_fused = true;
+    ctx->fnodes_G = G;
     return BH_OK;
 }
 
@@ -735,9 +737,13 @@ int prepare_walk(bh_context* ctx, double theta, double G, double soft2, bool fp6
 {
     const int64_t n = ctx->n;
     const int nd = fp64 ? 0 : (ctx->num_direct < 64 ? ctx->num_direct : 64);
-    fp32_nodes_kernel<<<grid_n(2 * n), 256, 0, ctx->stream>>>(ctx->counts, ctx->rec, G, ctx->fA, ctx->fB, ctx->fmeta,
-                                                              fp64 ? ctx->d4 : nullptr);
-    BH_LAUNCH_CHECK(ctx);
+    if (fp64 || !ctx->fnodes_fused || ctx->fnodes_G != G) {  // else they are current (the build wrote them)
+        fp32_nodes_kernel<<<grid_n(2 * n), 256, 0, ctx->stream>>>(ctx->counts, ctx->rec, G, ctx->fA, ctx->fB,
+                                                                  ctx->fmeta, fp64 ? ctx->d4 : nullptr);
+        BH_LAUNCH_CHECK(ctx);
+        ctx->fnodes_fused = true;
+        ctx->fnodes_G = G;
+    }
     if (nd > 0) {
         int rc = launch_direct_extract(ctx, G);
         if (rc) return rc;

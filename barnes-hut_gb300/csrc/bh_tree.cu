@@ -382,7 +382,31 @@ __device__ inline void finish_com(double m, double wx, double wy, double wz, Tre
     r.m = tot;
 }
 
-template <bool kMoments>
+// The far-field tree of the FP32 forms (direct bodies' masses zeroed) is not
+// the reference's tree, so its centres of mass need no bit-exact quotient:
+// w times the refined reciprocal of m (within 2 ulps), no merge step.  The
+// kernel also writes the FP32 walk's node records (hi + lo split of the
+// centre, G m and the topology word), which the walk would otherwise make in
+// a pass of its own.
+__device__ inline void far_com(double m, double wx, double wy, double wz, TreeRec& r)
+{
+    if (m > 0) {
+        const double q = rcp_nr(m);
+        r.cx = wx * q; r.cy = wy * q; r.cz = wz * q;
+    } else {
+        r.cx = wx; r.cy = wy; r.cz = wz;
+    }
+    r.m = m;
+}
+
+struct FarOut {
+    float4* A;       // {hi.x, hi.y, hi.z, G m}
+    float4* B;       // {lo.x, lo.y, lo.z, bits of child or leaf id}
+    uint32_t* meta;  // nchild | depth << 8 | leaf << 16 | massless << 17
+    double G;
+};
+
+template <bool kMoments, bool kFar>
 __global__ void finalize_kernel(const int32_t* __restrict__ counts, const int32_t* __restrict__ slot_ref,
                                 const uint8_t* __restrict__ slot_top, const double* __restrict__ lm,
                                 const double* __restrict__ lwx, const double* __restrict__ lwy,
@@ -393,7 +417,7 @@ __global__ void finalize_kernel(const int32_t* __restrict__ counts, const int32_
                                 TreeRec* __restrict__ rec, const double* __restrict__ lq,
                                 const double* __restrict__ nq, float* __restrict__ spread, int merge,
                                 const int32_t* __restrict__ leaf_first, const double* __restrict__ px,
-                                const double* __restrict__ py, const double* __restrict__ pz)
+                                const double* __restrict__ py, const double* __restrict__ pz, FarOut far)
 {
     const int S = counts[2];
     for (int s = blockIdx.x * blockDim.x + threadIdx.x; s < S; s += gridDim.x * blockDim.x) {
@@ -403,23 +427,39 @@ __global__ void finalize_kernel(const int32_t* __restrict__ counts, const int32_
         o.pad0 = 0;
         o.pad1 = 0;
         if (r >= 0) {
-            const int b = leaf_first[r];
-            const bool one = leaf_first[r + 1] == b + 1;
-            finish_com(lm[r], lwx[r], lwy[r], lwz[r], o, merge, one, one ? px[b] : 0.0, one ? py[b] : 0.0,
-                       one ? pz[b] : 0.0);
+            if (kFar) {
+                far_com(lm[r], lwx[r], lwy[r], lwz[r], o);
+            } else {
+                const int b = leaf_first[r];
+                const bool one = leaf_first[r + 1] == b + 1;
+                finish_com(lm[r], lwx[r], lwy[r], lwz[r], o, merge, one, one ? px[b] : 0.0, one ? py[b] : 0.0,
+                           one ? pz[b] : 0.0);
+            }
             o.child = -1;
             o.leaf = r;
             o.nchild = 0;
             o.depth = (uint8_t)kMaxDepth;
         } else {
             const int b = ~r;
-            finish_com(nm[b], nwx[b], nwy[b], nwz[b], o, merge, false, 0.0, 0.0, 0.0);
+            if (kFar) far_com(nm[b], nwx[b], nwy[b], nwz[b], o);
+            else finish_com(nm[b], nwx[b], nwy[b], nwz[b], o, merge, false, 0.0, 0.0, 0.0);
             o.child = node_cs[b] + 1;
             o.leaf = -1;
             o.nchild = (uint8_t)node_nchild[b];
             o.depth = node_depth[b];
         }
         rec[s] = o;
+        if (kFar) {  // the FP32 walk's records, as fp32_nodes_kernel makes them
+            const float hx = narrow_trunc(o.cx), hy = narrow_trunc(o.cy), hz = narrow_trunc(o.cz);
+            const float lx = narrow_trunc(o.cx - widen(hx));
+            const float ly = narrow_trunc(o.cy - widen(hy));
+            const float lz = narrow_trunc(o.cz - widen(hz));
+            const bool leaf = o.child < 0;
+            far.A[s] = make_float4(hx, hy, hz, narrow_trunc(far.G * o.m));
+            far.B[s] = make_float4(lx, ly, lz, __int_as_float(leaf ? o.leaf : o.child));
+            far.meta[s] = (uint32_t)o.nchild | ((uint32_t)o.depth << 8) | ((leaf ? 1u : 0u) << 16) |
+                          ((o.m == 0.0 ? 1u : 0u) << 17);
+        }
         if (kMoments) {
             const double m = r >= 0 ? lm[r] : nm[~r];
             const double q = r >= 0 ? lq[r] : nq[~r];
@@ -436,8 +476,9 @@ __global__ void slot_count_kernel(int32_t* counts, const int32_t* __restrict__ c
 
 }  // namespace
 
-int launch_build(bh_context* ctx, const double* mass, bool moments)
+int launch_build(bh_context* ctx, const double* mass, bool moments, bool far_fused, double G)
 {
+    ctx->fnodes_fused = false;
     const int64_t n = ctx->n;
     if (n == 0) return BH_OK;
     cudaStream_t st = ctx->stream;
@@ -507,21 +548,26 @@ int launch_build(bh_context* ctx, const double* mass, bool moments)
 
     // 5. traversal records
     const int gs = grid_for(2 * n, kThreads, maxb);
-    if (moments)
-        finalize_kernel<true><<<gs, kThreads, 0, st>>>(ctx->counts, ctx->slot_ref, ctx->slot_top, ctx->leaf_m,
-                                                       ctx->leaf_wx, ctx->leaf_wy, ctx->leaf_wz, ctx->node_m,
-                                                       ctx->node_wx, ctx->node_wy, ctx->node_wz, ctx->node_cs,
-                                                       ctx->node_nchild, ctx->node_depth, ctx->rec, ctx->leaf_q,
-                                                       ctx->node_q, ctx->fspread, ctx->build_merge ? 1 : 0,
-                                                       ctx->leaf_first, ctx->px, ctx->py, ctx->pz);
-    else
-        finalize_kernel<false><<<gs, kThreads, 0, st>>>(ctx->counts, ctx->slot_ref, ctx->slot_top, ctx->leaf_m,
-                                                        ctx->leaf_wx, ctx->leaf_wy, ctx->leaf_wz, ctx->node_m,
-                                                        ctx->node_wx, ctx->node_wy, ctx->node_wz, ctx->node_cs,
-                                                        ctx->node_nchild, ctx->node_depth, ctx->rec, ctx->leaf_q,
-                                                        ctx->node_q, ctx->fspread, ctx->build_merge ? 1 : 0,
-                                                       ctx->leaf_first, ctx->px, ctx->py, ctx->pz);
+    const FarOut far{ctx->fA, ctx->fB, ctx->fmeta, G};
+#define BH_FINALIZE(M, F)                                                                                      \
+    finalize_kernel<M, F><<<gs, kThreads, 0, st>>>(                                                            \
+        ctx->counts, ctx->slot_ref, ctx->slot_top, ctx->leaf_m, ctx->leaf_wx, ctx->leaf_wy, ctx->leaf_wz,       \
+        ctx->node_m, ctx->node_wx, ctx->node_wy, ctx->node_wz, ctx->node_cs, ctx->node_nchild, ctx->node_depth, \
+        ctx->rec, ctx->leaf_q, ctx->node_q, ctx->fspread, ctx->build_merge ? 1 : 0, ctx->leaf_first, ctx->px,  \
+        ctx->py, ctx->pz, far)
+    if (far_fused) {
+        if (moments) BH_FINALIZE(true, true);
+        else BH_FINALIZE(false, true);
+    } else {
+        if (moments) BH_FINALIZE(true, false);
+        else BH_FINALIZE(false, false);
+    }
+#undef BH_FINALIZE
     BH_LAUNCH_CHECK(ctx);
+    if (far_fused) {
+        ctx->fnodes_fused = true;
+        ctx->fnodes_G = G;
+    }
     return BH_OK;
 }
 
