@@ -119,6 +119,8 @@ def _sig(lib):
     f["bh_generate_system"] = (C.c_int, [C.c_uint64, _I64, _D, _D, _P, _P, _P, _P])
     f["bh_read_csv"] = (C.c_int, [C.c_char_p, _I64, C.POINTER(_I64), _P, _P, _P, _P])
     f["bh_write_csv"] = (C.c_int, [C.c_char_p, _I64, _P, _P, _P, _P])
+    f["bh_read_csv_gpu"] = (C.c_int, [C.c_char_p, _I64, C.POINTER(_I64), _P, _P, _P, _P])
+    f["bh_load_csv"] = (C.c_int, [_P, C.c_char_p, _I64, C.POINTER(_I64)])
     for name, (res, args) in f.items():
         if hasattr(lib, name):
             fn = getattr(lib, name)
@@ -202,6 +204,18 @@ def read_csv(path, body_count: int = -1):
     return ids, mass, pos, vel
 
 
+def read_csv_gpu(path, body_count: int = -1):
+    """readCSV parsed on the GPU: (ids, mass, pos, vel), as read_csv."""
+    lib = library()
+    n = _I64(0)
+    p = str(path).encode()
+    _check(lib.bh_read_csv_gpu(p, body_count, C.byref(n), None, None, None, None))
+    ids = np.empty(n.value, np.uint64); mass = np.empty(n.value); pos = np.empty((n.value, 3))
+    vel = np.empty((n.value, 3))
+    _check(lib.bh_read_csv_gpu(p, body_count, C.byref(n), _ptr(ids), _ptr(mass), _ptr(pos), _ptr(vel)))
+    return ids, mass, pos, vel
+
+
 def write_csv(path, ids, mass, pos, vel) -> None:
     ids = _u64(ids); mass = _f64(mass); pos = _f64(pos); vel = _f64(vel)
     _check(library().bh_write_csv(str(path).encode(), len(mass), _ptr(ids), _ptr(mass), _ptr(pos), _ptr(vel)))
@@ -274,6 +288,12 @@ class Context:
         mass = _f64(mass).reshape(n)
         ids = np.arange(n, dtype=np.uint64) if ids is None else _u64(ids)
         _check(library().bh_set_bodies(self._h, n, _ptr(pos), _ptr(vel), _ptr(mass), _ptr(ids)))
+
+    def load_csv(self, path, body_count: int = -1) -> int:
+        """readCSV parsed on the GPU into this context's bodies; returns n."""
+        n = _I64(0)
+        _check(library().bh_load_csv(self._h, str(path).encode(), body_count, C.byref(n)))
+        return n.value
 
     def set_accelerations(self, acc) -> None:
         acc = _f64(acc).reshape(-1, 3)

@@ -97,6 +97,22 @@ bool parse_double(const std::string& s, double* out)
 
 }  // namespace
 
+// One data row of readCSV (src/io.cpp:45-70): three skipped columns, then
+// mass, position and velocity through std::stod.  As in the reference, a
+// getline past the end of the row leaves `field` holding the previous
+// column, which is then parsed again.
+bool bh_parse_csv_row(const std::string& line, double v[7])
+{
+    std::stringstream ss(line);
+    std::string field;
+    for (int c = 0; c < 3; ++c) std::getline(ss, field, ',');
+    for (int c = 0; c < 7; ++c) {
+        std::getline(ss, field, ',');
+        if (!parse_double(field, &v[c])) return false;
+    }
+    return true;
+}
+
 extern "C" int bh_kepler_to_cartesian(const double* el, int64_t n, double* out)
 {
     if (n < 0 || (n > 0 && (!el || !out))) return bh_fail(BH_ERR_INVALID_ARGUMENT, "bh_kepler_to_cartesian: bad arguments");
@@ -177,17 +193,8 @@ extern "C" int bh_read_csv(const char* path, int64_t body_count, int64_t* n_out,
     int64_t n = 0;
     while (std::getline(f, line)) {
         if (body_count > 0 && n >= body_count) break;
-        std::stringstream ss(line);
-        std::string field;
         double v[7];
-        bool ok = true;
-        for (int c = 0; c < 3; ++c) std::getline(ss, field, ',');
-        // As in the reference, a getline past the end of the row leaves
-        // `field` holding the previous column, which is then parsed again.
-        for (int c = 0; c < 7 && ok; ++c) {
-            std::getline(ss, field, ',');
-            ok = parse_double(field, &v[c]);
-        }
+        const bool ok = bh_parse_csv_row(line, v);
         if (!ok) {
             std::fprintf(stderr, "Warning: Could not parse line, skipping: \"%s\"\n", line.c_str());
             continue;

@@ -22,6 +22,7 @@
 // sim_out and --vs to 10d, as in the reference.  --vs none turns them off.
 // The download of a frame waits for the GPU; its file is written by a host
 // thread while the next steps run.
+#include <algorithm>
 #include <chrono>
 #include <cmath>
 #include <cstdio>
@@ -120,16 +121,29 @@ int main(int argc, char** argv)
     std::vector<uint64_t> ids;
     std::vector<double> mass, pos, vel;
     int64_t n = 0;
+    bh_context* ctx = nullptr;
     if (generate > 0) {
         n = generate;
         ids.resize(n); mass.resize(n); pos.resize(3 * n); vel.resize(3 * n);
         check(bh_generate_system(seed, n, 0.10, 0.0, pos.data(), vel.data(), mass.data(), ids.data()),
               "bh_generate_system");
+        check(bh_context_create(n > 0 ? n : 1, 0, &ctx), "bh_context_create");
+        check(bh_set_bodies(ctx, n, pos.data(), vel.data(), mass.data(), ids.data()), "bh_set_bodies");
     } else {
+        // readCSV on the GPU straight into the device state; the context is
+        // sized by the file's line count (an upper bound on its rows).
         if (file.empty()) die("input file required (-f)");
-        check(bh_read_csv(file.c_str(), bodies, &n, nullptr, nullptr, nullptr, nullptr), "bh_read_csv");
+        int64_t lines = 1;
+        if (std::FILE* f = std::fopen(file.c_str(), "rb")) {
+            std::vector<char> buf(1 << 20);
+            size_t k;
+            while ((k = std::fread(buf.data(), 1, buf.size(), f)) > 0) lines += std::count(buf.data(), buf.data() + k, '\n');
+            std::fclose(f);
+        }
+        const int64_t cap = bodies > 0 ? std::min<int64_t>(lines, bodies) : lines;
+        check(bh_context_create(cap > 0 ? cap : 1, 0, &ctx), "bh_context_create");
+        check(bh_load_csv(ctx, file.c_str(), bodies, &n), "bh_load_csv");
         ids.resize(n); mass.resize(n); pos.resize(3 * n); vel.resize(3 * n);
-        check(bh_read_csv(file.c_str(), bodies, &n, ids.data(), mass.data(), pos.data(), vel.data()), "bh_read_csv");
     }
     std::cout << "Loaded " << n << " bodies\n";
     int64_t nsteps = steps;
@@ -139,9 +153,6 @@ int main(int argc, char** argv)
     }
     std::cout << "Starting simulation (dt=" << dt << ", tend=" << t_end << ")\n";
 
-    bh_context* ctx = nullptr;
-    check(bh_context_create(n > 0 ? n : 1, 0, &ctx), "bh_context_create");
-    check(bh_set_bodies(ctx, n, pos.data(), vel.data(), mass.data(), ids.data()), "bh_set_bodies");
     const double G = 1.48812e-34;
     double t = 0.0;
     const bool frames = vs_s != "none";

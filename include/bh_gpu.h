@@ -372,6 +372,19 @@ int bh_generate_system(uint64_t seed, int64_t n, double frac_outer, double frac_
  * Call with pos == NULL to get the row count only. */
 int bh_read_csv(const char *path, int64_t body_count, int64_t *n_out, uint64_t *ids, double *mass,
                 double *pos, double *vel);
+/* readCSV on the current GPU: the same rows, values (bit for bit: std::stod
+ * is correctly rounded and so is the device conversion), ids, body_count
+ * limit and warnings as bh_read_csv; the file is split and parsed on the
+ * device, and the rare fields it cannot decide there (hexadecimal, inf/nan,
+ * more than 19 significant digits, results outside the normal range, or
+ * within two units of a rounding boundary) are parsed on the host.  With
+ * pos == NULL only *n_out is set. */
+int bh_read_csv_gpu(const char *path, int64_t body_count, int64_t *n_out, uint64_t *ids, double *mass,
+                    double *pos, double *vel);
+/* The same, straight into the context's body state (as bh_set_bodies): no
+ * host copy of the bodies.  More bodies than the context holds returns
+ * BH_ERR_CAPACITY with *n_out set. */
+int bh_load_csv(bh_context *ctx, const char *path, int64_t body_count, int64_t *n_out);
 /* Writes the reference's state-vector CSV layout (header
  * id,name,class,mass,pos_x,pos_y,pos_z,vel_x,vel_y,vel_z). */
 int bh_write_csv(const char *path, int64_t n, const uint64_t *ids, const double *mass, const double *pos,

@@ -169,3 +169,29 @@ def test_let_bucket_boxes_match_fixture(bh, golden):
             assert_bits_equal(got, f[f"{system}/c{ci}/boxes"], f"{system} case {ci}")
             seen += 1
     assert seen >= 10
+
+
+def test_pow5_table_is_generated():
+    """The GPU CSV reader's table of 128-bit powers of five is exactly what
+    its generator (exact integer arithmetic) writes, and each entry brackets
+    5^q as the conversion assumes."""
+    import subprocess
+    import sys
+    from conftest import ROOT
+    csrc = ROOT / "barnes-hut_gb300" / "csrc"
+    out = subprocess.run([sys.executable, str(csrc / "gen_pow5_table.py")], capture_output=True, text=True,
+                         check=True).stdout
+    assert out == (csrc / "bh_pow5_table.h").read_text()
+    from fractions import Fraction
+    sys.path.insert(0, str(csrc))
+    import gen_pow5_table as g
+    for q in (-342, -300, -28, -27, -1, 0, 1, 27, 55, 56, 200, 308):
+        f, s = g.entry(q)
+        exact = Fraction(5) ** q
+        approx = Fraction(f) * Fraction(2) ** s
+        if 0 <= q <= 55:
+            assert approx == exact
+        elif q > 55:
+            assert exact - Fraction(2) ** s < approx <= exact
+        else:
+            assert exact <= approx < exact + Fraction(2) ** s

@@ -1,0 +1,154 @@
+"""readCSV on the GPU (bh_read_csv_gpu, bh_load_csv) against the host
+reader (bh_read_csv: std::getline + std::stod, the reference's rules) and
+against Python's correctly rounded float(): the same rows, ids, values bit
+for bit, body_count limit and warnings."""
+from __future__ import annotations
+
+import random
+import struct
+
+import numpy as np
+import pytest
+
+from conftest import assert_bits_equal
+
+pytestmark = pytest.mark.gpu
+
+HEADER = "id,name,class,mass,pos_x,pos_y,pos_z,vel_x,vel_y,vel_z"
+
+
+def _num(rng: random.Random) -> str:
+    """A decimal field in one of the forms state-vector files and std::stod
+    accept."""
+    k = rng.random()
+    x = struct.unpack("<d", struct.pack("<Q", rng.getrandbits(64) & ~(0x7FF << 52) |
+                                        (rng.randint(1023 - 60, 1023 + 60) << 52)))[0]
+    if k < 0.25:
+        return repr(x)
+    if k < 0.45:
+        return f"{x:.18e}"
+    if k < 0.55:
+        return f"{x:.19g}"
+    if k < 0.70:  # 19 significant digits, random exponent
+        w = rng.randint(10 ** 18, 10 ** 19 - 1)
+        return f"{'-' if rng.random() < 0.5 else ''}{w}e{rng.randint(-60, 40)}"
+    if k < 0.80:  # near a rounding boundary: the midpoint of two doubles to 19-20 digits
+        from decimal import Decimal, getcontext
+        getcontext().prec = 50
+        b = struct.unpack("<Q", struct.pack("<d", abs(x)))[0]
+        mid = (Decimal(abs(x)) + Decimal(struct.unpack("<d", struct.pack("<Q", b + 1))[0])) / 2
+        return f"{mid:.19e}" if rng.random() < 0.5 else f"{mid:.18e}"
+    if k < 0.85:
+        return str(rng.randint(-10 ** 6, 10 ** 6))
+    if k < 0.90:
+        return rng.choice([" +0.5", ".5", "5.", "1e", "1e+", "-0", "0.000", "  7.25e-3", "3.0\r", "1E5", "0e999"])
+    if k < 0.95:  # exact halves and small exact values
+        return f"{rng.randint(1, 10 ** 6)}.{rng.choice(['5', '25', '125', '0625'])}"
+    return f"{rng.randint(1, 99)}.{rng.randint(0, 10 ** 17):017d}e{rng.randint(-30, 30)}"
+
+
+def _odd_rows():
+    """Rows the device hands to the host or rejects, and getline quirks."""
+    return [
+        "9,odd,AST,0x1p3,1,2,3,4,5,6",                     # hexadecimal: host
+        "10,odd,AST,inf,1,2,3,4,5,6",                      # inf: host (valid for std::stod)
+        "11,odd,AST,1.2345678901234567890123,1,2,3,4,5,6",  # 23 digits: host
+        "12,odd,AST,1e-320,1,2,3,4,5,6",                   # subnormal: host (ERANGE -> skipped)
+        "13,odd,AST,1e400,1,2,3,4,5,6",                    # overflow: skipped
+        "14,odd,AST,abc,1,2,3,4,5,6",                      # no conversion: skipped
+        "15,odd,AST,1,2,3,4",                               # short row: fields repeat the last piece
+        "16,odd,AST,1,2,3,4,5,6,",                          # trailing comma: an empty field
+        "",                                                 # empty line: skipped
+        "17,odd,AST,1,2,3,4,5,6,7,extra,columns",           # extra columns are ignored
+        "18,odd,AST,nan,1,2,3,4,5,6",                      # nan: host
+        "19,odd,AST,.,1,2,3,4,5,6",                        # no digits: skipped
+    ]
+
+
+def _write(path, rows, crlf=False, final_newline=True):
+    nl = "\r\n" if crlf else "\n"
+    text = nl.join([HEADER] + rows) + (nl if final_newline else "")
+    path.write_bytes(text.encode())
+
+
+def _rows(rng, n):
+    return [f"{i},b{i},AST," + ",".join(_num(rng) for _ in range(7)) for i in range(n)]
+
+
+def _same(a, b):
+    for x, y, what in zip(a, b, ("ids", "mass", "pos", "vel")):
+        assert_bits_equal(x, y, what)
+
+
+def test_gpu_reader_matches_host_reader(bh, tmp_path, capfd):
+    rng = random.Random(11)
+    rows = _rows(rng, 60_000)
+    for k, r in enumerate(_odd_rows()):
+        rows.insert(100 + 977 * k, r)
+    f = tmp_path / "bodies.csv"
+    _write(f, rows)
+    capfd.readouterr()
+    host = bh.read_csv(f)
+    host_err = capfd.readouterr().err
+    gpu = bh.read_csv_gpu(f)
+    gpu_err = capfd.readouterr().err
+    assert len(host[0]) == len(rows) - 6  # abc, 1e400, 1e-320, the empty line, ".", the trailing comma
+    _same(gpu, host)
+    # the same warnings (each printed twice by the two-call reader)
+    assert sorted(set(gpu_err.splitlines())) == sorted(set(host_err.splitlines()))
+    assert len(set(host_err.splitlines())) == 6
+    # limits: the reference stops after body_count rows
+    for lim in (1, 101, 5000):
+        _same(bh.read_csv_gpu(f, lim), bh.read_csv(f, lim))
+
+
+def test_gpu_reader_values_are_correctly_rounded(bh, tmp_path):
+    """Every field equals Python's float() of its text (correct rounding),
+    including 19-digit mantissas and near-midpoint decimals."""
+    rng = random.Random(12)
+    fields = [_num(rng) for _ in range(7 * 40_000)]
+    fields = [s for s in fields if s.strip() not in ("1e", "1e+", "0e999")]
+    fields = fields[: 7 * (len(fields) // 7)]
+    rows = [f"{i},b,AST," + ",".join(fields[7 * i: 7 * i + 7]) for i in range(len(fields) // 7)]
+    f = tmp_path / "v.csv"
+    _write(f, rows)
+    ids, mass, pos, vel = bh.read_csv_gpu(f)
+    got = np.concatenate([mass[:, None], pos, vel], axis=1).reshape(-1)
+    want = np.array([float(s) for s in fields])
+    assert_bits_equal(got, want, "values")
+
+
+@pytest.mark.parametrize("crlf,final_newline", [(True, True), (False, False)])
+def test_gpu_reader_line_endings(bh, tmp_path, crlf, final_newline):
+    rng = random.Random(13)
+    rows = _rows(rng, 2000)
+    f = tmp_path / "e.csv"
+    _write(f, rows, crlf=crlf, final_newline=final_newline)
+    _same(bh.read_csv_gpu(f), bh.read_csv(f))
+
+
+def test_gpu_reader_empty_and_header_only(bh, tmp_path):
+    for text in (b"", HEADER.encode(), (HEADER + "\n").encode()):
+        f = tmp_path / "h.csv"
+        f.write_bytes(text)
+        assert len(bh.read_csv_gpu(f)[0]) == 0
+    with pytest.raises(bh.BhError):
+        bh.read_csv_gpu(tmp_path / "missing.csv")
+
+
+def test_load_csv_into_context(bh, tmp_path, golden):
+    """bh_load_csv fills the context's state without host arrays: the same
+    bodies as the host reader; a context too small is refused."""
+    g = golden("synthetic_19054.npz")
+    f = tmp_path / "s.csv"
+    bh.write_csv(f, g["ids"], g["mass"], g["pos"], g["vel"])
+    ids, mass, pos, vel = bh.read_csv(f)
+    with bh.Context(len(mass)) as ctx:
+        assert ctx.load_csv(f) == len(mass)
+        p, v, m, i, a = ctx.get_bodies()
+        assert_bits_equal(p, pos, "pos"); assert_bits_equal(v, vel, "vel")
+        assert_bits_equal(m, mass, "mass"); assert_bits_equal(i, ids, "ids")
+        assert ctx.load_csv(f, 100) == 100
+    with bh.Context(1000) as small:
+        with pytest.raises(bh.BhError):
+            small.load_csv(f)
