@@ -36,7 +36,8 @@ and seeded (the reference's 300k CSV is not part of its repository).
   as one span, with the final error and the energy/angular-momentum drift.
 * let_exchange: the locally essential tree export and import at 4M bodies
   split over 8 ranks, against the oracle on the host cores.
-  --no-north-star skips these five blocks.
+* csv_ingest: readCSV of a 1M-body file on the GPU against the host reader.
+  --no-north-star skips these six blocks.
 
 Multi-GPU: the path does not shard on one GPU per rank; ranks run replicas
 (weak scaling) and value is the sum of their body-steps over the slowest
@@ -607,6 +608,38 @@ def let_exchange(args, dev):
             "cpu_kind": kind, "timing": "host clock around the C-ABI call, results copied to the host"}
 
 
+def csv_ingest(args, dev, n=1_000_000):
+    """readCSV at 1M bodies: the state-vector CSV written once, then parsed
+    on the GPU straight into a context (bh_load_csv) and by the host reader
+    (std::getline + std::stod, one pass); the values are compared bit for
+    bit.  Host clock; the file is in the page cache for both."""
+    import tempfile
+    bh = importlib.import_module("barnes-hut_gb300")
+    pos, vel, mass, ids = bh.generate_system(SEED + 4, n, 0.10, 0.05)
+    with tempfile.TemporaryDirectory() as d:
+        f = Path(d) / "bodies.csv"
+        bh.write_csv(f, ids, mass, pos, vel)
+        size = f.stat().st_size
+        with bh.Context(n, dev) as ctx:
+            ctx.load_csv(f, 10)
+            t0 = time.perf_counter()
+            ctx.load_csv(f)
+            t_gpu = time.perf_counter() - t0
+            gp, gv, gm, gi, _ = ctx.get_bodies()
+        lib = bh.library()
+        import ctypes as C
+        hi = np.empty(n, np.uint64); hm = np.empty(n); hp = np.empty((n, 3)); hv = np.empty((n, 3))
+        k = C.c_int64(0)
+        t0 = time.perf_counter()
+        lib.bh_read_csv(str(f).encode(), -1, C.byref(k), hi.ctypes.data_as(C.c_void_p), hm.ctypes.data_as(C.c_void_p),
+                        hp.ctypes.data_as(C.c_void_p), hv.ctypes.data_as(C.c_void_p))
+        t_host = time.perf_counter() - t0
+    same = all(np.array_equal(np.ascontiguousarray(a).view(np.uint8), np.ascontiguousarray(b).view(np.uint8))
+               for a, b in ((gp, hp), (gv, hv), (gm, hm), (gi, hi)))
+    return {"bodies": n, "file_mb": size / 1e6, "gpu_load_csv_s": t_gpu, "host_read_csv_s": t_host,
+            "bits_equal": bool(same), "timing": "host clock, file in the page cache"}
+
+
 def hbm_peak_gbs():
     try:
         return float(json.loads((Path(__file__).resolve().parent / "MEASURED_PEAKS.json").read_text())["hbm_gbs"])
@@ -701,13 +734,14 @@ def run_ours(args, rank, ws, local):
     accuracy = {"median_rel_err": float(np.median(err)), "p99_rel_err": float(np.quantile(err, 0.99)),
                 "sample": int(len(sample)), "judge": "FP64 direct sum"}
 
-    ns = pr = le = runs = let = None
+    ns = pr = le = runs = let = ingest = None
     if rank == 0 and ws == 1 and not args.no_north_star:
         params, scale, info = train_model(args)
         ns = north_star(args, dev, params, scale, info)
         le = learned_eval(args, dev, params, scale)
         pr = precision_run(args, dev)
         let = let_exchange(args, dev)
+        ingest = csv_ingest(args, dev)
         runs = {"config2_300k_fp64_list_2000_steps": long_run(dev, N_BODIES, 0.10, 0.0, SEED, "fp64_list", 2000),
                 "config5_4m_fp32_learned_500_steps": long_run(dev, args.ns_bodies, 0.10, 0.05, SEED + 1, "learned",
                                                               500, params, scale, 1e-6, args.theta_max)}
@@ -753,6 +787,7 @@ def run_ours(args, rank, ws, local):
         "precision_run": pr,
         "long_runs": runs,
         "let_exchange": let,
+        "csv_ingest": ingest,
     }
     print(json.dumps(line), flush=True)
 
