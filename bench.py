@@ -23,7 +23,7 @@ and seeded (the reference's 300k CSV is not part of its repository).
   every host core) on the same workload, a bounded number of steps.
 * hbm_phases: achieved GB/s of the data-movement phases (algorithmic bytes
   per body / phase time) against the measured HBM copy bandwidth.
-* the benchmark spec: 4M bodies (85/10/5 with trojans), plain FP64 theta = 1.05
+* forms_4m: 4M bodies (85/10/5 with trojans), plain FP64 theta = 1.05
   against FP32 far field and FP32 + learned criterion (network trained first
   on 20 seeded 1M-body systems, ~10M pairs, by the engine's GPU kernels).
 * learned_eval: the learned criterion on 5 unseen 1M-body systems at budgets
@@ -37,7 +37,7 @@ and seeded (the reference's 300k CSV is not part of its repository).
 * let_exchange: the locally essential tree export and import at 4M bodies
   split over 8 ranks, against the oracle on the host cores.
 * csv_ingest: readCSV of a 1M-body file on the GPU against the host reader.
-  --no-north-star skips these six blocks.
+  --no-extras skips these six blocks.
 
 Multi-GPU: the path does not shard on one GPU per rank; ranks run replicas
 (weak scaling) and value is the sum of their body-steps over the slowest
@@ -97,7 +97,7 @@ def parse():
     ap.add_argument("--e2e-steps", type=int, default=5)
     ap.add_argument("--cpu-seconds", type=float, default=15.0, help="budget of the CPU-baseline sample")
     ap.add_argument("--no-cpu-baseline", action="store_true")
-    ap.add_argument("--no-north-star", action="store_true",
+    ap.add_argument("--no-extras", action="store_true",
                     help="skip the 4M-body comparison, the learned evaluation and the 1M precision run")
     ap.add_argument("--ns-bodies", type=int, default=4_000_000)
     ap.add_argument("--ns-steps", type=int, default=3)
@@ -430,7 +430,7 @@ def learned_eval(args, dev, params, scale):
             "mean_over_seeds": summary, "per_seed": rows}
 
 
-def north_star(args, dev, params, scale, info):
+def forms_4m(args, dev, params, scale, info):
     """The 4M-body combined-scale system (85 % inner belt, 10 % outer belt, 5 %
     trojans): plain FP64 theta=1.05 (fp64_list: the reference's interaction
     set in FP64) against FP32 far field and FP32 + learned criterion, each
@@ -732,12 +732,12 @@ def run_ours(args, rank, ws, local):
     acc = ctx.compute_accelerations(theta, G, 0.0, mode)
     err = np.linalg.norm(acc[sample] - ref, axis=1) / np.linalg.norm(ref, axis=1)
     accuracy = {"median_rel_err": float(np.median(err)), "p99_rel_err": float(np.quantile(err, 0.99)),
-                "sample": int(len(sample)), "judge": "FP64 direct sum"}
+                "sample": int(len(sample)), "against": "FP64 direct sum"}
 
     ns = pr = le = runs = let = ingest = None
-    if rank == 0 and ws == 1 and not args.no_north_star:
+    if rank == 0 and ws == 1 and not args.no_extras:
         params, scale, info = train_model(args)
-        ns = north_star(args, dev, params, scale, info)
+        ns = forms_4m(args, dev, params, scale, info)
         le = learned_eval(args, dev, params, scale)
         pr = precision_run(args, dev)
         let = let_exchange(args, dev)
@@ -782,7 +782,7 @@ def run_ours(args, rank, ws, local):
         "gpu_launches": launches,
         "clocks": clk.summary(),
         "cpu_baseline": cpu,
-        "north_star": ns,
+        "forms_4m": ns,
         "learned_eval": le,
         "precision_run": pr,
         "long_runs": runs,

@@ -788,7 +788,7 @@ int orc_simulate(int64_t n, double *pos, double *vel, double *mass, uint64_t *id
 
 /* ------------------------------------------------------------------ */
 /* FP64 direct sum over all sources for a sample of target bodies       */
-/* (no reference counterpart; the judge of every force error).          */
+/* (no reference counterpart; the yardstick of every force error).      */
 /* Self-exclusion is by index.                                          */
 /* ------------------------------------------------------------------ */
 void orc_direct_sum(int64_t n, const double *pos, const double *mass, int64_t ns, const int64_t *targets,

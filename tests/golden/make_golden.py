@@ -64,7 +64,7 @@ import numpy as np
 
 ROOT = Path(__file__).resolve().parents[2]
 sys.path.insert(0, str(ROOT))
-from oracle.oracle import Oracle, build_reference  # noqa: E402
+from oracle.oracle import REF_SRC, Oracle, build_reference  # noqa: E402
 
 HERE = Path(__file__).resolve().parent
 G = 1.48812e-34
@@ -325,7 +325,7 @@ def config1_fixture(ref):
 
 def scenario_fixture(ref, bh):
     # The reference's own scenario-1 CSV: digests only.
-    csv = Path("/root/reference/data/state_vectors_csvs/scenario1_19054.csv")
+    csv = REF_SRC / "data" / "state_vectors_csvs" / "scenario1_19054.csv"
     if csv.exists():
         ids, mass, pos, vel = bh.read_csv(csv)
         s = stages(ref, pos, vel, mass, ids)

@@ -118,7 +118,9 @@ def test_step_count_semantics(port, golden):
     assert steps == 241
 
 
-REF_CSV = Path("/root/reference/data/state_vectors_csvs/scenario1_19054.csv")
+from oracle.oracle import REF_SRC  # noqa: E402  (where the reference checkout lives, if anywhere)
+
+REF_CSV = REF_SRC / "data" / "state_vectors_csvs" / "scenario1_19054.csv"
 
 
 @pytest.mark.skipif(not REF_CSV.exists(), reason="the reference checkout is not on this host")
@@ -137,7 +139,7 @@ def test_scenario1_csv_digests(port, bh):
     assert digest(acc) == info["acc_digest"]
 
 
-@pytest.mark.skipif(not Path("/root/reference/src/traversal.cpp").exists(), reason="reference checkout absent")
+@pytest.mark.skipif(not (REF_SRC / "src" / "traversal.cpp").exists(), reason="reference checkout absent")
 def test_port_equals_compiled_reference_random(port):
     """Random systems, several theta: the port and the compiled reference agree bit for bit."""
     from oracle.oracle import Oracle, build_reference
