@@ -278,3 +278,50 @@ def test_let_forces_match_oracle_bits(bh, port):
         assert_bits_equal(a, b, "local tree")
     # the imported records move the forces by about the remote share
     assert np.median(np.linalg.norm(got[0] - plain, axis=1) / np.linalg.norm(plain, axis=1)) > 1e-9
+
+
+def test_let_edge_cases_match_oracle(bh, port):
+    """Small and degenerate inputs against the oracle: one body, two bodies
+    with one key, max_depth 0 and 1, no boxes, a box around everything,
+    records at depth 0 and at depth 21, a record with zero mass."""
+    rng = np.random.default_rng(5)
+    systems = {
+        "one": (np.array([[0.5, -0.25, 0.125]]), np.array([2.0e20])),
+        "two_same_key": (np.array([[1.0, 1.0, 1.0], [1.0, 1.0, 1.0 + 1e-15], [-3.0, 2.0, 0.5]]),
+                         np.array([1e18, 2e18, 3e18])),
+        "cluster": (rng.normal(0, 1, (500, 3)), rng.uniform(1e15, 1e20, 500)),
+    }
+    for name, (pos, mass) in systems.items():
+        n = len(mass)
+        vel = np.zeros((n, 3)); ids = np.arange(n, dtype=np.uint64)
+        bb = port.bbox(pos) if n > 1 else np.array([0.0, -1.0, -1.0, 1.0, 1.0, 1.0])
+        keys = port.keys(pos, bb)
+        sk, sp, sm, _, _, _ = port.sort(keys, pos, mass, vel, ids)
+        tree = port.tree(sk, sp, sm, merge=False)
+        box_sets = [np.array([[5.0, 5.0, 5.0, 6.0, 6.0, 6.0]]), np.array([[-9.0, -9.0, -9.0, 9.0, 9.0, 9.0]]),
+                    np.zeros((0, 6))]
+        with _local_ctx(bh, pos, vel, mass, ids, bb) as ctx:
+            for boxes in box_sets:
+                for theta, md in ((1.05, 21), (0.3, 0), (0.3, 1), (2.0, 25)):
+                    got = _sorted(*ctx.let_export(boxes, bb, theta * theta, md))
+                    want = port.let_export(tree, boxes, bb, theta * theta, md)
+                    for a, b, what in zip(got, want, ("prefix", "depth", "mass", "com")):
+                        assert_bits_equal(a, b, f"{name} {len(boxes)} boxes theta {theta} max_depth {md}: {what}")
+            recs = [
+                (np.array([0], np.uint64), np.array([0], np.uint8), np.array([5e19]), np.array([[3.0, 3.0, 3.0]])),
+                (np.array([sk[0]], np.uint64), np.array([21], np.uint8), np.array([1e19]), sp[:1] + 1e-3),
+                (np.array([0, sk[-1]], np.uint64), np.array([0, 21], np.uint8), np.array([0.0, 4e19]),
+                 np.array([[1.0, 1.0, 1.0], [-1.0, 0.0, 2.0]])),
+            ]
+            for r in recs:
+                t = port.pseudo_tree(*r)
+                want_map = t.records()
+                t.close()
+                got_map = ctx.pseudo_leaf_tree(*r)
+                for a, b, what in zip(got_map, want_map, ("prefix", "depth", "mass", "com")):
+                    assert_bits_equal(a, b, f"{name} pseudo map {what}")
+                for direct in (False, True):
+                    got = ctx.let_accelerations(*r, theta=1.05, direct=direct)
+                    want = port.let_accelerations(tree, r, sk, sp, 1.05, 1.48812e-34, bb, direct=direct)
+                    assert_bits_equal(got, want, f"{name} LET forces direct={direct}")
+        tree.close()
