@@ -22,6 +22,7 @@
 #include "bh_internal.cuh"
 
 #include <algorithm>
+#include <cmath>
 #include <cstring>
 
 namespace {
@@ -48,11 +49,25 @@ __device__ __forceinline__ uint32_t cell_axis(uint64_t prefix, int d, int axis)
     return v;
 }
 
+// FP32 prescreen of the box tests.  With every coordinate of the cell, the
+// boxes and the global box at most M in magnitude (2^-20 < M < 2^40), each
+// FP32 separation e_f lies within 2^-22 M of the exact one (the two operand
+// roundings, 2^-24 M each, and the FP32 subtraction's, 2^-23 M) and the
+// reference's FP64 separation within 2^-52 M of it, so within delta =
+// 2^-21 M of each other; the FP32 squares, sums and products stay within
+// 2^-20 relative.  A test is decided in FP32 when s^2 clears theta^2 d^2 by
+// those margins either way, and in FP64 otherwise.
+struct LetScreen {
+    int on;         // 0: every test in FP64
+    float delta;    // 2^-21 M
+    float theta2f;  // (float) theta2
+};
+
 // Whether the cell (prefix, d) fails the opening test against any of the nb
 // remote boxes; warp-uniform result.  Cell box: size = span / 2^d,
 // min = gmin + (ix * 2^-d) * span, max = min + size (all RN).
-__device__ bool cell_opens(uint64_t prefix, int d, const LetGeom& g, const double* __restrict__ boxes, int nb,
-                           double theta2, int lane)
+__device__ bool cell_opens(uint64_t prefix, int d, const LetGeom& g, const double* __restrict__ boxes,
+                           const float* __restrict__ boxf, int nb, double theta2, LetScreen sc, int lane)
 {
     const double scale = 1.0 / (double)(1ull << d);  // exact
     const double div = (double)(1 << d);
@@ -67,17 +82,46 @@ __device__ bool cell_opens(uint64_t prefix, int d, const LetGeom& g, const doubl
     s = ref_max(s, __dsub_rn(hi[1], lo[1]));
     s = ref_max(s, __dsub_rn(hi[2], lo[2]));
     const double s2 = __dmul_rn(s, s);
+    const float s2f = (float)s2;
+    float lof[3], hif[3];
+#pragma unroll
+    for (int a = 0; a < 3; ++a) {
+        lof[a] = (float)lo[a];
+        hif[a] = (float)hi[a];
+    }
+    constexpr float kUp = 1.0f + 0x1p-20f, kDn = 1.0f - 0x1p-20f;
     for (int k0 = 0; k0 < nb; k0 += 32) {
         const int k = k0 + lane;
         bool f = false;
         if (k < nb) {
-            const double* r = boxes + 6 * (int64_t)k;
-            double e[3];
+            bool decided = false;
+            if (sc.on) {
+                const float* rf = boxf + 6 * (int64_t)k;
+                float dlo = 0.0f, dhi = 0.0f;
 #pragma unroll
-            for (int a = 0; a < 3; ++a)
-                e[a] = ref_max(0.0, ref_max(__dsub_rn(lo[a], __ldg(r + 3 + a)), __dsub_rn(__ldg(r + a), hi[a])));
-            const double d2 = __dadd_rn(__dadd_rn(__dmul_rn(e[0], e[0]), __dmul_rn(e[1], e[1])), __dmul_rn(e[2], e[2]));
-            f = s2 >= __dmul_rn(theta2, d2);
+                for (int a = 0; a < 3; ++a) {
+                    const float ef = fmaxf(0.0f, fmaxf(lof[a] - __ldg(rf + 3 + a), __ldg(rf + a) - hif[a]));
+                    const float l = fmaxf(ef - sc.delta, 0.0f), h = ef + sc.delta;
+                    dlo = fmaf(l, l, dlo);
+                    dhi = fmaf(h, h, dhi);
+                }
+                if (s2f * kDn >= sc.theta2f * dhi * kUp) {
+                    f = true;
+                    decided = true;
+                } else if (s2f * kUp < sc.theta2f * dlo * kDn) {
+                    decided = true;
+                }
+            }
+            if (!decided) {
+                const double* r = boxes + 6 * (int64_t)k;
+                double e[3];
+#pragma unroll
+                for (int a = 0; a < 3; ++a)
+                    e[a] = ref_max(0.0, ref_max(__dsub_rn(lo[a], __ldg(r + 3 + a)), __dsub_rn(__ldg(r + a), hi[a])));
+                const double d2 =
+                    __dadd_rn(__dadd_rn(__dmul_rn(e[0], e[0]), __dmul_rn(e[1], e[1])), __dmul_rn(e[2], e[2]));
+                f = s2 >= __dmul_rn(theta2, d2);
+            }
         }
         if (__any_sync(0xffffffffu, f)) return true;
     }
@@ -94,9 +138,10 @@ __global__ void let_seed_kernel(int32_t* __restrict__ q0, int32_t* __restrict__ 
 // next level's nodes.
 __global__ void __launch_bounds__(kLetThreads) let_level_kernel(
     const bh::TreeRec* __restrict__ rec, const int32_t* __restrict__ slot_ref, const int32_t* __restrict__ node_a,
-    const uint64_t* __restrict__ leaf_key, const double* __restrict__ boxes, int nb, LetGeom g, double theta2,
-    int max_depth, const int32_t* __restrict__ q_in, const int32_t* __restrict__ cnt_in, int32_t* __restrict__ q_out,
-    int32_t* __restrict__ cnt_out, int32_t* __restrict__ keep)
+    const uint64_t* __restrict__ leaf_key, const double* __restrict__ boxes, const float* __restrict__ boxf, int nb,
+    LetGeom g, double theta2, LetScreen sc, int max_depth, const int32_t* __restrict__ q_in,
+    const int32_t* __restrict__ cnt_in, int32_t* __restrict__ q_out, int32_t* __restrict__ cnt_out,
+    int32_t* __restrict__ keep)
 {
     const int lane = threadIdx.x & 31;
     const int count = *cnt_in;
@@ -109,7 +154,7 @@ __global__ void __launch_bounds__(kLetThreads) let_level_kernel(
         int kept = -1;
         bool descend = false;
         for (int d = r.top;; ++d) {
-            const bool opens = cell_opens(key & bh::prefix_mask(d), d, g, boxes, nb, theta2, lane);
+            const bool opens = cell_opens(key & bh::prefix_mask(d), d, g, boxes, boxf, nb, theta2, sc, lane);
             if (!opens || d >= max_depth) { kept = d; break; }
             if (d < r.depth) continue;
             descend = r.nchild > 0;
@@ -160,7 +205,7 @@ __global__ void let_write_kernel(const int32_t* __restrict__ counts, const int32
 // remote boxes and the per-level counts; grown on demand, kept with the
 // context.
 struct LetLayout {
-    size_t q0, q1, keep, flag, prefix, depth, mass, com, boxes, cnt, total;
+    size_t q0, q1, keep, flag, prefix, depth, mass, com, boxes, boxf, cnt, total;
 };
 
 LetLayout let_layout(int64_t S, int64_t nb)
@@ -177,6 +222,7 @@ LetLayout let_layout(int64_t S, int64_t nb)
     L.mass = o; o += up(sizeof(double) * S);
     L.com = o; o += up(3 * sizeof(double) * S);
     L.boxes = o; o += up(6 * sizeof(double) * nb);
+    L.boxf = o; o += up(6 * sizeof(float) * nb);
     L.cnt = o; o += up(sizeof(int32_t) * (kLetLevels + 2));
     L.total = o;
     return L;
@@ -406,6 +452,7 @@ int bh_let_export(bh_context* ctx, const double* boxes, int64_t nboxes, const do
     double* o_mass = reinterpret_cast<double*>(base + L.mass);
     double* o_com = reinterpret_cast<double*>(base + L.com);
     double* d_boxes = reinterpret_cast<double*>(base + L.boxes);
+    float* d_boxf = reinterpret_cast<float*>(base + L.boxf);
     int32_t* cnt = reinterpret_cast<int32_t*>(base + L.cnt);
 
     LetGeom g;
@@ -414,6 +461,25 @@ int bh_let_export(bh_context* ctx, const double* boxes, int64_t nboxes, const do
         g.span[a] = bbox[3 + a] - bbox[a];
     }
     BH_CUDA_TRY(cudaMemcpyAsync(d_boxes, boxes, sizeof(double) * 6 * nboxes, cudaMemcpyHostToDevice, st));
+    // The FP32 prescreen's copies and bound (see LetScreen).
+    std::vector<float> hf((size_t)(6 * nboxes));
+    double mag = 0.0;
+    bool finite = true;
+    for (int64_t k = 0; k < 6 * nboxes; ++k) {
+        hf[(size_t)k] = (float)boxes[k];
+        finite = finite && std::isfinite(boxes[k]);
+        mag = std::max(mag, std::fabs(boxes[k]));
+    }
+    for (int a = 0; a < 6; ++a) {
+        finite = finite && std::isfinite(bbox[a]);
+        mag = std::max(mag, std::fabs(bbox[a]));
+    }
+    LetScreen sc{0, 0.0f, (float)theta2};
+    if (finite && theta2 >= 0.0 && theta2 < 1e30 && mag > 0x1p-20 && mag < 0x1p40) {
+        sc.on = 1;
+        sc.delta = (float)(mag * 0x1p-21);
+    }
+    BH_CUDA_TRY(cudaMemcpyAsync(d_boxf, hf.data(), sizeof(float) * 6 * nboxes, cudaMemcpyHostToDevice, st));
     BH_CUDA_TRY(cudaMemsetAsync(keep, 0xff, sizeof(int32_t) * S, st));
     BH_CUDA_TRY(cudaMemsetAsync(cnt, 0, sizeof(int32_t) * (kLetLevels + 2), st));
     let_seed_kernel<<<1, 1, 0, st>>>(q[0], cnt);
@@ -426,8 +492,8 @@ int bh_let_export(bh_context* ctx, const double* boxes, int64_t nboxes, const do
     // 21, so kLetLevels launches drain every frontier.
     for (int lv = 0; lv < kLetLevels; ++lv) {
         let_level_kernel<<<grid, kLetThreads, 0, st>>>(ctx->rec, ctx->slot_ref, ctx->node_a, ctx->leaf_key, d_boxes,
-                                                       (int)nboxes, g, theta2, max_depth, q[lv & 1], cnt + lv,
-                                                       q[(lv + 1) & 1], cnt + lv + 1, keep);
+                                                       d_boxf, (int)nboxes, g, theta2, sc, max_depth, q[lv & 1],
+                                                       cnt + lv, q[(lv + 1) & 1], cnt + lv + 1, keep);
         BH_LAUNCH_CHECK(ctx);
     }
     const int sgrid = (int)std::min<int64_t>((S + 255) / 256, (int64_t)dev_sms * 16);

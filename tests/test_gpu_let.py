@@ -298,11 +298,17 @@ def test_let_edge_cases_match_oracle(bh, port):
         keys = port.keys(pos, bb)
         sk, sp, sm, _, _, _ = port.sort(keys, pos, mass, vel, ids)
         tree = port.tree(sk, sp, sm, merge=False)
+        # boxes at exactly one root side from the root cell and from a
+        # depth-3 cell (ties of s^2 >= theta^2 d^2 at theta = 1, decided by
+        # the FP64 test behind the FP32 prescreen)
+        side = max(bb[3] - bb[0], bb[4] - bb[1], bb[5] - bb[2])
+        tie = np.array([[bb[3] + side, bb[1], bb[2], bb[3] + 2 * side, bb[4], bb[5]],
+                        [bb[0], bb[1], bb[2] - side / 8 - (bb[5] - bb[2]) / 8, bb[3], bb[4], bb[2] - side / 8]])
         box_sets = [np.array([[5.0, 5.0, 5.0, 6.0, 6.0, 6.0]]), np.array([[-9.0, -9.0, -9.0, 9.0, 9.0, 9.0]]),
-                    np.zeros((0, 6))]
+                    np.zeros((0, 6)), tie]
         with _local_ctx(bh, pos, vel, mass, ids, bb) as ctx:
             for boxes in box_sets:
-                for theta, md in ((1.05, 21), (0.3, 0), (0.3, 1), (2.0, 25)):
+                for theta, md in ((1.05, 21), (0.3, 0), (0.3, 1), (2.0, 25), (1.0, 21)):
                     got = _sorted(*ctx.let_export(boxes, bb, theta * theta, md))
                     want = port.let_export(tree, boxes, bb, theta * theta, md)
                     for a, b, what in zip(got, want, ("prefix", "depth", "mass", "com")):
