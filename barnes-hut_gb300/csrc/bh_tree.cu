@@ -332,8 +332,12 @@ __global__ void monopole_level_kernel(int depth, const int32_t* __restrict__ dep
         }
         nm[b] = sm; nwx[b] = sx; nwy[b] = sy; nwz[b] = sz;
         if (kMoments) {
+            // m_c |c_c - c|^2 = |w_c - m_c c|^2 / m_c: u = w_c - m_c c by FMA
+            // keeps the cancellation in FP64; the division by m_c needs only
+            // the feature's precision (an FP32 reciprocal, 2^-22).  Masses
+            // are >= 0, so "> 0" is a test on the bit pattern.
             double q = 0.0;
-            if (sm > 0) {
+            if (__double_as_longlong(sm) > 0) {
                 const double is = rcp_nr(sm);
                 const double gx = sx * is, gy = sy * is, gz = sz * is;
                 for (int s = s0; s < s1; ++s) {
@@ -341,10 +345,10 @@ __global__ void monopole_level_kernel(int depth, const int32_t* __restrict__ dep
                     double cm, wx, wy, wz, cq;
                     if (r >= 0) { cm = lm[r]; wx = lwx[r]; wy = lwy[r]; wz = lwz[r]; cq = lq[r]; }
                     else { const int c = ~r; cm = nm[c]; wx = nwx[c]; wy = nwy[c]; wz = nwz[c]; cq = nq[c]; }
-                    if (cm > 0) {
-                        const double ic = rcp_nr(cm);
-                        const double dx = wx * ic - gx, dy = wy * ic - gy, dz = wz * ic - gz;
-                        q += cq + cm * (dx * dx + dy * dy + dz * dz);
+                    if (__double_as_longlong(cm) > 0) {
+                        const double ux = fma(-cm, gx, wx), uy = fma(-cm, gy, wy), uz = fma(-cm, gz, wz);
+                        const double uu = fma(ux, ux, fma(uy, uy, uz * uz));
+                        q += cq + uu * widen(__frcp_rn(narrow_trunc(cm)));
                     }
                 }
             }
@@ -460,10 +464,10 @@ __global__ void finalize_kernel(const int32_t* __restrict__ counts, const int32_
             far.meta[s] = (uint32_t)o.nchild | ((uint32_t)o.depth << 8) | ((leaf ? 1u : 0u) << 16) |
                           ((o.m == 0.0 ? 1u : 0u) << 17);
         }
-        if (kMoments) {
+        if (kMoments) {  // a feature: FP32 after narrowing on the bit patterns
             const double m = r >= 0 ? lm[r] : nm[~r];
             const double q = r >= 0 ? lq[r] : nq[~r];
-            spread[s] = m > 0 ? sqrtf((float)(q * rcp_nr(m))) : 0.0f;
+            spread[s] = __double_as_longlong(m) > 0 ? sqrtf(narrow_trunc(q) * __frcp_rn(narrow_trunc(m))) : 0.0f;
         }
     }
 }
