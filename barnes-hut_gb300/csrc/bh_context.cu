@@ -96,10 +96,7 @@ void layout(bh_context* ctx, Carver& c)
     ctx->leaf_first = c.take<int32_t>(n + 1);
     ctx->body_leaf = c.take<int32_t>(n);
     ctx->leaf_key = c.take<uint64_t>(n);
-    ctx->leaf_m = c.take<double>(n);
-    ctx->leaf_wx = c.take<double>(n);
-    ctx->leaf_wy = c.take<double>(n);
-    ctx->leaf_wz = c.take<double>(n);
+    ctx->leaf_s = c.take<double4_32a>(n);
     ctx->cdep = c.take<int8_t>(n);
     ctx->rep_node = c.take<int32_t>(n);
     ctx->node_rep = c.take<int32_t>(n);
@@ -107,10 +104,7 @@ void layout(bh_context* ctx, Carver& c)
     ctx->node_nchild = c.take<int32_t>(n);
     ctx->node_cs = c.take<int32_t>(n);
     ctx->node_depth = c.take<uint8_t>(n);
-    ctx->node_m = c.take<double>(n);
-    ctx->node_wx = c.take<double>(n);
-    ctx->node_wy = c.take<double>(n);
-    ctx->node_wz = c.take<double>(n);
+    ctx->node_s = c.take<double4_32a>(n);
     ctx->slot_ref = c.take<int32_t>(2 * n);
     ctx->slot_top = c.take<uint8_t>(2 * n);
     ctx->depth_off = c.take<int32_t>(32);

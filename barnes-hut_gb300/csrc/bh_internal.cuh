@@ -303,7 +303,7 @@ struct bh_context {
     int32_t* leaf_first = nullptr;  // first body of each leaf, n + 1
     int32_t* body_leaf = nullptr;   // leaf id of each body
     uint64_t* leaf_key = nullptr;
-    double *leaf_m = nullptr, *leaf_wx = nullptr, *leaf_wy = nullptr, *leaf_wz = nullptr;
+    double4_32a* leaf_s = nullptr;  // leaf sums {m x, m y, m z, m}
     int8_t* cdep = nullptr;         // common depth of leaves j-1, j (boundary j)
     int32_t* rep_node = nullptr;    // branching-node id of a representative boundary
     int32_t* node_rep = nullptr;    // representative boundary of each node
@@ -311,7 +311,7 @@ struct bh_context {
     int32_t* node_nchild = nullptr;
     int32_t* node_cs = nullptr;     // first child slot
     uint8_t* node_depth = nullptr;
-    double *node_m = nullptr, *node_wx = nullptr, *node_wy = nullptr, *node_wz = nullptr;
+    double4_32a* node_s = nullptr;  // branching-node sums {m x, m y, m z, m}
     int32_t* slot_ref = nullptr;    // >= 0 leaf id, < 0 ~node id
     uint8_t* slot_top = nullptr;
     int32_t* depth_off = nullptr;   // 23 offsets into depth_nodes (by depth)

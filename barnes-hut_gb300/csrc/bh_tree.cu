@@ -115,8 +115,7 @@ template <bool kMoments>
 __global__ void leaf_sum_kernel(const int32_t* __restrict__ counts, const int32_t* __restrict__ leaf_first,
                                 const uint64_t* __restrict__ leaf_key, const double* __restrict__ px,
                                 const double* __restrict__ py, const double* __restrict__ pz,
-                                const double* __restrict__ m, double* __restrict__ lm, double* __restrict__ lwx,
-                                double* __restrict__ lwy, double* __restrict__ lwz, int8_t* __restrict__ cdep,
+                                const double* __restrict__ m, double4_32a* __restrict__ ls, int8_t* __restrict__ cdep,
                                 double* __restrict__ lq)
 {
     const int L = counts[0];
@@ -130,7 +129,7 @@ __global__ void leaf_sum_kernel(const int32_t* __restrict__ counts, const int32_
             sy = __dadd_rn(sy, __dmul_rn(py[b], mb));
             sz = __dadd_rn(sz, __dmul_rn(pz[b], mb));
         }
-        lm[l] = sm; lwx[l] = sx; lwy[l] = sy; lwz[l] = sz;
+        ls[l] = double4_32a{sx, sy, sz, sm};
         cdep[l] = l == 0 ? (int8_t)-1 : (int8_t)common_depth(leaf_key[l - 1], leaf_key[l]);
         if (kMoments) {
             double q = 0.0;
@@ -309,10 +308,8 @@ template <bool kMoments>
 __global__ void monopole_level_kernel(int depth, const int32_t* __restrict__ depth_off,
                                       const int32_t* __restrict__ depth_nodes, const int32_t* __restrict__ node_cs,
                                       const int32_t* __restrict__ node_nchild, const int32_t* __restrict__ slot_ref,
-                                      const double* __restrict__ lm, const double* __restrict__ lwx,
-                                      const double* __restrict__ lwy, const double* __restrict__ lwz,
-                                      double* __restrict__ nm, double* __restrict__ nwx, double* __restrict__ nwy,
-                                      double* __restrict__ nwz, const double* __restrict__ lq,
+                                      const double4_32a* __restrict__ ls, double4_32a* __restrict__ ns,
+                                      const double* __restrict__ lq,
                                       double* __restrict__ nq)
 {
     const int lo = depth_off[depth], hi = depth_off[depth + 1];
@@ -322,15 +319,13 @@ __global__ void monopole_level_kernel(int depth, const int32_t* __restrict__ dep
         double sm = 0.0, sx = 0.0, sy = 0.0, sz = 0.0;
         for (int s = s0; s < s1; ++s) {
             const int r = slot_ref[s];
-            double cm, cx, cy, cz;
-            if (r >= 0) { cm = lm[r]; cx = lwx[r]; cy = lwy[r]; cz = lwz[r]; }
-            else { const int c = ~r; cm = nm[c]; cx = nwx[c]; cy = nwy[c]; cz = nwz[c]; }
-            sm = __dadd_rn(sm, cm);
-            sx = __dadd_rn(sx, cx);
-            sy = __dadd_rn(sy, cy);
-            sz = __dadd_rn(sz, cz);
+            const double4_32a v = r >= 0 ? ls[r] : ns[~r];
+            sm = __dadd_rn(sm, v.w);
+            sx = __dadd_rn(sx, v.x);
+            sy = __dadd_rn(sy, v.y);
+            sz = __dadd_rn(sz, v.z);
         }
-        nm[b] = sm; nwx[b] = sx; nwy[b] = sy; nwz[b] = sz;
+        ns[b] = double4_32a{sx, sy, sz, sm};
         if (kMoments) {
             // m_c |c_c - c|^2 = |w_c - m_c c|^2 / m_c: u = w_c - m_c c by FMA
             // keeps the cancellation in FP64; the division by m_c needs only
@@ -342,9 +337,8 @@ __global__ void monopole_level_kernel(int depth, const int32_t* __restrict__ dep
                 const double gx = sx * is, gy = sy * is, gz = sz * is;
                 for (int s = s0; s < s1; ++s) {
                     const int r = slot_ref[s];
-                    double cm, wx, wy, wz, cq;
-                    if (r >= 0) { cm = lm[r]; wx = lwx[r]; wy = lwy[r]; wz = lwz[r]; cq = lq[r]; }
-                    else { const int c = ~r; cm = nm[c]; wx = nwx[c]; wy = nwy[c]; wz = nwz[c]; cq = nq[c]; }
+                    const double4_32a v = r >= 0 ? ls[r] : ns[~r];
+                    const double cm = v.w, wx = v.x, wy = v.y, wz = v.z, cq = r >= 0 ? lq[r] : nq[~r];
                     if (__double_as_longlong(cm) > 0) {
                         const double ux = fma(-cm, gx, wx), uy = fma(-cm, gy, wy), uz = fma(-cm, gz, wz);
                         const double uu = fma(ux, ux, fma(uy, uy, uz * uz));
@@ -412,11 +406,8 @@ struct FarOut {
 
 template <bool kMoments, bool kFar>
 __global__ void finalize_kernel(const int32_t* __restrict__ counts, const int32_t* __restrict__ slot_ref,
-                                const uint8_t* __restrict__ slot_top, const double* __restrict__ lm,
-                                const double* __restrict__ lwx, const double* __restrict__ lwy,
-                                const double* __restrict__ lwz, const double* __restrict__ nm,
-                                const double* __restrict__ nwx, const double* __restrict__ nwy,
-                                const double* __restrict__ nwz, const int32_t* __restrict__ node_cs,
+                                const uint8_t* __restrict__ slot_top, const double4_32a* __restrict__ ls,
+                                const double4_32a* __restrict__ ns, const int32_t* __restrict__ node_cs,
                                 const int32_t* __restrict__ node_nchild, const uint8_t* __restrict__ node_depth,
                                 TreeRec* __restrict__ rec, const double* __restrict__ lq,
                                 const double* __restrict__ nq, float* __restrict__ spread, int merge,
@@ -430,13 +421,14 @@ __global__ void finalize_kernel(const int32_t* __restrict__ counts, const int32_
         o.top = slot_top[s];
         o.pad0 = 0;
         o.pad1 = 0;
+        const double4_32a v = r >= 0 ? ls[r] : ns[~r];
         if (r >= 0) {
             if (kFar) {
-                far_com(lm[r], lwx[r], lwy[r], lwz[r], o);
+                far_com(v.w, v.x, v.y, v.z, o);
             } else {
                 const int b = leaf_first[r];
                 const bool one = leaf_first[r + 1] == b + 1;
-                finish_com(lm[r], lwx[r], lwy[r], lwz[r], o, merge, one, one ? px[b] : 0.0, one ? py[b] : 0.0,
+                finish_com(v.w, v.x, v.y, v.z, o, merge, one, one ? px[b] : 0.0, one ? py[b] : 0.0,
                            one ? pz[b] : 0.0);
             }
             o.child = -1;
@@ -445,8 +437,8 @@ __global__ void finalize_kernel(const int32_t* __restrict__ counts, const int32_
             o.depth = (uint8_t)kMaxDepth;
         } else {
             const int b = ~r;
-            if (kFar) far_com(nm[b], nwx[b], nwy[b], nwz[b], o);
-            else finish_com(nm[b], nwx[b], nwy[b], nwz[b], o, merge, false, 0.0, 0.0, 0.0);
+            if (kFar) far_com(v.w, v.x, v.y, v.z, o);
+            else finish_com(v.w, v.x, v.y, v.z, o, merge, false, 0.0, 0.0, 0.0);
             o.child = node_cs[b] + 1;
             o.leaf = -1;
             o.nchild = (uint8_t)node_nchild[b];
@@ -465,7 +457,7 @@ __global__ void finalize_kernel(const int32_t* __restrict__ counts, const int32_
                           ((o.m == 0.0 ? 1u : 0u) << 17);
         }
         if (kMoments) {  // a feature: FP32 after narrowing on the bit patterns
-            const double m = r >= 0 ? lm[r] : nm[~r];
+            const double m = v.w;
             const double q = r >= 0 ? lq[r] : nq[~r];
             spread[s] = __double_as_longlong(m) > 0 ? sqrtf(narrow_trunc(q) * __frcp_rn(narrow_trunc(m))) : 0.0f;
         }
@@ -498,12 +490,10 @@ int launch_build(bh_context* ctx, const double* mass, bool moments, bool far_fus
     BH_LAUNCH_CHECK(ctx);
     if (moments)
         leaf_sum_kernel<true><<<g, kThreads, 0, st>>>(ctx->counts, ctx->leaf_first, ctx->leaf_key, ctx->px, ctx->py,
-                                                      ctx->pz, mass, ctx->leaf_m, ctx->leaf_wx, ctx->leaf_wy,
-                                                      ctx->leaf_wz, ctx->cdep, ctx->leaf_q);
+                                                      ctx->pz, mass, ctx->leaf_s, ctx->cdep, ctx->leaf_q);
     else
         leaf_sum_kernel<false><<<g, kThreads, 0, st>>>(ctx->counts, ctx->leaf_first, ctx->leaf_key, ctx->px, ctx->py,
-                                                       ctx->pz, mass, ctx->leaf_m, ctx->leaf_wx, ctx->leaf_wy,
-                                                       ctx->leaf_wz, ctx->cdep, ctx->leaf_q);
+                                                       ctx->pz, mass, ctx->leaf_s, ctx->cdep, ctx->leaf_q);
     BH_LAUNCH_CHECK(ctx);
 
     // 2. branching nodes: representative flags -> ids -> ranges/child counts
@@ -539,13 +529,13 @@ int launch_build(bh_context* ctx, const double* mass, bool moments, bool far_fus
     for (int d = kMaxDepth - 1; d >= 0; --d) {
         if (moments)
             monopole_level_kernel<true><<<g, kThreads, 0, st>>>(
-                d, ctx->depth_off, ctx->depth_nodes, ctx->node_cs, ctx->node_nchild, ctx->slot_ref, ctx->leaf_m,
-                ctx->leaf_wx, ctx->leaf_wy, ctx->leaf_wz, ctx->node_m, ctx->node_wx, ctx->node_wy, ctx->node_wz,
+                d, ctx->depth_off, ctx->depth_nodes, ctx->node_cs, ctx->node_nchild, ctx->slot_ref, ctx->leaf_s,
+                ctx->node_s,
                 ctx->leaf_q, ctx->node_q);
         else
             monopole_level_kernel<false><<<g, kThreads, 0, st>>>(
-                d, ctx->depth_off, ctx->depth_nodes, ctx->node_cs, ctx->node_nchild, ctx->slot_ref, ctx->leaf_m,
-                ctx->leaf_wx, ctx->leaf_wy, ctx->leaf_wz, ctx->node_m, ctx->node_wx, ctx->node_wy, ctx->node_wz,
+                d, ctx->depth_off, ctx->depth_nodes, ctx->node_cs, ctx->node_nchild, ctx->slot_ref, ctx->leaf_s,
+                ctx->node_s,
                 ctx->leaf_q, ctx->node_q);
         BH_LAUNCH_CHECK(ctx);
     }
@@ -555,8 +545,8 @@ int launch_build(bh_context* ctx, const double* mass, bool moments, bool far_fus
     const FarOut far{ctx->fA, ctx->fB, ctx->fmeta, G};
 #define BH_FINALIZE(M, F)                                                                                      \
     finalize_kernel<M, F><<<gs, kThreads, 0, st>>>(                                                            \
-        ctx->counts, ctx->slot_ref, ctx->slot_top, ctx->leaf_m, ctx->leaf_wx, ctx->leaf_wy, ctx->leaf_wz,       \
-        ctx->node_m, ctx->node_wx, ctx->node_wy, ctx->node_wz, ctx->node_cs, ctx->node_nchild, ctx->node_depth, \
+        ctx->counts, ctx->slot_ref, ctx->slot_top, ctx->leaf_s, ctx->node_s, ctx->node_cs, ctx->node_nchild,     \
+        ctx->node_depth,                                                                                       \
         ctx->rec, ctx->leaf_q, ctx->node_q, ctx->fspread, ctx->build_merge ? 1 : 0, ctx->leaf_first, ctx->px,  \
         ctx->py, ctx->pz, far)
     if (far_fused) {
