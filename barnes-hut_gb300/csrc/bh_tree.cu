@@ -192,16 +192,20 @@ __global__ void node_children_kernel(const int32_t* __restrict__ counts, const u
                                      const int32_t* __restrict__ rep_node, const int32_t* __restrict__ node_rep,
                                      const int32_t* __restrict__ node_a, const uint8_t* __restrict__ node_depth,
                                      const int32_t* __restrict__ node_cs, int32_t* __restrict__ slot_ref,
-                                     uint8_t* __restrict__ slot_top)
+                                     uint8_t* __restrict__ slot_top, int32_t* __restrict__ leaf_parent,
+                                     int32_t* __restrict__ node_parent)
 {
     const int L = counts[0], B = counts[1];
     const int gid = blockIdx.x * blockDim.x + threadIdx.x;
     if (gid == 0) {
         if (L == 1) {
             slot_ref[0] = 0;
+            leaf_parent[0] = -1;
         } else {
             const int Dr = common_depth(K[0], K[L - 1]);
-            slot_ref[0] = ~rep_node[cell_end(K, L, 0, prefix_mask(Dr + 1))];
+            const int root = rep_node[cell_end(K, L, 0, prefix_mask(Dr + 1))];
+            slot_ref[0] = ~root;
+            node_parent[root] = -1;
         }
         slot_top[0] = 0;
     }
@@ -222,7 +226,90 @@ __global__ void node_children_kernel(const int32_t* __restrict__ counts, const u
             }
             slot_ref[s] = ref;
             slot_top[s] = (uint8_t)(D + 1);
+            if (ref >= 0) leaf_parent[ref] = b;
+            else node_parent[~ref] = b;
             u = v;
+        }
+    }
+}
+
+// One node's sums from its children, in slot (= octant) order from 0.0
+// (linear_octree.cpp:69-87), and with kMoments the second moment by the
+// parallel-axis rule (see below).  Children may have been written by other
+// threads of this launch: loads bypass L1.
+__device__ __forceinline__ double4_32a load_sums(const double4_32a* p)
+{
+    const double2 a = __ldcg(reinterpret_cast<const double2*>(p));
+    const double2 b = __ldcg(reinterpret_cast<const double2*>(p) + 1);
+    return double4_32a{a.x, a.y, b.x, b.y};
+}
+
+template <bool kMoments>
+__device__ void node_sums(int b, const int32_t* __restrict__ node_cs, const int32_t* __restrict__ node_nchild,
+                          const int32_t* __restrict__ slot_ref, const double4_32a* ls, double4_32a* ns,
+                          const double* lq, double* nq)
+{
+    const int s0 = node_cs[b] + 1, s1 = s0 + node_nchild[b];
+    double sm = 0.0, sx = 0.0, sy = 0.0, sz = 0.0;
+    for (int s = s0; s < s1; ++s) {
+        const int r = slot_ref[s];
+        const double4_32a v = load_sums(r >= 0 ? ls + r : ns + ~r);
+        sm = __dadd_rn(sm, v.w);
+        sx = __dadd_rn(sx, v.x);
+        sy = __dadd_rn(sy, v.y);
+        sz = __dadd_rn(sz, v.z);
+    }
+    ns[b] = double4_32a{sx, sy, sz, sm};
+    if (kMoments) {
+        // m_c |c_c - c|^2 = |w_c - m_c c|^2 / m_c: u = w_c - m_c c by FMA
+        // keeps the cancellation in FP64; the division by m_c needs only
+        // the feature's precision (an FP32 reciprocal, 2^-22).  Masses are
+        // >= 0, so "> 0" is a test on the bit pattern.
+        double q = 0.0;
+        if (__double_as_longlong(sm) > 0) {
+            const double is = rcp_nr(sm);
+            const double gx = sx * is, gy = sy * is, gz = sz * is;
+            for (int s = s0; s < s1; ++s) {
+                const int r = slot_ref[s];
+                const double4_32a v = load_sums(r >= 0 ? ls + r : ns + ~r);
+                const double cq = __ldcg(r >= 0 ? lq + r : nq + ~r);
+                if (__double_as_longlong(v.w) > 0) {
+                    const double ux = fma(-v.w, gx, v.x), uy = fma(-v.w, gy, v.y), uz = fma(-v.w, gz, v.z);
+                    const double uu = fma(ux, ux, fma(uy, uy, uz * uz));
+                    q += cq + uu * widen(__frcp_rn(narrow_trunc(v.w)));
+                }
+            }
+        }
+        nq[b] = q;
+    }
+}
+
+constexpr int64_t kUpsweepMaxBodies = 1000000;
+
+// Bottom-up sums without levels: one thread per leaf climbs towards the
+// root; at each node the thread whose arrival completes the node's children
+// (an atomic count) computes the node, the others stop.  No thread waits:
+// each node is computed exactly once, after all its children.  A thread's
+// writes are fenced before its arrival is counted.
+template <bool kMoments>
+__global__ void upsweep_kernel(const int32_t* __restrict__ counts, const int32_t* __restrict__ leaf_parent,
+                               const int32_t* __restrict__ node_parent, const int32_t* __restrict__ node_cs,
+                               const int32_t* __restrict__ node_nchild, const int32_t* __restrict__ slot_ref,
+                               const double4_32a* ls, double4_32a* ns, const double* lq, double* nq,
+                               unsigned* __restrict__ ctr)
+{
+    const int L = counts[0];
+    for (int l = blockIdx.x * blockDim.x + threadIdx.x; l < L; l += gridDim.x * blockDim.x) {
+        int b = leaf_parent[l];
+        bool wrote = false;  // the leaf's sums come from an earlier launch
+        while (b >= 0) {
+            if (wrote) __threadfence();
+            const unsigned arrived = atomicAdd(ctr + b, 1u);
+            if (arrived + 1u != (unsigned)node_nchild[b]) break;
+            __threadfence();
+            node_sums<kMoments>(b, node_cs, node_nchild, slot_ref, ls, ns, lq, nq);
+            wrote = true;
+            b = node_parent[b];
         }
     }
 }
@@ -300,55 +387,17 @@ __global__ void bucket_place_kernel(const int32_t* __restrict__ counts, const ui
     }
 }
 
-// Monopole of the branching nodes at one depth: children summed in key
-// (= octant) order from 0.0 (linear_octree.cpp:69-87).  kMoments: also the
-// second moment by the parallel-axis rule, Q = sum_c (Q_c + m_c |c_c - c|^2)
-// (it reads only the sums above, so the monopole bits are unchanged).
+// Monopole (and second moment) of the branching nodes at one depth, from
+// the sums of the level below (node_sums).
 template <bool kMoments>
 __global__ void monopole_level_kernel(int depth, const int32_t* __restrict__ depth_off,
                                       const int32_t* __restrict__ depth_nodes, const int32_t* __restrict__ node_cs,
                                       const int32_t* __restrict__ node_nchild, const int32_t* __restrict__ slot_ref,
-                                      const double4_32a* __restrict__ ls, double4_32a* __restrict__ ns,
-                                      const double* __restrict__ lq,
-                                      double* __restrict__ nq)
+                                      const double4_32a* ls, double4_32a* ns, const double* lq, double* nq)
 {
     const int lo = depth_off[depth], hi = depth_off[depth + 1];
-    for (int k = lo + blockIdx.x * blockDim.x + threadIdx.x; k < hi; k += gridDim.x * blockDim.x) {
-        const int b = depth_nodes[k];
-        const int s0 = node_cs[b] + 1, s1 = s0 + node_nchild[b];
-        double sm = 0.0, sx = 0.0, sy = 0.0, sz = 0.0;
-        for (int s = s0; s < s1; ++s) {
-            const int r = slot_ref[s];
-            const double4_32a v = r >= 0 ? ls[r] : ns[~r];
-            sm = __dadd_rn(sm, v.w);
-            sx = __dadd_rn(sx, v.x);
-            sy = __dadd_rn(sy, v.y);
-            sz = __dadd_rn(sz, v.z);
-        }
-        ns[b] = double4_32a{sx, sy, sz, sm};
-        if (kMoments) {
-            // m_c |c_c - c|^2 = |w_c - m_c c|^2 / m_c: u = w_c - m_c c by FMA
-            // keeps the cancellation in FP64; the division by m_c needs only
-            // the feature's precision (an FP32 reciprocal, 2^-22).  Masses
-            // are >= 0, so "> 0" is a test on the bit pattern.
-            double q = 0.0;
-            if (__double_as_longlong(sm) > 0) {
-                const double is = rcp_nr(sm);
-                const double gx = sx * is, gy = sy * is, gz = sz * is;
-                for (int s = s0; s < s1; ++s) {
-                    const int r = slot_ref[s];
-                    const double4_32a v = r >= 0 ? ls[r] : ns[~r];
-                    const double cm = v.w, wx = v.x, wy = v.y, wz = v.z, cq = r >= 0 ? lq[r] : nq[~r];
-                    if (__double_as_longlong(cm) > 0) {
-                        const double ux = fma(-cm, gx, wx), uy = fma(-cm, gy, wy), uz = fma(-cm, gz, wz);
-                        const double uu = fma(ux, ux, fma(uy, uy, uz * uz));
-                        q += cq + uu * widen(__frcp_rn(narrow_trunc(cm)));
-                    }
-                }
-            }
-            nq[b] = q;
-        }
-    }
+    for (int k = lo + blockIdx.x * blockDim.x + threadIdx.x; k < hi; k += gridDim.x * blockDim.x)
+        node_sums<kMoments>(depth_nodes[k], node_cs, node_nchild, slot_ref, ls, ns, lq, nq);
 }
 
 // com = w/m when m > 0 (linear_octree.cpp:95-104), then the merge of
@@ -512,32 +561,48 @@ int launch_build(bh_context* ctx, const double* mass, bool moments, bool far_fus
     BH_LAUNCH_CHECK(ctx);
     node_children_kernel<<<g, kThreads, 0, st>>>(ctx->counts, ctx->leaf_key, ctx->rep_node, ctx->node_rep,
                                                  ctx->node_a, ctx->node_depth, ctx->node_cs, ctx->slot_ref,
-                                                 ctx->slot_top);
+                                                 ctx->slot_top, ctx->leaf_parent, ctx->node_parent);
     BH_LAUNCH_CHECK(ctx);
 
-    // 3. depth buckets
-    const int nblk = (int)((n + kBucketThreads - 1) / kBucketThreads);
-    bucket_count_kernel<<<nblk, kBucketThreads, 0, st>>>(ctx->counts, ctx->node_depth, ctx->scan_tmp, nblk);
-    BH_LAUNCH_CHECK(ctx);
-    bucket_scan_kernel<<<1, 1024, 0, st>>>(ctx->scan_tmp, nblk, ctx->depth_off);
-    BH_LAUNCH_CHECK(ctx);
-    bucket_place_kernel<<<nblk, kBucketThreads, 0, st>>>(ctx->counts, ctx->node_depth, ctx->scan_tmp, nblk,
-                                                         ctx->depth_nodes);
-    BH_LAUNCH_CHECK(ctx);
-
-    // 4. level-synchronous monopole pass, deepest level first
-    for (int d = kMaxDepth - 1; d >= 0; --d) {
+    // 3./4. monopoles (and second moments), deepest first.  Below a
+    // million bodies one launch climbs from the leaves (launch overheads
+    // dominate there); above, the level-synchronous pass keeps more loads in
+    // flight.  Both sum each node's children in slot order from 0.0.
+    if (n < kUpsweepMaxBodies) {
+        BH_CUDA_TRY(cudaMemsetAsync(ctx->node_ctr, 0, sizeof(unsigned) * (size_t)n, st));
         if (moments)
-            monopole_level_kernel<true><<<g, kThreads, 0, st>>>(
-                d, ctx->depth_off, ctx->depth_nodes, ctx->node_cs, ctx->node_nchild, ctx->slot_ref, ctx->leaf_s,
-                ctx->node_s,
-                ctx->leaf_q, ctx->node_q);
+            upsweep_kernel<true><<<g, kThreads, 0, st>>>(ctx->counts, ctx->leaf_parent, ctx->node_parent,
+                                                         ctx->node_cs, ctx->node_nchild, ctx->slot_ref,
+                                                         ctx->leaf_s, ctx->node_s, ctx->leaf_q, ctx->node_q,
+                                                         ctx->node_ctr);
         else
-            monopole_level_kernel<false><<<g, kThreads, 0, st>>>(
-                d, ctx->depth_off, ctx->depth_nodes, ctx->node_cs, ctx->node_nchild, ctx->slot_ref, ctx->leaf_s,
-                ctx->node_s,
-                ctx->leaf_q, ctx->node_q);
+            upsweep_kernel<false><<<g, kThreads, 0, st>>>(ctx->counts, ctx->leaf_parent, ctx->node_parent,
+                                                          ctx->node_cs, ctx->node_nchild, ctx->slot_ref,
+                                                          ctx->leaf_s, ctx->node_s, ctx->leaf_q, ctx->node_q,
+                                                          ctx->node_ctr);
         BH_LAUNCH_CHECK(ctx);
+    } else {
+        const int nblk = (int)((n + kBucketThreads - 1) / kBucketThreads);
+        bucket_count_kernel<<<nblk, kBucketThreads, 0, st>>>(ctx->counts, ctx->node_depth, ctx->scan_tmp, nblk);
+        BH_LAUNCH_CHECK(ctx);
+        bucket_scan_kernel<<<1, 1024, 0, st>>>(ctx->scan_tmp, nblk, ctx->depth_off);
+        BH_LAUNCH_CHECK(ctx);
+        bucket_place_kernel<<<nblk, kBucketThreads, 0, st>>>(ctx->counts, ctx->node_depth, ctx->scan_tmp, nblk,
+                                                             ctx->depth_nodes);
+        BH_LAUNCH_CHECK(ctx);
+        for (int d = kMaxDepth - 1; d >= 0; --d) {
+            if (moments)
+                monopole_level_kernel<true><<<g, kThreads, 0, st>>>(d, ctx->depth_off, ctx->depth_nodes,
+                                                                    ctx->node_cs, ctx->node_nchild, ctx->slot_ref,
+                                                                    ctx->leaf_s, ctx->node_s, ctx->leaf_q,
+                                                                    ctx->node_q);
+            else
+                monopole_level_kernel<false><<<g, kThreads, 0, st>>>(d, ctx->depth_off, ctx->depth_nodes,
+                                                                     ctx->node_cs, ctx->node_nchild, ctx->slot_ref,
+                                                                     ctx->leaf_s, ctx->node_s, ctx->leaf_q,
+                                                                     ctx->node_q);
+            BH_LAUNCH_CHECK(ctx);
+        }
     }
 
     // 5. traversal records

@@ -151,6 +151,28 @@ def test_300k_against_oracle(bh, ctx, port):
     assert_bits_equal(s["acc"], acc, "accelerations")
 
 
+def test_level_build_path_against_oracle(bh, port):
+    """A million bodies (trojans included) build through the level-by-level
+    monopole pass (smaller sets climb in one launch, which the tests above
+    cover): the tree, with and without the merge, and the second moments'
+    tree bit for bit and to 1e-12 against the oracle's sums."""
+    n = 1_000_000
+    pos, vel, mass, ids = bh.generate_system(41, n, 0.1, 0.05)
+    bb = port.bbox(pos)
+    keys = port.keys(pos, bb)
+    sk, sp, sm, sv, si, _ = port.sort(keys, pos, mass, vel, ids)
+    with bh.Context(n) as c:
+        for merge in (True, False):
+            c.set_bodies(pos, vel, mass, ids)
+            c.compute_bbox(); c.compute_keys(); c.sort_bodies(); c.build_tree(merge=merge)
+            got = c.export_tree()
+            tree = port.tree(sk, sp, sm, merge=merge)
+            want = tree.records()
+            tree.close()
+            for a, b, name in zip(got, want, ("prefix", "depth", "mass", "com")):
+                assert_bits_equal(a, b, f"merge={merge} tree {name}")
+
+
 def test_stateless_entry_points(bh, port, golden):
     g = golden("synthetic_1000.npz")
     pos, vel, mass, ids = g["pos"], g["vel"], g["mass"], g["ids"]
