@@ -31,9 +31,11 @@ and seeded (the reference's 300k CSV is not part of its repository).
 * precision_run: the FP32 far-field form on 1M bodies at theta {0.5, 0.8,
   1.05}, then 1,000 steps with error, energy and angular-momentum drift every
   100 steps.
-* long_runs: the configurations' own run lengths, 2,000 steps of the 300k
-  FP64 list workload and 500 steps of the 4M FP32 + learned form, each timed
-  as one span, with the final error and the energy/angular-momentum drift.
+* long_runs: the configurations' own run lengths -- 240 steps of the 19,054-
+  body system in the bit-exact form (final state compared with the compiled
+  reference's run), 2,000 steps of the 300k FP64 list workload and 500 steps
+  of the 4M FP32 + learned form -- each timed as one span, with the final
+  error and the energy/angular-momentum drift.
 * let_exchange: the locally essential tree export and import at 4M bodies
   split over 8 ranks, against the oracle on the host cores.
 * csv_ingest: readCSV of a 1M-body file on the GPU against the host reader.
@@ -338,6 +340,40 @@ def long_run(dev, n, frac_outer, frac_trojan, seed, mode_name, steps, params=Non
             "final_median_rel_err": float(np.median(e)), "final_p99_rel_err": float(np.quantile(e, 0.99)),
             "rel_energy_drift": float((inv["E"] - inv0["E"]) / abs(inv0["E"])),
             "rel_angular_momentum_drift": float(np.linalg.norm(inv["L"] - inv0["L"]) / np.linalg.norm(inv0["L"]))}
+
+
+def config1_run(dev):
+    """The CPU-runnable configuration's whole run: 240 steps of 1 h at theta
+    1.05 on the 19,054-body system in the bit-exact form, from the inputs
+    stored with the test fixtures, timed as one span; the final state's
+    SHA-256 is compared with the compiled reference's own 240-step run
+    (tests/golden/config1_240_steps.json)."""
+    import hashlib
+    import torch
+    bh = importlib.import_module("barnes-hut_gb300")
+    g = np.load(ROOT / "tests" / "golden" / "synthetic_19054.npz")
+    want = json.loads((ROOT / "tests" / "golden" / "config1_240_steps.json").read_text())
+    n = len(g["mass"])
+    with bh.Context(n, dev) as ctx:
+        ext = torch.cuda.ExternalStream(ctx.stream(), device=dev)
+        ctx.set_bodies(g["pos"], g["vel"], g["mass"], g["ids"])
+        ctx.step(DT, THETA, G, 3, MODES["plain"], t=0.0)  # warm-up, then the run from the start
+        ctx.set_bodies(g["pos"], g["vel"], g["mass"], g["ids"])
+        torch.cuda.synchronize(dev)
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record(ext)
+        t = ctx.step(DT, THETA, G, 240, MODES["plain"], t=0.0)
+        e1.record(ext)
+        e1.synchronize()
+        ms = e0.elapsed_time(e1)
+        state = ctx.get_bodies()
+    h = hashlib.sha256()
+    for a in state:
+        h.update(np.ascontiguousarray(a).tobytes())
+    return {"bodies": n, "mode": "plain (bit-exact)", "steps": 240, "simulated_days": t, "ms_total": ms,
+            "body_steps_per_s": n * 240 / (ms * 1e-3),
+            "final_state_bits_equal_reference": h.hexdigest() == want["digest"] and t == want["t"]}
 
 
 def precision_run(args, dev):
@@ -742,7 +778,8 @@ def run_ours(args, rank, ws, local):
         pr = precision_run(args, dev)
         let = let_exchange(args, dev)
         ingest = csv_ingest(args, dev)
-        runs = {"config2_300k_fp64_list_2000_steps": long_run(dev, N_BODIES, 0.10, 0.0, SEED, "fp64_list", 2000),
+        runs = {"config1_19k_plain_240_steps": config1_run(dev),
+                "config2_300k_fp64_list_2000_steps": long_run(dev, N_BODIES, 0.10, 0.0, SEED, "fp64_list", 2000),
                 "config5_4m_fp32_learned_500_steps": long_run(dev, args.ns_bodies, 0.10, 0.05, SEED + 1, "learned",
                                                               500, params, scale, 1e-6, args.theta_max)}
 
