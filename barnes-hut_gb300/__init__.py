@@ -342,17 +342,23 @@ class Context:
         _check(library().bh_tree_info(self._h, C.byref(r), C.byref(nn), C.byref(nl)))
         return {"records": r.value, "nodes": nn.value, "leaves": nl.value}
 
+    def _tree_nodes(self) -> int:
+        """The device node count (counts only, no copy of the tree)."""
+        nn = _I64(0)
+        _check(library().bh_tree_info(self._h, None, C.byref(nn), None))
+        return nn.value
+
     def tree_slots(self):
         """(prefix u64, depth u8) of the reference cell each device node
         stands for (the deepest cell of its single-child chain)."""
-        k = self.tree_info()["nodes"]
+        k = self._tree_nodes()
         p = np.empty(k, np.uint64); d = np.empty(k, np.uint8)
         _check(library().bh_tree_slots(self._h, _ptr(p), _ptr(d)))
         return p, d
 
     def tree_spread(self) -> np.ndarray:
         """sqrt(Q/m) of the far-field masses per node (bh_tree_slots order)."""
-        out = np.empty(self.tree_info()["nodes"], np.float32)
+        out = np.empty(self._tree_nodes(), np.float32)
         _check(library().bh_tree_spread(self._h, _ptr(out)))
         return out
 
@@ -370,7 +376,7 @@ class Context:
         remote domain (boxes, (k, 6)) needs, as (prefix u64, depth u8,
         mass f64, com (k, 3) f64) in the tree's node order."""
         bx = _f64(boxes).reshape(-1, 6)
-        cap = self.tree_info()["nodes"]
+        cap = self._tree_nodes()
         prefix = np.empty(cap, np.uint64); depth = np.empty(cap, np.uint8); mass = np.empty(cap)
         com = np.empty((cap, 3))
         k = _I64(0)

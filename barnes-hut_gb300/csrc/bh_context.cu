@@ -648,11 +648,19 @@ int bh_tree_info(bh_context* ctx, int64_t* n_records, int64_t* n_nodes, int64_t*
         }
         return bh_fail(BH_ERR_STATE, "bh_tree_info: no tree built");
     }
+    if (!n_records) {  // the counts alone: no copy of the tree
+        int32_t c[4];
+        BH_CUDA_TRY(cudaMemcpyAsync(c, ctx->counts, sizeof(c), cudaMemcpyDeviceToHost, ctx->stream));
+        BH_CUDA_TRY(cudaStreamSynchronize(ctx->stream));
+        if (n_nodes) *n_nodes = c[2];
+        if (n_leaves) *n_leaves = c[0];
+        return BH_OK;
+    }
     HostTree h;
     if ((rc = fetch_tree(ctx, h))) return rc;
     int64_t recs = 0;
     for (const auto& r : h.rec) recs += (int64_t)r.depth - r.top + 1;
-    if (n_records) *n_records = recs;
+    *n_records = recs;
     if (n_nodes) *n_nodes = h.S;
     if (n_leaves) *n_leaves = h.L;
     return BH_OK;

@@ -1,5 +1,6 @@
-// readCSV (src/io.cpp:16-81) on the GPU: the file is read into pinned
-// memory once, copied to the device, and split and parsed there.
+// readCSV (src/io.cpp:16-81) on the GPU: the file is streamed to the device
+// through a small pinned ring (reader threads fill one bank of slots while
+// the previous bank's copies run), then split and parsed there.
 //
 //   1. newline positions: per-64 KiB-chunk counts, a scan, and an ordered
 //      write of each chunk's positions;
@@ -24,10 +25,16 @@
 // Lemire ("Number parsing at a gigabyte per second", 2021), restated.
 #include "bh_internal.cuh"
 
+#include <fcntl.h>
+#include <sys/stat.h>
+#include <unistd.h>
+
 #include <algorithm>
+#include <atomic>
 #include <cstdio>
 #include <cstring>
 #include <string>
+#include <thread>
 #include <vector>
 
 #include "bh_pow5_table.h"
@@ -173,12 +180,51 @@ __device__ int parse_number(const char* s, const char* e, double* out)
     return dec_to_double(w, q, neg, out);
 }
 
+// 16 bytes per thread per round (one 128-bit load, coalesced): 4,096 bytes a
+// round, 16 rounds a chunk.  Chunk starts are multiples of 64 KiB in a
+// cudaMalloc buffer, so every full 16-byte group is 16-byte aligned; the
+// file's last partial group is read byte by byte.
+constexpr int kGroup = 16;
+constexpr int64_t kRound = (int64_t)kGroup * kChunkThreads;
+
+// Bytes i0 .. i0 + 15 (those below b) as four words, and a per-byte mask of
+// newlines in each (0xFF where the byte is '\n', via the SIMD byte compare).
+__device__ __forceinline__ void newline_masks(const char* __restrict__ buf, int64_t i0, int64_t b,
+                                              unsigned m[4])
+{
+    unsigned v[4];
+    if (i0 + kGroup <= b) {
+        const uint4 q = __ldg(reinterpret_cast<const uint4*>(buf + i0));
+        v[0] = q.x; v[1] = q.y; v[2] = q.z; v[3] = q.w;
+    } else {
+        for (int k = 0; k < 4; ++k) {
+            unsigned w = 0;
+            for (int j = 0; j < 4; ++j) {
+                const int64_t i = i0 + 4 * k + j;
+                const unsigned c = i < b ? (unsigned)(unsigned char)buf[i] : 0u;
+                w |= c << (8 * j);
+            }
+            v[k] = w;
+        }
+    }
+    for (int k = 0; k < 4; ++k) m[k] = __vcmpeq4(v[k], 0x0A0A0A0Au);
+}
+
+__device__ __forceinline__ int mask_count(const unsigned m[4])
+{
+    return (__popc(m[0]) + __popc(m[1]) + __popc(m[2]) + __popc(m[3])) >> 3;
+}
+
 __global__ void __launch_bounds__(kChunkThreads) nl_count_kernel(const char* __restrict__ buf, int64_t size,
                                                                  int32_t* __restrict__ cnt)
 {
     const int64_t a = (int64_t)blockIdx.x * kChunk, b = min(a + kChunk, size);
     int c = 0;
-    for (int64_t i = a + threadIdx.x; i < b; i += blockDim.x) c += buf[i] == '\n';
+    for (int64_t i0 = a + kGroup * (int64_t)threadIdx.x; i0 < b; i0 += kRound) {
+        unsigned m[4];
+        newline_masks(buf, i0, b, m);
+        c += mask_count(m);
+    }
     c = __reduce_add_sync(0xffffffffu, c);
     __shared__ int ws[kChunkThreads / 32];
     if ((threadIdx.x & 31) == 0) ws[threadIdx.x >> 5] = c;
@@ -190,32 +236,53 @@ __global__ void __launch_bounds__(kChunkThreads) nl_count_kernel(const char* __r
     }
 }
 
-// Each thread owns a contiguous slice of the chunk; slices are numbered in
-// order, so the positions come out sorted.
+// The same rounds as nl_count_kernel: a block-wide exclusive scan of the
+// per-thread counts places each round's positions after the previous
+// round's, in file order.
 __global__ void __launch_bounds__(kChunkThreads) nl_write_kernel(const char* __restrict__ buf, int64_t size,
                                                                  const int32_t* __restrict__ off,
                                                                  int64_t* __restrict__ nl_pos)
 {
-    constexpr int64_t kSlice = kChunk / kChunkThreads;
-    const int64_t a = (int64_t)blockIdx.x * kChunk + (int64_t)threadIdx.x * kSlice;
-    const int64_t b = min(a + kSlice, size);
-    int c = 0;
-    for (int64_t i = a; i < b; ++i) c += buf[i] == '\n';
-    __shared__ int pre[kChunkThreads];
-    pre[threadIdx.x] = c;
-    __syncthreads();
-    if (threadIdx.x == 0) {
-        int run = 0;
-        for (int k = 0; k < kChunkThreads; ++k) {
-            const int v = pre[k];
-            pre[k] = run;
-            run += v;
+    __shared__ int warp_tot[kChunkThreads / 32];
+    __shared__ int round_tot;
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    const int64_t a = (int64_t)blockIdx.x * kChunk, b = min(a + kChunk, size);
+    int64_t o = off[blockIdx.x];
+    for (int64_t r = a; r < b; r += kRound) {  // the same trip count in every thread
+        const int64_t i0 = r + kGroup * (int64_t)threadIdx.x;
+        unsigned m[4] = {0u, 0u, 0u, 0u};
+        if (i0 < b) newline_masks(buf, i0, b, m);
+        const int mine = mask_count(m);
+        int incl = mine;
+#pragma unroll
+        for (int d = 1; d < 32; d <<= 1) {
+            const int t = __shfl_up_sync(0xffffffffu, incl, d);
+            if (lane >= d) incl += t;
         }
+        if (lane == 31) warp_tot[w] = incl;
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            int run = 0;
+            for (int k = 0; k < kChunkThreads / 32; ++k) {
+                const int t = warp_tot[k];
+                warp_tot[k] = run;
+                run += t;
+            }
+            round_tot = run;
+        }
+        __syncthreads();
+        int64_t p = o + warp_tot[w] + incl - mine;
+        for (int k = 0; k < 4; ++k) {
+            unsigned mk = m[k];
+            while (mk) {
+                const int byte = (__ffs(mk) - 1) >> 3;
+                nl_pos[p++] = i0 + 4 * k + byte;
+                mk &= ~(0xFFu << (8 * byte));
+            }
+        }
+        o += round_tot;
+        __syncthreads();
     }
-    __syncthreads();
-    int64_t o = (int64_t)off[blockIdx.x] + pre[threadIdx.x];
-    for (int64_t i = a; i < b; ++i)
-        if (buf[i] == '\n') nl_pos[o++] = i;
 }
 
 // Data row d is line d + 1 (line 0 is the header).
@@ -325,37 +392,122 @@ struct HostBuf {
     }
 };
 
+struct FileFd {
+    int fd = -1;
+    ~FileFd()
+    {
+        if (fd >= 0) ::close(fd);
+    }
+};
+
+struct Events {
+    cudaEvent_t e[2] = {nullptr, nullptr};
+    ~Events()
+    {
+        for (auto x : e)
+            if (x) cudaEventDestroy(x);
+    }
+};
+
+// Bytes [off, off + len) of the file, retrying short reads.
+bool read_at(int fd, char* dst, int64_t off, int64_t len)
+{
+    while (len > 0) {
+        const ssize_t r = ::pread(fd, dst, (size_t)len, (off_t)off);
+        if (r <= 0) return false;
+        dst += r;
+        off += r;
+        len -= r;
+    }
+    return true;
+}
+
+bool text_at(int fd, int64_t a, int64_t b, std::string& t)
+{
+    t.assign((size_t)std::max<int64_t>(b - a, 0), '\0');
+    return t.empty() || read_at(fd, &t[0], a, (int64_t)t.size());
+}
+
+constexpr int64_t kStage = 4 << 20;  // bytes per slot of the pinned ring
+constexpr int kReaders = 4;          // slots per bank, one reader thread each
+
+// The whole file to dst on the device, in order on stream st.  Two banks of
+// kReaders slots: a bank's slots are read in parallel (one thread each, the
+// caller's thread taking the first), then copied asynchronously; the bank is
+// reused once its copies have completed (an event per bank).
+int stream_file(int fd, int64_t size, char* dst, cudaStream_t st, const char* fn)
+{
+    const int64_t slots = 2 * kReaders;
+    const int64_t ring = std::min<int64_t>(size, slots * kStage);
+    HostBuf hb;
+    if (cudaMallocHost(reinterpret_cast<void**>(&hb.p), (size_t)ring) != cudaSuccess) {
+        cudaGetLastError();
+        return bh_fail(BH_ERR_OUT_OF_MEMORY, std::string(fn) + ": pinned staging buffer");
+    }
+    Events ev;
+    for (auto& x : ev.e) BH_CUDA_TRY(cudaEventCreateWithFlags(&x, cudaEventDisableTiming));
+    const int64_t nchunks = (size + kStage - 1) / kStage;
+    for (int64_t c0 = 0, round = 0; c0 < nchunks; c0 += kReaders, ++round) {
+        const int bank = (int)(round & 1);
+        if (round >= 2) BH_CUDA_TRY(cudaEventSynchronize(ev.e[bank]));
+        const int k = (int)std::min<int64_t>(kReaders, nchunks - c0);
+        std::atomic<bool> ok{true};
+        auto slot = [&](int j) { return hb.p + (int64_t)(bank * kReaders + j) * kStage; };
+        auto work = [&](int j) {
+            const int64_t off = (c0 + j) * kStage;
+            if (!read_at(fd, slot(j), off, std::min(kStage, size - off))) ok = false;
+        };
+        std::vector<std::thread> th;
+        int spawned = 1;
+        try {
+            for (; spawned < k; ++spawned) th.emplace_back(work, spawned);
+        } catch (...) {  // no thread to spare: the caller reads the rest
+        }
+        work(0);
+        for (int j = spawned; j < k; ++j) work(j);
+        for (auto& t : th) t.join();
+        if (!ok) return bh_fail(BH_ERR_IO, std::string(fn) + ": short read");
+        for (int j = 0; j < k; ++j) {
+            const int64_t off = (c0 + j) * kStage;
+            BH_CUDA_TRY(cudaMemcpyAsync(dst + off, slot(j), (size_t)std::min(kStage, size - off),
+                                        cudaMemcpyHostToDevice, st));
+        }
+        BH_CUDA_TRY(cudaEventRecord(ev.e[bank], st));
+    }
+    BH_CUDA_TRY(cudaStreamSynchronize(st));  // the ring is freed on return
+    return BH_OK;
+}
+
 struct Out7 {
     double *m, *x, *y, *z, *vx, *vy, *vz;
     uint64_t* id;
 };
 
+// The 8 arrays of n bodies in one device block (mass, x, y, z, vx, vy, vz,
+// then the ids).
+Out7 out7_of(double* b, int64_t n)
+{
+    return Out7{b, b + n, b + 2 * n, b + 3 * n, b + 4 * n, b + 5 * n, b + 6 * n, reinterpret_cast<uint64_t*>(b + 7 * n)};
+}
+
 // Parses `path` on ctx's device.  With `out` (room for `cap` bodies) the
-// bodies are written there; *n_out is the body count either way.
+// bodies are written there; otherwise, with `own`, into a block of exactly
+// the body count allocated there (out7_of layout); *n_out is the body count
+// either way.
 int csv_parse(bh_context* ctx, const char* path, int64_t body_count, const Out7* out, int64_t cap, int64_t* n_out,
-              const char* fn)
+              const char* fn, DevBuf* own = nullptr)
 {
     *n_out = 0;
-    std::FILE* f = std::fopen(path, "rb");
-    if (!f) return bh_fail(BH_ERR_IO, std::string(fn) + ": cannot open " + path);
-    std::fseek(f, 0, SEEK_END);
-    const long fsize = std::ftell(f);
-    std::fseek(f, 0, SEEK_SET);
-    if (fsize < 0) {
-        std::fclose(f);
+    FileFd file;
+    file.fd = ::open(path, O_RDONLY);
+    if (file.fd < 0) return bh_fail(BH_ERR_IO, std::string(fn) + ": cannot open " + path);
+    struct stat sb;
+    if (::fstat(file.fd, &sb) != 0 || !S_ISREG(sb.st_mode))
         return bh_fail(BH_ERR_IO, std::string(fn) + ": cannot size " + path);
-    }
-    const int64_t size = fsize;
-    HostBuf hb;
-    if (cudaMallocHost(reinterpret_cast<void**>(&hb.p), (size_t)size + 1) != cudaSuccess) {
-        std::fclose(f);
-        cudaGetLastError();
-        return bh_fail(BH_ERR_OUT_OF_MEMORY, std::string(fn) + ": pinned file buffer");
-    }
-    const size_t got = size ? std::fread(hb.p, 1, (size_t)size, f) : 0;
-    std::fclose(f);
-    if ((int64_t)got != size) return bh_fail(BH_ERR_IO, std::string(fn) + ": short read of " + path);
+    const int64_t size = (int64_t)sb.st_size;
     if (size == 0) return BH_OK;
+    char last = 0;
+    if (!read_at(file.fd, &last, size - 1, 1)) return bh_fail(BH_ERR_IO, std::string(fn) + ": short read of " + path);
 
     cudaStream_t st = ctx->stream;
     const int64_t nch = (size + kChunk - 1) / kChunk;
@@ -366,17 +518,18 @@ int csv_parse(bh_context* ctx, const char* path, int64_t body_count, const Out7*
     int32_t* cnt = dcnt.as<int32_t>();
     int32_t* tmp = cnt + nch;
     int32_t* small = dsmall.as<int32_t>();
-    BH_CUDA_TRY(cudaMemcpyAsync(dbuf.p, hb.p, (size_t)size, cudaMemcpyHostToDevice, st));
+    int rc = stream_file(file.fd, size, dbuf.as<char>(), st, fn);
+    if (rc) return rc;
     nl_count_kernel<<<(unsigned)nch, kChunkThreads, 0, st>>>(dbuf.as<char>(), size, cnt);
     BH_LAUNCH_CHECK(ctx);
-    int rc = bh::device_exclusive_scan_tmp(ctx, cnt, cnt, nch, nullptr, small, tmp);
+    rc = bh::device_exclusive_scan_tmp(ctx, cnt, cnt, nch, nullptr, small, tmp);
     if (rc) return rc;
     BH_CUDA_TRY(cudaMemcpyAsync(ctx->h_small, small, sizeof(int32_t), cudaMemcpyDeviceToHost, st));
     BH_CUDA_TRY(cudaStreamSynchronize(st));
     int32_t nl32 = 0;
     std::memcpy(&nl32, ctx->h_small, sizeof(int32_t));
     const int64_t nl = nl32;
-    const int64_t lines = nl + (hb.p[size - 1] != '\n' ? 1 : 0);
+    const int64_t lines = nl + (last != '\n' ? 1 : 0);
     const int64_t rows = lines - 1;  // line 0 is the header
     if (rows <= 0) return BH_OK;
     if (rows >= (int64_t)INT32_MAX) return bh_fail(BH_ERR_INVALID_ARGUMENT, std::string(fn) + ": too many rows");
@@ -411,7 +564,8 @@ int csv_parse(bh_context* ctx, const char* path, int64_t body_count, const Out7*
         std::vector<double> fix_vals;
         for (int64_t d : odd) {
             const int64_t a = hnl[(size_t)d] + 1, b = d + 1 < nl ? hnl[(size_t)(d + 1)] : size;
-            const std::string text(hb.p + a, hb.p + b);
+            std::string text;
+            if (!text_at(file.fd, a, b, text)) return bh_fail(BH_ERR_IO, std::string(fn) + ": short read of " + path);
             if (hst[(size_t)d] == kRowHost) {
                 double v[7] = {0, 0, 0, 0, 0, 0, 0};
                 const bool ok = bh_parse_csv_row(text, v);
@@ -461,6 +615,13 @@ int csv_parse(bh_context* ctx, const char* path, int64_t body_count, const Out7*
         }
     }
     *n_out = n;
+    Out7 mine;
+    if (!out && own && n > 0) {
+        BH_CUDA_TRY(cudaMalloc(&own->p, sizeof(double) * 8 * (size_t)n));
+        mine = out7_of(own->as<double>(), n);
+        out = &mine;
+        cap = n;
+    }
     if (!out) return BH_OK;
     if (n > cap) return bh_fail(BH_ERR_CAPACITY, std::string(fn) + ": more bodies than the output holds");
     row_emit_kernel<<<grid, 128, 0, st>>>(rows, n, status, flag, vals, out->m, out->x, out->y, out->z, out->vx,
@@ -489,17 +650,14 @@ extern "C" int bh_read_csv_gpu(const char* path, int64_t body_count, int64_t* n_
         ~Guard() { bh_context_destroy(c); }
     } guard{ctx};
     if (!fill) return csv_parse(ctx, path, body_count, nullptr, 0, n_out, "bh_read_csv_gpu");
-    // Count first, then parse into device arrays of that size.
+    // One parse into a device block of the body count, then to the caller's
+    // arrays (room for the count of the sizing call on the same file).
     int64_t n = 0;
-    if ((rc = csv_parse(ctx, path, body_count, nullptr, 0, &n, "bh_read_csv_gpu"))) return rc;
+    DevBuf d;
+    if ((rc = csv_parse(ctx, path, body_count, nullptr, 0, &n, "bh_read_csv_gpu", &d))) return rc;
     *n_out = n;
     if (n == 0) return BH_OK;
-    DevBuf d;
-    BH_CUDA_TRY(cudaMalloc(&d.p, sizeof(double) * 8 * (size_t)n));
-    double* b = d.as<double>();
-    const Out7 o{b, b + n, b + 2 * n, b + 3 * n, b + 4 * n, b + 5 * n, b + 6 * n, reinterpret_cast<uint64_t*>(b + 7 * n)};
-    int64_t n2 = 0;
-    if ((rc = csv_parse(ctx, path, body_count, &o, n, &n2, "bh_read_csv_gpu"))) return rc;
+    const double* b = d.as<double>();
     std::vector<double> h(8 * (size_t)n);
     BH_CUDA_TRY(cudaMemcpy(h.data(), b, sizeof(double) * 8 * (size_t)n, cudaMemcpyDeviceToHost));
     for (int64_t i = 0; i < n; ++i) {

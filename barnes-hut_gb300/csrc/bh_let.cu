@@ -24,6 +24,7 @@
 #include <algorithm>
 #include <cmath>
 #include <cstring>
+#include <limits>
 
 namespace {
 
@@ -63,18 +64,32 @@ struct LetScreen {
     float theta2f;  // (float) theta2
 };
 
+constexpr int kLetGroup = 32;  // boxes per group of the prefilter
+
 // Whether the cell (prefix, d) fails the opening test against any of the nb
 // remote boxes; warp-uniform result.  Cell box: size = span / 2^d,
 // min = gmin + (ix * 2^-d) * span, max = min + size (all RN).
+//
+// With the prescreen on, the boxes are first taken in groups of kLetGroup
+// consecutive boxes (bucket order, so spatially close), each with the FP32
+// hull of its members' FP32 copies (grpf: min of the minima, max of the
+// maxima).  Every step of the prescreen's lower bound dlo is monotone in the
+// box corners (RN subtraction, fmaxf, the FMA of non-negative terms), so a
+// hull's dlo is at most each member's; a group whose hull the prescreen
+// decides "does not open" holds no member the prescreen would not also
+// decide so, and is skipped.  Only the remaining groups are tested box by
+// box, exactly as before.
 __device__ bool cell_opens(uint64_t prefix, int d, const LetGeom& g, const double* __restrict__ boxes,
-                           const float* __restrict__ boxf, int nb, double theta2, LetScreen sc, int lane)
+                           const float* __restrict__ boxf, const float* __restrict__ grpf, int nb, double theta2,
+                           LetScreen sc, int lane)
 {
     const double scale = 1.0 / (double)(1ull << d);  // exact
-    const double div = (double)(1 << d);
     double lo[3], hi[3];
 #pragma unroll
     for (int a = 0; a < 3; ++a) {
-        const double size = __ddiv_rn(g.span[a], div);
+        // span / 2^d: the quotient by a power of two equals the product by
+        // its exact reciprocal (the same real number, rounded once).
+        const double size = __dmul_rn(g.span[a], scale);
         lo[a] = __dadd_rn(g.lo[a], __dmul_rn(__dmul_rn((double)cell_axis(prefix, d, a), scale), g.span[a]));
         hi[a] = __dadd_rn(lo[a], size);
     }
@@ -90,39 +105,58 @@ __device__ bool cell_opens(uint64_t prefix, int d, const LetGeom& g, const doubl
         hif[a] = (float)hi[a];
     }
     constexpr float kUp = 1.0f + 0x1p-20f, kDn = 1.0f - 0x1p-20f;
-    for (int k0 = 0; k0 < nb; k0 += 32) {
-        const int k = k0 + lane;
-        bool f = false;
-        if (k < nb) {
-            bool decided = false;
-            if (sc.on) {
-                const float* rf = boxf + 6 * (int64_t)k;
-                float dlo = 0.0f, dhi = 0.0f;
+    // The prescreen's lower bound on d^2 for an FP32 box r (min xyz, max xyz).
+    auto dlo_of = [&](const float* __restrict__ rf) {
+        float dlo = 0.0f;
 #pragma unroll
-                for (int a = 0; a < 3; ++a) {
-                    const float ef = fmaxf(0.0f, fmaxf(lof[a] - __ldg(rf + 3 + a), __ldg(rf + a) - hif[a]));
-                    const float l = fmaxf(ef - sc.delta, 0.0f), h = ef + sc.delta;
-                    dlo = fmaf(l, l, dlo);
-                    dhi = fmaf(h, h, dhi);
-                }
-                if (s2f * kDn >= sc.theta2f * dhi * kUp) {
-                    f = true;
-                    decided = true;
-                } else if (s2f * kUp < sc.theta2f * dlo * kDn) {
-                    decided = true;
-                }
+        for (int a = 0; a < 3; ++a) {
+            const float ef = fmaxf(0.0f, fmaxf(lof[a] - __ldg(rf + 3 + a), __ldg(rf + a) - hif[a]));
+            const float l = fmaxf(ef - sc.delta, 0.0f);
+            dlo = fmaf(l, l, dlo);
+        }
+        return dlo;
+    };
+    auto box_opens = [&](int k) {
+        if (sc.on) {
+            const float* rf = boxf + 6 * (int64_t)k;
+            float dlo = 0.0f, dhi = 0.0f;
+#pragma unroll
+            for (int a = 0; a < 3; ++a) {
+                const float ef = fmaxf(0.0f, fmaxf(lof[a] - __ldg(rf + 3 + a), __ldg(rf + a) - hif[a]));
+                const float l = fmaxf(ef - sc.delta, 0.0f), h = ef + sc.delta;
+                dlo = fmaf(l, l, dlo);
+                dhi = fmaf(h, h, dhi);
             }
-            if (!decided) {
-                const double* r = boxes + 6 * (int64_t)k;
-                double e[3];
+            if (s2f * kDn >= sc.theta2f * dhi * kUp) return true;
+            if (s2f * kUp < sc.theta2f * dlo * kDn) return false;
+        }
+        const double* r = boxes + 6 * (int64_t)k;
+        double e[3];
 #pragma unroll
-                for (int a = 0; a < 3; ++a)
-                    e[a] = ref_max(0.0, ref_max(__dsub_rn(lo[a], __ldg(r + 3 + a)), __dsub_rn(__ldg(r + a), hi[a])));
-                const double d2 =
-                    __dadd_rn(__dadd_rn(__dmul_rn(e[0], e[0]), __dmul_rn(e[1], e[1])), __dmul_rn(e[2], e[2]));
-                f = s2 >= __dmul_rn(theta2, d2);
+        for (int a = 0; a < 3; ++a)
+            e[a] = ref_max(0.0, ref_max(__dsub_rn(lo[a], __ldg(r + 3 + a)), __dsub_rn(__ldg(r + a), hi[a])));
+        const double d2 = __dadd_rn(__dadd_rn(__dmul_rn(e[0], e[0]), __dmul_rn(e[1], e[1])), __dmul_rn(e[2], e[2]));
+        return s2 >= __dmul_rn(theta2, d2);
+    };
+    if (sc.on) {
+        const int ng = (nb + kLetGroup - 1) / kLetGroup;
+        for (int g0 = 0; g0 < ng; g0 += 32) {
+            const int gi = g0 + lane;
+            const bool maybe = gi < ng && !(s2f * kUp < sc.theta2f * dlo_of(grpf + 6 * (int64_t)gi) * kDn);
+            unsigned todo = __ballot_sync(0xffffffffu, maybe);
+            while (todo) {
+                const int j = g0 + __ffs(todo) - 1;
+                todo &= todo - 1;
+                const int k = j * kLetGroup + lane;  // kLetGroup == 32: one box per lane
+                const bool f = k < nb && box_opens(k);
+                if (__any_sync(0xffffffffu, f)) return true;
             }
         }
+        return false;
+    }
+    for (int k0 = 0; k0 < nb; k0 += 32) {
+        const int k = k0 + lane;
+        const bool f = k < nb && box_opens(k);
         if (__any_sync(0xffffffffu, f)) return true;
     }
     return false;
@@ -138,8 +172,8 @@ __global__ void let_seed_kernel(int32_t* __restrict__ q0, int32_t* __restrict__ 
 // next level's nodes.
 __global__ void __launch_bounds__(kLetThreads) let_level_kernel(
     const bh::TreeRec* __restrict__ rec, const int32_t* __restrict__ slot_ref, const int32_t* __restrict__ node_a,
-    const uint64_t* __restrict__ leaf_key, const double* __restrict__ boxes, const float* __restrict__ boxf, int nb,
-    LetGeom g, double theta2, LetScreen sc, int max_depth, const int32_t* __restrict__ q_in,
+    const uint64_t* __restrict__ leaf_key, const double* __restrict__ boxes, const float* __restrict__ boxf,
+    const float* __restrict__ grpf, int nb, LetGeom g, double theta2, LetScreen sc, int max_depth, const int32_t* __restrict__ q_in,
     const int32_t* __restrict__ cnt_in, int32_t* __restrict__ q_out, int32_t* __restrict__ cnt_out,
     int32_t* __restrict__ keep)
 {
@@ -154,7 +188,7 @@ __global__ void __launch_bounds__(kLetThreads) let_level_kernel(
         int kept = -1;
         bool descend = false;
         for (int d = r.top;; ++d) {
-            const bool opens = cell_opens(key & bh::prefix_mask(d), d, g, boxes, boxf, nb, theta2, sc, lane);
+            const bool opens = cell_opens(key & bh::prefix_mask(d), d, g, boxes, boxf, grpf, nb, theta2, sc, lane);
             if (!opens || d >= max_depth) { kept = d; break; }
             if (d < r.depth) continue;
             descend = r.nchild > 0;
@@ -205,7 +239,7 @@ __global__ void let_write_kernel(const int32_t* __restrict__ counts, const int32
 // remote boxes and the per-level counts; grown on demand, kept with the
 // context.
 struct LetLayout {
-    size_t q0, q1, keep, flag, prefix, depth, mass, com, boxes, boxf, cnt, total;
+    size_t q0, q1, keep, flag, prefix, depth, mass, com, boxes, boxf, grpf, cnt, total;
 };
 
 LetLayout let_layout(int64_t S, int64_t nb)
@@ -223,6 +257,7 @@ LetLayout let_layout(int64_t S, int64_t nb)
     L.com = o; o += up(3 * sizeof(double) * S);
     L.boxes = o; o += up(6 * sizeof(double) * nb);
     L.boxf = o; o += up(6 * sizeof(float) * nb);
+    L.grpf = o; o += up(6 * sizeof(float) * ((nb + kLetGroup - 1) / kLetGroup));
     L.cnt = o; o += up(sizeof(int32_t) * (kLetLevels + 2));
     L.total = o;
     return L;
@@ -453,6 +488,7 @@ int bh_let_export(bh_context* ctx, const double* boxes, int64_t nboxes, const do
     double* o_com = reinterpret_cast<double*>(base + L.com);
     double* d_boxes = reinterpret_cast<double*>(base + L.boxes);
     float* d_boxf = reinterpret_cast<float*>(base + L.boxf);
+    float* d_grpf = reinterpret_cast<float*>(base + L.grpf);
     int32_t* cnt = reinterpret_cast<int32_t*>(base + L.cnt);
 
     LetGeom g;
@@ -479,7 +515,23 @@ int bh_let_export(bh_context* ctx, const double* boxes, int64_t nboxes, const do
         sc.on = 1;
         sc.delta = (float)(mag * 0x1p-21);
     }
+    // The prefilter's group hulls of the FP32 copies.
+    const int64_t ngroups = (nboxes + kLetGroup - 1) / kLetGroup;
+    std::vector<float> hg((size_t)(6 * ngroups));
+    for (int64_t j = 0; j < ngroups; ++j) {
+        float* h = &hg[(size_t)(6 * j)];
+        for (int a = 0; a < 3; ++a) {
+            h[a] = std::numeric_limits<float>::infinity();
+            h[3 + a] = -std::numeric_limits<float>::infinity();
+        }
+        for (int64_t k = j * kLetGroup; k < std::min<int64_t>(nboxes, (j + 1) * kLetGroup); ++k)
+            for (int a = 0; a < 3; ++a) {
+                h[a] = std::min(h[a], hf[(size_t)(6 * k + a)]);
+                h[3 + a] = std::max(h[3 + a], hf[(size_t)(6 * k + 3 + a)]);
+            }
+    }
     BH_CUDA_TRY(cudaMemcpyAsync(d_boxf, hf.data(), sizeof(float) * 6 * nboxes, cudaMemcpyHostToDevice, st));
+    BH_CUDA_TRY(cudaMemcpyAsync(d_grpf, hg.data(), sizeof(float) * 6 * ngroups, cudaMemcpyHostToDevice, st));
     BH_CUDA_TRY(cudaMemsetAsync(keep, 0xff, sizeof(int32_t) * S, st));
     BH_CUDA_TRY(cudaMemsetAsync(cnt, 0, sizeof(int32_t) * (kLetLevels + 2), st));
     let_seed_kernel<<<1, 1, 0, st>>>(q[0], cnt);
@@ -492,7 +544,7 @@ int bh_let_export(bh_context* ctx, const double* boxes, int64_t nboxes, const do
     // 21, so kLetLevels launches drain every frontier.
     for (int lv = 0; lv < kLetLevels; ++lv) {
         let_level_kernel<<<grid, kLetThreads, 0, st>>>(ctx->rec, ctx->slot_ref, ctx->node_a, ctx->leaf_key, d_boxes,
-                                                       d_boxf, (int)nboxes, g, theta2, sc, max_depth, q[lv & 1],
+                                                       d_boxf, d_grpf, (int)nboxes, g, theta2, sc, max_depth, q[lv & 1],
                                                        cnt + lv, q[(lv + 1) & 1], cnt + lv + 1, keep);
         BH_LAUNCH_CHECK(ctx);
     }

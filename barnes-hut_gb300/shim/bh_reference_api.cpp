@@ -210,8 +210,8 @@ std::vector<NodeRecord> createInteractionListForRank(const OctreeMap& tree, cons
     }
     const double gb[6] = {global_bb.min.x, global_bb.min.y, global_bb.min.z,
                           global_bb.max.x, global_bb.max.y, global_bb.max.z};
-    int64_t nrec = 0, nnodes = 0, nleaves = 0;
-    check(bh_tree_info(c, &nrec, &nnodes, &nleaves), "bh_tree_info");
+    int64_t nnodes = 0;
+    check(bh_tree_info(c, nullptr, &nnodes, nullptr), "bh_tree_info");
     std::vector<uint64_t> prefix(nnodes);
     std::vector<uint8_t> depth(nnodes);
     std::vector<double> mass(nnodes), com(3 * nnodes);

@@ -39,7 +39,7 @@ and seeded (the reference's 300k CSV is not part of its repository).
 * let_exchange: the locally essential tree export and import at 4M bodies
   split over 8 ranks, against the oracle on the host cores.
 * csv_ingest: readCSV of a 1M-body file on the GPU against the host reader.
-  --no-extras skips these six blocks.
+  --no-extras skips these six blocks; --blocks a,b runs only those.
 
 Multi-GPU: the path does not shard on one GPU per rank; ranks run replicas
 (weak scaling) and value is the sum of their body-steps over the slowest
@@ -71,6 +71,7 @@ N_BODIES = 300_149
 SEED = 2
 FLOPS_PER_INTERACTION = 20
 L2_FLUSH_BYTES = 256 << 20
+EXTRA_BLOCKS = ("forms_4m", "learned_eval", "precision_run", "long_runs", "let_exchange", "csv_ingest")
 WORKLOAD = "plain FP64 theta=1.05, dt=1h, 300,149 bodies (Sun, 8 planets, 300,140 asteroids, 10% outer belt)"
 MODES = {"plain": 0, "fp64_list": 1, "fp32": 2, "learned": 3}
 KERNEL = {0: "traverse_exact_kernel", 1: "traverse_masked_kernel<fp64>", 2: "traverse_masked_kernel<fp32>",
@@ -99,6 +100,8 @@ def parse():
     ap.add_argument("--e2e-steps", type=int, default=5)
     ap.add_argument("--cpu-seconds", type=float, default=15.0, help="budget of the CPU-baseline sample")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--blocks", default=None,
+                    help="comma-separated subset of the extra blocks: " + ",".join(EXTRA_BLOCKS))
     ap.add_argument("--no-extras", action="store_true",
                     help="skip the 4M-body comparison, the learned evaluation and the 1M precision run")
     ap.add_argument("--ns-bodies", type=int, default=4_000_000)
@@ -771,17 +774,22 @@ def run_ours(args, rank, ws, local):
                 "sample": int(len(sample)), "against": "FP64 direct sum"}
 
     ns = pr = le = runs = let = ingest = None
+    blocks = set(EXTRA_BLOCKS) if args.blocks is None else set(args.blocks.split(","))
     if rank == 0 and ws == 1 and not args.no_extras:
-        params, scale, info = train_model(args)
-        ns = forms_4m(args, dev, params, scale, info)
-        le = learned_eval(args, dev, params, scale)
-        pr = precision_run(args, dev)
-        let = let_exchange(args, dev)
-        ingest = csv_ingest(args, dev)
-        runs = {"config1_19k_plain_240_steps": config1_run(dev),
-                "config2_300k_fp64_list_2000_steps": long_run(dev, N_BODIES, 0.10, 0.0, SEED, "fp64_list", 2000),
-                "config5_4m_fp32_learned_500_steps": long_run(dev, args.ns_bodies, 0.10, 0.05, SEED + 1, "learned",
-                                                              500, params, scale, 1e-6, args.theta_max)}
+        needs_model = blocks & {"forms_4m", "learned_eval", "long_runs"}
+        params, scale, info = train_model(args) if needs_model else (None, None, None)
+        ns = forms_4m(args, dev, params, scale, info) if "forms_4m" in blocks else None
+        le = learned_eval(args, dev, params, scale) if "learned_eval" in blocks else None
+        pr = precision_run(args, dev) if "precision_run" in blocks else None
+        let = let_exchange(args, dev) if "let_exchange" in blocks else None
+        ingest = csv_ingest(args, dev) if "csv_ingest" in blocks else None
+        if "long_runs" in blocks:
+            runs = {"config1_19k_plain_240_steps": config1_run(dev),
+                    "config2_300k_fp64_list_2000_steps": long_run(dev, N_BODIES, 0.10, 0.0, SEED, "fp64_list",
+                                                                  2000),
+                    "config5_4m_fp32_learned_500_steps": long_run(dev, args.ns_bodies, 0.10, 0.05, SEED + 1,
+                                                                  "learned", 500, params, scale, 1e-6,
+                                                                  args.theta_max)}
 
     cpu = None
     if rank == 0 and not args.no_cpu_baseline:

@@ -132,7 +132,9 @@ int bh_build_tree_options(bh_context *ctx, int merge);
 int bh_build_tree(bh_context *ctx);
 /* Sizes of the last tree: n_records = nodes of the reference's uncompressed
  * OctreeMap; n_nodes = nodes of the compressed device octree; n_leaves =
- * distinct keys. */
+ * distinct keys.  Any pointer may be NULL; with n_records NULL only the
+ * counts are read back, otherwise the tree is copied to the host to count
+ * the records. */
 int bh_tree_info(bh_context *ctx, int64_t *n_records, int64_t *n_nodes, int64_t *n_leaves);
 /* The reference's node set (serializeTreeToRecords,
  * src/linear_octree.cpp:169-176, NodeRecord linear_octree.h:60-65) sorted by

@@ -152,3 +152,27 @@ def test_load_csv_into_context(bh, tmp_path, golden):
     with bh.Context(1000) as small:
         with pytest.raises(bh.BhError):
             small.load_csv(f)
+
+
+def test_gpu_reader_streams_large_files(bh, tmp_path):
+    """A file of several staging rounds (about 43 MB, beyond the two banks of
+    the pinned ring): the same bodies as the host reader, through both entry
+    points, with body_count limits that end inside later rounds."""
+    rng = np.random.default_rng(14)
+    n = 260_000
+    ids = np.arange(n, dtype=np.uint64)
+    mass = rng.uniform(1e-12, 1e-3, n)
+    pos = rng.normal(0.0, 3.0, (n, 3))
+    vel = rng.normal(0.0, 1e-2, (n, 3))
+    f = tmp_path / "big.csv"
+    bh.write_csv(f, ids, mass, pos, vel)
+    assert f.stat().st_size > 40 << 20
+    host = bh.read_csv(f)
+    _same(bh.read_csv_gpu(f), host)
+    with bh.Context(n) as ctx:
+        for lim in (-1, 200_001):
+            k = ctx.load_csv(f, lim)
+            assert k == (n if lim < 0 else lim)
+            p, v, m, i, _ = ctx.get_bodies()
+            assert_bits_equal(p, host[2][:k], "pos"); assert_bits_equal(v, host[3][:k], "vel")
+            assert_bits_equal(m, host[1][:k], "mass"); assert_bits_equal(i, host[0][:k], "ids")
