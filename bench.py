@@ -158,7 +158,7 @@ class ClockSampler:
 
     def _read(self):
         for line in self.proc.stdout:
-            self.lines.append(line.strip())
+            self.lines.append((time.perf_counter(), line.strip()))
 
     def __exit__(self, *exc):
         if self.proc:
@@ -168,10 +168,13 @@ class ClockSampler:
             except subprocess.TimeoutExpired:
                 self.proc.kill()
 
-    def summary(self):
-        sm, mx, reasons = [], None, set()
+    def summary(self, window=None):
+        """Median SM clock and the throttle reasons seen over every sample
+        (the pre-roll and the timed steps); samples_timed counts those that
+        arrived within `window` (perf_counter start, end)."""
+        sm, mx, reasons, inside = [], None, set(), 0
         names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
-        for ln in self.lines:
+        for ts, ln in self.lines:
             f = [x.strip() for x in ln.split(",")]
             if len(f) < 9:
                 continue
@@ -180,11 +183,17 @@ class ClockSampler:
                 mx = float(f[2])
             except ValueError:
                 continue
+            if window and window[0] <= ts <= window[1]:
+                inside += 1
             for nm, v in zip(names, f[5:9]):
                 if v.lower().startswith("active"):
                     reasons.add(nm)
-        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": mx, "reasons": sorted(reasons),
-                "samples": len(sm)}
+        out = {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": mx, "reasons": sorted(reasons),
+               "samples": len(sm)}
+        if window:
+            out["samples_timed"] = inside
+            out["window"] = "200 ms samples over a 1 s untimed pre-roll of the same step and the timed steps"
+        return out
 
 
 def cpu_baseline(pos, vel, mass, ids, budget_s: float, theta: float = THETA, nsteps_max: int = 20):
@@ -686,6 +695,18 @@ def hbm_peak_gbs():
         return 6800.0
 
 
+def hbm_view(traffic, ms):
+    """The force kernel against the HBM roofline: its measured DRAM traffic
+    per launch over the launch's duration, as a fraction of the measured
+    copy bandwidth (small: the kernel is not memory-bound)."""
+    if not traffic or not ms:
+        return None
+    gbs = traffic / (ms * 1e-3) / 1e9
+    peak = hbm_peak_gbs()
+    return {"achieved": gbs, "peak": peak, "unit": "GB/s", "frac": gbs / peak,
+            "peak_source": "MEASURED_PEAKS.json hbm_gbs (measured copy bandwidth)"}
+
+
 def hbm_phases(phases_ms, n):
     peak = hbm_peak_gbs()
     out = {}
@@ -717,10 +738,19 @@ def run_ours(args, rank, ws, local):
         t = ctx.step(DT, theta, G, 1, mode, t=t)
     peak = ctx.measure_fma_peak(mode <= 1)
 
-    l0 = ctx.launches()
     times, inter = [], 0
-    barrier(ws)
     with ClockSampler(dev) as clk:
+        # Untimed pre-roll of the same step, so that the sampler (which
+        # starts slowly) records the clocks under this load around the
+        # timed steps, which can be shorter than one sampling period.
+        t_pre = time.perf_counter() + 1.0
+        while time.perf_counter() < t_pre:
+            flush.fill_(1.0)
+            t = ctx.step(DT, theta, G, 1, mode, t=t)
+            torch.cuda.synchronize(dev)
+        barrier(ws)
+        l0 = ctx.launches()
+        w0 = time.perf_counter()
         for _ in range(args.steps):
             flush.fill_(1.0)
             torch.cuda.synchronize(dev)
@@ -732,6 +762,10 @@ def run_ours(args, rank, ws, local):
             e1.synchronize()
             times.append(e0.elapsed_time(e1))
             inter += ctx.interaction_count()
+        torch.cuda.synchronize(dev)
+        barrier(ws)
+        w1 = time.perf_counter()
+        time.sleep(0.25)  # the sample that covers the last timed step
     torch.cuda.synchronize(dev)
     launches = ctx.launches() - l0
     total_ms = sum(times)
@@ -816,7 +850,8 @@ def run_ours(args, rank, ws, local):
                      "peak_source": f"measured in-process: {fp.upper()} FMA chains (bh_measure_fma_peak)",
                      "work": f"{FLOPS_PER_INTERACTION} flops x {inter_per_step:.4g} interactions per launch",
                      "traffic": TRAFFIC_BYTES.get((args.mode, n)),
-                     "traffic_unit": "bytes per launch (ncu)"},
+                     "traffic_unit": "bytes per launch (ncu)",
+                     "hbm_view": hbm_view(TRAFFIC_BYTES.get((args.mode, n)), force_ms)},
         "phases_ms_per_step": {kk: v / k for kk, v in phases.items()},
         "hbm_phases": hbm_phases({kk: v / k for kk, v in phases.items()}, n),
         "interactions_per_body": inter_per_step / n,
@@ -825,7 +860,7 @@ def run_ours(args, rank, ws, local):
         "e2e": {"value": ws * n * e2e_steps / e2e_s, "unit": "body-steps/s", "h2d_bytes_per_step": h2d,
                 "d2h_bytes_per_step": d2h},
         "gpu_launches": launches,
-        "clocks": clk.summary(),
+        "clocks": clk.summary((w0, w1)),
         "cpu_baseline": cpu,
         "forms_4m": ns,
         "learned_eval": le,
