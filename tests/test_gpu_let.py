@@ -135,6 +135,40 @@ def _opens(lo, hi, boxes, theta2):
     return out
 
 
+def test_let_export_box_order_and_scale(bh, port):
+    """The group prefilter of the export against the oracle where its groups
+    are loose or it is off: the other ranks' bucket boxes in shuffled order
+    (hulls of scattered boxes), 3,000 random boxes, and the same system and
+    boxes scaled by 1e13 (coordinates beyond 2^40, where every box test is
+    FP64)."""
+    pos0, vel, mass, ids = bh.generate_system(33, 60_000, 0.1, 0.05)
+    rng = np.random.default_rng(34)
+    for scale in (1.0, 1e13):
+        pos = pos0 * scale
+        bb = port.bbox(pos)
+        keys = port.keys(pos, bb)
+        owner, doms = _bucket_domains(keys, 18, 4)
+        sel = np.nonzero(owner == 0)[0]
+        sk, sp, sm, _, _, _ = port.sort(keys[sel], pos[sel], mass[sel], vel[sel], ids[sel])
+        tree = port.tree(sk, sp, sm, merge=False)
+        lo, hi = bb[:3], bb[3:]
+        c = rng.uniform(lo, hi, (3000, 3))
+        h = rng.uniform(0.0, 0.02, (3000, 3)) * (hi - lo)
+        random_boxes = np.concatenate([c - h, c + h], axis=1)
+        with _local_ctx(bh, pos[sel], vel[sel], mass[sel], ids[sel], bb) as ctx:
+            for r in (1, 2, 3):
+                boxes = bh.let_bucket_boxes(doms[r], 18, bb)
+                for name, bx in (("bucket order", boxes), ("shuffled", boxes[rng.permutation(len(boxes))]),
+                                 ("random", random_boxes)):
+                    for theta in (0.7, 1.05):
+                        got = _sorted(*ctx.let_export(bx, bb, theta * theta, 21))
+                        want = port.let_export(tree, bx, bb, theta * theta, 21)
+                        assert len(got[0]) == len(want[0]) > 0, (scale, r, name, theta)
+                        for a, b, what in zip(got, want, ("prefix", "depth", "mass", "com")):
+                            assert_bits_equal(a, b, f"scale {scale} rank {r} {name} theta {theta}: {what}")
+        tree.close()
+
+
 def test_let_export_properties_4m(bh):
     """4,000,000 bodies, rank 0 of 8 (18-bit buckets) exporting to rank 1
     at theta 0.7:
