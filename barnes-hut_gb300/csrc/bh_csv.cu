@@ -31,6 +31,7 @@
 
 #include <algorithm>
 #include <atomic>
+#include <cerrno>
 #include <cstdio>
 #include <cstring>
 #include <string>
@@ -414,6 +415,7 @@ bool read_at(int fd, char* dst, int64_t off, int64_t len)
 {
     while (len > 0) {
         const ssize_t r = ::pread(fd, dst, (size_t)len, (off_t)off);
+        if (r < 0 && errno == EINTR) continue;
         if (r <= 0) return false;
         dst += r;
         off += r;
