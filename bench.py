@@ -253,7 +253,9 @@ def run_reference(args, rank):
     line = {"metric": "body-steps/s", "value": val, "unit": "body-steps/s", "n_gpus": args.gpus, "steps": k,
             "warmup": warm, "ms_per_step": 1e3 * secs / k, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f64", "data": "synthetic", "impl": "reference",
-            "config": {"workload": workload_name(args), "bodies": n, "theta": theta, "dt_days": DT},
+            "config": {"workload": workload_name(args), "bodies": n, "theta": theta, "dt_days": DT,
+                       "mode": f"CPU, {kind} ({'compiled reference sources' if kind == 'reference' else 'oracle port'})",
+                       "seed": SEED, "parallelism": f"OpenMP {cores} threads"},
             "cpu_baseline": {"value": val, "unit": "body-steps/s", "cores": cores, "kind": kind,
                              "sample": f"{k} timed full steps after {warm} warm-up steps, OpenMP {cores} threads"},
             "e2e": {"value": val, "unit": "body-steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
