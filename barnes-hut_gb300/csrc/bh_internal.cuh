@@ -80,13 +80,19 @@ __device__ __forceinline__ double rsqrt_hh(double x)
     return fma(y0, t, y0);
 }
 
+__device__ __forceinline__ float narrow_trunc(double x);
+
 // x^(-3/2), the r^-3 of a monopole term from r^2, for the non-bit-exact
 // FP64 walk and the direct terms: the FP32 estimate y0 of x^-1/2 as in
-// rsqrt_hh (a 24-bit value, so y0^2 is exact in FP64), e = 1 - x y0^2, and
-// x^-3/2 = y0^3 (1 - e)^-3/2 = y0^3 (1 + 3/2 e + 15/8 e^2 + ...): with
-// |e| < 2^-20 the next term is below 2^-58 relative.  Six FP64 operations
-// where rsqrt_hh and the cube take seven.  Within 4 ulps of
-// RN(1 / RN(x RN(sqrt(x)))) (checked by bh_selftest).
+// rsqrt_hh, e = 1 - x y0^2, and x^-3/2 = y0^3 (1 - e)^-3/2 =
+// y0^3 (1 + 3/2 e + 15/8 e^2 + ...): with |e| < 2^-20 the next term is below
+// 2^-58 relative.  Three FP64 operations:
+//  * y0 has a 24-bit significand s, so y0^2 (s^2 < 2^48) is formed exactly
+//    and y0^3 (s^3 < 2^72) rounded to nearest from integer products;
+//  * the e^2 term is below 2^-39: FP32 gives it to 2^-61 and it is added to 1
+//    exactly as a count of 2^-52 units (below 2^13);
+//  * then e, f = 3/2 e + (1 + 15/8 e^2) and y0^3 f in FP64.
+// Within 4 ulps of RN(1 / RN(x RN(sqrt(x)))) (checked by bh_selftest).
 __device__ __forceinline__ double rcube_hh(double x)
 {
     const long long xb = __double_as_longlong(x);
@@ -97,12 +103,34 @@ __device__ __forceinline__ double rcube_hh(double x)
     }
     const float xf = __int_as_float(((xe - 896) << 23) | (int)((xb >> 29) & 0x7FFFFF));
     const int yb = __float_as_int(rsqrtf(xf));
-    const double y0 = __longlong_as_double(((long long)(((yb >> 23) & 0xFF) + 896) << 52) |
-                                           ((long long)(yb & 0x7FFFFF) << 29));
-    const double y2 = y0 * y0;
+    const int ey = (yb >> 23) & 0xFF;  // y0 = s 2^(ey - 150), y0 in [2^-50, 2^50]
+    const unsigned long long sy = (unsigned long long)((yb & 0x7FFFFF) | 0x800000);
+    // y0^2 = s^2 2^(2 ey - 300) with s^2 in [2^46, 2^48): exact.
+    const unsigned long long s2 = sy * sy;
+    const int t2 = (int)(s2 >> 47);
+    const double y2 = __longlong_as_double(((long long)(2 * ey - 300 + 46 + t2 + 1023) << 52) |
+                                           (long long)((s2 << (6 - t2)) & 0xFFFFFFFFFFFFFull));
+    // y0^3 = s^3 2^(3 ey - 450) with s^3 in [2^69, 2^72): the leading 53 bits,
+    // rounded to nearest (half up).
+    const unsigned long long plo = s2 * sy;
+    const unsigned long long phi = __umul64hi(s2, sy);  // in [2^5, 2^8)
+    const int lp = 63 - __clzll((long long)phi);          // 5, 6 or 7
+    const int sh = lp + 12;                               // bits below the leading 53
+    const unsigned long long lo2 = plo + (1ull << (sh - 1));
+    const unsigned long long hi2 = phi + (lo2 < plo ? 1ull : 0ull);
+    unsigned long long top = (hi2 << (64 - sh)) | (lo2 >> sh);
+    int p3 = 64 + lp;
+    if (top >> 53) {  // the rounding carried into a new leading bit
+        top >>= 1;
+        ++p3;
+    }
+    const double y3 = __longlong_as_double(((long long)(p3 + 3 * ey - 450 + 1023) << 52) |
+                                           (long long)(top & 0xFFFFFFFFFFFFFull));
     const double e = fma(-x, y2, 1.0);
-    const double f = fma(e, fma(e, 1.875, 1.5), 1.0);
-    return (y2 * y0) * f;
+    const float ef = narrow_trunc(e);
+    const int cu = __float2int_rn(1.875f * ef * ef * 0x1p52f);
+    const double w = __longlong_as_double(0x3FF0000000000000ll + (long long)cu);  // 1 + 15/8 e^2
+    return y3 * fma(e, 1.5, w);
 }
 
 // norm + quantise of generateMortonCodes (src/morton_keys.cpp:77-94):
