@@ -114,7 +114,7 @@ __device__ __forceinline__ double rcube_hh(double x)
     // rounded to nearest (half up).
     const unsigned long long plo = s2 * sy;
     const unsigned long long phi = __umul64hi(s2, sy);  // in [2^5, 2^8)
-    const int lp = 63 - __clzll((long long)phi);          // 5, 6 or 7
+    const int lp = 31 - __clz((int)phi);                  // 5, 6 or 7
     const int sh = lp + 12;                               // bits below the leading 53
     const unsigned long long lo2 = plo + (1ull << (sh - 1));
     const unsigned long long hi2 = phi + (lo2 < plo ? 1ull : 0ull);
@@ -128,7 +128,10 @@ __device__ __forceinline__ double rcube_hh(double x)
                                            (long long)(top & 0xFFFFFFFFFFFFFull));
     const double e = fma(-x, y2, 1.0);
     const float ef = narrow_trunc(e);
-    const int cu = __float2int_rn(1.875f * ef * ef * 0x1p52f);
+    // round(15/8 e^2 2^52), below 2^13, read from the significand of its sum
+    // with 2^23 (an FP32 addition rounds it to an integer; no conversion
+    // instruction, which would share the FP64 pipe)
+    const int cu = __float_as_int(fmaf(1.875f * ef, ef * 0x1p52f, 0x1p23f)) - 0x4B000000;
     const double w = __longlong_as_double(0x3FF0000000000000ll + (long long)cu);  // 1 + 15/8 e^2
     return y3 * fma(e, 1.5, w);
 }

@@ -52,6 +52,7 @@ constexpr int kWarps = 4;
 constexpr int kThreads = 32 * kWarps;
 constexpr int kStack = 512;   // sibling-range entries per warp
 constexpr int kList = 96;     // staged interactions per warp
+constexpr int kSegs = 63;     // FP64 list evaluation: run slots body + thread, 0..62
 constexpr int kSlotBits = 28; // slot index bits of a stack entry (count - 1 in the top 3)
 constexpr float kMargin = 1e-5f;  // relative margin of the FP32 group tests
 constexpr float kAbsErr = 1e-6f;  // bound on FP32 coordinate error, relative to magnitudes
@@ -177,8 +178,8 @@ struct WalkSmem {
     int poff[kW64][33];                     // first pair of each lane, then the total
     double bpos[kW64][3][kFP64 ? 32 : 1];   // the bodies' positions
     int bleaf[kW64][kFP64 ? 32 : 1];        // the bodies' leaf ids
-    double bacc[kW64][3][kFP64 ? 32 : 1];   // the bodies' accumulated list terms
-    unsigned bcnt[kW64][kFP64 ? 32 : 1];    // and their interaction counts
+    double seg[kW64][3][kFP64 ? kSegs : 1];  // each (thread, body) run's partial sums
+    uint16_t segn[kW64][kFP64 ? kSegs : 1];  // and its interaction count
 };
 
 template <bool kFP64, int kLearn>
@@ -234,15 +235,12 @@ __global__ void __launch_bounds__(kThreads) traverse_masked_kernel(FParams p)
     }
     const float theta2f = (float)p.theta2;
     const double theta2 = p.theta2, soft2 = p.soft2;
+    const bool nosoft = (__double_as_longlong(soft2) << 1) == 0;  // soft2 is +-0
     if (kFP64) {
         sm.bpos[w][0][lane] = x;
         sm.bpos[w][1][lane] = y;
         sm.bpos[w][2][lane] = z;
         sm.bleaf[w][lane] = my_leaf;
-        sm.bacc[w][0][lane] = 0.0;
-        sm.bacc[w][1][lane] = 0.0;
-        sm.bacc[w][2][lane] = 0.0;
-        sm.bcnt[w][lane] = 0u;
         __syncwarp();
     }
     int2* stk = sm.stack[w];
@@ -538,10 +536,16 @@ __global__ void __launch_bounds__(kThreads) traverse_masked_kernel(FParams p)
                 // evaluates only pairs that count, however unevenly the
                 // bodies' shares of the list are spread.  A thread sums its
                 // consecutive pairs in registers while they belong to one
-                // body and adds the partial sum to that body's shared
-                // accumulator when the body changes.
+                // body, and stores each run's partial (a plain store: no
+                // atomics and no FP64 work in divergent code) in slot
+                // body + thread.  Along the pairs both indices only grow and
+                // every new run increments at least one, so the slot of a run
+                // is its own.  Each body's lane then adds the partials of its
+                // runs, one per thread its pairs reach, in thread order.
                 uint8_t (*PL)[32] = sm.plist[w];
                 int* OFF = sm.poff[w];
+                auto SG = sm.seg[w];  // [3][kSegs] in the FP64 walk
+                uint16_t* SN = sm.segn[w];
                 int mine = 0;
                 for (int j = 0; j < nlist; ++j)
                     if (LM[j] & me) PL[mine++][lane] = (uint8_t)j;
@@ -567,11 +571,11 @@ __global__ void __launch_bounds__(kThreads) traverse_masked_kernel(FParams p)
                     const int k = k0 + t;
                     const bool on = k < k1;
                     if (on) {
-                        while (k >= OFF[b + 1]) {  // the next body: hand over the partial sum
-                            atomicAdd(&sm.bacc[w][0][b], sx);
-                            atomicAdd(&sm.bacc[w][1][b], sy);
-                            atomicAdd(&sm.bacc[w][2][b], sz);
-                            atomicAdd(&sm.bcnt[w][b], sn);
+                        while (k >= OFF[b + 1]) {  // body b's run ends here
+                            SG[0][b + lane] = sx;
+                            SG[1][b + lane] = sy;
+                            SG[2][b + lane] = sz;
+                            SN[b + lane] = (uint16_t)sn;
                             sx = sy = sz = 0.0;
                             sn = 0;
                             ++b;
@@ -584,13 +588,24 @@ __global__ void __launch_bounds__(kThreads) traverse_masked_kernel(FParams p)
                     bool take = on;
                     if (on && LL[j] == sm.bleaf[w][b]) {
                         // Own leaf: skipped at depth 21 unless a chain cell above
-                        // it (depths top..20) accepts (traversal.cpp:70,78).
-                        const double r2e = __dadd_rn(__dadd_rn(__dadd_rn(__dmul_rn(dx, dx), __dmul_rn(dy, dy)),
-                                                               __dmul_rn(dz, dz)), soft2);
-                        take = p.rec[LN[j]].top <= kMaxDepth - 1 && sm.side2d[kMaxDepth - 1] < __dmul_rn(theta2, r2e);
+                        // it (depths top..20) accepts (traversal.cpp:70,78).  At
+                        // zero displacement and no softening r^2 is 0 and no
+                        // cell accepts (decided on the bit patterns).
+                        if (nosoft && ((__double_as_longlong(dx) | __double_as_longlong(dy) |
+                                        __double_as_longlong(dz)) << 1) == 0) {
+                            take = false;
+                        } else {
+                            const double r2e = __dadd_rn(
+                                __dadd_rn(__dadd_rn(__dmul_rn(dx, dx), __dmul_rn(dy, dy)), __dmul_rn(dz, dz)), soft2);
+                            take = p.rec[LN[j]].top <= kMaxDepth - 1 &&
+                                   sm.side2d[kMaxDepth - 1] < __dmul_rn(theta2, r2e);
+                        }
                     }
                     const double r2 = fma(dx, dx, fma(dy, dy, fma(dz, dz, soft2)));
-                    double sc = r.w * rcube_hh(r2);
+                    // A pair not taken (an own leaf at r2 = 0, or a lane past
+                    // its share) gets an argument on the fast path, so that no
+                    // lane diverges into the out-of-range branch for it.
+                    double sc = r.w * rcube_hh(take ? r2 : 1.0);
                     if (!take) sc = 0.0;
                     sx = fma(sc, dx, sx);
                     sy = fma(sc, dy, sy);
@@ -598,10 +613,21 @@ __global__ void __launch_bounds__(kThreads) traverse_masked_kernel(FParams p)
                     sn += take ? 1u : 0u;
                 }
                 if (k0 < k1) {
-                    atomicAdd(&sm.bacc[w][0][b], sx);
-                    atomicAdd(&sm.bacc[w][1][b], sy);
-                    atomicAdd(&sm.bacc[w][2][b], sz);
-                    atomicAdd(&sm.bcnt[w][b], sn);
+                    SG[0][b + lane] = sx;
+                    SG[1][b + lane] = sy;
+                    SG[2][b + lane] = sz;
+                    SN[b + lane] = (uint16_t)sn;
+                }
+                __syncwarp();
+                const int f0 = OFF[lane], f1 = OFF[lane + 1];  // this lane's body: its pairs
+                if (f1 > f0) {
+                    const int l1 = (f1 - 1) / per;
+                    for (int l = f0 / per; l <= l1; ++l) {
+                        adx += SG[0][lane + l];
+                        ady += SG[1][lane + l];
+                        adz += SG[2][lane + l];
+                        cnt += SN[lane + l];
+                    }
                 }
                 __syncwarp();
             } else {
@@ -630,13 +656,6 @@ __global__ void __launch_bounds__(kThreads) traverse_masked_kernel(FParams p)
     }
     if (overflow && lane == 0) atomicOr(p.err, kErrOverflow);
     if (kLearn == kLearnCollect) return;
-    if (kFP64) {
-        __syncwarp();
-        adx += sm.bacc[w][0][lane];
-        ady += sm.bacc[w][1][lane];
-        adz += sm.bacc[w][2][lane];
-        cnt += sm.bcnt[w][lane];
-    }
 
     if (valid) {
         p.ax[i] = adx;
