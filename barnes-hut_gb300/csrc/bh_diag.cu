@@ -1,5 +1,5 @@
 // Diagnostics with no reference counterpart: the FP64 direct-sum sampler
-// that judges every force error, and the invariants (energy, linear and
+// that every force error is measured against, and the invariants (energy, linear and
 // angular momentum) whose drift is reported over a run.
 #include <vector>
 

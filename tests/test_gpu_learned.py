@@ -2,7 +2,7 @@
 against the FP64 CPU restatement, the traversal's fused (mma.sync) inference
 against the same, and the end-to-end pipeline -- pairs labelled by the plain
 walk at theta = 0.5, training on the GPU, and what the trained network gains
-over the theta criterion without it, judged by the FP64 direct sum."""
+over the theta criterion without it, measured against the FP64 direct sum."""
 from __future__ import annotations
 
 import numpy as np

@@ -1,4 +1,4 @@
-"""The FP32 far-field precision form (BH_MODE_FP32_FAR): accelerations judged
+"""The FP32 far-field precision form (BH_MODE_FP32_FAR): accelerations measured
 against the FP64 direct-sum sampler, and against the plain FP64 mode."""
 from __future__ import annotations
 
