@@ -192,28 +192,44 @@ def selftest(which: int, n: int, seed: int = 1) -> int:
     return f.value
 
 
+def _line_bound(path, body_count: int) -> int:
+    """An upper bound on a CSV file's data rows: its newline count plus one
+    (fewer with a body_count limit)."""
+    lines = 1
+    with open(path, "rb") as fh:
+        while True:
+            chunk = fh.read(16 << 20)
+            if not chunk:
+                break
+            lines += chunk.count(b"\n")
+    return min(lines, body_count) if body_count > 0 else lines
+
+
+def _read_csv_with(fn, path, body_count: int):
+    """One call of a reader entry point into arrays sized by the file's line
+    count, so each skipped row's warning is printed once, as readCSV prints
+    it."""
+    p = str(path).encode()
+    try:
+        cap = _line_bound(path, body_count)
+    except OSError:
+        cap = 0  # the entry point reports the missing file
+    ids = np.empty(cap, np.uint64); mass = np.empty(cap); pos = np.empty((max(cap, 1), 3))
+    vel = np.empty((max(cap, 1), 3))
+    n = _I64(0)
+    _check(fn(p, body_count, C.byref(n), _ptr(ids), _ptr(mass), _ptr(pos), _ptr(vel)))
+    k = n.value
+    return ids[:k].copy(), mass[:k].copy(), pos[:k].copy(), vel[:k].copy()
+
+
 def read_csv(path, body_count: int = -1):
     """readCSV: (ids, mass, pos, vel)."""
-    lib = library()
-    n = _I64(0)
-    p = str(path).encode()
-    _check(lib.bh_read_csv(p, body_count, C.byref(n), None, None, None, None))
-    ids = np.empty(n.value, np.uint64); mass = np.empty(n.value); pos = np.empty((n.value, 3))
-    vel = np.empty((n.value, 3))
-    _check(lib.bh_read_csv(p, body_count, C.byref(n), _ptr(ids), _ptr(mass), _ptr(pos), _ptr(vel)))
-    return ids, mass, pos, vel
+    return _read_csv_with(library().bh_read_csv, path, body_count)
 
 
 def read_csv_gpu(path, body_count: int = -1):
     """readCSV parsed on the GPU: (ids, mass, pos, vel), as read_csv."""
-    lib = library()
-    n = _I64(0)
-    p = str(path).encode()
-    _check(lib.bh_read_csv_gpu(p, body_count, C.byref(n), None, None, None, None))
-    ids = np.empty(n.value, np.uint64); mass = np.empty(n.value); pos = np.empty((n.value, 3))
-    vel = np.empty((n.value, 3))
-    _check(lib.bh_read_csv_gpu(p, body_count, C.byref(n), _ptr(ids), _ptr(mass), _ptr(pos), _ptr(vel)))
-    return ids, mass, pos, vel
+    return _read_csv_with(library().bh_read_csv_gpu, path, body_count)
 
 
 def write_csv(path, ids, mass, pos, vel) -> None:

@@ -231,12 +231,14 @@ extern "C" int bh_write_csv(const char* path, int64_t n, const uint64_t* ids, co
 // with the same elements, array names, types and number formatting (the
 // default stream formatting, 6 significant digits): Points "position";
 // PointData "rank", "body_id", "velocity", "mass", "acceleration" (the
-// magnitude); Verts "offsets" / "connectivity", one vertex per body.
+// magnitude); Verts "offsets" / "connectivity", one vertex per body.  An
+// empty state writes no file (io.cpp:95).
 extern "C" int bh_write_vtp(const char* path, int rank, int64_t n, const uint64_t* ids, const double* mass,
                             const double* pos, const double* vel, const double* acc)
 {
     if (!path || n < 0 || n > INT32_MAX || (n > 0 && (!ids || !mass || !pos || !vel || !acc)))
         return bh_fail(BH_ERR_INVALID_ARGUMENT, "bh_write_vtp: bad arguments");
+    if (n == 0) return BH_OK;
     std::ofstream os(path);
     if (!os) return bh_fail(BH_ERR_IO, std::string("bh_write_vtp: cannot open ") + path);
     const std::string I1 = "    ", I2 = I1 + I1, I3 = I2 + I1, I4 = I3 + I1;

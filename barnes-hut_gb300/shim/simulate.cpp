@@ -10,7 +10,9 @@
 // 10d at 1h runs 241 steps); --steps overrides it.  -r writes the final
 // positions to reference/final_ref.csv (io.cpp:716-722 layout); without -r
 // an existing reference file is compared by body id and SUMMED_DIST_ERROR
-// printed (io.cpp:759-780).  TOTAL_TIME covers the step loop (main.cpp:185,323).
+// printed (io.cpp:759-780), with 4 decimals as main.cpp:333-334 prints it and
+// again at full precision (SUMMED_DIST_ERROR_FULL, %.17g).  TOTAL_TIME covers
+// the step loop (main.cpp:185,323).
 // --dump writes the final state at full precision in the state-vector CSV
 // layout (what -f reads), bodies in the engine's final (key-sorted) order.
 //
@@ -247,6 +249,9 @@ int main(int argc, char** argv)
     std::cout << std::fixed << std::setprecision(4);
     std::cout << "TOTAL_TIME          " << secs << std::endl;
     std::cout << "SUMMED_DIST_ERROR   " << summed << std::endl;
+    char full[64];
+    std::snprintf(full, sizeof full, "%.17g", summed);
+    std::cout << "SUMMED_DIST_ERROR_FULL " << full << std::endl;
     std::cout << "BODY_STEPS_PER_S    " << std::setprecision(1) << (secs > 0 ? n * (double)nsteps / secs : 0.0)
               << std::endl;
     return 0;

@@ -394,7 +394,8 @@ int bh_write_csv(const char *path, int64_t n, const uint64_t *ids, const double 
 /* writeSnapshot (src/io.cpp:84-232): one VTK XML PolyData snapshot of n
  * bodies (pos, vel, acc: 3 per body) in the reference's layout and number
  * formatting, for ParaView; rank is the value of the "rank" array (0 for the
- * single-rank path).  Host function: no device work. */
+ * single-rank path).  As in the reference, n == 0 writes no file.  Host
+ * function: no device work. */
 int bh_write_vtp(const char *path, int rank, int64_t n, const uint64_t *ids, const double *mass, const double *pos,
                  const double *vel, const double *acc);
 

@@ -1,8 +1,9 @@
 /* Single-rank stand-in for <mpi.h>, used only to compile the reference's own
  * sources into the oracle library (oracle/_ref).  It provides exactly what
  * those translation units name: the MPI_Allreduce that compute_global_bbox
- * calls (src/bounding_box.cpp:46-52) and the gathers and all-to-alls of
- * src/exchange.cpp.  On one rank each copies the send buffer into the
+ * calls (src/bounding_box.cpp:46-52), the gathers and all-to-alls of
+ * src/exchange.cpp and the MPI_Reduce of computeDistanceSum
+ * (src/io.cpp:776).  On one rank each copies the send buffer into the
  * receive buffer (at the first displacement).  A datatype's value is its
  * size in bytes.  No other MPI behaviour is modelled.  Test infrastructure
  * only. */
@@ -57,5 +58,13 @@ static inline int MPI_Alltoallv(const void* send, const int* scounts, const int*
     (void)rcounts; (void)comm;
     memcpy((char*)recv + (size_t)rdispls[0] * (size_t)rtype, (const char*)send + (size_t)sdispls[0] * (size_t)stype,
            (size_t)scounts[0] * (size_t)stype);
+    return 0;
+}
+
+static inline int MPI_Reduce(const void* send, void* recv, int count, MPI_Datatype type, MPI_Op op, int root,
+                             MPI_Comm comm)
+{
+    (void)op; (void)root; (void)comm;
+    memcpy(recv, send, (size_t)count * (size_t)type);
     return 0;
 }

@@ -15,6 +15,7 @@ reference legs use this module.
 from __future__ import annotations
 
 import ctypes as C
+import os
 import subprocess
 from pathlib import Path
 
@@ -23,7 +24,8 @@ import numpy as np
 HERE = Path(__file__).resolve().parent
 PORT_LIB = HERE / "_build" / "libbhoracle.so"
 REF_LIB = HERE / "_ref" / "libbhref.so"
-REF_SRC = Path("/root/reference")
+# The reference checkout: $BH_REFERENCE_DIR, else its usual location.
+REF_SRC = Path(os.environ.get("BH_REFERENCE_DIR") or "/root/reference")
 
 _P = C.c_void_p
 _I64 = C.c_int64
@@ -103,6 +105,14 @@ class Oracle:
             self._pseudo = f("pseudo_tree", _P, [_P, _P, _P, _P, _I64])
             self._letacc = f("let_accelerations", None, [_P, _P, _P, _P, _P, _I64, _I64, _P, _P, _D, _D, _D, _P,
                                                           C.c_int, _P])
+            # src/io.cpp through oracle/ref_io_harness.cpp
+            self._read_csv = f("read_csv", _I64, [C.c_char_p, C.c_int, _P, _P, _P, _P, _I64])
+            self._snapshot = f("write_snapshot", None, [C.c_int, C.c_int, _I64, _P, _P, _P, _P, _P, C.c_char_p])
+            self._pvd = f("update_pvd", None, [C.c_int, C.POINTER(C.c_char_p), C.c_int, C.c_int, _D, C.c_char_p])
+            self._save_ref = f("save_reference_csv", None, [C.c_char_p, _I64, _P, _P])
+            self._load_ref = f("load_reference_csv", C.c_int, [C.c_char_p, C.c_int, _P])
+            self._dist = f("compute_distance_sum", _D, [_I64, _P, _P, _I64, _P])
+            self._cli = f("run_cli", C.c_int, [C.c_int, C.POINTER(C.c_char_p), _P, _P, _P, _P])
 
     # -- stages ---------------------------------------------------------
     def bbox(self, pos) -> np.ndarray:
@@ -229,6 +239,63 @@ class Oracle:
 
     def threads(self) -> int:
         return int(self._threads()) if self.kind == "port" else -1
+
+    # -- the reference's I/O (src/io.cpp; reference kind only) -----------
+    def read_csv(self, path, body_count=-1, cap=None):
+        """readCSV (src/io.cpp:16-81): (ids, mass, pos, vel).  `cap` bounds
+        the rows copied (default: the file's line count)."""
+        path = str(path)
+        if cap is None:
+            with open(path, "rb") as fh:
+                cap = fh.read().count(b"\n") + 1
+        ids = np.empty(cap, np.uint64); mass = np.empty(cap); pos = np.empty((cap, 3)); vel = np.empty((cap, 3))
+        n = int(self._read_csv(path.encode(), int(body_count), _ptr(ids), _ptr(mass), _ptr(pos), _ptr(vel), cap))
+        if n < 0:
+            raise FileNotFoundError(path)
+        k = min(n, cap)
+        return ids[:k], mass[:k], pos[:k], vel[:k]
+
+    def write_snapshot(self, rank, vs_counter, ids, mass, pos, vel, acc, vs_dir):
+        """writeSnapshot (src/io.cpp:84-232) into <vs_dir>/<rank>/sim.<k>.vtp."""
+        i = np.ascontiguousarray(ids, np.uint64); m = np.ascontiguousarray(mass, np.float64)
+        p, v, a = (np.ascontiguousarray(x, np.float64).reshape(-1, 3) for x in (pos, vel, acc))
+        self._snapshot(int(rank), int(vs_counter), len(m), _ptr(i), _ptr(m), _ptr(p), _ptr(v), _ptr(a),
+                       str(vs_dir).encode())
+
+    @staticmethod
+    def _argv(args):
+        arr = (C.c_char_p * (len(args) + 1))(*[a.encode() for a in ["simulate", *args]])
+        return len(args) + 1, arr
+
+    def update_pvd(self, args, size, vs_counter, t, vs_dir):
+        """updatePVDFile (src/io.cpp:234-298) for the command line `args`."""
+        argc, argv = self._argv(args)
+        self._pvd(argc, argv, int(size), int(vs_counter), float(t), str(vs_dir).encode())
+
+    def save_reference_csv(self, d, pos, ids):
+        p = np.ascontiguousarray(pos, np.float64).reshape(-1, 3); i = np.ascontiguousarray(ids, np.uint64)
+        self._save_ref(str(d).encode(), len(i), _ptr(p), _ptr(i))
+
+    def load_reference_csv(self, d, n):
+        out = np.empty((n, 3))
+        if self._load_ref(str(d).encode(), int(n), _ptr(out)):
+            raise FileNotFoundError(f"{d}/final_ref.csv")
+        return out
+
+    def distance_sum(self, pos, ids, ref_pos) -> float:
+        p = np.ascontiguousarray(pos, np.float64).reshape(-1, 3); i = np.ascontiguousarray(ids, np.uint64)
+        r = np.ascontiguousarray(ref_pos, np.float64).reshape(-1, 3)
+        return float(self._dist(len(i), _ptr(p), _ptr(i), len(r), _ptr(r)))
+
+    def run_cli(self, args):
+        """The reference driver (src/main.cpp) on one rank for the tree force
+        path with command line `args`, in the current directory: returns
+        (SUMMED_DIST_ERROR, bodies, steps, frames)."""
+        argc, argv = self._argv(args)
+        s = _D(); n = _I64(); k = _I64(); fr = _I64()
+        if self._cli(argc, argv, C.byref(s), C.byref(n), C.byref(k), C.byref(fr)):
+            raise FileNotFoundError("input file")
+        return s.value, n.value, k.value, fr.value
 
 
 class OracleTree:

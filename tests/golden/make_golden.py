@@ -45,8 +45,19 @@ Outputs (all produced by the compiled reference, strict IEEE build):
                              (pos, vel, mass, ids, acc in the final sorted
                              order) and the final time.
 * ``scenario1.json``      -- digests of the same stages on the reference's own
-                             data/state_vectors_csvs/scenario1_19054.csv (the
-                             file itself is not copied here).
+                             data/state_vectors_csvs/scenario1_19054.csv, read
+                             by the reference's readCSV (the file itself is not
+                             copied here).
+* ``io.npz``              -- the reference's I/O code (src/io.cpp, compiled by
+                             the same recipe): readCSV on the seeded CSV files
+                             of csv_cases.py (counts, digests, warnings; full
+                             arrays for the small files); the bytes
+                             writeSnapshot writes for a state of awkward values;
+                             the .pvd updatePVDFile builds over three frames;
+                             and the reference driver (main.cpp, one rank, tree
+                             path) run on a 1,000-body CSV: every snapshot and
+                             .pvd file it writes, final_ref.csv of a -r run and
+                             SUMMED_DIST_ERROR of a rerun against it.
 
 Inputs of the synthetic systems come from the engine's generator
 (``bh_generate_system``) and are stored, so the fixtures do not depend on the
@@ -54,10 +65,13 @@ platform's libm.
 """
 from __future__ import annotations
 
+import contextlib
 import hashlib
 import importlib
 import json
+import os
 import sys
+import tempfile
 from pathlib import Path
 
 import numpy as np
@@ -67,6 +81,9 @@ sys.path.insert(0, str(ROOT))
 from oracle.oracle import REF_SRC, Oracle, build_reference  # noqa: E402
 
 HERE = Path(__file__).resolve().parent
+sys.path.insert(0, str(HERE))
+import csv_cases  # noqa: E402
+
 G = 1.48812e-34
 THETA = 1.05
 DT = 1.0 / 24.0
@@ -186,7 +203,7 @@ def main() -> None:
         raise SystemExit("the reference checkout is needed to regenerate the fixtures")
     ref = Oracle("reference")
     bh = importlib.import_module("barnes-hut_gb300")
-    want = set(sys.argv[1:]) or {"edge", "synthetic", "let", "pseudo", "config1", "scenario"}
+    want = set(sys.argv[1:]) or {"edge", "synthetic", "let", "pseudo", "config1", "scenario", "io"}
     if "edge" in want:
         edge_fixtures(ref, bh)
     if "synthetic" in want:
@@ -198,7 +215,9 @@ def main() -> None:
     if "config1" in want:
         config1_fixture(ref)
     if "scenario" in want:
-        scenario_fixture(ref, bh)
+        scenario_fixture(ref)
+    if "io" in want:
+        io_fixtures(ref)
     print("fixtures written to", HERE)
 
 
@@ -323,11 +342,11 @@ def config1_fixture(ref):
     (HERE / "config1_240_steps.json").write_text(json.dumps(info, indent=1) + "\n")
 
 
-def scenario_fixture(ref, bh):
-    # The reference's own scenario-1 CSV: digests only.
+def scenario_fixture(ref):
+    # The reference's own scenario-1 CSV, read by its readCSV: digests only.
     csv = REF_SRC / "data" / "state_vectors_csvs" / "scenario1_19054.csv"
     if csv.exists():
-        ids, mass, pos, vel = bh.read_csv(csv)
+        ids, mass, pos, vel = ref.read_csv(csv)
         s = stages(ref, pos, vel, mass, ids)
         info = dict(n=int(len(mass)), input_digest=digest(pos, vel, mass, ids), bbox=s["bbox"].tolist(),
                     keys_digest=digest(s["keys"]), sorted_ids_digest=digest(s["sorted_ids"]),
@@ -337,6 +356,131 @@ def scenario_fixture(ref, bh):
                     tree_digest=digest(s["tree_prefix"], s["tree_depth"], s["tree_mass"], s["tree_com"]),
                     acc_digest=digest(s["acc"]))
         (HERE / "scenario1.json").write_text(json.dumps(info, indent=1) + "\n")
+
+
+@contextlib.contextmanager
+def captured_stderr(lines: list):
+    """Collects what C++ code writes to fd 2 (std::cerr) into `lines`."""
+    sys.stderr.flush()
+    saved = os.dup(2)
+    with tempfile.TemporaryFile() as tmp:
+        os.dup2(tmp.fileno(), 2)
+        try:
+            yield
+        finally:
+            os.dup2(saved, 2)
+            os.close(saved)
+            tmp.seek(0)
+            lines.extend(tmp.read().decode(errors="replace").splitlines())
+
+
+def awkward_state(n=50, seed=3):
+    """A state with values the number formatting must get right: wide
+    exponents, signed zeros, inf/nan, a subnormal, large ids."""
+    rng = np.random.default_rng(seed)
+    pos = rng.normal(0, 3, (n, 3)) * 10.0 ** rng.integers(-12, 12, (n, 3))
+    vel = rng.normal(0, 1e-2, (n, 3))
+    acc = rng.normal(0, 1e-5, (n, 3))
+    pos[0] = [-0.0, 0.0, 1e300]
+    vel[1] = [np.inf, -np.inf, np.nan]
+    acc[2] = [1e-310, 0.0, 0.0]
+    acc[3] = [1e200, 1e200, 0.0]  # |a| overflows to inf
+    mass = rng.uniform(1e15, 1e25, n)
+    mass[4] = 0.0
+    ids = np.arange(n, dtype=np.uint64) * np.uint64(1 << 40) + np.uint64(7)
+    return ids, mass, pos, vel, acc
+
+
+# The reference driver runs the I/O fixtures pin: (name, command line).  The
+# input is bodies.csv (synthetic_1000's state); runs share one directory, so
+# the rerun finds the -r run's reference/final_ref.csv.
+CLI_RUNS = (
+    ("frames", ["-f", "bodies.csv", "--dt", "1h", "--tend", "1d", "--vs", "6h", "-o", "frames", "--fc", "tree"]),
+    ("limit", ["-f", "bodies.csv", "--dt", "2h", "--tend", "12h", "--vs", "4h", "-o", "limit", "-b", "400",
+               "--theta", "0.8", "--fc", "tree"]),
+    ("reference", ["-f", "bodies.csv", "--dt", "1h", "--tend", "6h", "--vs", "1d", "-o", "ref_out", "--fc", "tree",
+                   "-r"]),
+    ("rerun", ["-f", "bodies.csv", "--dt", "1h", "--tend", "6h", "--vs", "1d", "-o", "rerun_out", "--theta", "0.5",
+               "--fc", "tree"]),
+)
+
+
+def io_fixtures(ref):
+    out = {}
+    with tempfile.TemporaryDirectory() as d:
+        d = Path(d)
+        # readCSV (src/io.cpp:16-81)
+        for name, (make_rows, crlf, final_nl, limits) in csv_cases.cases().items():
+            f = d / f"{name}.csv"
+            out[f"csv/{name}/sha256"] = np.array([csv_cases.write(f, make_rows(), crlf, final_nl)])
+            for lim in limits:
+                warn = []
+                with captured_stderr(warn):
+                    ids, mass, pos, vel = ref.read_csv(f, lim)
+                key = f"csv/{name}/lim{lim}"
+                out[f"{key}/n"] = np.array([len(mass)])
+                out[f"{key}/digest"] = np.array([digest(ids, mass, pos, vel)])
+                out[f"{key}/warnings"] = np.array(["\n".join(warn)])
+                if len(mass) <= 4000:
+                    out[f"{key}/ids"] = ids; out[f"{key}/mass"] = mass; out[f"{key}/pos"] = pos
+                    out[f"{key}/vel"] = vel
+        for name, data in (("empty", b""), ("header_only", csv_cases.HEADER.encode()),
+                           ("header_newline", (csv_cases.HEADER + "\n").encode())):
+            f = d / f"{name}.csv"
+            f.write_bytes(data)
+            out[f"csv/{name}/n"] = np.array([len(ref.read_csv(f)[1])])
+        # writeSnapshot (src/io.cpp:84-232): rank 3, counter 2; and an empty state
+        ids, mass, pos, vel, acc = awkward_state()
+        ref.write_snapshot(3, 2, ids, mass, pos, vel, acc, d / "snap")
+        out.update({"vtp/ids": ids, "vtp/mass": mass, "vtp/pos": pos, "vtp/vel": vel, "vtp/acc": acc,
+                    "vtp/bytes": np.frombuffer((d / "snap" / "3" / "sim.2.vtp").read_bytes(), np.uint8)})
+        ref.write_snapshot(0, 0, ids[:0], mass[:0], pos[:0], vel[:0], acc[:0], d / "empty")
+        out["vtp/empty_writes_file"] = np.array([(d / "empty" / "0" / "sim.0.vtp").exists()])
+        # updatePVDFile (src/io.cpp:234-298) over three frames
+        args = ["-f", "data/bodies.csv", "--dt", "1h", "--tend", "10d", "--theta", "0.8", "-b", "500", "--fc", "tree"]
+        times = (0.0, 0.29166666666666663, 10.0 / 3.0)
+        (d / "pvd").mkdir()  # the driver creates it (main.cpp:125)
+        for k, t in enumerate(times):
+            ref.update_pvd(args, 1, k, t, d / "pvd")
+        (pvd,) = (d / "pvd").glob("*.pvd")
+        out.update({"pvd/args": np.array(args), "pvd/times": np.array(times), "pvd/name": np.array([pvd.name]),
+                    "pvd/bytes": np.frombuffer(pvd.read_bytes(), np.uint8)})
+        # The reference driver on one rank (main.cpp, --fc tree)
+        g = np.load(HERE / "synthetic_1000.npz")
+        run = d / "cli"
+        run.mkdir()
+        out["cli/bodies_sha256"] = np.array([csv_cases.write_bodies(run / "bodies.csv", g["ids"], g["mass"], g["pos"],
+                                                              g["vel"])])
+        cwd = os.getcwd()
+        os.chdir(run)
+        try:
+            for name, cli in CLI_RUNS:
+                summed, n, steps, frames = ref.run_cli(cli)
+                odir = run / cli[cli.index("-o") + 1]
+                files = sorted(str(p.relative_to(odir)) for p in odir.rglob("*") if p.is_file())
+                out[f"cli/{name}/args"] = np.array(cli)
+                out[f"cli/{name}/summed"] = np.array([summed])
+                out[f"cli/{name}/counts"] = np.array([n, steps, frames])
+                out[f"cli/{name}/files"] = np.array(files)
+                out[f"cli/{name}/sha256"] = np.array([hashlib.sha256((odir / f).read_bytes()).hexdigest()
+                                                      for f in files])
+                if name == "frames":
+                    for f in files:
+                        if f.endswith(".pvd") or f == "0/sim.0.vtp":
+                            out[f"cli/{name}/bytes/{f}"] = np.frombuffer((odir / f).read_bytes(), np.uint8)
+                if name == "reference":
+                    out["cli/final_ref_csv"] = np.frombuffer((run / "reference" / "final_ref.csv").read_bytes(),
+                                                             np.uint8)
+        finally:
+            os.chdir(cwd)
+        # loadReferenceCSV + computeDistanceSum on their own: the -r file
+        # against the 1,000-body state with ids in reverse order
+        n = len(g["mass"])
+        rp = ref.load_reference_csv(run / "reference", n)
+        out["cli/final_ref_loaded"] = rp
+        order = np.arange(n)[::-1]
+        out["cli/distance_sum_reversed"] = np.array([ref.distance_sum(g["pos"][order], g["ids"][order], rp)])
+    np.savez_compressed(HERE / "io.npz", **out)
 
 
 if __name__ == "__main__":

@@ -1,78 +1,31 @@
 """readCSV on the GPU (bh_read_csv_gpu, bh_load_csv) against the host
 reader (bh_read_csv: std::getline + std::stod, the reference's rules) and
 against Python's correctly rounded float(): the same rows, ids, values bit
-for bit, body_count limit and warnings."""
+for bit, body_count limit and warnings.  The comparisons with the
+reference's own readCSV are in test_io_pin.py."""
 from __future__ import annotations
 
 import random
-import struct
+import sys
 
 import numpy as np
 import pytest
 
-from conftest import assert_bits_equal
+from conftest import GOLDEN, assert_bits_equal
+
+sys.path.insert(0, str(GOLDEN))
+import csv_cases  # noqa: E402
 
 pytestmark = pytest.mark.gpu
 
-HEADER = "id,name,class,mass,pos_x,pos_y,pos_z,vel_x,vel_y,vel_z"
-
-
-def _num(rng: random.Random) -> str:
-    """A decimal field in one of the forms state-vector files and std::stod
-    accept."""
-    k = rng.random()
-    x = struct.unpack("<d", struct.pack("<Q", rng.getrandbits(64) & ~(0x7FF << 52) |
-                                        (rng.randint(1023 - 60, 1023 + 60) << 52)))[0]
-    if k < 0.25:
-        return repr(x)
-    if k < 0.45:
-        return f"{x:.18e}"
-    if k < 0.55:
-        return f"{x:.19g}"
-    if k < 0.70:  # 19 significant digits, random exponent
-        w = rng.randint(10 ** 18, 10 ** 19 - 1)
-        return f"{'-' if rng.random() < 0.5 else ''}{w}e{rng.randint(-60, 40)}"
-    if k < 0.80:  # near a rounding boundary: the midpoint of two doubles to 19-20 digits
-        from decimal import Decimal, getcontext
-        getcontext().prec = 50
-        b = struct.unpack("<Q", struct.pack("<d", abs(x)))[0]
-        mid = (Decimal(abs(x)) + Decimal(struct.unpack("<d", struct.pack("<Q", b + 1))[0])) / 2
-        return f"{mid:.19e}" if rng.random() < 0.5 else f"{mid:.18e}"
-    if k < 0.85:
-        return str(rng.randint(-10 ** 6, 10 ** 6))
-    if k < 0.90:
-        return rng.choice([" +0.5", ".5", "5.", "1e", "1e+", "-0", "0.000", "  7.25e-3", "3.0\r", "1E5", "0e999"])
-    if k < 0.95:  # exact halves and small exact values
-        return f"{rng.randint(1, 10 ** 6)}.{rng.choice(['5', '25', '125', '0625'])}"
-    return f"{rng.randint(1, 99)}.{rng.randint(0, 10 ** 17):017d}e{rng.randint(-30, 30)}"
-
-
-def _odd_rows():
-    """Rows the device hands to the host or rejects, and getline quirks."""
-    return [
-        "9,odd,AST,0x1p3,1,2,3,4,5,6",                     # hexadecimal: host
-        "10,odd,AST,inf,1,2,3,4,5,6",                      # inf: host (valid for std::stod)
-        "11,odd,AST,1.2345678901234567890123,1,2,3,4,5,6",  # 23 digits: host
-        "12,odd,AST,1e-320,1,2,3,4,5,6",                   # subnormal: host (ERANGE -> skipped)
-        "13,odd,AST,1e400,1,2,3,4,5,6",                    # overflow: skipped
-        "14,odd,AST,abc,1,2,3,4,5,6",                      # no conversion: skipped
-        "15,odd,AST,1,2,3,4",                               # short row: fields repeat the last piece
-        "16,odd,AST,1,2,3,4,5,6,",                          # trailing comma: an empty field
-        "",                                                 # empty line: skipped
-        "17,odd,AST,1,2,3,4,5,6,7,extra,columns",           # extra columns are ignored
-        "18,odd,AST,nan,1,2,3,4,5,6",                      # nan: host
-        "19,odd,AST,.,1,2,3,4,5,6",                        # no digits: skipped
-    ]
+HEADER = csv_cases.HEADER
+_num = csv_cases.num
+_odd_rows = csv_cases.odd_rows
+_rows = csv_cases.rows
 
 
 def _write(path, rows, crlf=False, final_newline=True):
-    nl = "\r\n" if crlf else "\n"
-    text = nl.join([HEADER] + rows) + (nl if final_newline else "")
-    path.write_bytes(text.encode())
-
-
-def _rows(rng, n):
-    return [f"{i},b{i},AST," + ",".join(_num(rng) for _ in range(7)) for i in range(n)]
+    csv_cases.write(path, rows, crlf, final_newline)
 
 
 def _same(a, b):
@@ -94,7 +47,7 @@ def test_gpu_reader_matches_host_reader(bh, tmp_path, capfd):
     gpu_err = capfd.readouterr().err
     assert len(host[0]) == len(rows) - 6  # abc, 1e400, 1e-320, the empty line, ".", the trailing comma
     _same(gpu, host)
-    # the same warnings (each printed twice by the two-call reader)
+    # the same warnings
     assert sorted(set(gpu_err.splitlines())) == sorted(set(host_err.splitlines()))
     assert len(set(host_err.splitlines())) == 6
     # limits: the reference stops after body_count rows
