@@ -2,6 +2,7 @@
 // transfers, the hot path stage by stage, the step loop and the stateless
 // host-buffer entry points.
 #include <algorithm>
+#include <atomic>
 #include <cmath>
 #include <cstdio>
 #include <cstring>
@@ -42,7 +43,7 @@ int grid256(int64_t n)
 {
     int64_t b = (n + 255) / 256;
     if (b < 1) b = 1;
-    return (int)std::min<int64_t>(b, 8 * bh::kNumSMs);
+    return (int)std::min<int64_t>(b, 8 * bh::num_sms());
 }
 
 // Carves one device allocation into aligned sub-buffers.
@@ -89,7 +90,7 @@ void layout(bh_context* ctx, Carver& c)
     ctx->lookback = c.take<uint32_t>(bh::kSortPasses * ctx->max_tiles * bh::kRadix);
     ctx->tile_ctr = c.take<uint32_t>(bh::kSortPasses);
     ctx->bbox = c.take<double>(8);
-    ctx->bbox_blocks = (int)std::min<int64_t>(std::max<int64_t>((n + 255) / 256, 1), 4 * bh::kNumSMs);
+    ctx->bbox_blocks = (int)std::min<int64_t>(std::max<int64_t>((n + 255) / 256, 1), 4 * bh::num_sms());
     ctx->bbox_part = reinterpret_cast<double*>(c.take<char>(bh::bbox_partial_bytes(ctx->bbox_blocks)));
     ctx->bbox_ticket = c.take<unsigned>(1);
     ctx->head = c.take<int32_t>(n + 1);
@@ -144,6 +145,19 @@ void collect_phases(bh_context* ctx);
 }  // namespace
 
 // Waits for the stream and turns a raised device error word into a status.
+int bh::num_sms()
+{
+    constexpr int kMaxDevices = 64;
+    static std::atomic<int> cache[kMaxDevices];
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= kMaxDevices) return 1;
+    int v = cache[dev].load(std::memory_order_relaxed);
+    if (v > 0) return v;
+    if (cudaDeviceGetAttribute(&v, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || v < 1) return 1;
+    cache[dev].store(v, std::memory_order_relaxed);
+    return v;
+}
+
 int bh::finish(bh_context* ctx, const char* fn)
 {
     BH_CUDA_TRY(cudaMemcpyAsync(ctx->h_err, ctx->err, sizeof(unsigned), cudaMemcpyDeviceToHost, ctx->stream));

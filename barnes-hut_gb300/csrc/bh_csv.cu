@@ -546,7 +546,7 @@ int csv_parse(bh_context* ctx, const char* path, int64_t body_count, const Out7*
     uint8_t* status = dstat.as<uint8_t>();
     nl_write_kernel<<<(unsigned)nch, kChunkThreads, 0, st>>>(dbuf.as<char>(), size, cnt, nl_pos);
     BH_LAUNCH_CHECK(ctx);
-    const int grid = (int)std::min<int64_t>((rows + 127) / 128, 64 * (int64_t)bh::kNumSMs);
+    const int grid = (int)std::min<int64_t>((rows + 127) / 128, 64 * (int64_t)bh::num_sms());
     row_parse_kernel<<<grid, 128, 0, st>>>(dbuf.as<char>(), size, nl_pos, nl, rows, vals, status);
     BH_LAUNCH_CHECK(ctx);
 

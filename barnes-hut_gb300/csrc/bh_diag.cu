@@ -240,7 +240,7 @@ int bh_measure_fma_peak(bh_context* ctx, int fp64, double* tflops_out)
 {
     if (!ctx || !tflops_out) return bh_fail(BH_ERR_INVALID_ARGUMENT, "bh_measure_fma_peak: bad arguments");
     BH_CUDA_TRY(cudaSetDevice(ctx->device));
-    const int blocks = 8 * bh::kNumSMs, threads = 256;
+    const int blocks = 8 * bh::num_sms(), threads = 256;
     const int iters = fp64 ? 2048 : 32768;
     void* out = nullptr;
     BH_CUDA_TRY(cudaMallocAsync(&out, sizeof(double) * blocks * threads, ctx->stream));
@@ -295,7 +295,7 @@ int bh_invariants(bh_context* ctx, double G, double theta, double out[9])
         if ((rc = bh::launch_direct_extract(ctx, G))) return rc;
     }
     // Every kernel below writes one partial per block into its own column.
-    const int blocks = 8 * bh::kNumSMs;
+    const int blocks = 8 * bh::num_sms();
     double* part = nullptr;
     BH_CUDA_TRY(cudaMallocAsync(&part, sizeof(double) * blocks * 9, ctx->stream));
     BH_CUDA_TRY(cudaMemsetAsync(part, 0, sizeof(double) * blocks * 9, ctx->stream));

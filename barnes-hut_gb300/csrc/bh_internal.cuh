@@ -30,7 +30,11 @@ constexpr int kRadix = 256;
 constexpr int kSortThreads = 512;      // onesweep tile: 512 threads x 8 keys
 constexpr int kSortItems = 8;
 constexpr int kSortTile = kSortThreads * kSortItems;
-constexpr int kNumSMs = 152;
+
+// SM count of the current device (cudaDevAttrMultiProcessorCount), read once
+// per device and cached; grids are sized in multiples of it.  1 when the
+// device cannot be queried (the launch that follows reports the error).
+int num_sms();
 
 // Device error word bits (OR-ed by kernels, read back by bh_context_sync).
 enum : unsigned {

@@ -67,7 +67,7 @@ extern "C" int bh_kepler_to_cartesian_gpu(const double* el, int64_t n, double* o
     if (e == cudaSuccess) e = cudaMemcpy(del, el, sizeof(double) * 8 * n, cudaMemcpyHostToDevice);
     if (e == cudaSuccess) {
         const int64_t want = (n + 255) / 256;
-        const int blocks = (int)(want > 16 * bh::kNumSMs ? 16 * bh::kNumSMs : want);
+        const int blocks = (int)(want > 16 * bh::num_sms() ? 16 * bh::num_sms() : want);
         kepler_kernel<<<blocks, 256>>>(n, del, dout);
         e = cudaGetLastError();
     }

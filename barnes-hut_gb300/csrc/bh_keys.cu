@@ -212,7 +212,7 @@ int launch_hist(bh_context* ctx)
     if (ctx->n == 0) return BH_OK;
     BH_CUDA_TRY(cudaMemsetAsync(ctx->hist, 0, sizeof(uint32_t) * kSortPasses * kRadix, ctx->stream));
     int64_t want = (ctx->n + kKeyThreads * 4 - 1) / (kKeyThreads * 4);
-    const int blocks = (int)(want < 1 ? 1 : (want > 4 * kNumSMs ? 4 * kNumSMs : want));
+    const int blocks = (int)(want < 1 ? 1 : (want > 4 * bh::num_sms() ? 4 * bh::num_sms() : want));
     hist_kernel<<<blocks, kKeyThreads, 0, ctx->stream>>>(ctx->n, ctx->key, ctx->hist);
     BH_LAUNCH_CHECK(ctx);
     return BH_OK;
@@ -236,7 +236,7 @@ int launch_keys(bh_context* ctx, bool with_hist)
     if (ctx->n == 0) return BH_OK;
     if (with_hist) BH_CUDA_TRY(cudaMemsetAsync(ctx->hist, 0, sizeof(uint32_t) * kSortPasses * kRadix, ctx->stream));
     int64_t want = (ctx->n + kKeyThreads * 4 - 1) / (kKeyThreads * 4);
-    const int blocks = (int)(want < 1 ? 1 : (want > 4 * kNumSMs ? 4 * kNumSMs : want));
+    const int blocks = (int)(want < 1 ? 1 : (want > 4 * bh::num_sms() ? 4 * bh::num_sms() : want));
     keys_kernel<<<blocks, kKeyThreads, 0, ctx->stream>>>(ctx->n, ctx->px, ctx->py, ctx->pz, ctx->bbox, ctx->key,
                                                          ctx->hist, with_hist ? 1 : 0);
     BH_LAUNCH_CHECK(ctx);

@@ -225,7 +225,7 @@ int bh_learned_collect(bh_context* ctx, double theta, double theta_label, double
     if (cudaStreamSynchronize(st) != cudaSuccess) { cleanup(); return bh_fail(BH_ERR_CUDA, "bh_learned_collect: collection failed"); }
     const int64_t np = (int64_t)total < max_pairs ? (int64_t)total : max_pairs;
     if (np > 0) {
-        const int64_t blocks = std::min<int64_t>((np + kLW - 1) / kLW, 16 * kNumSMs);
+        const int64_t blocks = std::min<int64_t>((np + kLW - 1) / kLW, 16 * bh::num_sms());
         label_kernel<<<(unsigned)blocks, 32 * kLW, 0, st>>>(np, grp, slot, mask, asc, ctx->n, ctx->px, ctx->py, ctx->pz,
                                                             ctx->body_leaf, ctx->rec, ctx->bbox,
                                                             theta_label * theta_label, G, lab, ctx->err);

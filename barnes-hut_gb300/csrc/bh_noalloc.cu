@@ -89,7 +89,7 @@ namespace bh {
 int launch_digit_hist(int64_t n, const uint64_t* keys, uint32_t* hist, cudaStream_t st)
 {
     int64_t blocks = (n + kHistThreads * 4 - 1) / (kHistThreads * 4);
-    if (blocks > 4 * bh::kNumSMs) blocks = 4 * bh::kNumSMs;
+    if (blocks > 4 * bh::num_sms()) blocks = 4 * bh::num_sms();
     if (blocks < 1) blocks = 1;
     noalloc_hist_kernel<<<(unsigned)blocks, kHistThreads, 0, st>>>(n, keys, hist);
     BH_CUDA_TRY(cudaGetLastError());
@@ -122,7 +122,8 @@ extern "C" int bh_sort_keys_noalloc(const uint64_t* keys_in, uint64_t* keys_out,
     unsigned* err = reinterpret_cast<unsigned*>(base + kOffErr);
 
     if (n == 1) {
-        BH_CUDA_TRY(cudaMemcpyAsync(keys_out, keys_in, sizeof(uint64_t), cudaMemcpyDeviceToDevice, st));
+        if (keys_out != keys_in)
+            BH_CUDA_TRY(cudaMemcpyAsync(keys_out, keys_in, sizeof(uint64_t), cudaMemcpyDeviceToDevice, st));
         BH_CUDA_TRY(cudaMemsetAsync(perm_out, 0, sizeof(uint32_t), st));
         BH_CUDA_TRY(cudaStreamSynchronize(st));
         return BH_OK;

@@ -97,7 +97,7 @@ extern "C" int bh_selftest(int which, int64_t n, uint64_t seed, int64_t* failure
     BH_CUDA_TRY(cudaMalloc(&d, sizeof(unsigned long long)));
     BH_CUDA_TRY(cudaMemset(d, 0, sizeof(unsigned long long)));
     const int64_t blocks64 = (n + 255) / 256;
-    const int blocks = (int)(blocks64 < 1 ? 1 : (blocks64 > 8 * bh::kNumSMs ? 8 * bh::kNumSMs : blocks64));
+    const int blocks = (int)(blocks64 < 1 ? 1 : (blocks64 > 8 * bh::num_sms() ? 8 * bh::num_sms() : blocks64));
     selftest_kernel<<<blocks, 256>>>(which, n, seed, d);
     cudaError_t e = cudaGetLastError();
     if (e == cudaSuccess) e = cudaDeviceSynchronize();

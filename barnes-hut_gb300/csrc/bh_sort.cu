@@ -288,7 +288,7 @@ int launch_permute(bh_context* ctx)
     const int64_t n = ctx->n;
     if (n == 0) return BH_OK;
     int64_t want = (n + kPermThreads - 1) / kPermThreads;
-    const int blocks = (int)(want > 8 * kNumSMs ? 8 * kNumSMs : want);
+    const int blocks = (int)(want > 8 * bh::num_sms() ? 8 * bh::num_sms() : want);
     permute_kernel<<<blocks, kPermThreads, 0, ctx->stream>>>(n, ctx->perm, ctx->px, ctx->py, ctx->pz, ctx->vx, ctx->vy,
                                                              ctx->vz, ctx->m, ctx->id, ctx->px2, ctx->py2, ctx->pz2,
                                                              ctx->vx2, ctx->vy2, ctx->vz2, ctx->m2, ctx->id2);

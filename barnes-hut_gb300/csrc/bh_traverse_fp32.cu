@@ -693,7 +693,7 @@ int grid_n(int64_t n)
 {
     int64_t b = (n + 255) / 256;
     if (b < 1) b = 1;
-    return (int)(b > 8 * kNumSMs ? 8 * kNumSMs : b);
+    return (int)(b > 8 * bh::num_sms() ? 8 * bh::num_sms() : b);
 }
 
 template <bool kFP64, int kLearn>

@@ -527,7 +527,7 @@ int launch_build(bh_context* ctx, const double* mass, bool moments, bool far_fus
     const int64_t n = ctx->n;
     if (n == 0) return BH_OK;
     cudaStream_t st = ctx->stream;
-    const int maxb = 8 * kNumSMs;
+    const int maxb = 8 * bh::num_sms();
     const int g = grid_for(n, kThreads, maxb);
 
     // 1. leaves

@@ -222,15 +222,27 @@ def cpu_baseline(pos, vel, mass, ids, budget_s: float, theta: float = THETA, nst
             "sample": f"{steps} full steps of the {n:,}-body workload ({secs:.1f} s, OpenMP {cores} threads)"}
 
 
+DATA = "synthetic (seeded solar system: the engine's generator; the reference arm uses its bit-exact restatement)"
+
+
+def bench_config(args, n: int, ws: int) -> dict:
+    """The workload description both arms print (same keys and values)."""
+    return {"workload": workload_name(args), "bodies": n, "theta": args.theta, "dt_days": DT, "mode": args.mode,
+            "seed": SEED, "outer": args.outer, "trojan": args.trojan,
+            "l2": "flushed before every timed step (256 MiB write)", "parallelism": f"replicas x{ws}"}
+
+
 def run_reference(args, rank):
-    """The reference arm: the reference's CPU path (compiled sources where the
-    checkout exists, else the oracle port) on every host core, rank 0 only."""
+    """The reference arm: the reference's CPU path (its compiled sources
+    where they were built on this host, else the oracle port) on every host
+    core, rank 0 only.  The inputs come from the oracle's restatement of the
+    seeded generator, so this arm loads nothing of the engine."""
     if rank != 0:
         return
-    bh = importlib.import_module("barnes-hut_gb300")
-    pos, vel, mass, ids = bh.generate_system(SEED, args.bodies, args.outer, args.trojan)
     from oracle.oracle import Oracle
-    o, kind = Oracle("port"), "port"
+    port = Oracle("port")
+    pos, vel, mass, ids = port.generate_system(SEED, args.bodies, args.outer, args.trojan)
+    o, kind = port, "port"
     try:
         o, kind = Oracle("reference"), "reference"
     except (FileNotFoundError, OSError):
@@ -249,13 +261,14 @@ def run_reference(args, rank):
     o.simulate(p, v, m, i, DT, theta, G, k, t=t, acc=a)
     secs = time.perf_counter() - t0
     val = n * k / secs
-    cores = Oracle("port").threads()
+    cores = port.threads()
+    what = "the reference's own sources compiled on this host" if kind == "reference" else \
+        "the oracle port (C restatement of the reference's path; the reference checkout is not on this host)"
     line = {"metric": "body-steps/s", "value": val, "unit": "body-steps/s", "n_gpus": args.gpus, "steps": k,
             "warmup": warm, "ms_per_step": 1e3 * secs / k, "higher_is_better": True, "scaling": "weak",
-            "vs_baseline": None, "dtype": "f64", "data": "synthetic", "impl": "reference",
-            "config": {"workload": workload_name(args), "bodies": n, "theta": theta, "dt_days": DT,
-                       "mode": f"CPU, {kind} ({'compiled reference sources' if kind == 'reference' else 'oracle port'})",
-                       "seed": SEED, "parallelism": f"OpenMP {cores} threads"},
+            "vs_baseline": None, "dtype": "f64", "data": DATA, "impl": "reference",
+            "config": bench_config(args, n, args.gpus),
+            "reference_impl": f"CPU, {what}, OpenMP {cores} threads",
             "cpu_baseline": {"value": val, "unit": "body-steps/s", "cores": cores, "kind": kind,
                              "sample": f"{k} timed full steps after {warm} warm-up steps, OpenMP {cores} threads"},
             "e2e": {"value": val, "unit": "body-steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
@@ -843,10 +856,8 @@ def run_ours(args, rank, ws, local):
         "metric": "body-steps/s", "value": value, "unit": "body-steps/s", "n_gpus": ws, "steps": k,
         "warmup": args.warmup, "ms_per_step": total_ms / k, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f64" if mode <= 1 else "f32 far field + f64 state/direct terms",
-        "data": "synthetic (seeded solar system generated through bh_generate_system)",
-        "config": {"workload": workload_name(args), "bodies": n, "theta": theta, "dt_days": DT, "mode": args.mode,
-                   "seed": SEED, "l2": "flushed before every timed step (256 MiB write)",
-                   "parallelism": f"replicas x{ws}"},
+        "data": DATA,
+        "config": bench_config(args, n, ws),
         "roofline": {"kernel": KERNEL[mode], "bound": fp, "achieved": achieved,
                      "peak": peak, "unit": "TFLOP/s", "frac": achieved / peak,
                      "peak_source": f"measured in-process: {fp.upper()} FMA chains (bh_measure_fma_peak)",

@@ -389,72 +389,118 @@ int orc_tree_records(void *h, uint64_t *prefix, uint8_t *depth, double *mass, do
 /* side(d) = maxspan/2^d.  Summation order equals the reference's.      */
 /* n_inter (optional): accepted interactions per body.                  */
 /* ------------------------------------------------------------------ */
-int orc_accelerations(void *h, int64_t n, const uint64_t *key, const double *pos, double theta,
-                      double G, double soft2, const double bb[6], double *acc, int64_t *n_inter)
+typedef struct {
+    double theta2;
+    double side2[ORC_MAX_DEPTH + 1];
+    uint64_t stride[ORC_MAX_DEPTH + 1];
+} orc_walk_params;
+
+static void orc_walk_init(orc_walk_params *w, double theta, const double bb[6])
 {
-    const orc_tree *t = (const orc_tree *)h;
-    const double theta2 = theta * theta;
+    w->theta2 = theta * theta;
     double dx = bb[3] - bb[0], dy = bb[4] - bb[1], dz = bb[5] - bb[2];
     double L = dx;
     if (L < dy) L = dy;
     if (L < dz) L = dz;
-    double side2[ORC_MAX_DEPTH + 1];
-    uint64_t stride[ORC_MAX_DEPTH + 1];
     for (int d = 0; d <= ORC_MAX_DEPTH; ++d) {
         double side = L / (double)(1ULL << d);
-        side2[d] = side * side;
-        stride[d] = 1ULL << (63 - 3 * d);
+        w->side2[d] = side * side;
+        w->stride[d] = 1ULL << (63 - 3 * d);
     }
+}
+
+/* One body's walk (traversal.cpp:57-101): its acceleration into a[3] and
+ * its accepted interactions into *cnt_out; returns ORC_ERR_STACK when the
+ * 256-entry stack would overflow. */
+static int orc_walk_one(const orc_tree *t, const orc_walk_params *w, uint64_t key, const double p[3], double G,
+                        double soft2, double a[3], int64_t *cnt_out)
+{
+    uint64_t sp[ORC_STACK_MAX];
+    int sd[ORC_STACK_MAX];
+    int top = 0, err = ORC_OK;
+    double ax = 0.0, ay = 0.0, az = 0.0;
+    int64_t cnt = 0;
+    const double px = p[0], py = p[1], pz = p[2];
+    sp[top] = 0;
+    sd[top] = 0;
+    top++;
+    while (top) {
+        --top;
+        uint64_t pref = sp[top];
+        int dep = sd[top];
+        const orc_node *nd = orc_tree_find(t, pref, dep);
+        if (!nd || nd->mass == 0.0) continue;
+        if (dep == ORC_MAX_DEPTH && pref == key) continue;
+        double ex = nd->cx - px, ey = nd->cy - py, ez = nd->cz - pz;
+        double r2 = ex * ex + ey * ey + ez * ez + soft2;
+        if (dep == ORC_MAX_DEPTH || w->side2[dep] < w->theta2 * r2) {
+            double invR = 1.0 / sqrt(r2);
+            double invR3 = invR * invR * invR;
+            double s = G * nd->mass * invR3;
+            ax += s * ex;
+            ay += s * ey;
+            az += s * ez;
+            cnt++;
+        } else {
+            int cd = dep + 1;
+            for (int oc = 0; oc < 8; ++oc) {
+                uint64_t c = pref + w->stride[cd] * (uint64_t)oc;
+                if (!orc_tree_find(t, c, cd)) continue;
+                if (top >= ORC_STACK_MAX) {
+                    err = ORC_ERR_STACK;
+                    top = 0;
+                    break;
+                }
+                sp[top] = c;
+                sd[top] = cd;
+                top++;
+            }
+        }
+    }
+    a[0] = ax;
+    a[1] = ay;
+    a[2] = az;
+    *cnt_out = cnt;
+    return err;
+}
+
+int orc_accelerations(void *h, int64_t n, const uint64_t *key, const double *pos, double theta,
+                      double G, double soft2, const double bb[6], double *acc, int64_t *n_inter)
+{
+    const orc_tree *t = (const orc_tree *)h;
+    orc_walk_params w;
+    orc_walk_init(&w, theta, bb);
     int err = ORC_OK;
 #pragma omp parallel for schedule(dynamic, 256)
     for (int64_t i = 0; i < n; ++i) {
-        uint64_t sp[ORC_STACK_MAX];
-        int sd[ORC_STACK_MAX];
-        int top = 0;
-        double ax = 0.0, ay = 0.0, az = 0.0;
-        int64_t cnt = 0;
-        const double px = pos[3 * i], py = pos[3 * i + 1], pz = pos[3 * i + 2];
-        sp[top] = 0;
-        sd[top] = 0;
-        top++;
-        while (top) {
-            --top;
-            uint64_t pref = sp[top];
-            int dep = sd[top];
-            const orc_node *nd = orc_tree_find(t, pref, dep);
-            if (!nd || nd->mass == 0.0) continue;
-            if (dep == ORC_MAX_DEPTH && pref == key[i]) continue;
-            double ex = nd->cx - px, ey = nd->cy - py, ez = nd->cz - pz;
-            double r2 = ex * ex + ey * ey + ez * ez + soft2;
-            if (dep == ORC_MAX_DEPTH || side2[dep] < theta2 * r2) {
-                double invR = 1.0 / sqrt(r2);
-                double invR3 = invR * invR * invR;
-                double s = G * nd->mass * invR3;
-                ax += s * ex;
-                ay += s * ey;
-                az += s * ez;
-                cnt++;
-            } else {
-                int cd = dep + 1;
-                for (int oc = 0; oc < 8; ++oc) {
-                    uint64_t c = pref + stride[cd] * (uint64_t)oc;
-                    if (!orc_tree_find(t, c, cd)) continue;
-                    if (top >= ORC_STACK_MAX) {
+        int64_t cnt;
+        if (orc_walk_one(t, &w, key[i], pos + 3 * i, G, soft2, acc + 3 * i, &cnt) != ORC_OK) {
 #pragma omp atomic write
-                        err = ORC_ERR_STACK;
-                        top = 0;
-                        break;
-                    }
-                    sp[top] = c;
-                    sd[top] = cd;
-                    top++;
-                }
-            }
+            err = ORC_ERR_STACK;
         }
-        acc[3 * i + 0] = ax;
-        acc[3 * i + 1] = ay;
-        acc[3 * i + 2] = az;
         if (n_inter) n_inter[i] = cnt;
+    }
+    return err;
+}
+
+/* The same walk for a sample of bodies: body targets[k] (an index into
+ * key/pos) gives acc[3k..3k+2] and n_inter[k] (optional). */
+int orc_accelerations_at(void *h, int64_t ns, const int64_t *targets, const uint64_t *key, const double *pos,
+                         double theta, double G, double soft2, const double bb[6], double *acc, int64_t *n_inter)
+{
+    const orc_tree *t = (const orc_tree *)h;
+    orc_walk_params w;
+    orc_walk_init(&w, theta, bb);
+    int err = ORC_OK;
+#pragma omp parallel for schedule(dynamic, 16)
+    for (int64_t k = 0; k < ns; ++k) {
+        const int64_t i = targets[k];
+        int64_t cnt;
+        if (orc_walk_one(t, &w, key[i], pos + 3 * i, G, soft2, acc + 3 * k, &cnt) != ORC_OK) {
+#pragma omp atomic write
+            err = ORC_ERR_STACK;
+        }
+        if (n_inter) n_inter[k] = cnt;
     }
     return err;
 }
@@ -888,6 +934,117 @@ void orc_kepler_to_cartesian(const double *el, int64_t n, double *out)
         o[4] = R21 * vxo + R22 * vyo;
         o[5] = R31 * vxo + R32 * vyo;
     }
+}
+
+/* ------------------------------------------------------------------ */
+/* The seeded synthetic solar system the configurations name (no        */
+/* reference counterpart: the reference reads CSV files).  Restates the */
+/* engine's generator draw for draw so the reference arm of the bench    */
+/* and the tests can make the same inputs without the engine's library: */
+/* the Sun at rest at the origin; the eight planets on circular          */
+/* coplanar orbits (mass and a from the reference's                      */
+/* data/orbital_elements_raw_csvs/planets_and_moons.csv:2-9), mean       */
+/* anomaly U[0,2pi); then inner-belt, outer-belt and trojan asteroids    */
+/* (a, e, i, Omega, omega, M as documented in include/bh_gpu.h), mass    */
+/* log-uniform on [1e12, 1e20] kg; each converted by the Kepler          */
+/* conversion above with mu = G M_sun and epoch J2000.  Uniform draws    */
+/* are the top 53 bits of one mt19937_64 output (Matsumoto-Nishimura     */
+/* 64-bit Mersenne Twister, seeded by its standard linear recurrence)    */
+/* scaled by 2^-53.                                                     */
+/* ------------------------------------------------------------------ */
+typedef struct {
+    uint64_t mt[312];
+    int idx;
+} orc_mt64;
+
+static void orc_mt64_seed(orc_mt64 *g, uint64_t seed)
+{
+    g->mt[0] = seed;
+    for (int i = 1; i < 312; ++i)
+        g->mt[i] = 6364136223846793005ULL * (g->mt[i - 1] ^ (g->mt[i - 1] >> 62)) + (uint64_t)i;
+    g->idx = 312;
+}
+
+static uint64_t orc_mt64_next(orc_mt64 *g)
+{
+    if (g->idx >= 312) {
+        for (int i = 0; i < 312; ++i) {
+            uint64_t y = (g->mt[i] & 0xFFFFFFFF80000000ULL) | (g->mt[(i + 1) % 312] & 0x7FFFFFFFULL);
+            uint64_t v = g->mt[(i + 156) % 312] ^ (y >> 1);
+            if (y & 1ULL) v ^= 0xB5026F5AA96619E9ULL;
+            g->mt[i] = v;
+        }
+        g->idx = 0;
+    }
+    uint64_t x = g->mt[g->idx++];
+    x ^= (x >> 29) & 0x5555555555555555ULL;
+    x ^= (x << 17) & 0x71D67FFFEDA60000ULL;
+    x ^= (x << 37) & 0xFFF7EEE000000000ULL;
+    x ^= x >> 43;
+    return x;
+}
+
+static double orc_u(orc_mt64 *g, double lo, double hi)
+{
+    double u = (double)(orc_mt64_next(g) >> 11) * (1.0 / 9007199254740992.0);
+    return lo + (hi - lo) * u;
+}
+
+int orc_generate_system(uint64_t seed, int64_t n, double frac_outer, double frac_trojan, double *pos, double *vel,
+                        double *mass, uint64_t *ids)
+{
+    static const double pm[8] = {3.301011e+23, 4.86732e+24, 5.972186e+24, 6.416928e+23,
+                                 1.89813e+27, 5.683191e+26, 8.681013e+25, 1.024096e+26};
+    static const double pa[8] = {0.3870982252718477, 0.723326849675607, 1.000371833994387, 1.52367818431121,
+                                 5.205108585205607, 9.581451990534042, 19.22994588008584, 30.10071183142183};
+    const double pi = 3.14159265358979323846, two_pi = 2.0 * pi, deg = pi / 180.0;
+    const double sun = 1.989e30, mu = 1.48812e-34 * sun, j2000 = 2451544.5;
+    if (n < 9 || frac_outer < 0 || frac_trojan < 0 || frac_outer + frac_trojan > 1) return 1;
+    orc_mt64 *g = (orc_mt64 *)malloc(sizeof(orc_mt64));
+    if (!g) return ORC_ERR_OOM;
+    orc_mt64_seed(g, seed);
+    const int64_t nast = n - 9;
+    const int64_t n_outer = (int64_t)llround(frac_outer * (double)nast);
+    const int64_t n_troj = (int64_t)llround(frac_trojan * (double)nast);
+    const int64_t n_inner = nast - n_outer - n_troj;
+    double q[8], st[6];
+    for (int a = 0; a < 3; ++a) pos[a] = vel[a] = 0.0;
+    mass[0] = sun;
+    double lambda_j = 0.0;
+    for (int k = 0; k < 8; ++k) {
+        const double M = orc_u(g, 0.0, two_pi);
+        if (k == 4) lambda_j = M;
+        q[0] = 0.0; q[1] = pa[k]; q[2] = 0.0; q[3] = 0.0; q[4] = 0.0; q[5] = M; q[6] = j2000; q[7] = mu;
+        orc_kepler_to_cartesian(q, 1, st);
+        for (int a = 0; a < 3; ++a) { pos[3 * (1 + k) + a] = st[a]; vel[3 * (1 + k) + a] = st[3 + a]; }
+        mass[1 + k] = pm[k];
+    }
+    const double lmin = log(1e12), lmax = log(1e20);
+    for (int64_t k = 0; k < nast; ++k) {
+        const int64_t b = 9 + k;
+        double a, e, inc, Om, w, M;
+        if (k < n_inner) {
+            a = orc_u(g, 2.1, 3.3); e = orc_u(g, 0.0, 0.3); inc = orc_u(g, 0.0, 20.0) * deg;
+            Om = orc_u(g, 0.0, two_pi); w = orc_u(g, 0.0, two_pi); M = orc_u(g, 0.0, two_pi);
+        } else if (k < n_inner + n_outer) {
+            a = orc_u(g, 30.0, 50.0); e = orc_u(g, 0.0, 0.2); inc = orc_u(g, 0.0, 30.0) * deg;
+            Om = orc_u(g, 0.0, two_pi); w = orc_u(g, 0.0, two_pi); M = orc_u(g, 0.0, two_pi);
+        } else {
+            a = 5.2; e = orc_u(g, 0.0, 0.1); inc = orc_u(g, 0.0, 20.0) * deg;
+            Om = orc_u(g, 0.0, two_pi); w = orc_u(g, 0.0, two_pi);
+            const double side = ((k - n_inner - n_outer) & 1) ? -60.0 : 60.0;
+            const double lam = lambda_j + (side + orc_u(g, -30.0, 30.0)) * deg;
+            M = fmod(lam - Om - w, two_pi);
+            if (M < 0) M += two_pi;
+        }
+        mass[b] = exp(orc_u(g, lmin, lmax));
+        q[0] = e; q[1] = a; q[2] = inc; q[3] = w; q[4] = Om; q[5] = M; q[6] = j2000; q[7] = mu;
+        orc_kepler_to_cartesian(q, 1, st);
+        for (int c = 0; c < 3; ++c) { pos[3 * b + c] = st[c]; vel[3 * b + c] = st[3 + c]; }
+    }
+    for (int64_t i = 0; i < n; ++i) ids[i] = (uint64_t)i;
+    free(g);
+    return ORC_OK;
 }
 
 int orc_num_threads(void)

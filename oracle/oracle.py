@@ -81,6 +81,8 @@ class Oracle:
             self._records = f("tree_records", C.c_int, [_P, _P, _P, _P, _P])
             self._free = f("tree_free", None, [_P])
             self._accel = f("accelerations", C.c_int, [_P, _I64, _P, _P, _D, _D, _D, _P, _P, _P])
+            self._gen = f("generate_system", C.c_int, [C.c_uint64, _I64, _D, _D, _P, _P, _P, _P])
+            self._accel_at = f("accelerations_at", C.c_int, [_P, _I64, _P, _P, _P, _D, _D, _D, _P, _P, _P])
             self._sim = f("simulate", C.c_int, [_I64, _P, _P, _P, _P, _P, _D, _D, _D, _I64, _P, _P])
             self._kepler = f("kepler_to_cartesian", None, [_P, _I64, _P])
             self._direct = f("direct_sum", None, [_I64, _P, _P, _I64, _P, _D, _P])
@@ -163,6 +165,22 @@ class Oracle:
         self._accel(tree.h, len(k), _ptr(k), _ptr(p), theta, G, soft2, _ptr(bb), _ptr(acc))
         return acc
 
+    def accelerations_at(self, tree, keys, pos, targets, theta, G, soft2, bbox):
+        """computeAccelerations' walk for the bodies `targets` (indices into
+        keys/pos) only: (acc (k, 3), interactions (k,)).  Port only."""
+        k = np.ascontiguousarray(keys, np.uint64)
+        p = np.ascontiguousarray(pos, np.float64).reshape(-1, 3)
+        t = np.ascontiguousarray(targets, np.int64)
+        if len(t) and (t.min() < 0 or t.max() >= len(k)):
+            raise IndexError("target out of range")
+        bb = np.ascontiguousarray(bbox, np.float64)
+        acc = np.empty((len(t), 3))
+        cnt = np.empty(len(t), np.int64)
+        rc = self._accel_at(tree.h, len(t), _ptr(t), _ptr(k), _ptr(p), theta, G, soft2, _ptr(bb), _ptr(acc), _ptr(cnt))
+        if rc:
+            raise RuntimeError(f"oracle traversal failed: {rc}")
+        return acc, cnt
+
     def let_export(self, tree, boxes, bbox, theta2, max_depth=21):
         """createInteractionListForRank (src/exchange.cpp:117-179) on `tree`:
         the exported cells (prefix, depth, mass, com) sorted by (depth, prefix)."""
@@ -236,6 +254,15 @@ class Oracle:
         out = np.empty(9)
         self._inv(len(m), _ptr(p), _ptr(v), _ptr(m), G, _ptr(out))
         return out
+
+    def generate_system(self, seed, n, frac_outer=0.0, frac_trojan=0.0):
+        """The seeded synthetic solar system (port only): (pos, vel, mass,
+        ids), the engine generator's draws restated."""
+        pos = np.empty((n, 3)); vel = np.empty((n, 3)); mass = np.empty(n); ids = np.empty(n, np.uint64)
+        if self._gen(int(seed), int(n), float(frac_outer), float(frac_trojan), _ptr(pos), _ptr(vel), _ptr(mass),
+                     _ptr(ids)):
+            raise ValueError("generate_system: need n >= 9 and fractions in [0, 1]")
+        return pos, vel, mass, ids
 
     def threads(self) -> int:
         return int(self._threads()) if self.kind == "port" else -1

@@ -211,39 +211,57 @@ def test_errors_are_statuses(bh, ctx):
     ctx.step(DT, THETA, G, 1)
 
 
-def test_4m_properties(bh):
-    """The combined-scale size (4,000,000 bodies, 85/10/5): size-independent checks."""
+def test_4m_against_oracle(bh, port):
+    """The combined-scale size (4,000,000 bodies, 85/10/5): bbox, keys,
+    permutation and the whole tree (node set, masses, centres of mass after
+    the single-rank merge) bit for bit against the oracle; for 2,048 seeded
+    bodies the plain mode's accelerations equal the oracle's walk
+    (traversal.cpp:13-103) bit for bit and the FP64 list mode's per-body
+    interaction counts equal the oracle's (its accelerations within 1e-13 of
+    the plain mode's); the sort is stable on equal keys; the median error
+    against the FP64 direct sum stays under 1e-5."""
+    import ctypes as C
     n = 4_000_000
     pos, vel, mass, ids = bh.generate_system(5, n, 0.10, 0.05)
+    bb = port.bbox(pos)
+    keys = port.keys(pos, bb)
+    sk, sp, sm, sv, si, _ = port.sort(keys, pos, mass, vel, ids)
     with bh.Context(n) as c:
         c.set_bodies(pos, vel, mass, ids)
-        bb = c.compute_bbox()
-        assert np.array_equal(bb[:3], pos.min(axis=0)) and np.array_equal(bb[3:], pos.max(axis=0))
-        keys = c.compute_keys()
+        assert_bits_equal(c.compute_bbox(), bb, "bbox")
+        assert_bits_equal(c.compute_keys(), keys, "keys")
         perm = c.sort_bodies()
-        assert np.array_equal(np.sort(perm), np.arange(n))
-        sk = keys[perm]
-        assert np.all(sk[1:] >= sk[:-1])
-        # stability: equal keys keep their input order
-        eq = sk[1:] == sk[:-1]
-        assert np.all(perm[1:][eq] > perm[:-1][eq])
+        assert_bits_equal(ids[perm], si, "permutation")
+        eq = keys[perm][1:] == keys[perm][:-1]
+        assert np.all(perm[1:][eq] > perm[:-1][eq]), "equal keys keep their input order"
         c.build_tree()
-        info = c.tree_info()
-        assert info["leaves"] == len(np.unique(sk))
-        acc = c.compute_accelerations()
-        assert np.all(np.isfinite(acc))
-        _, _, m_sorted, ids_sorted, _ = c.get_bodies()
-        assert np.array_equal(ids_sorted, ids[perm])
-        rng = np.random.default_rng(0)
-        sample = rng.choice(n, 256, replace=False)
+        got_tree = c.export_tree()
+        acc = c.compute_accelerations(THETA, G, 0.0, bh.MODE_PLAIN_FP64)
+        counts_plain = c.interaction_counts()
+        acc_list = c.compute_accelerations(THETA, G, 0.0, bh.MODE_FP64_LIST)
+        counts_list = c.interaction_counts()
+        p_sorted, _, _, ids_sorted, _ = c.get_bodies()
+        assert_bits_equal(p_sorted, sp, "sorted positions")
+        sample = np.random.default_rng(0).choice(n, 256, replace=False)
         ref = np.empty((256, 3))
-        lib = bh.library()
-        import ctypes as C
         tgt = np.ascontiguousarray(sample, np.int64)
-        rc = lib.bh_direct_sum(c.handle, 256, tgt.ctypes.data_as(C.c_void_p), G, ref.ctypes.data_as(C.c_void_p))
-        assert rc == 0
-        err = np.linalg.norm(acc[sample] - ref, axis=1) / np.linalg.norm(ref, axis=1)
-        assert np.median(err) < 1e-5
+        assert bh.library().bh_direct_sum(c.handle, 256, tgt.ctypes.data_as(C.c_void_p), G,
+                                          ref.ctypes.data_as(C.c_void_p)) == 0
+    tree = port.tree(sk, sp, sm, merge=True)
+    want_tree = tree.records()
+    for a, b, name in zip(got_tree, want_tree, ("prefix", "depth", "mass", "com")):
+        assert_bits_equal(a, b, f"tree {name}")
+    del got_tree, want_tree
+    targets = np.sort(np.random.default_rng(44).choice(n, 2048, replace=False))
+    want_acc, want_cnt = port.accelerations_at(tree, sk, sp, targets, THETA, G, 0.0, bb)
+    tree.close()
+    assert_bits_equal(acc[targets], want_acc, "plain-mode accelerations (2,048 bodies)")
+    assert np.array_equal(counts_plain[targets], want_cnt), "plain-mode interaction counts"
+    assert np.array_equal(counts_list[targets], want_cnt), "FP64 list interaction counts"
+    rel = np.linalg.norm(acc_list[targets] - want_acc, axis=1) / np.linalg.norm(want_acc, axis=1)
+    assert rel.max() <= 1e-13
+    err = np.linalg.norm(acc[sample] - ref, axis=1) / np.linalg.norm(ref, axis=1)
+    assert np.median(err) < 1e-5
 
 
 def test_fp64_list_mode_same_interaction_set(bh, ctx, golden, port):

@@ -244,3 +244,17 @@ def test_let_forces_match_reference(port, golden):
         want = f[k]
         rel = np.linalg.norm(a - want, axis=1) / np.linalg.norm(want, axis=1)
         assert rel.max() <= 1e-13, k
+
+
+def test_oracle_generator_matches_engine(bh, port):
+    """The oracle's restatement of the seeded generator (used by the bench's
+    reference arm, which must not load the engine's library) gives the
+    engine's bodies bit for bit: every configuration's mix, small sizes and
+    odd fractions."""
+    from conftest import assert_bits_equal
+    for seed, n, outer, trojan in ((2, 300_149, 0.1, 0.0), (5, 100_000, 0.10, 0.05), (1, 19_054, 0.0, 0.0),
+                                   (7, 1000, 0.1, 0.05), (3, 9, 0.0, 0.0), (4, 12, 0.5, 0.5)):
+        got = port.generate_system(seed, n, outer, trojan)
+        want = bh.generate_system(seed, n, outer, trojan)
+        for a, b, name in zip(got, want, ("pos", "vel", "mass", "ids")):
+            assert_bits_equal(a, b, f"seed {seed} n {n} {name}")

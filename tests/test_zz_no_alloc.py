@@ -38,15 +38,23 @@ def _existing_sort(bh, keys):
     return sk, si.astype(np.int64)
 
 
-def _noalloc_sort(fn, keys):
+def _noalloc_sort(fn, keys, in_place=False):
+    """Calls the entry point on device copies of `keys`; with in_place the
+    same buffer is passed as keys_in and keys_out."""
     import torch
     n = len(keys)
-    d_in = torch.from_numpy(keys.view(np.int64).copy()).cuda()
-    d_out = torch.full_like(d_in, -1)
-    d_perm = torch.full((n,), -1, dtype=torch.int32, device="cuda")
+    d_in = torch.from_numpy(np.ascontiguousarray(keys).view(np.int64).copy()).cuda()
+    d_out = d_in if in_place else torch.full_like(d_in, -1)
+    d_perm = torch.full((max(n, 1),), -1, dtype=torch.int32, device="cuda")
     torch.cuda.synchronize()
     rc = fn(d_in.data_ptr(), d_out.data_ptr(), d_perm.data_ptr(), n, None)
-    return rc, d_out.cpu().numpy().view(np.uint64), d_perm.cpu().numpy().astype(np.int64)
+    return rc, d_out.cpu().numpy().view(np.uint64)[:n], d_perm.cpu().numpy().astype(np.int64)[:n]
+
+
+def _stable_sort(keys):
+    """An independent stable sort: numpy's, on the unsigned keys."""
+    perm = np.argsort(keys, kind="stable")
+    return keys[perm], perm.astype(np.int64)
 
 
 def test_noalloc_sort_matches_existing_entry_point_on_consecutive_calls(bh):
@@ -67,6 +75,28 @@ def test_noalloc_sort_matches_existing_entry_point_on_consecutive_calls(bh):
         assert rc == 0, lib.bh_last_error()
         assert np.array_equal(got_keys, ref_keys)
         assert np.array_equal(got_perm, ref_perm)
+        want_keys, want_perm = _stable_sort(keys)
+        assert np.array_equal(got_keys, want_keys) and np.array_equal(got_perm, want_perm)
+
+
+def test_noalloc_sort_in_place_single_key_and_top_bit(bh):
+    """keys_in == keys_out (the header allows it), twice in a row; a single
+    key in place and not; keys with bit 63 set among ties and small values
+    (the eight digit passes cover all 64 bits); each against numpy's stable
+    sort."""
+    lib, fn = _entry(bh)
+    rng = np.random.default_rng(9)
+    big = rng.integers(0, 1 << 63, 200_000, dtype=np.uint64) | (rng.integers(0, 2, 200_000, dtype=np.uint64) << 63)
+    big[rng.integers(0, 200_000, 20_000)] = big[:20_000]
+    big[:7] = [np.uint64(0xFFFFFFFFFFFFFFFF), 0, np.uint64(1 << 63), 0, np.uint64(0xFFFFFFFFFFFFFFFF), 1,
+               np.uint64(1 << 63)]
+    for keys, in_place in ((big, True), (big, True), (big[:1], True), (big[:1], False), (big[:2], True),
+                           (big[:4096 * 3 + 5], False)):
+        rc, got_keys, got_perm = _noalloc_sort(fn, keys, in_place=in_place)
+        assert rc == 0, lib.bh_last_error()
+        want_keys, want_perm = _stable_sort(keys)
+        assert np.array_equal(got_keys, want_keys), (len(keys), in_place)
+        assert np.array_equal(got_perm, want_perm), (len(keys), in_place)
 
 
 def test_noalloc_sort_rejects_sizes_beyond_its_scratch(bh):
