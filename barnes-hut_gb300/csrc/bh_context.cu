@@ -98,10 +98,17 @@ void layout(bh_context* ctx, Carver& c)
     ctx->body_leaf = c.take<int32_t>(n);
     ctx->leaf_key = c.take<uint64_t>(n);
     ctx->leaf_s = c.take<double4_32a>(n);
-    ctx->cdep = c.take<int8_t>(n);
+    ctx->cdep = c.take<int8_t>(n + 1);
+    ctx->bnd_pl = c.take<int32_t>(n + 1);
+    ctx->bnd_pr = c.take<int32_t>(n + 1);
+    ctx->bnd_next = c.take<int32_t>(n + 1);
+    ctx->split_node = c.take<int32_t>(n + 1);
+    ctx->split_rank = c.take<int8_t>(n + 1);
+    ctx->ansv_blk = c.take<int32_t>(bh::boundary_pass_ints(n));
     ctx->rep_node = c.take<int32_t>(n);
     ctx->node_rep = c.take<int32_t>(n);
     ctx->node_a = c.take<int32_t>(n);
+    ctx->node_e = c.take<int32_t>(n);
     ctx->node_nchild = c.take<int32_t>(n);
     ctx->node_cs = c.take<int32_t>(n);
     ctx->node_depth = c.take<uint8_t>(n);

@@ -339,10 +339,17 @@ struct bh_context {
     int32_t* body_leaf = nullptr;   // leaf id of each body
     uint64_t* leaf_key = nullptr;
     double4_32a* leaf_s = nullptr;  // leaf sums {m x, m y, m z, m}
-    int8_t* cdep = nullptr;         // common depth of leaves j-1, j (boundary j)
+    int8_t* cdep = nullptr;         // common depth of leaves j-1, j (boundary j), n + 1
+    int32_t* bnd_pl = nullptr;      // boundary j: start leaf of the node it splits, n + 1
+    int32_t* bnd_pr = nullptr;      // boundary j: end leaf (exclusive) of that node, n + 1
+    int32_t* bnd_next = nullptr;    // boundary j: next boundary no deeper than j, n + 1
+    int32_t* split_node = nullptr;  // boundary j: the branching node it splits, n + 1
+    int8_t* split_rank = nullptr;   // boundary j: its rank among that node's splits, n + 1
+    int32_t* ansv_blk = nullptr;    // per-block summaries of the boundary pass
     int32_t* rep_node = nullptr;    // branching-node id of a representative boundary
     int32_t* node_rep = nullptr;    // representative boundary of each node
     int32_t* node_a = nullptr;      // first leaf of each node
+    int32_t* node_e = nullptr;      // end leaf (exclusive) of each node
     int32_t* node_nchild = nullptr;
     int32_t* node_cs = nullptr;     // first child slot
     uint8_t* node_depth = nullptr;
@@ -383,7 +390,10 @@ struct bh_context {
     double* node_q = nullptr;
     bh::MlpDev* mlp_dev = nullptr;      // learned model (bh_learned_set_model)
     double learn_theta_max = 0.0;
-    unsigned long long* lstats = nullptr;  // candidates, accepted, fallbacks
+    double learn_budget = 0.0;   // per-body error budget of the learned criterion
+    double learn_band = 1.0;     // decades around the allowance the network decides
+    double learn_frac = 0.25;    // largest share of the remaining allowance one candidate takes
+    unsigned long long* lstats = nullptr;  // candidates, network accepts, fallbacks, analytic accepts
     double* direct = nullptr;   // 4 doubles per direct body: x, y, z, G m (by id)
     int32_t* direct_present = nullptr;  // 1 when body id k was found
 
@@ -430,6 +440,9 @@ int launch_hist(bh_context* ctx);
 int bbox_partial_bytes(int blocks);
 size_t sort_smem_bytes();
 int64_t scan_tmp_ints(int64_t n_max);
+// Ints of the per-block summaries of the tree build's boundary pass for up
+// to n bodies.
+int64_t boundary_pass_ints(int64_t n);
 int launch_sort(bh_context* ctx);
 int launch_permute(bh_context* ctx);
 // The permutation gathers into the second body set; the two sets then trade

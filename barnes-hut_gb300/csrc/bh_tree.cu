@@ -28,6 +28,8 @@
 // step mass' = 0 + mass, com' = (0*0 + mass*com) / mass'.  All with IEEE
 // double intrinsics (no contraction), so masses and centres of mass are bit
 // for bit the reference's.
+#include <climits>
+
 #include "bh_internal.cuh"
 
 namespace bh {
@@ -40,44 +42,6 @@ inline int grid_for(int64_t n, int threads, int max_blocks)
     int64_t b = (n + threads - 1) / threads;
     if (b < 1) b = 1;
     return (int)(b > max_blocks ? max_blocks : b);
-}
-
-// First index v in (u, L] whose key leaves u's cell under `mask`.
-__device__ int cell_end(const uint64_t* __restrict__ K, int L, int u, uint64_t mask)
-{
-    const uint64_t p = K[u] & mask;
-    int lo = u, hi = L, step = 1;
-    for (;;) {
-        const int64_t probe = (int64_t)u + step;
-        if (probe >= L) break;
-        if ((K[probe] & mask) != p) { hi = (int)probe; break; }
-        lo = (int)probe;
-        step <<= 1;
-    }
-    while (hi - lo > 1) {
-        const int mid = lo + (hi - lo) / 2;
-        if ((K[mid] & mask) == p) lo = mid; else hi = mid;
-    }
-    return hi;
-}
-
-// First index t in [0, u] whose key is in u's cell under `mask`.
-__device__ int cell_start(const uint64_t* __restrict__ K, int u, uint64_t mask)
-{
-    const uint64_t p = K[u] & mask;
-    int hi = u, lo = -1, step = 1;
-    for (;;) {
-        const int probe = u - step;
-        if (probe < 0) break;
-        if ((K[probe] & mask) != p) { lo = probe; break; }
-        hi = probe;
-        step <<= 1;
-    }
-    while (hi - lo > 1) {
-        const int mid = lo + (hi - lo) / 2;
-        if ((K[mid] & mask) == p) hi = mid; else lo = mid;
-    }
-    return hi;
 }
 
 __device__ inline bool is_head(const uint64_t* __restrict__ key, int64_t i)
@@ -131,6 +95,7 @@ __global__ void leaf_sum_kernel(const int32_t* __restrict__ counts, const int32_
         }
         ls[l] = double4_32a{sx, sy, sz, sm};
         cdep[l] = l == 0 ? (int8_t)-1 : (int8_t)common_depth(leaf_key[l - 1], leaf_key[l]);
+        if (l == L - 1) cdep[L] = -1;  // right sentinel of the boundary pass
         if (kMoments) {
             double q = 0.0;
             if (b1 - b0 > 1 && sm > 0) {
@@ -146,90 +111,263 @@ __global__ void leaf_sum_kernel(const int32_t* __restrict__ counts, const int32_
     }
 }
 
-// flag[j] = 1 when boundary j is the first child boundary of its node.
-__global__ void rep_flag_kernel(const int32_t* __restrict__ counts, const uint64_t* __restrict__ K,
-                                const int8_t* __restrict__ cdep, int32_t* __restrict__ flag, int64_t cap)
+// ---- Tree structure from the boundary depths ---------------------------
+// With d(j) = cdep[j] for the boundaries 1 <= j < L and d(0) = d(L) = -1,
+// the branching node that boundary j splits (the cell of depth d(j) holding
+// leaves j-1 and j) spans the leaves [pl(j), pr(j)) between the nearest
+// shallower boundaries
+//   pl(j) = max{k < j : d(k) < d(j)},   pr(j) = min{k > j : d(k) < d(j)};
+// its splits are the boundaries of depth d(j) in between (at most 7: eight
+// octants), and the first of them represents it (j is first exactly when
+// max{k < j : d(k) <= d(j)} is pl(j)).  next(j) = min{k > j : d(k) <= d(j)}
+// is j's next split when d(next(j)) = d(j).  These nearest-value queries are
+// answered from ballots: for each of the 22 thresholds t (d <= t - 1,
+// t = 0..21) a warp's ballot marks its positions at or below t - 1; a query
+// looks in its own warp's mask first, then in the other warps of its block
+// (prefix / suffix over the warps' extreme positions), then in the other
+// blocks (prefix / suffix over the blocks' extreme positions, from a pass over
+// block summaries).  No searches and no atomics.
+constexpr int kNT = kMaxDepth + 1;  // thresholds t: d <= t - 1
+constexpr int kBT = 1024;           // boundary positions per block
+constexpr int kBW = kBT / 32;
+
+__device__ __forceinline__ int bnd_depth(const int8_t* __restrict__ cdep, int L, int64_t j)
 {
+    return j <= L ? (int)cdep[j] : 127;  // cdep[0] = cdep[L] = -1; past L: no threshold
+}
+
+// Per block: for every threshold the last and the first position at or below it.
+__global__ void __launch_bounds__(kBT) bnd_summary_kernel(const int32_t* __restrict__ counts,
+                                                          const int8_t* __restrict__ cdep,
+                                                          int32_t* __restrict__ blast, int32_t* __restrict__ bfirst)
+{
+    __shared__ int wl[kBW][kNT], wf[kBW][kNT];
     const int L = counts[0];
-    for (int j = blockIdx.x * blockDim.x + threadIdx.x; j < cap; j += gridDim.x * blockDim.x) {
-        int f = 0;
-        if (j >= 1 && j < L) {
-            const int D = cdep[j];
-            const int t = cell_start(K, j - 1, prefix_mask(D + 1));
-            f = (t == 0 || cdep[t] < D) ? 1 : 0;
+    const int64_t j = (int64_t)blockIdx.x * kBT + threadIdx.x;
+    const int v = bnd_depth(cdep, L, j);
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    const int wbase = (int)(j - lane);
+#pragma unroll
+    for (int t = 0; t < kNT; ++t) {
+        const unsigned m = __ballot_sync(0xffffffffu, v <= t - 1);
+        if (lane == t) {
+            wl[w][t] = m ? wbase + 31 - __clz(m) : -1;
+            wf[w][t] = m ? wbase + __ffs(m) - 1 : INT_MAX;
         }
-        flag[j] = f;
+    }
+    __syncthreads();
+    if (threadIdx.x < kNT) {
+        const int t = threadIdx.x;
+        int l = -1, f = INT_MAX;
+        for (int ww = 0; ww < kBW; ++ww) {
+            l = max(l, wl[ww][t]);
+            f = min(f, wf[ww][t]);
+        }
+        blast[(int64_t)blockIdx.x * kNT + t] = l;
+        bfirst[(int64_t)blockIdx.x * kNT + t] = f;
     }
 }
 
-// Node ids, first leaf, depth and child count of each branching node.
-// excl is the exclusive scan of the flags: the node id of a representative.
-__global__ void node_init_kernel(const int32_t* __restrict__ counts, const uint64_t* __restrict__ K,
-                                 const int8_t* __restrict__ cdep, const int32_t* __restrict__ flag,
-                                 const int32_t* __restrict__ excl, int32_t* __restrict__ node_rep,
-                                 int32_t* __restrict__ node_a, uint8_t* __restrict__ node_depth,
-                                 int32_t* __restrict__ node_nchild)
+// Exclusive scan of one int per thread over the block (max, or min with
+// kMin), continued from `carry`; returns the thread's exclusive value and
+// advances `carry` past the whole block.
+template <bool kMin>
+__device__ int block_excl_extreme(int x, int& carry, int* wsum)
+{
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    auto op = [](int a, int b) { return kMin ? min(a, b) : max(a, b); };
+    const int ident = kMin ? INT_MAX : -1;
+    int inc = x;
+#pragma unroll
+    for (int off = 1; off < 32; off <<= 1) {
+        const int y = __shfl_up_sync(0xffffffffu, inc, off);
+        if (lane >= off) inc = op(inc, y);
+    }
+    int ex = __shfl_up_sync(0xffffffffu, inc, 1);
+    if (lane == 0) ex = ident;
+    if (lane == 31) wsum[w] = inc;
+    __syncthreads();
+    if (w == 0) {
+        int sw = lane < (int)(blockDim.x >> 5) ? wsum[lane] : ident;
+#pragma unroll
+        for (int off = 1; off < 32; off <<= 1) {
+            const int y = __shfl_up_sync(0xffffffffu, sw, off);
+            if (lane >= off) sw = op(sw, y);
+        }
+        wsum[lane] = sw;
+    }
+    __syncthreads();
+    const int res = op(carry, op(w ? wsum[w - 1] : ident, ex));
+    carry = op(carry, wsum[(blockDim.x >> 5) - 1]);
+    __syncthreads();
+    return res;
+}
+
+// One block per threshold: the blocks' exclusive prefix of last positions
+// (max) and exclusive suffix of first positions (min).
+__global__ void __launch_bounds__(1024) bnd_scan_kernel(int nblk, const int32_t* __restrict__ blast,
+                                                        const int32_t* __restrict__ bfirst,
+                                                        int32_t* __restrict__ bpre, int32_t* __restrict__ bsuf)
+{
+    __shared__ int wsum[32];
+    const int t = blockIdx.x;
+    int carry = -1;
+    for (int base = 0; base < nblk; base += blockDim.x) {
+        const int b = base + threadIdx.x;
+        const int x = b < nblk ? blast[(int64_t)b * kNT + t] : -1;
+        const int ex = block_excl_extreme<false>(x, carry, wsum);
+        if (b < nblk) bpre[(int64_t)b * kNT + t] = ex;
+    }
+    carry = INT_MAX;
+    for (int base = 0; base < nblk; base += blockDim.x) {
+        const int b = nblk - 1 - (base + (int)threadIdx.x);
+        const int x = b >= 0 ? bfirst[(int64_t)b * kNT + t] : INT_MAX;
+        const int ex = block_excl_extreme<true>(x, carry, wsum);
+        if (b >= 0) bsuf[(int64_t)b * kNT + t] = ex;
+    }
+}
+
+// Per boundary: the representative flag (flag[j], 0 for j = 0 and j >= L up
+// to cap), pl, pr and next.
+__global__ void __launch_bounds__(kBT) bnd_resolve_kernel(const int32_t* __restrict__ counts,
+                                                          const int8_t* __restrict__ cdep,
+                                                          const int32_t* __restrict__ bpre,
+                                                          const int32_t* __restrict__ bsuf, int32_t* __restrict__ flag,
+                                                          int32_t* __restrict__ pl, int32_t* __restrict__ pr,
+                                                          int32_t* __restrict__ nxt, int64_t cap)
+{
+    __shared__ unsigned wm[kBW][kNT];
+    __shared__ int wl[kBW][kNT], wf[kBW][kNT];
+    const int L = counts[0];
+    const int64_t j = (int64_t)blockIdx.x * kBT + threadIdx.x;
+    const int v = bnd_depth(cdep, L, j);
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    const int wbase = (int)(j - lane);
+#pragma unroll
+    for (int t = 0; t < kNT; ++t) {
+        const unsigned m = __ballot_sync(0xffffffffu, v <= t - 1);
+        if (lane == t) {
+            wm[w][t] = m;
+            wl[w][t] = m ? wbase + 31 - __clz(m) : -1;
+            wf[w][t] = m ? wbase + __ffs(m) - 1 : INT_MAX;
+        }
+    }
+    __syncthreads();
+    // Each warp's answer from outside it: exclusive prefix (max) and suffix
+    // (min) over the warps, started from the other blocks'.
+    if (threadIdx.x < kNT) {
+        const int t = threadIdx.x;
+        int run = bpre[(int64_t)blockIdx.x * kNT + t];
+        for (int ww = 0; ww < kBW; ++ww) {
+            const int x = wl[ww][t];
+            wl[ww][t] = run;
+            run = max(run, x);
+        }
+        run = bsuf[(int64_t)blockIdx.x * kNT + t];
+        for (int ww = kBW - 1; ww >= 0; --ww) {
+            const int x = wf[ww][t];
+            wf[ww][t] = run;
+            run = min(run, x);
+        }
+    }
+    __syncthreads();
+    if (j >= cap) return;
+    int f = 0;
+    if (j >= 1 && j < L) {
+        const unsigned below = (1u << lane) - 1u, above = ~below & ~(1u << lane);
+        auto prev = [&](int t) {
+            const unsigned m = wm[w][t] & below;
+            return m ? wbase + 31 - __clz(m) : wl[w][t];
+        };
+        auto next = [&](int t) {
+            const unsigned m = wm[w][t] & above;
+            return m ? wbase + __ffs(m) - 1 : wf[w][t];
+        };
+        const int PL = prev(v), PLE = prev(v + 1);
+        f = PLE == PL ? 1 : 0;
+        pl[j] = PL;
+        pr[j] = next(v);
+        nxt[j] = next(v + 1);
+    }
+    flag[j] = f;
+}
+
+// Each branching node from its representative: depth, leaf range and its
+// splits (at most 7) with their ranks; child count = splits + 1.
+__global__ void node_split_kernel(const int32_t* __restrict__ counts, const int8_t* __restrict__ cdep,
+                                  const int32_t* __restrict__ flag, const int32_t* __restrict__ excl,
+                                  const int32_t* __restrict__ pl, const int32_t* __restrict__ pr,
+                                  const int32_t* __restrict__ nxt, int32_t* __restrict__ node_rep,
+                                  int32_t* __restrict__ node_a, int32_t* __restrict__ node_e,
+                                  uint8_t* __restrict__ node_depth, int32_t* __restrict__ node_nchild,
+                                  int32_t* __restrict__ split_node, int8_t* __restrict__ split_rank,
+                                  unsigned* __restrict__ err)
 {
     const int L = counts[0];
     for (int j = blockIdx.x * blockDim.x + threadIdx.x; j < L; j += gridDim.x * blockDim.x) {
         if (j == 0 || !flag[j]) continue;
         const int b = excl[j];
-        const int D = cdep[j];
-        const uint64_t mc = prefix_mask(D + 1);
-        const int a = cell_start(K, j - 1, mc);
-        const int e = cell_end(K, L, j, prefix_mask(D));
-        int nc = 1;  // the child [a, j)
-        for (int u = j; u < e; u = cell_end(K, L, u, mc)) ++nc;
+        const int c = cdep[j];
         node_rep[b] = j;
-        node_a[b] = a;
-        node_depth[b] = (uint8_t)D;
-        node_nchild[b] = nc;
+        node_a[b] = pl[j];
+        node_e[b] = pr[j];
+        node_depth[b] = (uint8_t)c;
+        int k = j, r = 0;
+        for (;;) {
+            split_node[k] = b;
+            split_rank[k] = (int8_t)r;
+            ++r;
+            k = nxt[k];
+            if (k >= L || cdep[k] != c || r >= 7) break;
+        }
+        if (k < L && cdep[k] == c) atomicOr(err, kErrOverflow);  // an eighth split: impossible for an octree
+        node_nchild[b] = r + 1;
     }
 }
 
-// Child slots of every branching node; slot 0 is the root.
-__global__ void node_children_kernel(const int32_t* __restrict__ counts, const uint64_t* __restrict__ K,
-                                     const int32_t* __restrict__ rep_node, const int32_t* __restrict__ node_rep,
-                                     const int32_t* __restrict__ node_a, const uint8_t* __restrict__ node_depth,
-                                     const int32_t* __restrict__ node_cs, int32_t* __restrict__ slot_ref,
-                                     uint8_t* __restrict__ slot_top, int32_t* __restrict__ leaf_parent,
-                                     int32_t* __restrict__ node_parent)
+// Child slots: every leaf and branching node finds its parent from the
+// boundaries at its two ends (the deeper one splits the parent; both
+// sentinels: the root) and its place among the parent's children from that
+// split's rank.  Slot 0 is the root.
+__global__ void node_place_kernel(const int32_t* __restrict__ counts, const int8_t* __restrict__ cdep,
+                                  const int32_t* __restrict__ node_a, const int32_t* __restrict__ node_e,
+                                  const uint8_t* __restrict__ node_depth, const int32_t* __restrict__ node_cs,
+                                  const int32_t* __restrict__ split_node, const int8_t* __restrict__ split_rank,
+                                  int32_t* __restrict__ slot_ref, uint8_t* __restrict__ slot_top,
+                                  int32_t* __restrict__ leaf_parent, int32_t* __restrict__ node_parent,
+                                  unsigned* __restrict__ err)
 {
-    const int L = counts[0], B = counts[1];
-    const int gid = blockIdx.x * blockDim.x + threadIdx.x;
-    if (gid == 0) {
-        if (L == 1) {
-            slot_ref[0] = 0;
-            leaf_parent[0] = -1;
+    const int L = counts[0], B = counts[1], S = counts[2];
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < L + B; i += gridDim.x * blockDim.x) {
+        int a, e, ref;
+        if (i < L) {
+            a = i; e = i + 1; ref = i;
         } else {
-            const int Dr = common_depth(K[0], K[L - 1]);
-            const int root = rep_node[cell_end(K, L, 0, prefix_mask(Dr + 1))];
-            slot_ref[0] = ~root;
-            node_parent[root] = -1;
+            const int b = i - L;
+            a = node_a[b]; e = node_e[b]; ref = ~b;
         }
-        slot_top[0] = 0;
-    }
-    for (int b = gid; b < B; b += gridDim.x * blockDim.x) {
-        const int D = node_depth[b];
-        const uint64_t mc = prefix_mask(D + 1);
-        const int a = node_a[b];
-        const int e = cell_end(K, L, node_rep[b], prefix_mask(D));
-        int s = node_cs[b] + 1;
-        for (int u = a; u < e; ++s) {
-            const int v = cell_end(K, L, u, mc);
-            int ref;
-            if (v - u == 1) {
-                ref = u;
-            } else {
-                const int cd = common_depth(K[u], K[v - 1]);
-                ref = ~rep_node[cell_end(K, L, u, prefix_mask(cd + 1))];
+        const int ca = a == 0 ? -1 : cdep[a];
+        const int ce = e >= L ? -1 : cdep[e];
+        int P = -1, s = 0, top = 0;
+        if (ca >= 0 || ce >= 0) {
+            const bool left = ca >= ce;
+            const int k = left ? a : e;
+            P = split_node[k];
+            if ((unsigned)P >= (unsigned)B) {  // every boundary splits a node: a broken invariant
+                atomicOr(err, kErrOverflow);
+                continue;
             }
-            slot_ref[s] = ref;
-            slot_top[s] = (uint8_t)(D + 1);
-            if (ref >= 0) leaf_parent[ref] = b;
-            else node_parent[~ref] = b;
-            u = v;
+            s = node_cs[P] + 1 + split_rank[k] + (left ? 1 : 0);
+            top = node_depth[P] + 1;
+            if (s < 1 || s >= S) {
+                atomicOr(err, kErrOverflow);
+                continue;
+            }
         }
+        slot_ref[s] = ref;
+        slot_top[s] = (uint8_t)top;
+        if (ref >= 0) leaf_parent[ref] = P;
+        else node_parent[~ref] = P;
     }
 }
 
@@ -521,6 +659,12 @@ __global__ void slot_count_kernel(int32_t* counts, const int32_t* __restrict__ c
 
 }  // namespace
 
+int64_t boundary_pass_ints(int64_t n)
+{
+    const int64_t nb = (n + 1 + kBT - 1) / kBT;
+    return 4 * kNT * nb;
+}
+
 int launch_build(bh_context* ctx, const double* mass, bool moments, bool far_fused, double G)
 {
     ctx->fnodes_fused = false;
@@ -545,23 +689,38 @@ int launch_build(bh_context* ctx, const double* mass, bool moments, bool far_fus
                                                        ctx->pz, mass, ctx->leaf_s, ctx->cdep, ctx->leaf_q);
     BH_LAUNCH_CHECK(ctx);
 
-    // 2. branching nodes: representative flags -> ids -> ranges/child counts
-    rep_flag_kernel<<<g, kThreads, 0, st>>>(ctx->counts, ctx->leaf_key, ctx->cdep, ctx->head, n);
-    BH_LAUNCH_CHECK(ctx);
+    // 2. branching nodes: the boundary pass (representative flags, node
+    // ranges, split chains) -> node ids -> child counts -> child slots
+    {
+        const int nb = (int)((n + 1 + kBT - 1) / kBT);
+        int32_t* blast = ctx->ansv_blk;
+        int32_t* bfirst = blast + (int64_t)nb * kNT;
+        int32_t* bpre = bfirst + (int64_t)nb * kNT;
+        int32_t* bsuf = bpre + (int64_t)nb * kNT;
+        bnd_summary_kernel<<<nb, kBT, 0, st>>>(ctx->counts, ctx->cdep, blast, bfirst);
+        BH_LAUNCH_CHECK(ctx);
+        bnd_scan_kernel<<<kNT, 1024, 0, st>>>(nb, blast, bfirst, bpre, bsuf);
+        BH_LAUNCH_CHECK(ctx);
+        bnd_resolve_kernel<<<nb, kBT, 0, st>>>(ctx->counts, ctx->cdep, bpre, bsuf, ctx->head, ctx->bnd_pl, ctx->bnd_pr,
+                                                ctx->bnd_next, n);
+        BH_LAUNCH_CHECK(ctx);
+    }
     // rep_node[j] = exclusive count of representatives before j, i.e. the
     // node id of boundary j when it is a representative.
     rc = device_exclusive_scan(ctx, ctx->head, ctx->rep_node, n, nullptr, ctx->counts + 1);
     if (rc) return rc;
-    node_init_kernel<<<g, kThreads, 0, st>>>(ctx->counts, ctx->leaf_key, ctx->cdep, ctx->head, ctx->rep_node,
-                                             ctx->node_rep, ctx->node_a, ctx->node_depth, ctx->node_nchild);
+    node_split_kernel<<<g, kThreads, 0, st>>>(ctx->counts, ctx->cdep, ctx->head, ctx->rep_node, ctx->bnd_pl,
+                                              ctx->bnd_pr, ctx->bnd_next, ctx->node_rep, ctx->node_a, ctx->node_e,
+                                              ctx->node_depth, ctx->node_nchild, ctx->split_node, ctx->split_rank,
+                                              ctx->err);
     BH_LAUNCH_CHECK(ctx);
     rc = device_exclusive_scan(ctx, ctx->node_nchild, ctx->node_cs, n, ctx->counts + 1, ctx->counts + 3);
     if (rc) return rc;
     slot_count_kernel<<<1, 1, 0, st>>>(ctx->counts, ctx->counts + 3);
     BH_LAUNCH_CHECK(ctx);
-    node_children_kernel<<<g, kThreads, 0, st>>>(ctx->counts, ctx->leaf_key, ctx->rep_node, ctx->node_rep,
-                                                 ctx->node_a, ctx->node_depth, ctx->node_cs, ctx->slot_ref,
-                                                 ctx->slot_top, ctx->leaf_parent, ctx->node_parent);
+    node_place_kernel<<<grid_for(2 * n, kThreads, maxb), kThreads, 0, st>>>(
+        ctx->counts, ctx->cdep, ctx->node_a, ctx->node_e, ctx->node_depth, ctx->node_cs, ctx->split_node,
+        ctx->split_rank, ctx->slot_ref, ctx->slot_top, ctx->leaf_parent, ctx->node_parent, ctx->err);
     BH_LAUNCH_CHECK(ctx);
 
     // 3./4. monopoles (and second moments), deepest first.  Below a
