@@ -112,6 +112,9 @@ def _sig(lib):
     f["bh_learned_collect"] = (C.c_int, [_P, _D, _D, _D, _D, _I64, _P, _P, C.POINTER(_I64)])
     f["bh_learned_set_model"] = (C.c_int, [_P, _P, _P, _D, _D])
     f["bh_learned_stats"] = (C.c_int, [_P, _P])
+    f["bh_learned_set_criterion"] = (C.c_int, [_P, _D, _D])
+    f["bh_mlp_save"] = (C.c_int, [C.c_char_p, _P, _P])
+    f["bh_mlp_load"] = (C.c_int, [C.c_char_p, _P, _P])
     f["bh_compute_local_bbox"] = (C.c_int, [_P, _I64, _P])
     f["bh_generate_morton_codes"] = (C.c_int, [_P, _I64, _P, _P])
     f["bh_sort_bodies_by_morton_key"] = (C.c_int, [_I64, _P, _P, _P, _P, _P])
@@ -498,10 +501,15 @@ class Context:
         p = np.ascontiguousarray(params, np.float32); sc = np.ascontiguousarray(scale, np.float32)
         _check(library().bh_learned_set_model(self._h, _ptr(p), _ptr(sc), budget, theta_max))
 
+    def learned_set_criterion(self, band: float = 0.5, frac: float = 0.25) -> None:
+        """Decades around the allowance the network decides; largest share of
+        the remaining allowance one candidate takes."""
+        _check(library().bh_learned_set_criterion(self._h, band, frac))
+
     def learned_stats(self) -> dict:
-        v = np.zeros(3, np.int64)
+        v = np.zeros(4, np.int64)
         _check(library().bh_learned_stats(self._h, _ptr(v)))
-        return {"candidates": int(v[0]), "accepted": int(v[1]), "fallback": int(v[2])}
+        return {"candidates": int(v[0]), "accepted": int(v[1]), "fallback": int(v[2]), "analytic": int(v[3])}
 
     def step(self, dt, theta=THETA_DEFAULT, G=G_DEFAULT, nsteps=1, mode=MODE_PLAIN_FP64, t=None) -> float:
         tv = _D(0.0 if t is None else t)
@@ -535,6 +543,21 @@ def mlp_train(features, labels, epochs=20, batch=4096, lr=2e-3, seed=0):
     _check(library().bh_mlp_train(_ptr(F), _ptr(L), len(L), epochs, batch, lr, seed, _ptr(params), _ptr(scale),
                                   _ptr(losses)))
     return params, scale, losses
+
+
+def mlp_save(path, params, scale) -> None:
+    """Writes a trained model (parameters and feature scaling) to a file."""
+    p = np.ascontiguousarray(params, np.float32); sc = np.ascontiguousarray(scale, np.float32)
+    if p.size != MLP_PARAMS or sc.size != MLP_SCALE:
+        raise ValueError("mlp_save: wrong parameter or scale count")
+    _check(library().bh_mlp_save(str(path).encode(), _ptr(p), _ptr(sc)))
+
+
+def mlp_load(path):
+    """(params, scale) of a model file written by mlp_save / bh_mlp_save."""
+    p = np.empty(MLP_PARAMS, np.float32); sc = np.empty(MLP_SCALE, np.float32)
+    _check(library().bh_mlp_load(str(path).encode(), _ptr(p), _ptr(sc)))
+    return p, sc
 
 
 def mlp_predict(params, scale, features):

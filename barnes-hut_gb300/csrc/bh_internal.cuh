@@ -391,7 +391,7 @@ struct bh_context {
     bh::MlpDev* mlp_dev = nullptr;      // learned model (bh_learned_set_model)
     double learn_theta_max = 0.0;
     double learn_budget = 0.0;   // per-body error budget of the learned criterion
-    double learn_band = 1.0;     // decades around the allowance the network decides
+    double learn_band = 0.5;     // decades around the allowance the network decides
     double learn_frac = 0.25;    // largest share of the remaining allowance one candidate takes
     unsigned long long* lstats = nullptr;  // candidates, network accepts, fallbacks, analytic accepts
     double* direct = nullptr;   // 4 doubles per direct body: x, y, z, G m (by id)

@@ -11,6 +11,8 @@
 // node's subtree summed by the plain per-body walk at theta_label (0.5) in
 // FP64, and a_scale is the group's smallest direct-term acceleration (the
 // Sun's pull dominates every body's acceleration).
+#include <cstdio>
+#include <cstring>
 #include <string>
 #include <vector>
 
@@ -260,17 +262,82 @@ int bh_learned_set_model(bh_context* ctx, const float* params, const float* scal
     BH_CUDA_TRY(cudaMemcpyAsync(ctx->mlp_dev, &m, sizeof(MlpDev), cudaMemcpyHostToDevice, ctx->stream));
     BH_CUDA_TRY(cudaStreamSynchronize(ctx->stream));
     ctx->learn_theta_max = theta_max;
+    ctx->learn_budget = budget;
     return BH_OK;
 }
 
-int bh_learned_stats(bh_context* ctx, int64_t out[3])
+int bh_learned_set_criterion(bh_context* ctx, double band, double frac)
+{
+    if (!ctx || !(band >= 0.0) || !(frac > 0.0) || !(frac <= 1.0))
+        return bh_fail(BH_ERR_INVALID_ARGUMENT, "bh_learned_set_criterion: need band >= 0 and 0 < frac <= 1");
+    ctx->learn_band = band;
+    ctx->learn_frac = frac;
+    return BH_OK;
+}
+
+int bh_learned_stats(bh_context* ctx, int64_t out[4])
 {
     if (!ctx || !out) return bh_fail(BH_ERR_INVALID_ARGUMENT, "bh_learned_stats: bad arguments");
     BH_CUDA_TRY(cudaSetDevice(ctx->device));
-    unsigned long long v[3];
+    unsigned long long v[4];
     BH_CUDA_TRY(cudaMemcpyAsync(v, ctx->lstats, sizeof(v), cudaMemcpyDeviceToHost, ctx->stream));
     BH_CUDA_TRY(cudaStreamSynchronize(ctx->stream));
-    for (int k = 0; k < 3; ++k) out[k] = (int64_t)v[k];
+    for (int k = 0; k < 4; ++k) out[k] = (int64_t)v[k];
+    return BH_OK;
+}
+
+namespace {
+constexpr char kModelTag[8] = {'B', 'H', 'M', 'L', 'P', '0', '0', '1'};
+
+void put_u32(unsigned char* b, uint32_t v)
+{
+    for (int k = 0; k < 4; ++k) b[k] = (unsigned char)(v >> (8 * k));
+}
+
+uint32_t get_u32(const unsigned char* b)
+{
+    uint32_t v = 0;
+    for (int k = 0; k < 4; ++k) v |= (uint32_t)b[k] << (8 * k);
+    return v;
+}
+}  // namespace
+
+int bh_mlp_save(const char* path, const float* params, const float* scale)
+{
+    if (!path || !params || !scale) return bh_fail(BH_ERR_INVALID_ARGUMENT, "bh_mlp_save: bad arguments");
+    std::vector<unsigned char> buf(16 + 4 * (size_t)(kParams + kScaleFloats));
+    std::memcpy(buf.data(), kModelTag, 8);
+    put_u32(buf.data() + 8, (uint32_t)kParams);
+    put_u32(buf.data() + 12, (uint32_t)kScaleFloats);
+    size_t o = 16;
+    for (int k = 0; k < kParams + kScaleFloats; ++k, o += 4) {
+        uint32_t u;
+        std::memcpy(&u, k < kParams ? params + k : scale + (k - kParams), 4);
+        put_u32(buf.data() + o, u);
+    }
+    FILE* f = std::fopen(path, "wb");
+    if (!f) return bh_fail(BH_ERR_IO, std::string("bh_mlp_save: cannot open ") + path);
+    const bool ok = std::fwrite(buf.data(), 1, buf.size(), f) == buf.size();
+    const bool closed = std::fclose(f) == 0;
+    return ok && closed ? BH_OK : bh_fail(BH_ERR_IO, std::string("bh_mlp_save: write failed: ") + path);
+}
+
+int bh_mlp_load(const char* path, float* params_out, float* scale_out)
+{
+    if (!path || !params_out || !scale_out) return bh_fail(BH_ERR_INVALID_ARGUMENT, "bh_mlp_load: bad arguments");
+    FILE* f = std::fopen(path, "rb");
+    if (!f) return bh_fail(BH_ERR_IO, std::string("bh_mlp_load: cannot open ") + path);
+    std::vector<unsigned char> buf(16 + 4 * (size_t)(kParams + kScaleFloats) + 1);
+    const size_t got = std::fread(buf.data(), 1, buf.size(), f);
+    std::fclose(f);
+    if (got != buf.size() - 1 || std::memcmp(buf.data(), kModelTag, 8) != 0 ||
+        get_u32(buf.data() + 8) != (uint32_t)kParams || get_u32(buf.data() + 12) != (uint32_t)kScaleFloats)
+        return bh_fail(BH_ERR_INVALID_ARGUMENT, std::string("bh_mlp_load: not a model file: ") + path);
+    size_t o = 16;
+    for (int k = 0; k < kParams + kScaleFloats; ++k, o += 4) {
+        const uint32_t u = get_u32(buf.data() + o);
+        std::memcpy(k < kParams ? params_out + k : scale_out + (k - kParams), &u, 4);
+    }
     return BH_OK;
 }
 

@@ -51,6 +51,8 @@ struct MlpScale {
     float lstd;
 };
 
+constexpr int kScaleFloats = (int)(sizeof(MlpScale) / sizeof(float));  // 34
+
 // A trained model laid out for the traversal's fused inference: the weights
 // as mma.sync m16n8k16 B fragments (BF16 pairs, one per lane), biases and the
 // last layer in FP32, the feature scaling and the acceptance threshold.

@@ -22,6 +22,7 @@ constexpr uint32_t kFlagAgg = 1u << 30;
 constexpr uint32_t kFlagIncl = 2u << 30;
 constexpr uint32_t kCountMask = (1u << 30) - 1;
 constexpr int kSpinLimit = 1 << 22;
+constexpr int kBatch = 8;  // look-back: predecessors read per round
 
 struct SortSmem {
     uint32_t warp_hist[kWarps][kRadix];  // per-warp digit counts, then warp prefixes
@@ -131,27 +132,45 @@ __global__ void __launch_bounds__(kSortThreads) onesweep_kernel(
         s.digit_excl[d] = scan256(tile_count, s.scan);
     }
 
-    // Decoupled look-back: thread d sums earlier tiles' counts of digit d.
+    // Decoupled look-back: thread d sums earlier tiles' counts of digit d,
+    // reading kBatch predecessors per round (independent loads in flight)
+    // and stopping at the nearest inclusive prefix.  A predecessor that has
+    // not published yet is read again (bounded).
     if (threadIdx.x < kRadix) {
         const int d = threadIdx.x;
         uint32_t excl = 0;
         if (tile > 0) {
+            const volatile uint32_t* lbv = lookback;
             int64_t k = (int64_t)tile - 1;
             int spins = 0;
             while (k >= 0) {
-                const uint32_t v = ((volatile uint32_t*)lookback)[(size_t)k * kRadix + d];
-                const uint32_t f = v & ~kCountMask;
-                if (f == 0u) {
+                uint32_t v[kBatch];
+#pragma unroll
+                for (int q = 0; q < kBatch; ++q) v[q] = k - q >= 0 ? lbv[(size_t)(k - q) * kRadix + d] : kFlagIncl;
+                int used = 0;
+                bool found = false, stall = false;
+#pragma unroll
+                for (int q = 0; q < kBatch; ++q) {
+                    if (!found && !stall && k - q >= 0) {
+                        const uint32_t f = v[q] & ~kCountMask;
+                        if (f == 0u) {
+                            stall = true;  // not published yet: read again from here
+                        } else {
+                            excl += v[q] & kCountMask;
+                            ++used;
+                            found = f == kFlagIncl;
+                        }
+                    }
+                }
+                if (found) break;
+                if (stall) {
                     if (++spins > kSpinLimit) {
                         atomicOr(err, kErrTimeout);
                         break;
                     }
                     __nanosleep(32);
-                    continue;
                 }
-                excl += v & kCountMask;
-                if (f == kFlagIncl) break;
-                --k;
+                k -= used;
             }
             __threadfence();
             ((volatile uint32_t*)lookback)[(size_t)tile * kRadix + d] = kFlagIncl | ((excl + tile_count) & kCountMask);

@@ -56,6 +56,8 @@ constexpr int kSegs = 63;     // FP64 list evaluation: run slots body + thread, 
 constexpr int kSlotBits = 28; // slot index bits of a stack entry (count - 1 in the top 3)
 constexpr float kMargin = 1e-5f;  // relative margin of the FP32 group tests
 constexpr float kAbsErr = 1e-6f;  // bound on FP32 coordinate error, relative to magnitudes
+constexpr int kPendFlush = 16;    // learned: run the network once this many candidates wait
+constexpr int kPendCap = 32;      // learned: deferred candidates per warp
 
 enum { kLearnNone = 0, kLearnInfer = 1, kLearnCollect = 2 };
 
@@ -145,7 +147,10 @@ struct FParams {
     // learned criterion
     const MlpDev* mlp;
     float theta_max2;
-    unsigned long long* lstats;  // candidates, accepted by the network, fallbacks
+    float l_budget;  // per-body error budget (relative to the group's direct-term acceleration)
+    float l_band;    // analytic estimate decides outside +-l_band decades of the allowance
+    float l_frac;    // a candidate may take at most this fraction of the remaining allowance
+    unsigned long long* lstats;  // candidates, network accepts, fallbacks, analytic accepts
     // collection
     int32_t* c_group;
     int32_t* c_slot;
@@ -173,6 +178,8 @@ struct WalkSmem {
     float side2f[kMaxDepth + 1];
     double side2d[kMaxDepth + 1];
     float feat[kF ? kWarps : 1][kF ? 32 : 1][9];
+    int pend_node[kF ? kWarps : 1][kF ? 32 : 1];      // learned: candidates deferred to the network
+    unsigned pend_mask[kF ? kWarps : 1][kF ? 32 : 1];
     uint8_t plist[kW64][kFP64 ? kList : 1][32];  // FP64: each lane's own entries, in order
     // FP64: the balanced evaluation's per-warp tables (see the flush).
     int poff[kW64][33];                     // first pair of each lane, then the total
@@ -183,7 +190,7 @@ struct WalkSmem {
 };
 
 template <bool kFP64, int kLearn>
-__global__ void __launch_bounds__(kThreads) traverse_masked_kernel(FParams p)
+__global__ void __launch_bounds__(kThreads, kLearn == kLearnInfer ? 5 : (kFP64 ? 6 : 8)) traverse_masked_kernel(FParams p)
 {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     WalkSmem<kFP64, kLearn>& sm = *reinterpret_cast<WalkSmem<kFP64, kLearn>*>(smem_raw);
@@ -287,7 +294,8 @@ __global__ void __launch_bounds__(kThreads) traverse_masked_kernel(FParams p)
     // Per-walk logarithms of the learned features (base 2).
     const float lext = kLearn ? __log2f(fmaxf(gextent, 1e-30f)) : 0.0f;
     const float lascale = kLearn ? __log2f(ascale) : 0.0f;
-    unsigned long long ncand = 0, nacc = 0, nfall = 0;
+    unsigned long long ncand = 0, nacc = 0, nfall = 0, nana = 0;
+    float grel = kLearn == kLearnInfer ? p.l_budget : 0.0f;  // remaining per-body allowance (units of a_scale)
 
     int nlist = 0;
     int sp = 1;
@@ -296,8 +304,25 @@ __global__ void __launch_bounds__(kThreads) traverse_masked_kernel(FParams p)
     bool overflow = false;
     int64_t pops = 0;
 
-    while (sp > 0 || nlist > 0) {
-        if (sp > 0) {
+    int npend = 0;  // learned: deferred candidates waiting for the network
+    while (sp > 0 || nlist > 0 || npend > 0) {
+        // The learned walk defers the candidates the network must decide and
+        // evaluates them in batches: this iteration takes the deferred nodes
+        // instead of the stack's when enough wait (or nothing else is left).
+        const bool from_pend = kLearn == kLearnInfer && npend > 0 && (npend >= kPendFlush || sp == 0);
+        if (sp > 0 || from_pend) {
+            int R = 0, T = 0, f_r = 0, s_r = 0;
+            unsigned m_r = 0;
+            float plerr = 0.0f;  // network's predicted log10 error of deferred row `lane`
+            if (kLearn == kLearnInfer && from_pend) {
+                const float yrow = mlp_predict_warp(p.mlp, sm.feat[w], lane, npend);
+                plerr = yrow * p.mlp->sc.lstd + p.mlp->sc.lmean;
+                T = npend;
+                if (sp + T > kStack) {
+                    overflow = true;
+                    break;
+                }
+            } else {
             // Pop whole ranges from the top while they fit in 32 lanes.
             const int avail = sp < 32 ? sp : 32;
             int rfirst = 0, rcnt = 0;
@@ -315,18 +340,19 @@ __global__ void __launch_bounds__(kThreads) traverse_masked_kernel(FParams p)
                 if (lane >= off) incl += t;
             }
             const bool take = lane < avail && incl <= 32;
-            const int R = __popc(__ballot_sync(0xffffffffu, take));
-            const int T = __shfl_sync(0xffffffffu, incl, R - 1);
+            R = __popc(__ballot_sync(0xffffffffu, take));
+            T = __shfl_sync(0xffffffffu, incl, R - 1);
             const int rstart = incl - rcnt;
             const unsigned starts = __reduce_or_sync(0xffffffffu, take ? (1u << rstart) : 0u);
             const int rj = __popc(starts & ((2u << lane) - 1u)) - 1;
-            const int f_r = __shfl_sync(0xffffffffu, rfirst, rj);
-            const int s_r = __shfl_sync(0xffffffffu, rstart, rj);
-            const unsigned m_r = __shfl_sync(0xffffffffu, rmask, rj);
+            f_r = __shfl_sync(0xffffffffu, rfirst, rj);
+            s_r = __shfl_sync(0xffffffffu, rstart, rj);
+            m_r = __shfl_sync(0xffffffffu, rmask, rj);
             pops += T;
             if (sp - R + T > kStack || pops > p.max_pops) {
                 overflow = true;
                 break;
+            }
             }
             const int k = T;
             int node = -1;
@@ -336,8 +362,13 @@ __global__ void __launch_bounds__(kThreads) traverse_masked_kernel(FParams p)
             float dmin2 = 0.f, dmax2 = 0.f, s2 = 0.f, nerr = 0.f;
             float4 e = make_float4(0.f, 0.f, 0.f, 0.f);
             if (lane < k) {
-                node = f_r + (lane - s_r);
-                M = m_r;
+                if (kLearn == kLearnInfer && from_pend) {
+                    node = sm.pend_node[w][lane];
+                    M = sm.pend_mask[w][lane];
+                } else {
+                    node = f_r + (lane - s_r);
+                    M = m_r;
+                }
                 const float4 a = __ldg(p.A + node);
                 const float4 b = __ldg(p.B + node);
                 const uint32_t mt = __ldg(p.meta + node);
@@ -368,7 +399,7 @@ __global__ void __launch_bounds__(kThreads) traverse_masked_kernel(FParams p)
                     if (s2 * (1.0f + kMargin) < theta2f * dlo * dlo) {
                         A = M;
                     } else {
-                        if (kLearn) cand = M != 0 && dmin2 > 0.0f && s2 < p.theta_max2 * dmin2;
+                        if (kLearn) cand = !from_pend && M != 0 && dmin2 > 0.0f && s2 < p.theta_max2 * dmin2;
                         if (s2 * (1.0f - kMargin) > theta2f * dhi * dhi) A = 0;
                         else mixed = true;
                     }
@@ -376,7 +407,8 @@ __global__ void __launch_bounds__(kThreads) traverse_masked_kernel(FParams p)
             }
             __syncwarp();
             sp -= R;
-            if (kLearn && !kFP64) {
+            if (kLearn == kLearnInfer) npend = from_pend ? 0 : npend;
+            if (kLearn == kLearnCollect) {
                 const unsigned cb = __ballot_sync(0xffffffffu, cand);
                 if (cb) {
                     float f[kFeat];
@@ -402,7 +434,7 @@ __global__ void __launch_bounds__(kThreads) traverse_masked_kernel(FParams p)
                         f[6] = kL * (lspr - 0.5f * l2s);
                         f[7] = kL * (0.5f * __log2f(fmaxf(dcx * dcx + dcy * dcy + dcz * dcz, 1e-36f)) - ldmin);
                     }
-                    if (kLearn == kLearnCollect) {
+                    {
                         const int leader = __ffs(cb) - 1;
                         unsigned long long basec = 0;
                         if (lane == leader) basec = atomicAdd(p.c_count, (unsigned long long)__popc(cb));
@@ -416,36 +448,104 @@ __global__ void __launch_bounds__(kThreads) traverse_masked_kernel(FParams p)
 #pragma unroll
                             for (int q = 0; q < kFeat; ++q) p.c_feat[slot * kFeat + q] = f[q];
                         }
-                    } else {
-                        // Candidates are packed into rows 0..ncand-1 so that
-                        // one 16-row tile suffices for up to 16 of them.
-                        const MlpDev* md = p.mlp;
-                        float (*F)[9] = sm.feat[w];
-                        const int row = __popc(cb & lt);
-                        const int nrows = __popc(cb);
-                        bool inr = cand;
-#pragma unroll
-                        for (int q = 0; q < kFeat; ++q) {
-                            const float zq = (f[q] - md->sc.mean[q]) * md->sc.inv_std[q];
-                            inr = inr && zq >= md->sc.lo[q] && zq <= md->sc.hi[q];
-                            if (cand) F[row][q] = fminf(fmaxf(zq, -64.0f), 64.0f);
-                        }
-                        __syncwarp();
-                        const float yrow = mlp_predict_warp(md, F, lane, nrows);
-                        const float yhat = __shfl_sync(0xffffffffu, yrow, row);
-                        __syncwarp();
-                        if (cand) {
-                            ++ncand;
-                            if (!inr) {
-                                ++nfall;
-                            } else if (yhat * md->sc.lstd + md->sc.lmean < md->log_thresh) {
-                                A = M;
-                                mixed = false;
-                                ++nacc;
-                            }
-                        }
                     }
                 }
+            }
+            if (kLearn == kLearnInfer) {
+                // Per-body budget: the group's remaining allowance grel (the
+                // smallest of its bodies' budgets, in units of a_scale) pays
+                // for every accepted candidate's error.  The analytic
+                // estimate log10(G m s^2 / (dmin^4 a_scale)) (s the spread)
+                // accepts a candidate far below the allowance and leaves one
+                // far above it to the theta test; the network predicts the
+                // error of the others, deferred and evaluated in batches.
+                // Out-of-range features: the theta test (the fallback).
+                const MlpDev* md = p.mlp;
+                const float lallow = grel > 0.0f ? __log10f(p.l_frac * grel) : -1e30f;
+                bool take = false, defer = false;
+                float lerr = 0.0f;
+                if (from_pend) {
+                    take = lane < k && M != 0 && plerr < lallow;
+                    lerr = plerr;
+                } else if (__ballot_sync(0xffffffffu, cand)) {
+                    constexpr float kL = 0.30102999566f;  // log10(2)
+                    float l2dmin = 0.0f, lspr = 0.0f, lest = 0.0f;
+                    if (cand) {
+                        l2dmin = __log2f(dmin2);
+                        lspr = __log2f(fmaxf(__ldg(p.spread + node), 1e-8f * sqrtf(s2)));
+                        lest = kL * (__log2f(e.w) - l2dmin - lascale) + 2.0f * kL * (lspr - 0.5f * l2dmin);
+                    }
+                    const bool sure = cand && lest + p.l_band < lallow;
+                    const bool band = cand && !sure && lest - p.l_band <= lallow;
+                    bool inr = false;
+                    float zq[kFeat];
+                    if (band) {
+                        // the features, as the collection computes them
+                        const float l2s = __log2f(s2);
+                        const float dcx = e.x - bcx, dcy = e.y - bcy, dcz = e.z - bcz;
+                        const float ldmin = 0.5f * l2dmin;
+                        float f[kFeat];
+                        f[0] = kL * (0.5f * l2s - ldmin);
+                        f[1] = kL * (lspr - ldmin);
+                        f[2] = kL * (lext - ldmin);
+                        f[3] = kL * (__log2f(e.w) - l2dmin - lascale);
+                        f[4] = kL * 0.5f * (__log2f(dmax2) - l2dmin);
+                        f[5] = (float)depth * (1.0f / kMaxDepth);
+                        f[6] = kL * (lspr - 0.5f * l2s);
+                        f[7] = kL * (0.5f * __log2f(fmaxf(dcx * dcx + dcy * dcy + dcz * dcz, 1e-36f)) - ldmin);
+                        inr = true;
+#pragma unroll
+                        for (int q = 0; q < kFeat; ++q) {
+                            zq[q] = (f[q] - md->sc.mean[q]) * md->sc.inv_std[q];
+                            inr = inr && zq[q] >= md->sc.lo[q] && zq[q] <= md->sc.hi[q];
+                        }
+                    }
+                    const unsigned wb = __ballot_sync(0xffffffffu, band && inr);
+                    const int slot = npend + __popc(wb & lt);
+                    defer = band && inr && slot < kPendCap;
+                    if (defer) {
+                        float (*F)[9] = sm.feat[w];
+#pragma unroll
+                        for (int q = 0; q < kFeat; ++q) F[slot][q] = fminf(fmaxf(zq[q], -64.0f), 64.0f);
+                        sm.pend_node[w][slot] = node;
+                        sm.pend_mask[w][slot] = M;
+                    }
+                    npend = min(kPendCap, npend + __popc(wb));
+                    take = sure;
+                    lerr = lest;
+                    if (cand) {
+                        ++ncand;
+                        if (band && !defer) ++nfall;  // outside the training range, or no room: theta
+                    }
+                }
+                if (__any_sync(0xffffffffu, take)) {
+                    // The accepted errors, in lane order, must fit in the
+                    // allowance: a prefix of the candidates passes.
+                    const float ec = take ? exp10f(lerr) : 0.0f;
+                    float incl = ec;
+#pragma unroll
+                    for (int off = 1; off < 32; off <<= 1) {
+                        const float t = __shfl_up_sync(0xffffffffu, incl, off);
+                        if (lane >= off) incl += t;
+                    }
+                    take = take && incl <= grel;
+                    float spent = take ? ec : 0.0f;
+#pragma unroll
+                    for (int off = 16; off > 0; off >>= 1) spent += __shfl_xor_sync(0xffffffffu, spent, off);
+                    grel -= spent;
+                }
+                if (take) {
+                    A = M;
+                    mixed = false;
+                    if (from_pend) ++nacc;
+                    else ++nana;
+                }
+                if (defer) {  // decided later, when the network has run
+                    A = 0;
+                    M = 0;
+                    mixed = false;
+                }
+                __syncwarp();
             }
             // Mixed nodes: every lane of the mask applies its own test.
             unsigned mb = __ballot_sync(0xffffffffu, mixed);
@@ -680,11 +780,13 @@ __global__ void __launch_bounds__(kThreads) traverse_masked_kernel(FParams p)
             ncand += __shfl_down_sync(0xffffffffu, ncand, off);
             nacc += __shfl_down_sync(0xffffffffu, nacc, off);
             nfall += __shfl_down_sync(0xffffffffu, nfall, off);
+            nana += __shfl_down_sync(0xffffffffu, nana, off);
         }
         if (lane == 0) {
             atomicAdd(p.lstats, ncand);
             atomicAdd(p.lstats + 1, nacc);
             atomicAdd(p.lstats + 2, nfall);
+            atomicAdd(p.lstats + 3, nana);
         }
     }
 }
@@ -818,8 +920,11 @@ int launch_traverse_learned(bh_context* ctx, double theta, double G, double soft
     p.kick_h = kick_h;
     p.mlp = ctx->mlp_dev;
     p.theta_max2 = (float)(ctx->learn_theta_max * ctx->learn_theta_max);
+    p.l_budget = (float)ctx->learn_budget;
+    p.l_band = (float)ctx->learn_band;
+    p.l_frac = (float)ctx->learn_frac;
     p.lstats = ctx->lstats;
-    BH_CUDA_TRY(cudaMemsetAsync(ctx->lstats, 0, 3 * sizeof(unsigned long long), ctx->stream));
+    BH_CUDA_TRY(cudaMemsetAsync(ctx->lstats, 0, 4 * sizeof(unsigned long long), ctx->stream));
     return launch_walk<false, kLearnInfer>(ctx, p);
 }
 

@@ -4,7 +4,8 @@
 //
 //   simulate -f bodies.csv --dt 1h --tend 10d --theta 1.05 [-b N] [-r]
 //            [--fc let|tree|let_direct] [--steps K] [--vs 10d|none] [-o sim_out]
-//            [--mode plain|fp64_list|fp32] [--generate N --seed S] [--dump FILE]
+//            [--mode plain|fp64_list|fp32|learned] [--generate N --seed S] [--dump FILE]
+//            [--model FILE --budget B --theta-max T --band D --frac F]
 //
 // --tend uses the reference's loop (`for (t = 0; t < t_end; t += dt)`, so
 // 10d at 1h runs 241 steps); --steps overrides it.  -r writes the final
@@ -24,6 +25,14 @@
 // sim_out and --vs to 10d, as in the reference.  --vs none turns them off.
 // The download of a frame waits for the GPU; its file is written by a host
 // thread while the next steps run.
+//
+// --mode selects the force form: plain (the reference's arithmetic, bit
+// for bit), fp64_list (the reference's interaction set in FP64), fp32 (FP32
+// far field, FP64 Sun and planet terms) or learned (fp32 with the learned
+// acceptance criterion: --model names a file written by bh_mlp_save, --budget
+// is each body's relative error budget, default 1e-5; --theta-max bounds
+// the candidates, default 3; --band and --frac tune the criterion, see
+// bh_learned_set_criterion; --theta stays the fallback criterion).
 #include <algorithm>
 #include <chrono>
 #include <cmath>
@@ -73,8 +82,8 @@ void check(int rc, const char* what)
 int main(int argc, char** argv)
 {
     std::string file, fc = "let", mode_s = "plain", dt_s = "1d", tend_s = "1y", dump, vs_s = "10d",
-                out_dir = "sim_out";
-    double theta = 1.05;
+                out_dir = "sim_out", model;
+    double theta = 1.05, budget = 1e-5, theta_max = 3.0, band = 0.5, frac = 0.25;
     long long bodies = -1, steps = -1, generate = 0;
     unsigned long long seed = 1;
     bool reference = false;
@@ -100,10 +109,16 @@ int main(int argc, char** argv)
         else if (k == "--generate") generate = std::stoll(val());
         else if (k == "--seed") seed = std::stoull(val());
         else if (k == "--dump") dump = val();
+        else if (k == "--model") model = val();
+        else if (k == "--budget") budget = std::stod(val());
+        else if (k == "--theta-max") theta_max = std::stod(val());
+        else if (k == "--band") band = std::stod(val());
+        else if (k == "--frac") frac = std::stod(val());
         else if (k == "-h" || k == "--help") {
             std::cout << "simulate -f FILE [--dt 1h] [--tend 1y] [--theta 1.05] [-b N] [-r] [--steps K]\n"
                          "         [--fc let|tree|let_direct] (one rank: the same step)\n"
-                         "         [--vs 10d|none] [-o sim_out] [--mode plain|fp64_list|fp32]\n"
+                         "         [--vs 10d|none] [-o sim_out] [--mode plain|fp64_list|fp32|learned]\n"
+                         "         [--model FILE --budget 1e-5 --theta-max 3 --band 0.5 --frac 0.25]\n"
                          "         [--generate N --seed S] [--dump FILE]\n";
             return 0;
         } else die("unknown option " + k);
@@ -117,7 +132,13 @@ int main(int argc, char** argv)
     int mode = BH_MODE_PLAIN_FP64;
     if (mode_s == "fp64_list") mode = BH_MODE_FP64_LIST;
     else if (mode_s == "fp32") mode = BH_MODE_FP32_FAR;
+    else if (mode_s == "learned") mode = BH_MODE_LEARNED;
     else if (mode_s != "plain") die("unknown --mode " + mode_s);
+    std::vector<float> params(BH_MLP_PARAMS), scale(BH_MLP_SCALE);
+    if (mode == BH_MODE_LEARNED) {
+        if (model.empty()) die("--mode learned needs --model FILE");
+        check(bh_mlp_load(model.c_str(), params.data(), scale.data()), "bh_mlp_load");
+    }
     const double dt = parse_time(dt_s), t_end = parse_time(tend_s);
 
     std::vector<uint64_t> ids;
@@ -146,6 +167,10 @@ int main(int argc, char** argv)
         check(bh_context_create(cap > 0 ? cap : 1, 0, &ctx), "bh_context_create");
         check(bh_load_csv(ctx, file.c_str(), bodies, &n), "bh_load_csv");
         ids.resize(n); mass.resize(n); pos.resize(3 * n); vel.resize(3 * n);
+    }
+    if (mode == BH_MODE_LEARNED) {
+        check(bh_learned_set_model(ctx, params.data(), scale.data(), budget, theta_max), "bh_learned_set_model");
+        check(bh_learned_set_criterion(ctx, band, frac), "bh_learned_set_criterion");
     }
     std::cout << "Loaded " << n << " bodies\n";
     int64_t nsteps = steps;

@@ -299,6 +299,14 @@ int bh_mlp_gradient(const float *params, const float *X, const float *T, int64_t
 int bh_mlp_train(const float *features, const float *labels, int64_t n, int epochs, int batch, float lr,
                  uint64_t seed, float *params_out, float *scale_out, float *loss_out);
 
+/* A trained model (BH_MLP_PARAMS parameters and BH_MLP_SCALE scaling
+ * floats) as a file: an 8-byte tag "BHMLP001", the two counts as uint32,
+ * then the floats, all little-endian.  Host functions; BH_ERR_IO on a file
+ * that cannot be written or read, BH_ERR_INVALID_ARGUMENT on one that is
+ * not such a model. */
+int bh_mlp_save(const char *path, const float *params, const float *scale);
+int bh_mlp_load(const char *path, float *params_out, float *scale_out);
+
 /* Network outputs (predicted log10 error) for raw feature rows through the
  * same fused mma.sync inference the traversal uses; in_range (may be NULL)
  * flags rows inside the model's training range. */
@@ -312,14 +320,28 @@ int bh_mlp_predict(const float *params, const float *scale, const float *feature
  * instead of walking its subtree at theta_label.  *n_out pairs are written. */
 int bh_learned_collect(bh_context *ctx, double theta, double theta_label, double theta_max, double G,
                        int64_t max_pairs, float *features_out, float *labels_out, int64_t *n_out);
-/* Model for BH_MODE_LEARNED: a candidate node (side < theta_max d_min) is
- * accepted for the whole group when the predicted error is below `budget`
- * (relative, per node) and its features are inside the training range;
+/* Model for BH_MODE_LEARNED.  `budget` is each body's error budget relative
+ * to its acceleration: a warp group of 32 bodies starts with an allowance of
+ * budget x the smallest of its bodies' direct-term (Sun and planet)
+ * accelerations, and every candidate node it accepts unopened pays its
+ * predicted error out of it, so the errors a body accepts sum to at most its
+ * budget.  A candidate (a node the theta test does not accept for the whole
+ * group, side < theta_max d_min) is accepted for the whole group when its
+ * predicted error fits both the allowance and its share of it (see
+ * bh_learned_set_criterion) and its features are inside the training range;
  * otherwise the theta criterion decides. */
 int bh_learned_set_model(bh_context *ctx, const float *params, const float *scale, double budget, double theta_max);
+/* Tuning of the criterion (defaults band 0.5, frac 0.25): the analytic error
+ * estimate G m s^2 / d_min^4 (s the node's mass spread) decides candidates
+ * more than `band` decades below or above the allowance without the network;
+ * the network predicts the error of the others.  One candidate takes at most
+ * `frac` of the remaining allowance. */
+int bh_learned_set_criterion(bh_context *ctx, double band, double frac);
 /* Counters of the last BH_MODE_LEARNED traversal: candidates, candidates
- * accepted by the network, candidates that fell back to theta. */
-int bh_learned_stats(bh_context *ctx, int64_t out[3]);
+ * accepted on the network's prediction, candidates that fell back to theta
+ * (features outside the training range), candidates accepted on the
+ * analytic estimate. */
+int bh_learned_stats(bh_context *ctx, int64_t out[4]);
 
 /* ---- stateless host-buffer entry points ------------------------------ */
 /* Each copies its inputs to the device, runs the kernel, copies back.  They

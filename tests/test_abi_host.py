@@ -195,3 +195,29 @@ def test_pow5_table_is_generated():
             assert exact - Fraction(2) ** s < approx <= exact
         else:
             assert exact <= approx < exact + Fraction(2) ** s
+
+
+def test_model_file_round_trip(bh, tmp_path):
+    """bh_mlp_save / bh_mlp_load (host functions): the parameters and scaling
+    come back bit for bit; truncated, extended, foreign and missing files are
+    refused with a status."""
+    rng = np.random.default_rng(4)
+    params = rng.normal(size=bh.MLP_PARAMS).astype(np.float32)
+    scale = rng.normal(size=bh.MLP_SCALE).astype(np.float32)
+    f = tmp_path / "m.bhmlp"
+    bh.mlp_save(f, params, scale)
+    assert f.stat().st_size == 16 + 4 * (bh.MLP_PARAMS + bh.MLP_SCALE)
+    p, s = bh.mlp_load(f)
+    assert np.array_equal(p.view(np.uint32), params.view(np.uint32))
+    assert np.array_equal(s.view(np.uint32), scale.view(np.uint32))
+    data = f.read_bytes()
+    for bad in (data[:-4], data + b"\0", b"XXXXXXXX" + data[8:]):
+        f.write_bytes(bad)
+        with pytest.raises(bh.BhError) as e:
+            bh.mlp_load(f)
+        assert e.value.status == 1  # BH_ERR_INVALID_ARGUMENT
+    with pytest.raises(bh.BhError) as e:
+        bh.mlp_load(tmp_path / "missing.bhmlp")
+    assert e.value.status == 9  # BH_ERR_IO
+    with pytest.raises(ValueError):
+        bh.mlp_save(f, params[:10], scale)

@@ -8,9 +8,10 @@ from __future__ import annotations
 import numpy as np
 import pytest
 
-from conftest import G, THETA
+from conftest import DT, G, ROOT, THETA, assert_bits_equal
 
 pytestmark = pytest.mark.gpu
+SIMULATE = ROOT / "barnes-hut_gb300" / "_build" / "simulate"
 
 
 def he_params(rng):
@@ -73,34 +74,115 @@ def _system(bh, seed, n):
     return c
 
 
-def test_learned_pipeline_gains_over_theta(bh):
+def test_learned_pipeline_what_the_network_gains(bh):
+    """Pairs labelled by the plain walk at theta = 0.5 on three 60k systems,
+    the network trained on the GPU, then on an unseen system:
+
+    * the network predicts the candidates' errors more tightly than the
+      analytic estimate G m s^2 / d_min^4 it refines (the 5-95 % band of the
+      residuals);
+    * at the same per-body budget, the criterion that asks the network about
+      the candidates near the allowance is as accurate as the analytic
+      estimate alone (median within 5 %) with at most 5 % more interactions
+      (on this 60k system the network decides few candidates; on the 4M
+      system the bench compares the two at every budget);
+    * against the method without it (the theta test at 1.05) it makes fewer
+      interactions, and the bodies' errors stay within their budget.
+
+    What it does not gain, measured in the bench and stated in the design:
+    a plain theta test at a wider angle is faster at equal error on this
+    walk (the walk's per-node cost, not the interactions, bounds it there)."""
     feats, labels = [], []
     for seed in (101, 102, 103):
         with _system(bh, seed, 60_000) as c:
-            f, l = c.learned_collect(THETA, 0.5, 3.0, G, max_pairs=1_500_000)
-            ok = np.all(np.isfinite(f), axis=1) & np.isfinite(l)
-            feats.append(f[ok]); labels.append(l[ok])
+            f, lab = c.learned_collect(THETA, 0.5, 3.0, G, max_pairs=1_500_000)
+            ok = np.all(np.isfinite(f), axis=1) & np.isfinite(lab)
+            feats.append(f[ok]); labels.append(lab[ok])
     F = np.concatenate(feats); L = np.concatenate(labels)
     assert len(L) > 50_000
     params, scale, losses = bh.mlp_train(F, L, epochs=8, batch=2048, lr=2e-3, seed=0)
     # standardised MSE (1.0 = predicting the mean): the network learns the labels
     assert losses[-1] < 0.3 and losses[-1] < losses[0]
-    # unseen system: theta criterion alone vs learned criterion at budget 1e-5
     with _system(bh, 104, 60_000) as c:
+        f, lab = c.learned_collect(THETA, 0.5, 3.0, G, max_pairs=400_000)
+        ok = np.all(np.isfinite(f), axis=1) & np.isfinite(lab)
+        f, lab = f[ok], lab[ok]
+        pred, inr = bh.mlp_predict(params, scale, f)
+        r_net = (lab - pred)[inr]
+        r_ana = lab - (f[:, 3] + 2.0 * f[:, 1])
+        band = lambda r: float(np.percentile(r, 95) - np.percentile(r, 5))  # noqa: E731
+        print(f"residual 5-95 % band: network {band(r_net):.3f}, analytic {band(r_ana):.3f} decades")
+        assert inr.mean() > 0.95
+        assert band(r_net) < 0.9 * band(r_ana)
+
         rng = np.random.default_rng(2)
         sample = np.sort(rng.choice(c.n, 1024, replace=False))
         ref = c.direct_sum(sample, G)
-        a_theta = c.compute_accelerations(THETA, G, 0.0, bh.MODE_FP32_FAR)
+        rel = lambda a: np.linalg.norm(a[sample] - ref, axis=1) / np.linalg.norm(ref, axis=1)  # noqa: E731
+        e_theta = rel(c.compute_accelerations(THETA, G, 0.0, bh.MODE_FP32_FAR))
         n_theta = c.interaction_count()
-        c.learned_set_model(params, scale, budget=1e-6, theta_max=3.0)
-        a_learn = c.compute_accelerations(THETA, G, 0.0, bh.MODE_LEARNED)
-        n_learn = c.interaction_count()
+        rows = {}
+        for budget in (1e-6, 1e-5):
+            for name, b in (("network", 0.5), ("analytic", 0.0)):
+                c.learned_set_model(params, scale, budget=budget, theta_max=3.0)
+                c.learned_set_criterion(b, 0.25)
+                e = rel(c.compute_accelerations(THETA, G, 0.0, bh.MODE_LEARNED))
+                rows[(budget, name)] = (float(np.median(e)), c.interaction_count(), c.learned_stats(), e)
+    print(f"theta {THETA}: median {np.median(e_theta):.3g}, {n_theta} interactions")
+    for budget in (1e-6, 1e-5):
+        med_n, n_n, st, e_n = rows[(budget, "network")]
+        med_a, n_a, _, _ = rows[(budget, "analytic")]
+        print(f"budget {budget:g}: network median {med_n:.3g} / {n_n} interactions, analytic {med_a:.3g} / {n_a}; "
+              f"within budget {np.mean(e_n <= budget):.3f}; stats {st}")
+    for budget in (1e-6, 1e-5):
+        med_n, n_n, st, e_n = rows[(budget, "network")]
+        med_a, n_a, _, _ = rows[(budget, "analytic")]
+        assert st["candidates"] > 0 and st["accepted"] > 0 and st["fallback"] < 0.05 * st["candidates"]
+        assert med_n <= 1.05 * med_a and n_n <= 1.05 * n_a
+        assert n_n < n_theta
+        assert np.mean(e_n <= budget) >= 0.95  # the bodies' errors within their budget
+    assert rows[(1e-5, "network")][0] <= 1e-5
+
+
+def test_simulate_learned_mode_matches_api(bh, tmp_path):
+    """simulate --mode learned --model FILE (the reference's CLI, extended):
+    a model saved with mlp_save drives the same steps as the C ABI with the
+    same model, budget and criterion; 3 steps of 2,000 bodies, bit for bit."""
+    import subprocess
+    if not SIMULATE.exists():
+        pytest.skip("simulate not built (run build())")
+    feats, labels = [], []
+    with _system(bh, 201, 60_000) as c:
+        f, lab = c.learned_collect(THETA, 0.5, 3.0, G, max_pairs=800_000)
+        ok = np.all(np.isfinite(f), axis=1) & np.isfinite(lab)
+        feats.append(f[ok]); labels.append(lab[ok])
+    params, scale, _ = bh.mlp_train(np.concatenate(feats), np.concatenate(labels), epochs=4, batch=2048, lr=2e-3,
+                                    seed=0)
+    model = tmp_path / "model.bhmlp"
+    bh.mlp_save(model, params, scale)
+    p2, s2 = bh.mlp_load(model)
+    assert_bits_equal(p2, params, "saved parameters"); assert_bits_equal(s2, scale, "saved scaling")
+    dump = tmp_path / "final.csv"
+    r = subprocess.run([str(SIMULATE), "--generate", "2000", "--seed", "3", "--steps", "3", "--dt", "1h",
+                        "--mode", "learned", "--model", str(model), "--budget", "1e-5", "--band", "0.5",
+                        "--frac", "0.25", "--vs", "none", "--dump", str(dump)], capture_output=True, text=True,
+                       cwd=tmp_path)
+    assert r.returncode == 0, r.stdout + r.stderr
+    assert "Loaded 2000 bodies" in r.stdout
+    pos, vel, mass, ids = bh.generate_system(3, 2000, 0.10, 0.0)
+    with bh.Context(2000) as c:
+        c.learned_set_model(params, scale, budget=1e-5, theta_max=3.0)
+        c.learned_set_criterion(0.5, 0.25)
+        c.set_bodies(pos, vel, mass, ids)
+        c.step(DT, THETA, G, 3, bh.MODE_LEARNED, t=0.0)
+        p, v, m, i, _ = c.get_bodies()
+        c.compute_accelerations(THETA, G, 0.0, bh.MODE_LEARNED, download=False)
         stats = c.learned_stats()
-    e_theta = np.linalg.norm(a_theta[sample] - ref, axis=1) / np.linalg.norm(ref, axis=1)
-    e_learn = np.linalg.norm(a_learn[sample] - ref, axis=1) / np.linalg.norm(ref, axis=1)
-    print(f"theta: {n_theta} interactions, median err {np.median(e_theta):.3g}; learned: {n_learn} "
-          f"interactions, median err {np.median(e_learn):.3g}; stats {stats}")
-    assert stats["candidates"] > 0 and stats["accepted"] > 0
-    assert stats["fallback"] < 0.5 * stats["candidates"]
-    assert n_learn < n_theta          # the gain: fewer interactions ...
-    assert np.median(e_learn) <= 1e-5  # ... within the metric's error budget
+    _, rmass, rpos, rvel = bh.read_csv(dump)
+    rids = np.loadtxt(dump, delimiter=",", skiprows=1, usecols=0, dtype=np.uint64)
+    assert_bits_equal(rids, i, "ids"); assert_bits_equal(rmass, m, "masses")
+    assert_bits_equal(rpos, p, "positions"); assert_bits_equal(rvel, v, "velocities")
+    assert stats["candidates"] > 0
+    r = subprocess.run([str(SIMULATE), "--generate", "100", "--mode", "learned", "--vs", "none"],
+                       capture_output=True, text=True, cwd=tmp_path)
+    assert r.returncode == 1 and "--model" in r.stderr
