@@ -278,14 +278,17 @@ int step_once(bh_context* ctx, double dt, double theta, double G, int mode)
 // and leaves the state in the other, so there is one graph per starting set;
 // after a replay the host pointers trade places as step_once's permutation
 // would make them.  The kernels read no host state that the key leaves out:
-// buffers live in the context's single allocation and the learned model in a
-// fixed device block.
+// buffers live in the context's single allocation, the learned model in a
+// fixed device block, and the learned walk's scalar parameters (baked into
+// its launch) are part of the key.
 int step_graph(bh_context* ctx, double dt, double theta, double G, int mode)
 {
     const int merge = ctx->build_merge ? 1 : 0;
+    const double learn[4] = {ctx->learn_theta_max, ctx->learn_budget, ctx->learn_band, ctx->learn_frac};
     bh_context::StepGraph& g = ctx->sg[ctx->px < ctx->px2 ? 0 : 1];
+    const bool same_learn = mode != BH_MODE_LEARNED || std::equal(learn, learn + 4, g.learn);
     if (!(g.exec && g.n == ctx->n && g.mode == mode && g.dt == dt && g.theta == theta && g.G == G &&
-          g.merge == merge && g.nd == ctx->num_direct)) {
+          g.merge == merge && g.nd == ctx->num_direct && same_learn)) {
         if (g.exec) {
             cudaGraphExecDestroy(g.exec);
             g.exec = nullptr;
@@ -317,6 +320,7 @@ int step_graph(bh_context* ctx, double dt, double theta, double G, int mode)
         g.G = G;
         g.merge = merge;
         g.nd = ctx->num_direct;
+        std::copy(learn, learn + 4, g.learn);
     }
     BH_CUDA_TRY(cudaGraphLaunch(g.exec, ctx->stream));
     bh::swap_body_sets(ctx);

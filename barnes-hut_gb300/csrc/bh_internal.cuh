@@ -414,6 +414,7 @@ struct bh_context {
         int64_t n = -1, launches = 0;
         int mode = -1, merge = -1, nd = -1;
         double dt = 0.0, theta = 0.0, G = 0.0;
+        double learn[4] = {0.0, 0.0, 0.0, 0.0};  // learned walk: theta_max, budget, band, frac
     } sg[2];
 
     // Error word raised by kernels and a pinned mirror for readback.

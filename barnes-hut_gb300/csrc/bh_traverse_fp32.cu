@@ -1,6 +1,7 @@
-// The masked warp walk behind BH_MODE_FP64_LIST, BH_MODE_FP32_FAR and
-// BH_MODE_LEARNED, and the collection of training pairs for the learned
-// criterion.  No reference counterpart: the reference walks one body at a
+// The masked warp walk behind BH_MODE_FP64_LIST and BH_MODE_FP32_FAR, and
+// the collection of training pairs for the learned criterion (the learned
+// walk itself, BH_MODE_LEARNED, is bh_traverse_learned.cu).  No reference
+// counterpart: the reference walks one body at a
 // time (src/traversal.cpp:53-102).
 //
 // A warp owns 32 Morton-consecutive bodies.  Stack entries are sibling
@@ -31,35 +32,14 @@
 //   here, and three FP64 subtractions per visit would cost more than the
 //   interaction).  FP32 partials of each staged list are added into FP64
 //   accumulators.
-// BH_MODE_LEARNED: BH_MODE_FP32_FAR plus the learned criterion: a node the
-//   theta test would not accept for the whole group, but which is within
-//   theta_max (side < theta_max dmin), is a candidate; the warp evaluates
-//   the network on its up-to-32 candidates at once (mma.sync, BF16) and
-//   accepts a candidate for all its lanes when the predicted log10 error is
-//   below the threshold.  Candidates whose features fall outside the
-//   training range use the theta test (the fallback), and are counted.
 // Collection (bh_learned_collect): the FP32 walk with the theta test only,
 //   recording every candidate's group, slot, lane mask and raw features.
 #include <climits>
 
-#include "bh_internal.cuh"
-#include "bh_mlp.cuh"
+#include "bh_walk.cuh"
 
 namespace bh {
 namespace {
-
-constexpr int kWarps = 4;
-constexpr int kThreads = 32 * kWarps;
-constexpr int kStack = 512;   // sibling-range entries per warp
-constexpr int kList = 96;     // staged interactions per warp
-constexpr int kSegs = 63;     // FP64 list evaluation: run slots body + thread, 0..62
-constexpr int kSlotBits = 28; // slot index bits of a stack entry (count - 1 in the top 3)
-constexpr float kMargin = 1e-5f;  // relative margin of the FP32 group tests
-constexpr float kAbsErr = 1e-6f;  // bound on FP32 coordinate error, relative to magnitudes
-constexpr int kPendFlush = 16;    // learned: run the network once this many candidates wait
-constexpr int kPendCap = 32;      // learned: deferred candidates per warp
-
-enum { kLearnNone = 0, kLearnInfer = 1, kLearnCollect = 2 };
 
 __global__ void far_mass_kernel(int64_t n, const double* __restrict__ m, const uint64_t* __restrict__ id, int nd,
                                 double* __restrict__ m_far)
@@ -113,85 +93,49 @@ __global__ void direct_extract_kernel(int64_t n, const double* __restrict__ px, 
 
 }  // namespace
 
-struct FParams {
-    int64_t n;
-    const double* px;
-    const double* py;
-    const double* pz;
-    const uint64_t* id;
-    const int32_t* body_leaf;
-    const float4* A;
-    const float4* B;
-    const uint32_t* meta;
-    const TreeRec* rec;
-    const double4_32a* d4;
-    const float* spread;
-    const double* bbox;
-    double theta2;
-    double soft2;
-    double G;
-    const double* direct;
-    const int32_t* present;
-    int nd;
-    double kick_h;
-    double* ax;
-    double* ay;
-    double* az;
-    double* vx;
-    double* vy;
-    double* vz;
-    unsigned long long* inter_count;
-    int32_t* body_count;
-    unsigned* err;
-    int64_t max_pops;
-    // learned criterion
-    const MlpDev* mlp;
-    float theta_max2;
-    float l_budget;  // per-body error budget (relative to the group's direct-term acceleration)
-    float l_band;    // analytic estimate decides outside +-l_band decades of the allowance
-    float l_frac;    // a candidate may take at most this fraction of the remaining allowance
-    unsigned long long* lstats;  // candidates, network accepts, fallbacks, analytic accepts
-    // collection
-    int32_t* c_group;
-    int32_t* c_slot;
-    uint32_t* c_mask;
-    float* c_feat;
-    float* c_ascale;
-    unsigned long long* c_count;
-    int64_t c_cap;
-};
-
 namespace {
 
-// Per-block shared memory of the walk.  Tables a variant does not use shrink
-// to one element, so that the FP32 walk fits 8 blocks (32 warps) per SM.
-template <bool kFP64, int kLearn>
-struct WalkSmem {
-    static constexpr int kW64 = kFP64 ? kWarps : 1;      // FP64-only tables
-    static constexpr bool kLL = kFP64 || kLearn == 1;     // leaf ids kept for the evaluation's own-leaf test
-    static constexpr bool kF = kLearn == 1;              // network input rows
-    int2 stack[kWarps][kStack];  // sibling ranges: {first | (count - 1) << 28, lane mask}
-    float4 lst[kFP64 ? 1 : kWarps][kFP64 ? 1 : kList];  // FP32 node data of the staged entries
-    int lst_node[kWarps][kList];
-    int lst_leaf[kLL ? kWarps : 1][kLL ? kList : 1];
-    unsigned lst_mask[kWarps][kList];
-    float side2f[kMaxDepth + 1];
-    double side2d[kMaxDepth + 1];
-    float feat[kF ? kWarps : 1][kF ? 32 : 1][9];
-    int pend_node[kF ? kWarps : 1][kF ? 32 : 1];      // learned: candidates deferred to the network
-    unsigned pend_mask[kF ? kWarps : 1][kF ? 32 : 1];
-    uint8_t plist[kW64][kFP64 ? kList : 1][32];  // FP64: each lane's own entries, in order
-    // FP64: the balanced evaluation's per-warp tables (see the flush).
-    int poff[kW64][33];                     // first pair of each lane, then the total
-    double bpos[kW64][3][kFP64 ? 32 : 1];   // the bodies' positions
-    int bleaf[kW64][kFP64 ? 32 : 1];        // the bodies' leaf ids
-    double seg[kW64][3][kFP64 ? kSegs : 1];  // each (thread, body) run's partial sums
-    uint16_t segn[kW64][kFP64 ? kSegs : 1];  // and its interaction count
-};
+// Packed FP32 pairs (two floats in one 64-bit register): one f32x2
+// instruction does two FP32 operations, each rounded as the scalar one.
+using f32x2 = unsigned long long;
+
+__device__ __forceinline__ f32x2 pk(float lo, float hi)
+{
+    f32x2 d;
+    asm("mov.b64 %0, {%1, %2};" : "=l"(d) : "f"(lo), "f"(hi));
+    return d;
+}
+
+__device__ __forceinline__ void upk(f32x2 v, float& lo, float& hi)
+{
+    asm("mov.b64 {%0, %1}, %2;" : "=f"(lo), "=f"(hi) : "l"(v));
+}
+
+__device__ __forceinline__ f32x2 sub2(f32x2 a, f32x2 b)
+{
+    f32x2 d;
+    asm("sub.rn.f32x2 %0, %1, %2;" : "=l"(d) : "l"(a), "l"(b));
+    return d;
+}
+
+__device__ __forceinline__ f32x2 mul2(f32x2 a, f32x2 b)
+{
+    f32x2 d;
+    asm("mul.rn.f32x2 %0, %1, %2;" : "=l"(d) : "l"(a), "l"(b));
+    return d;
+}
+
+__device__ __forceinline__ f32x2 fma2(f32x2 a, f32x2 b, f32x2 c)
+{
+    f32x2 d;
+    asm("fma.rn.f32x2 %0, %1, %2, %3;" : "=l"(d) : "l"(a), "l"(b), "l"(c));
+    return d;
+}
 
 template <bool kFP64, int kLearn>
-__global__ void __launch_bounds__(kThreads, kLearn == kLearnInfer ? 5 : (kFP64 ? 6 : 8)) traverse_masked_kernel(FParams p)
+__global__ void __launch_bounds__(kThreads) traverse_masked_kernel(FParams p)
 {
+    static_assert(kLearn != kLearnInfer, "the learned walk is traverse_learned_kernel");
     extern __shared__ __align__(16) unsigned char smem_raw[];
     WalkSmem<kFP64, kLearn>& sm = *reinterpret_cast<WalkSmem<kFP64, kLearn>*>(smem_raw);
     if (threadIdx.x <= kMaxDepth) {
@@ -203,7 +147,18 @@ __global__ void __launch_bounds__(kThreads, kLearn == kLearnInfer ? 5 : (kFP64 ?
         if (L < dz) L = dz;
         const double side = __ddiv_rn(L, (double)(1ull << threadIdx.x));
         sm.side2d[threadIdx.x] = __dmul_rn(side, side);
-        sm.side2f[threadIdx.x] = (float)sm.side2d[threadIdx.x];
+        const float s2f = (float)sm.side2d[threadIdx.x];
+        sm.side2f[threadIdx.x] = s2f;
+        if (!kFP64) {
+            // The FP32 walk's group-test distances: a node of this depth is
+            // accepted by every body when dmin > S+ + err and opened by
+            // every body when dmax < S- - err, S+- = side sqrt((1 +-
+            // margin) / theta^2) (theta = 0: infinite, so that nothing is
+            // accepted and all is opened).
+            const float th2f = (float)p.theta2;
+            sm.sthr[threadIdx.x] =
+                make_float2(sqrtf(s2f * (1.0f + kMargin) / th2f), sqrtf(s2f * (1.0f - kMargin) / th2f));
+        }
     }
     __syncthreads();
 
@@ -294,8 +249,6 @@ __global__ void __launch_bounds__(kThreads, kLearn == kLearnInfer ? 5 : (kFP64 ?
     // Per-walk logarithms of the learned features (base 2).
     const float lext = kLearn ? __log2f(fmaxf(gextent, 1e-30f)) : 0.0f;
     const float lascale = kLearn ? __log2f(ascale) : 0.0f;
-    unsigned long long ncand = 0, nacc = 0, nfall = 0, nana = 0;
-    float grel = kLearn == kLearnInfer ? p.l_budget : 0.0f;  // remaining per-body allowance (units of a_scale)
 
     int nlist = 0;
     int sp = 1;
@@ -304,25 +257,8 @@ __global__ void __launch_bounds__(kThreads, kLearn == kLearnInfer ? 5 : (kFP64 ?
     bool overflow = false;
     int64_t pops = 0;
 
-    int npend = 0;  // learned: deferred candidates waiting for the network
-    while (sp > 0 || nlist > 0 || npend > 0) {
-        // The learned walk defers the candidates the network must decide and
-        // evaluates them in batches: this iteration takes the deferred nodes
-        // instead of the stack's when enough wait (or nothing else is left).
-        const bool from_pend = kLearn == kLearnInfer && npend > 0 && (npend >= kPendFlush || sp == 0);
-        if (sp > 0 || from_pend) {
-            int R = 0, T = 0, f_r = 0, s_r = 0;
-            unsigned m_r = 0;
-            float plerr = 0.0f;  // network's predicted log10 error of deferred row `lane`
-            if (kLearn == kLearnInfer && from_pend) {
-                const float yrow = mlp_predict_warp(p.mlp, sm.feat[w], lane, npend);
-                plerr = yrow * p.mlp->sc.lstd + p.mlp->sc.lmean;
-                T = npend;
-                if (sp + T > kStack) {
-                    overflow = true;
-                    break;
-                }
-            } else {
+    while (sp > 0 || nlist > 0) {
+        if (sp > 0) {
             // Pop whole ranges from the top while they fit in 32 lanes.
             const int avail = sp < 32 ? sp : 32;
             int rfirst = 0, rcnt = 0;
@@ -340,19 +276,18 @@ __global__ void __launch_bounds__(kThreads, kLearn == kLearnInfer ? 5 : (kFP64 ?
                 if (lane >= off) incl += t;
             }
             const bool take = lane < avail && incl <= 32;
-            R = __popc(__ballot_sync(0xffffffffu, take));
-            T = __shfl_sync(0xffffffffu, incl, R - 1);
+            const int R = __popc(__ballot_sync(0xffffffffu, take));
+            const int T = __shfl_sync(0xffffffffu, incl, R - 1);
             const int rstart = incl - rcnt;
             const unsigned starts = __reduce_or_sync(0xffffffffu, take ? (1u << rstart) : 0u);
             const int rj = __popc(starts & ((2u << lane) - 1u)) - 1;
-            f_r = __shfl_sync(0xffffffffu, rfirst, rj);
-            s_r = __shfl_sync(0xffffffffu, rstart, rj);
-            m_r = __shfl_sync(0xffffffffu, rmask, rj);
+            const int f_r = __shfl_sync(0xffffffffu, rfirst, rj);
+            const int s_r = __shfl_sync(0xffffffffu, rstart, rj);
+            const unsigned m_r = __shfl_sync(0xffffffffu, rmask, rj);
             pops += T;
             if (sp - R + T > kStack || pops > p.max_pops) {
                 overflow = true;
                 break;
-            }
             }
             const int k = T;
             int node = -1;
@@ -362,13 +297,8 @@ __global__ void __launch_bounds__(kThreads, kLearn == kLearnInfer ? 5 : (kFP64 ?
             float dmin2 = 0.f, dmax2 = 0.f, s2 = 0.f, nerr = 0.f;
             float4 e = make_float4(0.f, 0.f, 0.f, 0.f);
             if (lane < k) {
-                if (kLearn == kLearnInfer && from_pend) {
-                    node = sm.pend_node[w][lane];
-                    M = sm.pend_mask[w][lane];
-                } else {
-                    node = f_r + (lane - s_r);
-                    M = m_r;
-                }
+                node = f_r + (lane - s_r);
+                M = m_r;
                 const float4 a = __ldg(p.A + node);
                 const float4 b = __ldg(p.B + node);
                 const uint32_t mt = __ldg(p.meta + node);
@@ -390,25 +320,37 @@ __global__ void __launch_bounds__(kThreads, kLearn == kLearnInfer ? 5 : (kFP64 ?
                     const float fz = fmaxf(fabsf(cz - bminz), fabsf(cz - bmaxz));
                     dmin2 = ex * ex + ey * ey + ez * ez;
                     dmax2 = fx * fx + fy * fy + fz * fz;
-                    s2 = sm.side2f[depth];
                     nc = (int)(mt & 0xFF);
                     // Absolute error of the FP32 group-relative distances.
                     const float err = kAbsErr * (fmaxf(fabsf(cx), fmaxf(fabsf(cy), fabsf(cz))) + bmag);
                     nerr = err;
-                    const float dlo = fmaxf(sqrtf(dmin2) - err, 0.0f), dhi = sqrtf(dmax2) + err;
-                    if (s2 * (1.0f + kMargin) < theta2f * dlo * dlo) {
-                        A = M;
-                    } else {
-                        if (kLearn) cand = !from_pend && M != 0 && dmin2 > 0.0f && s2 < p.theta_max2 * dmin2;
-                        if (s2 * (1.0f - kMargin) > theta2f * dhi * dhi) A = 0;
+                    if (kFP64) {
+                        s2 = sm.side2f[depth];
+                        const float dlo = fmaxf(sqrtf(dmin2) - err, 0.0f), dhi = sqrtf(dmax2) + err;
+                        if (s2 * (1.0f + kMargin) < theta2f * dlo * dlo) A = M;
+                        else if (s2 * (1.0f - kMargin) > theta2f * dhi * dhi) A = 0;
                         else mixed = true;
+                    } else {
+                        // The same tests squared on the distance side:
+                        // side^2 (1 + margin) < theta^2 (dmin - err)^2 and
+                        // side^2 (1 - margin) > theta^2 (dmax + err)^2, with
+                        // no square roots.
+                        if (kLearn) s2 = sm.side2f[depth];
+                        const float2 st = sm.sthr[depth];
+                        const float ta = st.x + err, to = st.y - err;
+                        if (ta * ta < dmin2) {
+                            A = M;
+                        } else {
+                            if (kLearn) cand = M != 0 && dmin2 > 0.0f && s2 < p.theta_max2 * dmin2;
+                            if (to > 0.0f && to * to > dmax2) A = 0;
+                            else mixed = true;
+                        }
                     }
                 }
             }
             __syncwarp();
             sp -= R;
-            if (kLearn == kLearnInfer) npend = from_pend ? 0 : npend;
-            if (kLearn == kLearnCollect) {
+            if (kLearn && !kFP64) {
                 const unsigned cb = __ballot_sync(0xffffffffu, cand);
                 if (cb) {
                     float f[kFeat];
@@ -434,7 +376,7 @@ __global__ void __launch_bounds__(kThreads, kLearn == kLearnInfer ? 5 : (kFP64 ?
                         f[6] = kL * (lspr - 0.5f * l2s);
                         f[7] = kL * (0.5f * __log2f(fmaxf(dcx * dcx + dcy * dcy + dcz * dcz, 1e-36f)) - ldmin);
                     }
-                    {
+                    if (kLearn == kLearnCollect) {
                         const int leader = __ffs(cb) - 1;
                         unsigned long long basec = 0;
                         if (lane == leader) basec = atomicAdd(p.c_count, (unsigned long long)__popc(cb));
@@ -450,102 +392,6 @@ __global__ void __launch_bounds__(kThreads, kLearn == kLearnInfer ? 5 : (kFP64 ?
                         }
                     }
                 }
-            }
-            if (kLearn == kLearnInfer) {
-                // Per-body budget: the group's remaining allowance grel (the
-                // smallest of its bodies' budgets, in units of a_scale) pays
-                // for every accepted candidate's error.  The analytic
-                // estimate log10(G m s^2 / (dmin^4 a_scale)) (s the spread)
-                // accepts a candidate far below the allowance and leaves one
-                // far above it to the theta test; the network predicts the
-                // error of the others, deferred and evaluated in batches.
-                // Out-of-range features: the theta test (the fallback).
-                const MlpDev* md = p.mlp;
-                const float lallow = grel > 0.0f ? __log10f(p.l_frac * grel) : -1e30f;
-                bool take = false, defer = false;
-                float lerr = 0.0f;
-                if (from_pend) {
-                    take = lane < k && M != 0 && plerr < lallow;
-                    lerr = plerr;
-                } else if (__ballot_sync(0xffffffffu, cand)) {
-                    constexpr float kL = 0.30102999566f;  // log10(2)
-                    float l2dmin = 0.0f, lspr = 0.0f, lest = 0.0f;
-                    if (cand) {
-                        l2dmin = __log2f(dmin2);
-                        lspr = __log2f(fmaxf(__ldg(p.spread + node), 1e-8f * sqrtf(s2)));
-                        lest = kL * (__log2f(e.w) - l2dmin - lascale) + 2.0f * kL * (lspr - 0.5f * l2dmin);
-                    }
-                    const bool sure = cand && lest + p.l_band < lallow;
-                    const bool band = cand && !sure && lest - p.l_band <= lallow;
-                    bool inr = false;
-                    float zq[kFeat];
-                    if (band) {
-                        // the features, as the collection computes them
-                        const float l2s = __log2f(s2);
-                        const float dcx = e.x - bcx, dcy = e.y - bcy, dcz = e.z - bcz;
-                        const float ldmin = 0.5f * l2dmin;
-                        float f[kFeat];
-                        f[0] = kL * (0.5f * l2s - ldmin);
-                        f[1] = kL * (lspr - ldmin);
-                        f[2] = kL * (lext - ldmin);
-                        f[3] = kL * (__log2f(e.w) - l2dmin - lascale);
-                        f[4] = kL * 0.5f * (__log2f(dmax2) - l2dmin);
-                        f[5] = (float)depth * (1.0f / kMaxDepth);
-                        f[6] = kL * (lspr - 0.5f * l2s);
-                        f[7] = kL * (0.5f * __log2f(fmaxf(dcx * dcx + dcy * dcy + dcz * dcz, 1e-36f)) - ldmin);
-                        inr = true;
-#pragma unroll
-                        for (int q = 0; q < kFeat; ++q) {
-                            zq[q] = (f[q] - md->sc.mean[q]) * md->sc.inv_std[q];
-                            inr = inr && zq[q] >= md->sc.lo[q] && zq[q] <= md->sc.hi[q];
-                        }
-                    }
-                    const unsigned wb = __ballot_sync(0xffffffffu, band && inr);
-                    const int slot = npend + __popc(wb & lt);
-                    defer = band && inr && slot < kPendCap;
-                    if (defer) {
-                        float (*F)[9] = sm.feat[w];
-#pragma unroll
-                        for (int q = 0; q < kFeat; ++q) F[slot][q] = fminf(fmaxf(zq[q], -64.0f), 64.0f);
-                        sm.pend_node[w][slot] = node;
-                        sm.pend_mask[w][slot] = M;
-                    }
-                    npend = min(kPendCap, npend + __popc(wb));
-                    take = sure;
-                    lerr = lest;
-                    if (cand) {
-                        ++ncand;
-                        if (band && !defer) ++nfall;  // outside the training range, or no room: theta
-                    }
-                }
-                if (__any_sync(0xffffffffu, take)) {
-                    // The accepted errors, in lane order, must fit in the
-                    // allowance: a prefix of the candidates passes.
-                    const float ec = take ? exp10f(lerr) : 0.0f;
-                    float incl = ec;
-#pragma unroll
-                    for (int off = 1; off < 32; off <<= 1) {
-                        const float t = __shfl_up_sync(0xffffffffu, incl, off);
-                        if (lane >= off) incl += t;
-                    }
-                    take = take && incl <= grel;
-                    float spent = take ? ec : 0.0f;
-#pragma unroll
-                    for (int off = 16; off > 0; off >>= 1) spent += __shfl_xor_sync(0xffffffffu, spent, off);
-                    grel -= spent;
-                }
-                if (take) {
-                    A = M;
-                    mixed = false;
-                    if (from_pend) ++nacc;
-                    else ++nana;
-                }
-                if (defer) {  // decided later, when the network has run
-                    A = 0;
-                    M = 0;
-                    mixed = false;
-                }
-                __syncwarp();
             }
             // Mixed nodes: every lane of the mask applies its own test.
             unsigned mb = __ballot_sync(0xffffffffu, mixed);
@@ -609,8 +455,14 @@ __global__ void __launch_bounds__(kThreads, kLearn == kLearnInfer ? 5 : (kFP64 ?
             const unsigned am = __ballot_sync(0xffffffffu, stage);
             if (stage) {
                 const int pos = nlist + __popc(am & lt);
-                if (!kFP64) L[pos] = e;
-                LN[pos] = node;
+                if (!kFP64) {  // entry pairs {x0, x1, y0, y1}, {z0, z1, w0, w1}
+                    float* P = reinterpret_cast<float*>(L + (pos & ~1)) + (pos & 1);
+                    P[0] = e.x;
+                    P[2] = e.y;
+                    P[4] = e.z;
+                    P[6] = e.w;
+                }
+                if (kFP64) LN[pos] = node;
                 if (WalkSmem<kFP64, kLearn>::kLL) LL[pos] = leaf ? ref : -1;  // for the own-leaf test
                 LM[pos] = A;
             }
@@ -731,24 +583,46 @@ __global__ void __launch_bounds__(kThreads, kLearn == kLearnInfer ? 5 : (kFP64 ?
                 }
                 __syncwarp();
             } else {
-                float fx = 0.f, fy = 0.f, fz = 0.f;
-                for (int j = 0; j < nlist; ++j) {
-                    const float4 q = L[j];
-                    const unsigned mj = LM[j];
-                    const bool take = (mj & me) != 0u && (kLearn == kLearnNone || LL[j] != my_leaf);
-                    const float dx = q.x - rx, dy = q.y - ry, dz = q.z - rz;
-                    const float r2 = fmaf(dx, dx, fmaf(dy, dy, fmaf(dz, dz, (float)soft2)));
-                    const float inv = rsqrtf(r2);
-                    float sc = q.w * (inv * inv * inv);
-                    if (!take) sc = 0.0f;
-                    fx = fmaf(sc, dx, fx);
-                    fy = fmaf(sc, dy, fy);
-                    fz = fmaf(sc, dz, fz);
-                    cnt += take ? 1u : 0u;
+                // Two entries per iteration in packed pairs (even, odd); an
+                // odd count is padded with a zero entry taken by no lane.
+                // Each half rounds as the scalar form; the two halves are
+                // separate partial sums, added at the end.
+                if (nlist & 1) {
+                    if (lane == 0) {
+                        float* P = reinterpret_cast<float*>(L + (nlist - 1)) + 1;
+                        P[0] = P[2] = P[4] = P[6] = 0.0f;
+                        LM[nlist] = 0u;
+                    }
+                    __syncwarp();
                 }
-                adx += (double)fx;
-                ady += (double)fy;
-                adz += (double)fz;
+                const f32x2 rx2 = pk(rx, rx), ry2 = pk(ry, ry), rz2 = pk(rz, rz);
+                const f32x2 sf2 = pk((float)soft2, (float)soft2);
+                f32x2 fx = 0ull, fy = 0ull, fz = 0ull;  // +0.0f pairs
+                for (int j = 0; j < nlist; j += 2) {
+                    const ulonglong2 xy = *reinterpret_cast<const ulonglong2*>(L + j);
+                    const ulonglong2 zw = *reinterpret_cast<const ulonglong2*>(L + j + 1);
+                    const uint2 mj = *reinterpret_cast<const uint2*>(LM + j);
+                    const f32x2 dx = sub2(xy.x, rx2), dy = sub2(xy.y, ry2), dz = sub2(zw.x, rz2);
+                    const f32x2 r2 = fma2(dx, dx, fma2(dy, dy, fma2(dz, dz, sf2)));
+                    float r0, r1;
+                    upk(r2, r0, r1);
+                    const f32x2 inv = pk(rsqrtf(r0), rsqrtf(r1));
+                    float s0, s1;
+                    upk(mul2(zw.y, mul2(mul2(inv, inv), inv)), s0, s1);
+                    const bool t0 = (mj.x & me) != 0u, t1 = (mj.y & me) != 0u;
+                    const f32x2 sc = pk(t0 ? s0 : 0.0f, t1 ? s1 : 0.0f);
+                    fx = fma2(sc, dx, fx);
+                    fy = fma2(sc, dy, fy);
+                    fz = fma2(sc, dz, fz);
+                    cnt += (t0 ? 1u : 0u) + (t1 ? 1u : 0u);
+                }
+                float fx0, fx1, fy0, fy1, fz0, fz1;
+                upk(fx, fx0, fx1);
+                upk(fy, fy0, fy1);
+                upk(fz, fz0, fz1);
+                adx += (double)(fx0 + fx1);
+                ady += (double)(fy0 + fy1);
+                adz += (double)(fz0 + fz1);
             }
             nlist = 0;
             __syncwarp();
@@ -773,21 +647,6 @@ __global__ void __launch_bounds__(kThreads, kLearn == kLearnInfer ? 5 : (kFP64 ?
 #pragma unroll
         for (int off = 16; off > 0; off >>= 1) c += __shfl_down_sync(0xffffffffu, c, off);
         if (lane == 0) atomicAdd(p.inter_count, c);
-    }
-    if (kLearn == kLearnInfer && p.lstats) {
-#pragma unroll
-        for (int off = 16; off > 0; off >>= 1) {
-            ncand += __shfl_down_sync(0xffffffffu, ncand, off);
-            nacc += __shfl_down_sync(0xffffffffu, nacc, off);
-            nfall += __shfl_down_sync(0xffffffffu, nfall, off);
-            nana += __shfl_down_sync(0xffffffffu, nana, off);
-        }
-        if (lane == 0) {
-            atomicAdd(p.lstats, ncand);
-            atomicAdd(p.lstats + 1, nacc);
-            atomicAdd(p.lstats + 2, nfall);
-            atomicAdd(p.lstats + 3, nana);
-        }
     }
 }
 
@@ -852,8 +711,6 @@ int launch_direct_extract(bh_context* ctx, double G)
     return BH_OK;
 }
 
-// Prepares the FP32 node records and the direct bodies and fills the walk's
-// parameters (kick_h and the learned/collection fields are the caller's).
 int prepare_walk(bh_context* ctx, double theta, double G, double soft2, bool fp64, FParams& p)
 {
     const int64_t n = ctx->n;
@@ -905,27 +762,6 @@ int launch_traverse_masked(bh_context* ctx, double theta, double G, double soft2
     if (rc) return rc;
     p.kick_h = kick_h;
     return fp64 ? launch_walk<true, kLearnNone>(ctx, p) : launch_walk<false, kLearnNone>(ctx, p);
-}
-
-int launch_traverse_learned(bh_context* ctx, double theta, double G, double soft2, double kick_h)
-{
-    if (ctx->n == 0) return BH_OK;
-    if (2 * ctx->n >= (int64_t(1) << kSlotBits))
-        return bh_fail(BH_ERR_CAPACITY, "masked walk: more than 2^27 bodies");
-    if (!ctx->mlp_dev) return bh_fail(BH_ERR_STATE, "learned mode: no model set (bh_learned_set_model)");
-    if (!ctx->tree_moments) return bh_fail(BH_ERR_STATE, "learned mode: the tree was built without second moments");
-    FParams p;
-    int rc = prepare_walk(ctx, theta, G, soft2, false, p);
-    if (rc) return rc;
-    p.kick_h = kick_h;
-    p.mlp = ctx->mlp_dev;
-    p.theta_max2 = (float)(ctx->learn_theta_max * ctx->learn_theta_max);
-    p.l_budget = (float)ctx->learn_budget;
-    p.l_band = (float)ctx->learn_band;
-    p.l_frac = (float)ctx->learn_frac;
-    p.lstats = ctx->lstats;
-    BH_CUDA_TRY(cudaMemsetAsync(ctx->lstats, 0, 4 * sizeof(unsigned long long), ctx->stream));
-    return launch_walk<false, kLearnInfer>(ctx, p);
 }
 
 int launch_collect(bh_context* ctx, double theta, double G, double theta_max, int32_t* c_group, int32_t* c_slot,

@@ -812,12 +812,19 @@ def run_ours(args, rank, ws, local):
     with ClockSampler(dev) as clk:
         # Untimed pre-roll of the same step, so that the sampler (which
         # starts slowly) records the clocks under this load around the
-        # timed steps, which can be shorter than one sampling period.
+        # timed steps, which can be shorter than one sampling period.  It
+        # runs for a time, not a step count, so the state is put back after
+        # it: the timed steps and the accuracy sample then see the same
+        # state however fast the pre-roll went.
+        snap, t_snap = ctx.get_bodies(), t
         t_pre = time.perf_counter() + 1.0
         while time.perf_counter() < t_pre:
             flush.fill_(1.0)
             t = ctx.step(DT, theta, G, 1, mode, t=t)
             torch.cuda.synchronize(dev)
+        ctx.set_bodies(*snap[:4])
+        ctx.set_accelerations(snap[4])
+        t = t_snap
         barrier(ws)
         l0 = ctx.launches()
         w0 = time.perf_counter()

@@ -186,3 +186,34 @@ def test_simulate_learned_mode_matches_api(bh, tmp_path):
     r = subprocess.run([str(SIMULATE), "--generate", "100", "--mode", "learned", "--vs", "none"],
                        capture_output=True, text=True, cwd=tmp_path)
     assert r.returncode == 1 and "--model" in r.stderr
+
+
+def test_step_graphs_follow_learned_parameters(bh):
+    """Steps replayed from a captured graph take a changed budget, criterion
+    and theta_max: 3 steps at one setting, then 3 at each of two others,
+    with graphs on and off, bit for bit, and the settings change the
+    interaction count.  (The analytic estimate alone decides at band 0, so
+    an untrained network suffices.)"""
+    rng = np.random.default_rng(5)
+    params = he_params(rng)
+    scale = np.concatenate([np.zeros(8, np.float32), np.ones(8, np.float32), np.full(8, -64.0, np.float32),
+                            np.full(8, 64.0, np.float32), np.array([-6.0, 2.0], np.float32)])
+    pos, vel, mass, ids = bh.generate_system(7, 20_000, 0.1, 0.05)
+    settings = ((1e-7, 3.0, 0.0), (1e-4, 3.0, 0.0), (1e-4, 1.5, 0.0))
+    runs = []
+    for graphs in (True, False):
+        with bh.Context(20_000) as c:
+            c.set_step_graphs(graphs)
+            c.set_bodies(pos, vel, mass, ids)
+            counts = []
+            for k, (budget, theta_max, band) in enumerate(settings):
+                c.learned_set_model(params, scale, budget=budget, theta_max=theta_max)
+                c.learned_set_criterion(band, 0.25)
+                c.step(DT, THETA, G, 3, bh.MODE_LEARNED, t=0.0 if k == 0 else None)
+                counts.append(c.interaction_count())
+            runs.append((c.get_bodies()[:2], counts))
+    (p_g, v_g), n_g = runs[0]
+    (p_e, v_e), n_e = runs[1]
+    assert_bits_equal(p_g, p_e, "positions"); assert_bits_equal(v_g, v_e, "velocities")
+    assert n_g == n_e
+    assert len(set(n_g)) == 3, n_g
