@@ -395,13 +395,13 @@ __global__ void __launch_bounds__(kThreads) traverse_masked_kernel(FParams p)
             }
             // Mixed nodes: every lane of the mask applies its own test.
             unsigned mb = __ballot_sync(0xffffffffu, mixed);
-            while (mb) {
-                const int j = __ffs(mb) - 1;
-                mb &= mb - 1;
-                const unsigned Mj = __shfl_sync(0xffffffffu, M, j);
-                const int dj = __shfl_sync(0xffffffffu, depth, j);
-                bool acc = false;
-                if (kFP64) {
+            if (kFP64) {
+                while (mb) {
+                    const int j = __ffs(mb) - 1;
+                    mb &= mb - 1;
+                    const unsigned Mj = __shfl_sync(0xffffffffu, M, j);
+                    const int dj = __shfl_sync(0xffffffffu, depth, j);
+                    bool acc = false;
                     // Each lane's FP64 test (the reference's rounding) decides
                     // only where the FP32 distance, with the same error
                     // allowance as the group tests, cannot.
@@ -424,15 +424,32 @@ __global__ void __launch_bounds__(kThreads) traverse_masked_kernel(FParams p)
                             __dadd_rn(__dadd_rn(__dmul_rn(dx, dx), __dmul_rn(dy, dy)), __dmul_rn(dz, dz)), soft2);
                         acc = sm.side2d[dj] < __dmul_rn(theta2, r2);
                     }
-                } else {
-                    const float cx = __shfl_sync(0xffffffffu, e.x, j);
-                    const float cy = __shfl_sync(0xffffffffu, e.y, j);
-                    const float cz = __shfl_sync(0xffffffffu, e.z, j);
-                    const float dx = cx - rx, dy = cy - ry, dz = cz - rz;
-                    acc = sm.side2f[dj] < theta2f * (dx * dx + dy * dy + dz * dz);
+                    const unsigned Aj = __ballot_sync(0xffffffffu, acc) & Mj;
+                    if (lane == j) A = Aj;
                 }
-                const unsigned Aj = __ballot_sync(0xffffffffu, acc) & Mj;
-                if (lane == j) A = Aj;
+            } else if (mb) {
+                // The mixed nodes {c, side^2} go to free entry slots past the
+                // staged list (from the first even position, which leaves the
+                // last entry pair whole; the list holds at most kList - 32
+                // entries here), and every lane tests its body against each
+                // of them, read by broadcast.  Lane q keeps the lanes that
+                // accept slot q.
+                float4* X = L + ((nlist + 1) & ~1);
+                const int nm = __popc(mb);
+                const int slot = __popc(mb & lt);
+                if (mixed) X[slot] = make_float4(e.x, e.y, e.z, sm.side2f[depth]);
+                __syncwarp();
+                unsigned res = 0;
+#pragma unroll 2
+                for (int q = 0; q < nm; ++q) {
+                    const float4 v = X[q];
+                    const float dx = v.x - rx, dy = v.y - ry, dz = v.z - rz;
+                    const unsigned bq = __ballot_sync(0xffffffffu, v.w < theta2f * (dx * dx + dy * dy + dz * dz));
+                    if (lane == q) res = bq;
+                }
+                const unsigned acc = __shfl_sync(0xffffffffu, res, slot & 31);
+                if (mixed) A = acc & M;
+                __syncwarp();
             }
             if (!kFP64 && kLearn == kLearnNone) {
                 // A body never interacts with its own leaf (traversal.cpp:70,
