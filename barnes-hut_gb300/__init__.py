@@ -43,6 +43,7 @@ MODE_PLAIN_FP64 = 0
 MODE_FP64_LIST = 1
 MODE_FP32_FAR = 2
 MODE_LEARNED = 3
+MODE_FP32_GROUP = 4
 
 STATUS = {
     0: "BH_OK", 1: "BH_ERR_INVALID_ARGUMENT", 2: "BH_ERR_CUDA", 3: "BH_ERR_OUT_OF_MEMORY",

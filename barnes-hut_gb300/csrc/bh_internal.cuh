@@ -237,6 +237,28 @@ __device__ __forceinline__ float narrow_trunc(double x)
     return __int_as_float(sign | ((e - 896) << 23) | (int)((xb >> 29) & 0x7FFFFF));
 }
 
+// narrow_trunc(x - widen(narrow_trunc(x))): the part of x below its FP32
+// truncation, itself truncated to FP32, from the bit patterns.  Where
+// narrow_trunc keeps x's exponent, x - hi is x's low 29 significand bits
+// times 2^(e - 1075), exactly; the FP64 subtraction is left for the other
+// exponents.
+__device__ __forceinline__ double widen(float f);
+__device__ __forceinline__ float low_part(double x)
+{
+    const long long xb = __double_as_longlong(x);
+    const int e = (int)((xb >> 52) & 0x7FF);
+    if (e <= 896 || e >= 1151) return narrow_trunc(x - widen(narrow_trunc(x)));
+    const unsigned low = (unsigned)(xb & 0x1FFFFFFFll);
+    if (low == 0) return 0.0f;  // x - hi = +0.0
+    const int p = 31 - __clz((int)low);  // leading bit of the remainder, 0..28
+    const int ed = e - 52 + p;           // its FP64 exponent
+    const unsigned sign = (unsigned)((unsigned long long)xb >> 63) << 31;
+    if (ed <= 896) return __int_as_float((int)sign);
+    const unsigned frac = low - (1u << p);
+    const unsigned m23 = p <= 23 ? frac << (23 - p) : frac >> (p - 23);
+    return __int_as_float((int)(sign | ((unsigned)(ed - 896) << 23) | m23));
+}
+
 __device__ __forceinline__ double widen(float f)
 {
     const int b = __float_as_int(f);
@@ -470,7 +492,8 @@ int finish(bh_context* ctx, const char* fn);
 int launch_direct_extract(bh_context* ctx, double G);
 
 int launch_traverse(bh_context* ctx, double theta, double G, double soft2, int mode, double kick_h);
-int launch_traverse_masked(bh_context* ctx, double theta, double G, double soft2, double kick_h, bool fp64);
+int launch_traverse_masked(bh_context* ctx, double theta, double G, double soft2, double kick_h, bool fp64,
+                           bool group = false);
 int launch_traverse_learned(bh_context* ctx, double theta, double G, double soft2, double kick_h);
 // FP32 node records (hi/lo centres, G m, topology) from the FP64 records.
 int launch_fp32_nodes(bh_context* ctx, double G);

@@ -28,6 +28,7 @@ __device__ inline double with_exp(uint64_t r, int e)
 // which = 2: rsqrt_hh(x) within 2 ulps of RN(1 / RN(sqrt(x)))
 // which = 3: div_exact(w, m, rcp_nr(m)) == RN(w / m)
 // which = 4: rcube_hh(x) within 4 ulps of RN(1 / RN(x RN(sqrt(x))))
+// which = 5: low_part(x) == narrow_trunc(x - widen(narrow_trunc(x)))
 __global__ void selftest_kernel(int which, int64_t n, uint64_t seed, unsigned long long* fails)
 {
     unsigned long long bad = 0;
@@ -75,6 +76,18 @@ __global__ void selftest_kernel(int which, int64_t n, uint64_t seed, unsigned lo
             const double got = bh::rcube_hh(x);
             const long long d = __double_as_longlong(want) - __double_as_longlong(got);
             bad += (d > 4 || d < -4);
+        } else if (which == 5) {
+            // either sign, exponents 2^-300 .. 2^300 (both ends of the FP32
+            // range and past them); one in 8 with the low 29 bits clear, one
+            // in 8 with only a few low bits set
+            uint64_t bits = ((uint64_t)(723 + (int)(r1 % 600)) << 52) | (r0 & 0x000FFFFFFFFFFFFFull);
+            const int kind = (int)((r2 >> 7) & 7);
+            if (kind == 0) bits &= ~0x1FFFFFFFull;
+            if (kind == 1) bits = (bits & ~0x1FFFFFFFull) | (r3 & 0xFFull);
+            if ((r2 >> 3) & 1) bits |= 1ull << 63;
+            const double x = __longlong_as_double((long long)bits);
+            const float want = bh::narrow_trunc(x - bh::widen(bh::narrow_trunc(x)));
+            bad += __float_as_int(want) != __float_as_int(bh::low_part(x));
         } else {
             const double x = with_exp(r0, -90 + (int)(r1 % 180));
             const double want = __drcp_rn(__dsqrt_rn(x));
@@ -90,7 +103,7 @@ __global__ void selftest_kernel(int which, int64_t n, uint64_t seed, unsigned lo
 
 extern "C" int bh_selftest(int which, int64_t n, uint64_t seed, int64_t* failures)
 {
-    if (which < 0 || which > 4 || n < 0 || !failures) return bh_fail(BH_ERR_INVALID_ARGUMENT, "bh_selftest: bad arguments");
+    if (which < 0 || which > 5 || n < 0 || !failures) return bh_fail(BH_ERR_INVALID_ARGUMENT, "bh_selftest: bad arguments");
     int dev = 0;
     BH_CUDA_TRY(cudaGetDevice(&dev));
     unsigned long long* d = nullptr;

@@ -312,6 +312,8 @@ int launch_traverse(bh_context* ctx, double theta, double G, double soft2, int m
         return launch_traverse_masked(ctx, theta, G, soft2, kick_h, false);
     case BH_MODE_LEARNED:
         return launch_traverse_learned(ctx, theta, G, soft2, kick_h);
+    case BH_MODE_FP32_GROUP:
+        return launch_traverse_masked(ctx, theta, G, soft2, kick_h, false, true);
     default:
         return bh_fail(BH_ERR_INVALID_ARGUMENT, "bh_compute_accelerations: mode not available");
     }

@@ -61,15 +61,11 @@ __global__ void fp32_nodes_kernel(const int32_t* __restrict__ counts, const Tree
         if (d4) d4[s] = double4_32a{r.cx, r.cy, r.cz, G * r.m};
         // hi + lo splits by truncation on the bit patterns: c - hi is exact,
         // and hi + lo represents c to about 2^-46 relative.
-        const float hx = narrow_trunc(r.cx), hy = narrow_trunc(r.cy), hz = narrow_trunc(r.cz);
-        const float lx = narrow_trunc(r.cx - widen(hx));
-        const float ly = narrow_trunc(r.cy - widen(hy));
-        const float lz = narrow_trunc(r.cz - widen(hz));
         const bool leaf = r.child < 0;
-        A[s] = make_float4(hx, hy, hz, narrow_trunc(G * r.m));
-        B[s] = make_float4(lx, ly, lz, __int_as_float(leaf ? r.leaf : r.child));
+        A[s] = make_float4(narrow_trunc(r.cx), narrow_trunc(r.cy), narrow_trunc(r.cz), narrow_trunc(G * r.m));
+        B[s] = make_float4(low_part(r.cx), low_part(r.cy), low_part(r.cz), __int_as_float(leaf ? r.leaf : r.child));
         meta[s] = (uint32_t)r.nchild | ((uint32_t)r.depth << 8) | ((leaf ? 1u : 0u) << 16) |
-                  ((r.m == 0.0 ? 1u : 0u) << 17);
+                  ((__double_as_longlong(r.m) << 1) == 0 ? 1u << 17 : 0u);
     }
 }
 
@@ -132,10 +128,11 @@ __device__ __forceinline__ f32x2 fma2(f32x2 a, f32x2 b, f32x2 c)
     return d;
 }
 
-template <bool kFP64, int kLearn>
+template <bool kFP64, int kLearn, bool kGroup = false>
 __global__ void __launch_bounds__(kThreads) traverse_masked_kernel(FParams p)
 {
     static_assert(kLearn != kLearnInfer, "the learned walk is traverse_learned_kernel");
+    static_assert(!kGroup || (!kFP64 && kLearn == kLearnNone), "the group test is an FP32 far-field walk");
     extern __shared__ __align__(16) unsigned char smem_raw[];
     WalkSmem<kFP64, kLearn>& sm = *reinterpret_cast<WalkSmem<kFP64, kLearn>*>(smem_raw);
     if (threadIdx.x <= kMaxDepth) {
@@ -215,6 +212,8 @@ __global__ void __launch_bounds__(kThreads) traverse_masked_kernel(FParams p)
 
     double adx = 0.0, ady = 0.0, adz = 0.0;
     unsigned cnt = 0;
+    // The group form's own-leaf terms (evaluated where the leaf is met).
+    float ox = 0.0f, oy = 0.0f, oz = 0.0f;
 
     // FP64 direct terms from the direct bodies first (FP32 modes): they set
     // the group's acceleration scale for the learned criterion.
@@ -448,7 +447,9 @@ __global__ void __launch_bounds__(kThreads) traverse_masked_kernel(FParams p)
                     if (lane == q) res = bq;
                 }
                 const unsigned acc = __shfl_sync(0xffffffffu, res, slot & 31);
-                if (mixed) A = acc & M;
+                // The group form accepts a mixed node only when every body
+                // of the mask does, and otherwise opens it for all of them.
+                if (mixed) A = kGroup ? ((acc & M) == M ? M : 0u) : acc & M;
                 __syncwarp();
             }
             if (!kFP64 && kLearn == kLearnNone) {
@@ -465,7 +466,27 @@ __global__ void __launch_bounds__(kThreads) traverse_masked_kernel(FParams p)
                     const int lj = __shfl_sync(0xffffffffu, ref, j);
                     const unsigned own = __ballot_sync(0xffffffffu, my_leaf == lj);
                     if (lane == j) A &= ~own;
+                    if (kGroup) {
+                        // The group form stages only entries that all its
+                        // lanes take: an own leaf is evaluated here, for the
+                        // lanes of its mask that do not belong to it.
+                        const unsigned Aj = __shfl_sync(0xffffffffu, A, j);
+                        const float cx = __shfl_sync(0xffffffffu, e.x, j);
+                        const float cy = __shfl_sync(0xffffffffu, e.y, j);
+                        const float cz = __shfl_sync(0xffffffffu, e.z, j);
+                        const float gm = __shfl_sync(0xffffffffu, e.w, j);
+                        if (Aj & me) {
+                            const float dx = cx - rx, dy = cy - ry, dz = cz - rz;
+                            const float inv = rsqrtf(fmaf(dx, dx, fmaf(dy, dy, fmaf(dz, dz, (float)soft2))));
+                            const float sc = gm * (inv * inv * inv);
+                            ox = fmaf(sc, dx, ox);
+                            oy = fmaf(sc, dy, oy);
+                            oz = fmaf(sc, dz, oz);
+                            ++cnt;
+                        }
+                    }
                 }
+                if (kGroup && own_cand) A = 0;  // evaluated above, not staged
             }
             // Stage the accepted (node, lanes) entries.
             const bool stage = A != 0;
@@ -606,8 +627,11 @@ __global__ void __launch_bounds__(kThreads) traverse_masked_kernel(FParams p)
                 // separate partial sums, added at the end.
                 if (nlist & 1) {
                     if (lane == 0) {
+                        // The pad entry: massless, and far enough away
+                        // (r^2 = 3e36) that its r^-3 is 0 in FP32.
                         float* P = reinterpret_cast<float*>(L + (nlist - 1)) + 1;
-                        P[0] = P[2] = P[4] = P[6] = 0.0f;
+                        P[0] = P[2] = P[4] = kGroup ? 1e18f : 0.0f;
+                        P[6] = 0.0f;
                         LM[nlist] = 0u;
                     }
                     __syncwarp();
@@ -615,6 +639,23 @@ __global__ void __launch_bounds__(kThreads) traverse_masked_kernel(FParams p)
                 const f32x2 rx2 = pk(rx, rx), ry2 = pk(ry, ry), rz2 = pk(rz, rz);
                 const f32x2 sf2 = pk((float)soft2, (float)soft2);
                 f32x2 fx = 0ull, fy = 0ull, fz = 0ull;  // +0.0f pairs
+                if (kGroup) {
+                    // Every staged entry is taken by every lane: no masks.
+                    for (int j = 0; j < nlist; j += 2) {
+                        const ulonglong2 xy = *reinterpret_cast<const ulonglong2*>(L + j);
+                        const ulonglong2 zw = *reinterpret_cast<const ulonglong2*>(L + j + 1);
+                        const f32x2 dx = sub2(xy.x, rx2), dy = sub2(xy.y, ry2), dz = sub2(zw.x, rz2);
+                        const f32x2 r2 = fma2(dx, dx, fma2(dy, dy, fma2(dz, dz, sf2)));
+                        float r0, r1;
+                        upk(r2, r0, r1);
+                        const f32x2 inv = pk(rsqrtf(r0), rsqrtf(r1));
+                        const f32x2 sc = mul2(zw.y, mul2(mul2(inv, inv), inv));
+                        fx = fma2(sc, dx, fx);
+                        fy = fma2(sc, dy, fy);
+                        fz = fma2(sc, dz, fz);
+                    }
+                    cnt += (unsigned)nlist;
+                } else
                 for (int j = 0; j < nlist; j += 2) {
                     const ulonglong2 xy = *reinterpret_cast<const ulonglong2*>(L + j);
                     const ulonglong2 zw = *reinterpret_cast<const ulonglong2*>(L + j + 1);
@@ -647,6 +688,11 @@ __global__ void __launch_bounds__(kThreads) traverse_masked_kernel(FParams p)
     }
     if (overflow && lane == 0) atomicOr(p.err, kErrOverflow);
     if (kLearn == kLearnCollect) return;
+    if (kGroup) {
+        adx += (double)ox;
+        ady += (double)oy;
+        adz += (double)oz;
+    }
 
     if (valid) {
         p.ax[i] = adx;
@@ -674,23 +720,23 @@ int grid_n(int64_t n)
     return (int)(b > 8 * bh::num_sms() ? 8 * bh::num_sms() : b);
 }
 
-template <bool kFP64, int kLearn>
+template <bool kFP64, int kLearn, bool kGroup = false>
 int launch_walk(bh_context* ctx, const FParams& p)
 {
     const size_t smem = sizeof(WalkSmem<kFP64, kLearn>);
-    BH_CUDA_TRY(cudaFuncSetAttribute(traverse_masked_kernel<kFP64, kLearn>,
+    BH_CUDA_TRY(cudaFuncSetAttribute(traverse_masked_kernel<kFP64, kLearn, kGroup>,
                                      cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     // The plain walks keep their working set in shared memory and L2 (L1
     // hit rates are low): shared memory takes the whole carveout, for more
     // resident blocks.  The learned walk reads the network's weights through
     // L1 and keeps the default split.
     if (kLearn == kLearnNone)
-        BH_CUDA_TRY(cudaFuncSetAttribute(traverse_masked_kernel<kFP64, kLearn>,
+        BH_CUDA_TRY(cudaFuncSetAttribute(traverse_masked_kernel<kFP64, kLearn, kGroup>,
                                          cudaFuncAttributePreferredSharedMemoryCarveout,
                                          (int)cudaSharedmemCarveoutMaxShared));
     const int64_t groups = (p.n + 31) / 32;
     const int64_t blocks = (groups + kWarps - 1) / kWarps;
-    traverse_masked_kernel<kFP64, kLearn><<<(unsigned)blocks, kThreads, smem, ctx->stream>>>(p);
+    traverse_masked_kernel<kFP64, kLearn, kGroup><<<(unsigned)blocks, kThreads, smem, ctx->stream>>>(p);
     BH_LAUNCH_CHECK(ctx);
     return BH_OK;
 }
@@ -769,7 +815,8 @@ int prepare_walk(bh_context* ctx, double theta, double G, double soft2, bool fp6
     return BH_OK;
 }
 
-int launch_traverse_masked(bh_context* ctx, double theta, double G, double soft2, double kick_h, bool fp64)
+int launch_traverse_masked(bh_context* ctx, double theta, double G, double soft2, double kick_h, bool fp64,
+                           bool group)
 {
     if (ctx->n == 0) return BH_OK;
     if (2 * ctx->n >= (int64_t(1) << kSlotBits))
@@ -778,7 +825,8 @@ int launch_traverse_masked(bh_context* ctx, double theta, double G, double soft2
     int rc = prepare_walk(ctx, theta, G, soft2, fp64, p);
     if (rc) return rc;
     p.kick_h = kick_h;
-    return fp64 ? launch_walk<true, kLearnNone>(ctx, p) : launch_walk<false, kLearnNone>(ctx, p);
+    if (fp64) return launch_walk<true, kLearnNone>(ctx, p);
+    return group ? launch_walk<false, kLearnNone, true>(ctx, p) : launch_walk<false, kLearnNone>(ctx, p);
 }
 
 int launch_collect(bh_context* ctx, double theta, double G, double theta_max, int32_t* c_group, int32_t* c_slot,

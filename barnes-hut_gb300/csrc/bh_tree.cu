@@ -37,6 +37,13 @@ namespace {
 
 constexpr int kThreads = 256;
 
+// 0.0 + v in round-to-nearest: v itself, except -0.0 -> +0.0.
+__device__ __forceinline__ double plus_zero(double v)
+{
+    const long long b = __double_as_longlong(v);
+    return __longlong_as_double(b == (long long)0x8000000000000000ull ? 0ll : b);
+}
+
 inline int grid_for(int64_t n, int threads, int max_blocks)
 {
     int64_t b = (n + threads - 1) / threads;
@@ -86,12 +93,22 @@ __global__ void leaf_sum_kernel(const int32_t* __restrict__ counts, const int32_
     for (int l = blockIdx.x * blockDim.x + threadIdx.x; l < L; l += gridDim.x * blockDim.x) {
         double sm = 0.0, sx = 0.0, sy = 0.0, sz = 0.0;
         const int b0 = leaf_first[l], b1 = leaf_first[l + 1];
-        for (int b = b0; b < b1; ++b) {
-            const double mb = m[b];
-            sm = __dadd_rn(sm, mb);
-            sx = __dadd_rn(sx, __dmul_rn(px[b], mb));
-            sy = __dadd_rn(sy, __dmul_rn(py[b], mb));
-            sz = __dadd_rn(sz, __dmul_rn(pz[b], mb));
+        if (b1 == b0 + 1) {
+            // One body: each sum is 0.0 + v, which is v except that -0.0
+            // becomes +0.0; decided on the bit patterns (no FP64 addition).
+            const double mb = m[b0];
+            sm = plus_zero(mb);
+            sx = plus_zero(__dmul_rn(px[b0], mb));
+            sy = plus_zero(__dmul_rn(py[b0], mb));
+            sz = plus_zero(__dmul_rn(pz[b0], mb));
+        } else {
+            for (int b = b0; b < b1; ++b) {
+                const double mb = m[b];
+                sm = __dadd_rn(sm, mb);
+                sx = __dadd_rn(sx, __dmul_rn(px[b], mb));
+                sy = __dadd_rn(sy, __dmul_rn(py[b], mb));
+                sz = __dadd_rn(sz, __dmul_rn(pz[b], mb));
+            }
         }
         ls[l] = double4_32a{sx, sy, sz, sm};
         cdep[l] = l == 0 ? (int8_t)-1 : (int8_t)common_depth(leaf_key[l - 1], leaf_key[l]);
@@ -156,15 +173,20 @@ __global__ void __launch_bounds__(kBT) bnd_summary_kernel(const int32_t* __restr
         }
     }
     __syncthreads();
-    if (threadIdx.x < kNT) {
-        const int t = threadIdx.x;
-        int l = -1, f = INT_MAX;
-        for (int ww = 0; ww < kBW; ++ww) {
-            l = max(l, wl[ww][t]);
-            f = min(f, wf[ww][t]);
+    // Warp t reduces threshold t over the block's warps (lane = warp).
+    static_assert(kBW == 32 && kNT <= kBW, "one lane per warp, one warp per threshold");
+    if (w < kNT) {
+        const int t = w;
+        int l = wl[lane][t], f = wf[lane][t];
+#pragma unroll
+        for (int off = 16; off > 0; off >>= 1) {
+            l = max(l, __shfl_xor_sync(0xffffffffu, l, off));
+            f = min(f, __shfl_xor_sync(0xffffffffu, f, off));
         }
-        blast[(int64_t)blockIdx.x * kNT + t] = l;
-        bfirst[(int64_t)blockIdx.x * kNT + t] = f;
+        if (lane == 0) {
+            blast[(int64_t)blockIdx.x * kNT + t] = l;
+            bfirst[(int64_t)blockIdx.x * kNT + t] = f;
+        }
     }
 }
 
@@ -254,21 +276,28 @@ __global__ void __launch_bounds__(kBT) bnd_resolve_kernel(const int32_t* __restr
     }
     __syncthreads();
     // Each warp's answer from outside it: exclusive prefix (max) and suffix
-    // (min) over the warps, started from the other blocks'.
-    if (threadIdx.x < kNT) {
-        const int t = threadIdx.x;
-        int run = bpre[(int64_t)blockIdx.x * kNT + t];
-        for (int ww = 0; ww < kBW; ++ww) {
-            const int x = wl[ww][t];
-            wl[ww][t] = run;
-            run = max(run, x);
+    // (min) over the warps, started from the other blocks'.  Warp t scans
+    // threshold t, one lane per warp of the block.
+    if (w < kNT) {
+        const int t = w;
+        int inc = wl[lane][t];
+#pragma unroll
+        for (int off = 1; off < 32; off <<= 1) {
+            const int y = __shfl_up_sync(0xffffffffu, inc, off);
+            if (lane >= off) inc = max(inc, y);
         }
-        run = bsuf[(int64_t)blockIdx.x * kNT + t];
-        for (int ww = kBW - 1; ww >= 0; --ww) {
-            const int x = wf[ww][t];
-            wf[ww][t] = run;
-            run = min(run, x);
+        int ex = __shfl_up_sync(0xffffffffu, inc, 1);
+        if (lane == 0) ex = -1;
+        wl[lane][t] = max(bpre[(int64_t)blockIdx.x * kNT + t], ex);
+        int sinc = wf[lane][t];
+#pragma unroll
+        for (int off = 1; off < 32; off <<= 1) {
+            const int y = __shfl_down_sync(0xffffffffu, sinc, off);
+            if (lane + off < 32) sinc = min(sinc, y);
         }
+        int sex = __shfl_down_sync(0xffffffffu, sinc, 1);
+        if (lane == 31) sex = INT_MAX;
+        wf[lane][t] = min(bsuf[(int64_t)blockIdx.x * kNT + t], sex);
     }
     __syncthreads();
     if (j >= cap) return;
@@ -382,20 +411,36 @@ __device__ __forceinline__ double4_32a load_sums(const double4_32a* p)
     return double4_32a{a.x, a.y, b.x, b.y};
 }
 
+// A node has at most 8 children: their slot entries are loaded together,
+// then their sums four at a time, before the additions (independent loads
+// in flight instead of a chain of dependent ones), which still run in slot
+// order.
 template <bool kMoments>
 __device__ void node_sums(int b, const int32_t* __restrict__ node_cs, const int32_t* __restrict__ node_nchild,
                           const int32_t* __restrict__ slot_ref, const double4_32a* ls, double4_32a* ns,
                           const double* lq, double* nq)
 {
-    const int s0 = node_cs[b] + 1, s1 = s0 + node_nchild[b];
+    const int s0 = node_cs[b] + 1, nc = node_nchild[b];
+    int rr[8];
+#pragma unroll
+    for (int c = 0; c < 8; ++c) rr[c] = c < nc ? slot_ref[s0 + c] : 0;
     double sm = 0.0, sx = 0.0, sy = 0.0, sz = 0.0;
-    for (int s = s0; s < s1; ++s) {
-        const int r = slot_ref[s];
-        const double4_32a v = load_sums(r >= 0 ? ls + r : ns + ~r);
-        sm = __dadd_rn(sm, v.w);
-        sx = __dadd_rn(sx, v.x);
-        sy = __dadd_rn(sy, v.y);
-        sz = __dadd_rn(sz, v.z);
+#pragma unroll
+    for (int h = 0; h < 8; h += 4) {
+        if (h >= nc) break;
+        double4_32a vv[4];
+#pragma unroll
+        for (int c = 0; c < 4; ++c)
+            if (h + c < nc) vv[c] = load_sums(rr[h + c] >= 0 ? ls + rr[h + c] : ns + ~rr[h + c]);
+#pragma unroll
+        for (int c = 0; c < 4; ++c) {
+            if (h + c < nc) {
+                sm = __dadd_rn(sm, vv[c].w);
+                sx = __dadd_rn(sx, vv[c].x);
+                sy = __dadd_rn(sy, vv[c].y);
+                sz = __dadd_rn(sz, vv[c].z);
+            }
+        }
     }
     ns[b] = double4_32a{sx, sy, sz, sm};
     if (kMoments) {
@@ -407,8 +452,8 @@ __device__ void node_sums(int b, const int32_t* __restrict__ node_cs, const int3
         if (__double_as_longlong(sm) > 0) {
             const double is = rcp_nr(sm);
             const double gx = sx * is, gy = sy * is, gz = sz * is;
-            for (int s = s0; s < s1; ++s) {
-                const int r = slot_ref[s];
+            for (int c = 0; c < nc; ++c) {
+                const int r = slot_ref[s0 + c];
                 const double4_32a v = load_sums(r >= 0 ? ls + r : ns + ~r);
                 const double cq = __ldcg(r >= 0 ? lq + r : nq + ~r);
                 if (__double_as_longlong(v.w) > 0) {
@@ -453,7 +498,7 @@ __global__ void upsweep_kernel(const int32_t* __restrict__ counts, const int32_t
 }
 
 // Depth buckets of the branching nodes (depths 0..20), three kernels:
-// per-block counts, one scan over (depth, block), per-block placement.
+// per-block counts, a scan of each depth's block counts, per-block placement.
 constexpr int kBucketThreads = 1024;
 constexpr int kDepths = kMaxDepth;  // branching depths 0..20
 
@@ -470,19 +515,21 @@ __global__ void bucket_count_kernel(const int32_t* __restrict__ counts, const ui
     if (threadIdx.x < kDepths) blk_cnt[threadIdx.x * nblk + blockIdx.x] = c[threadIdx.x];
 }
 
-__global__ void bucket_scan_kernel(int32_t* __restrict__ blk_cnt, int nblk, int32_t* __restrict__ depth_off)
+// One block per depth: the exclusive scan of that depth's per-block counts
+// (offsets within the depth's bucket) and the depth's total.
+__global__ void __launch_bounds__(kBucketThreads) bucket_scan_kernel(int32_t* __restrict__ blk_cnt, int nblk,
+                                                                      int32_t* __restrict__ depth_tot)
 {
-    // Single block: exclusive scan of kDepths*nblk counts, depth-major.
     __shared__ int32_t warp_tot[32];
-    __shared__ int32_t carry;
-    const int total = kDepths * nblk;
-    if (threadIdx.x == 0) carry = 0;
-    __syncthreads();
-    for (int base = 0; base < total; base += blockDim.x) {
+    const int d = blockIdx.x;
+    int32_t* c = blk_cnt + (int64_t)d * nblk;
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    int carry = 0;
+    for (int base = 0; base < nblk; base += kBucketThreads) {
         const int i = base + threadIdx.x;
-        const int v = i < total ? blk_cnt[i] : 0;
+        const int v = i < nblk ? c[i] : 0;
         int x = v;
-        const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+#pragma unroll
         for (int off = 1; off < 32; off <<= 1) {
             const int y = __shfl_up_sync(0xffffffffu, x, off);
             if (lane >= off) x += y;
@@ -490,7 +537,8 @@ __global__ void bucket_scan_kernel(int32_t* __restrict__ blk_cnt, int nblk, int3
         if (lane == 31) warp_tot[w] = x;
         __syncthreads();
         if (w == 0) {
-            int t = lane < (int)(blockDim.x >> 5) ? warp_tot[lane] : 0;
+            int t = warp_tot[lane];
+#pragma unroll
             for (int off = 1; off < 32; off <<= 1) {
                 const int y = __shfl_up_sync(0xffffffffu, t, off);
                 if (lane >= off) t += y;
@@ -498,30 +546,39 @@ __global__ void bucket_scan_kernel(int32_t* __restrict__ blk_cnt, int nblk, int3
             warp_tot[lane] = t;
         }
         __syncthreads();
-        const int before = (w > 0 ? warp_tot[w - 1] : 0) + carry;
-        if (i < total) {
-            blk_cnt[i] = before + x - v;
-            if (i % nblk == 0) depth_off[i / nblk] = before + x - v;
-        }
-        __syncthreads();
-        if (threadIdx.x == blockDim.x - 1) carry = before + x;
+        if (i < nblk) c[i] = carry + (w > 0 ? warp_tot[w - 1] : 0) + x - v;
+        carry += warp_tot[31];
         __syncthreads();
     }
-    if (threadIdx.x == 0) depth_off[kDepths] = carry;
+    if (threadIdx.x == 0) depth_tot[d] = carry;
 }
 
+// Each block: the depth offsets from the totals (block 0 also stores them
+// for the level launches), then its nodes into their depth buckets.
 __global__ void bucket_place_kernel(const int32_t* __restrict__ counts, const uint8_t* __restrict__ node_depth,
-                                    const int32_t* __restrict__ blk_off, int nblk, int32_t* __restrict__ depth_nodes)
+                                    const int32_t* __restrict__ blk_off, int nblk,
+                                    const int32_t* __restrict__ depth_tot, int32_t* __restrict__ depth_off,
+                                    int32_t* __restrict__ depth_nodes)
 {
     __shared__ int32_t c[kDepths];
+    __shared__ int32_t off[kDepths + 1];
     if (threadIdx.x < kDepths) c[threadIdx.x] = 0;
+    if (threadIdx.x == 0) {
+        int run = 0;
+        for (int d = 0; d < kDepths; ++d) {
+            off[d] = run;
+            run += depth_tot[d];
+        }
+        off[kDepths] = run;
+    }
     __syncthreads();
+    if (blockIdx.x == 0 && threadIdx.x <= kDepths) depth_off[threadIdx.x] = off[threadIdx.x];
     const int B = counts[1];
     const int b = blockIdx.x * kBucketThreads + threadIdx.x;
     if (b < B) {
         const int d = node_depth[b];
         const int r = atomicAdd(&c[d], 1);  // order inside a bucket is irrelevant
-        depth_nodes[blk_off[d * nblk + blockIdx.x] + r] = b;
+        depth_nodes[off[d] + blk_off[d * nblk + blockIdx.x] + r] = b;
     }
 }
 
@@ -573,9 +630,11 @@ __device__ inline void finish_com(double m, double wx, double wy, double wz, Tre
 // kernel also writes the FP32 walk's node records (hi + lo split of the
 // centre, G m and the topology word), which the walk would otherwise make in
 // a pass of its own.
+// Masses are >= 0, so "m > 0" is a test on the bit pattern.  A leaf of one
+// body takes the body's position (the quotient w/m would round it).
 __device__ inline void far_com(double m, double wx, double wy, double wz, TreeRec& r)
 {
-    if (m > 0) {
+    if (__double_as_longlong(m) > 0) {
         const double q = rcp_nr(m);
         r.cx = wx * q; r.cy = wy * q; r.cz = wz * q;
     } else {
@@ -611,7 +670,12 @@ __global__ void finalize_kernel(const int32_t* __restrict__ counts, const int32_
         const double4_32a v = r >= 0 ? ls[r] : ns[~r];
         if (r >= 0) {
             if (kFar) {
-                far_com(v.w, v.x, v.y, v.z, o);
+                const int b = leaf_first[r];
+                if (leaf_first[r + 1] == b + 1 && __double_as_longlong(v.w) > 0) {
+                    o.cx = px[b]; o.cy = py[b]; o.cz = pz[b]; o.m = v.w;
+                } else {
+                    far_com(v.w, v.x, v.y, v.z, o);
+                }
             } else {
                 const int b = leaf_first[r];
                 const bool one = leaf_first[r + 1] == b + 1;
@@ -633,15 +697,13 @@ __global__ void finalize_kernel(const int32_t* __restrict__ counts, const int32_
         }
         rec[s] = o;
         if (kFar) {  // the FP32 walk's records, as fp32_nodes_kernel makes them
-            const float hx = narrow_trunc(o.cx), hy = narrow_trunc(o.cy), hz = narrow_trunc(o.cz);
-            const float lx = narrow_trunc(o.cx - widen(hx));
-            const float ly = narrow_trunc(o.cy - widen(hy));
-            const float lz = narrow_trunc(o.cz - widen(hz));
             const bool leaf = o.child < 0;
-            far.A[s] = make_float4(hx, hy, hz, narrow_trunc(far.G * o.m));
-            far.B[s] = make_float4(lx, ly, lz, __int_as_float(leaf ? o.leaf : o.child));
+            far.A[s] = make_float4(narrow_trunc(o.cx), narrow_trunc(o.cy), narrow_trunc(o.cz),
+                                   narrow_trunc(far.G * o.m));
+            far.B[s] = make_float4(low_part(o.cx), low_part(o.cy), low_part(o.cz),
+                                   __int_as_float(leaf ? o.leaf : o.child));
             far.meta[s] = (uint32_t)o.nchild | ((uint32_t)o.depth << 8) | ((leaf ? 1u : 0u) << 16) |
-                          ((o.m == 0.0 ? 1u : 0u) << 17);
+                          ((__double_as_longlong(o.m) << 1) == 0 ? 1u << 17 : 0u);
         }
         if (kMoments) {  // a feature: FP32 after narrowing on the bit patterns
             const double m = v.w;
@@ -744,10 +806,11 @@ int launch_build(bh_context* ctx, const double* mass, bool moments, bool far_fus
         const int nblk = (int)((n + kBucketThreads - 1) / kBucketThreads);
         bucket_count_kernel<<<nblk, kBucketThreads, 0, st>>>(ctx->counts, ctx->node_depth, ctx->scan_tmp, nblk);
         BH_LAUNCH_CHECK(ctx);
-        bucket_scan_kernel<<<1, 1024, 0, st>>>(ctx->scan_tmp, nblk, ctx->depth_off);
+        int32_t* depth_tot = ctx->scan_tmp + (int64_t)kDepths * nblk;
+        bucket_scan_kernel<<<kDepths, kBucketThreads, 0, st>>>(ctx->scan_tmp, nblk, depth_tot);
         BH_LAUNCH_CHECK(ctx);
         bucket_place_kernel<<<nblk, kBucketThreads, 0, st>>>(ctx->counts, ctx->node_depth, ctx->scan_tmp, nblk,
-                                                             ctx->depth_nodes);
+                                                             depth_tot, ctx->depth_off, ctx->depth_nodes);
         BH_LAUNCH_CHECK(ctx);
         for (int d = kMaxDepth - 1; d >= 0; --d) {
             if (moments)

@@ -4,7 +4,7 @@
 //
 //   simulate -f bodies.csv --dt 1h --tend 10d --theta 1.05 [-b N] [-r]
 //            [--fc let|tree|let_direct] [--steps K] [--vs 10d|none] [-o sim_out]
-//            [--mode plain|fp64_list|fp32|learned] [--generate N --seed S] [--dump FILE]
+//            [--mode plain|fp64_list|fp32|fp32_group|learned] [--generate N --seed S] [--dump FILE]
 //            [--model FILE --budget B --theta-max T --band D --frac F]
 //
 // --tend uses the reference's loop (`for (t = 0; t < t_end; t += dt)`, so
@@ -28,7 +28,8 @@
 //
 // --mode selects the force form: plain (the reference's arithmetic, bit
 // for bit), fp64_list (the reference's interaction set in FP64), fp32 (FP32
-// far field, FP64 Sun and planet terms) or learned (fp32 with the learned
+// far field, FP64 Sun and planet terms), fp32_group (fp32 with one
+// acceptance test per warp group of 32 bodies) or learned (fp32 with the learned
 // acceptance criterion: --model names a file written by bh_mlp_save, --budget
 // is each body's relative error budget, default 1e-5; --theta-max bounds
 // the candidates, default 3; --band and --frac tune the criterion, see
@@ -117,7 +118,7 @@ int main(int argc, char** argv)
         else if (k == "-h" || k == "--help") {
             std::cout << "simulate -f FILE [--dt 1h] [--tend 1y] [--theta 1.05] [-b N] [-r] [--steps K]\n"
                          "         [--fc let|tree|let_direct] (one rank: the same step)\n"
-                         "         [--vs 10d|none] [-o sim_out] [--mode plain|fp64_list|fp32|learned]\n"
+                         "         [--vs 10d|none] [-o sim_out] [--mode plain|fp64_list|fp32|fp32_group|learned]\n"
                          "         [--model FILE --budget 1e-5 --theta-max 3 --band 0.5 --frac 0.25]\n"
                          "         [--generate N --seed S] [--dump FILE]\n";
             return 0;
@@ -133,6 +134,7 @@ int main(int argc, char** argv)
     if (mode_s == "fp64_list") mode = BH_MODE_FP64_LIST;
     else if (mode_s == "fp32") mode = BH_MODE_FP32_FAR;
     else if (mode_s == "learned") mode = BH_MODE_LEARNED;
+    else if (mode_s == "fp32_group") mode = BH_MODE_FP32_GROUP;
     else if (mode_s != "plain") die("unknown --mode " + mode_s);
     std::vector<float> params(BH_MLP_PARAMS), scale(BH_MLP_SCALE);
     if (mode == BH_MODE_LEARNED) {

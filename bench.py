@@ -77,9 +77,9 @@ FLOPS_PER_INTERACTION = 20
 L2_FLUSH_BYTES = 256 << 20
 EXTRA_BLOCKS = ("forms_4m", "learned_eval", "precision_run", "long_runs", "let_exchange", "csv_ingest")
 WORKLOAD = "plain FP64 theta=1.05, dt=1h, 300,149 bodies (Sun, 8 planets, 300,140 asteroids, 10% outer belt)"
-MODES = {"plain": 0, "fp64_list": 1, "fp32": 2, "learned": 3}
+MODES = {"plain": 0, "fp64_list": 1, "fp32": 2, "learned": 3, "fp32_group": 4}
 KERNEL = {0: "traverse_exact_kernel", 1: "traverse_masked_kernel<fp64>", 2: "traverse_masked_kernel<fp32>",
-          3: "traverse_masked_kernel<fp32, learned>"}
+          3: "traverse_learned_kernel", 4: "traverse_masked_kernel<fp32, group>"}
 
 
 def workload_name(args) -> str:
@@ -471,6 +471,7 @@ def learned_eval(args, dev, params, scale):
     n = min(args.ns_bodies, 1_000_000)
     rows = []
     cases = [(f"theta_{th:g}", bh.MODE_FP32_FAR, None, th) for th in THETA_SWEEP]
+    cases += [(f"group_theta_{th:g}", bh.MODE_FP32_GROUP, None, th) for th in THETA_SWEEP]
     cases += [(f"budget_{b:g}", bh.MODE_LEARNED, b, THETA) for b in LEARNED_BUDGETS]
     with bh.Context(n, dev) as ctx:
         ext = torch.cuda.ExternalStream(ctx.stream(), device=dev)
@@ -506,7 +507,7 @@ def _against_theta(rows):
     at equal or lower median error, and the time ratio (above 1: the learned
     form is faster)."""
     out = {}
-    thetas = {k: r for k, r in rows.items() if k.startswith("theta_")}
+    thetas = {k: r for k, r in rows.items() if k.startswith(("theta_", "group_theta_"))}
     for k, r in rows.items():
         if not k.startswith("budget_"):
             continue
@@ -546,6 +547,7 @@ def forms_4m(args, dev, params, scale, info):
         rows = {}
         cases = [("plain_fp64", bh.MODE_FP64_LIST, None, THETA)]
         cases += [(f"theta_{th:g}", bh.MODE_FP32_FAR, None, th) for th in THETA_SWEEP]
+        cases += [(f"group_theta_{th:g}", bh.MODE_FP32_GROUP, None, th) for th in THETA_SWEEP]
         cases += [(f"budget_{b:g}", bh.MODE_LEARNED, b, THETA) for b in LEARNED_BUDGETS]
         for name, mode, budget, theta in cases:
             if budget is not None:
@@ -573,13 +575,14 @@ def forms_4m(args, dev, params, scale, info):
             ph = {k: v / 2 for k, v in phases.items()}
             row.update({"ms_per_step": ms, "body_steps_per_s": n / (ms * 1e-3), "interactions_per_body": ipb,
                         "phases_ms_per_step": ph})
-            if mode == bh.MODE_FP32_FAR and theta == THETA:
+            if mode in (bh.MODE_FP32_FAR, bh.MODE_FP32_GROUP) and theta == THETA:
                 achieved = ipb * n * FLOPS_PER_INTERACTION / (ph["forces"] * 1e-3) / 1e12
+                key = "fp32" if mode == bh.MODE_FP32_FAR else "fp32_group"
                 row["roofline"] = {"kernel": KERNEL[mode], "bound": "fp32", "achieved": achieved, "peak": peak32,
                                    "unit": "TFLOP/s", "frac": achieved / peak32,
                                    "peak_source": "measured in-process: FP32 FMA chains (bh_measure_fma_peak)",
                                    "work": f"{FLOPS_PER_INTERACTION} flops x {ipb * n:.4g} interactions per launch",
-                                   "traffic": TRAFFIC_BYTES.get(("fp32", n)), "traffic_unit": "bytes per launch (ncu)"}
+                                   "traffic": TRAFFIC_BYTES.get((key, n)), "traffic_unit": "bytes per launch (ncu)"}
             rows[name] = row
         out["hbm_phases"] = hbm_phases(rows[f"theta_{THETA:g}"]["phases_ms_per_step"], n)
     out["forms"] = rows
@@ -592,9 +595,21 @@ def forms_4m(args, dev, params, scale, info):
           "plain_fp64": {k: base[k] for k in ("ms_per_step", "body_steps_per_s", "median_rel_err")},
           "fp32_theta_1.05": {k: rows[f"theta_{THETA:g}"][k] for k in ("ms_per_step", "body_steps_per_s",
                                                                         "median_rel_err")},
+          "fp32_group_theta_1.05": {k: rows[f"group_theta_{THETA:g}"][k]
+                                    for k in ("ms_per_step", "body_steps_per_s", "median_rel_err")},
           "fp32_learned": None, "learned_vs_plain_fp64": None, "best_theta_fp32": None,
           "learned_vs_best_theta": None,
-          "roofline_fp32_walk": rows[f"theta_{THETA:g}"].get("roofline")}
+          "roofline_fp32_walk": rows[f"theta_{THETA:g}"].get("roofline"),
+          "roofline_fp32_group_walk": rows[f"group_theta_{THETA:g}"].get("roofline")}
+    # The fastest network-free FP32 run at an error no higher than the plain
+    # FP64 form's, and its ratio to it.
+    free = [k for k in rows if k.startswith(("theta_", "group_theta_"))
+            and rows[k]["median_rel_err"] <= base["median_rel_err"]]
+    if free:
+        f = max(free, key=lambda k: rows[k]["body_steps_per_s"])
+        ns["fastest_fp32_without_network"] = {"form": f, "ms_per_step": rows[f]["ms_per_step"],
+                                              "median_rel_err": rows[f]["median_rel_err"],
+                                              "vs_plain_fp64": rows[f]["body_steps_per_s"] / base["body_steps_per_s"]}
     if best:
         r = rows[best]
         ns["fp32_learned"] = {"budget": r["budget"], "ms_per_step": r["ms_per_step"],

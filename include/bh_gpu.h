@@ -67,7 +67,16 @@ enum bh_mode {
     BH_MODE_FP32_FAR = 2,
     /* BH_MODE_FP32_FAR with the learned acceptance criterion (see
      * bh_learned_*).  No reference counterpart. */
-    BH_MODE_LEARNED = 3
+    BH_MODE_LEARNED = 3,
+    /* BH_MODE_FP32_FAR with one acceptance decision per warp group of 32
+     * Morton-consecutive bodies: a node is accepted for the whole group when
+     * every body's own theta test (src/traversal.cpp:78) accepts it, and
+     * opened for the whole group otherwise.  Each body's interaction set is
+     * then at least as fine as its own test at the same theta gives (more
+     * accurate, more interactions per body), and every staged node is
+     * evaluated for all the warp's lanes, none masked.  No reference
+     * counterpart. */
+    BH_MODE_FP32_GROUP = 4
 };
 
 #define BH_MAX_DEPTH 21   /* reference MAX_L / MAX_DEPTH (traversal.cpp:28) */
@@ -273,8 +282,10 @@ int bh_invariants(bh_context *ctx, double G, double theta, double out[9]);
  * reciprocal square root against RN(1 / RN(sqrt x)) (more than 2 ulps
  * apart counts); 3: the division-free centre-of-mass quotient against
  * RN(w / m); 4: the fused r^-3 of the FP64 list form and the direct terms
- * against RN(1 / RN(x RN(sqrt x))) (more than 4 ulps apart counts).  No
- * reference counterpart. */
+ * against RN(1 / RN(x RN(sqrt x))) (more than 4 ulps apart counts); 5: the
+ * FP32 walk's low part of a centre-of-mass coordinate, formed from the bit
+ * patterns, against the FP64 subtraction it replaces.  No reference
+ * counterpart. */
 int bh_selftest(int which, int64_t n, uint64_t seed, int64_t *failures);
 
 /* ---- learned acceptance (no reference counterpart) ------------------- */

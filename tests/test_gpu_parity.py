@@ -300,7 +300,7 @@ def test_fp64_list_mode_300k_counts(bh, ctx, port):
 
 
 @pytest.mark.parametrize("which,n", [(0, 50_000_000), (1, 50_000_000), (2, 20_000_000), (3, 50_000_000),
-                                     (4, 20_000_000)])
+                                     (4, 20_000_000), (5, 50_000_000)])
 def test_division_free_helpers_match_ieee(bh, which, n):
     """The helpers that replace IEEE divisions (single-rank merge quotient and
     one-body centre of mass; key quantisation; the general centre-of-mass
@@ -308,7 +308,8 @@ def test_division_free_helpers_match_ieee(bh, which, n):
     square root is within 2 ulps of RN(1/RN(sqrt x)) and the fused r^-3 of
     the FP64 list form within 4 ulps of RN(1/RN(x RN(sqrt x))), on 5e7 / 2e7
     seeded inputs including powers of two, largest mantissas and points
-    within 2^-30 of a key cell boundary."""
+    within 2^-30 of a key cell boundary; the FP32 records' low parts
+    formed on the bit patterns equal the FP64 subtraction's."""
     assert bh.selftest(which, n, seed=12345) == 0
 
 

@@ -92,6 +92,48 @@ def test_fp32_far_interaction_set_tracks_per_body_theta(bh, system, port):
     assert abs(c32.sum() / c64.sum() - 1) < 0.15
 
 
+@pytest.mark.parametrize("theta", [0.8, 1.05, 1.6])
+def test_fp32_group_refines_each_bodys_own_set(bh, system, theta):
+    """BH_MODE_FP32_GROUP accepts a node for the whole warp group only when
+    every body's own test accepts it: each body's interaction set is then
+    its own set or a refinement of it, so its count is never lower than in
+    BH_MODE_FP32_FAR at the same theta, and its error against the FP64
+    direct sum is no higher in the median (tolerance: FP32 rounding, 2e-8)."""
+    ctx, sample, ref = system
+    a_b = ctx.compute_accelerations(theta, G, 0.0, bh.MODE_FP32_FAR)
+    c_b = ctx.interaction_counts().astype(np.int64)
+    a_g = ctx.compute_accelerations(theta, G, 0.0, bh.MODE_FP32_GROUP)
+    c_g = ctx.interaction_counts().astype(np.int64)
+    assert np.all(np.isfinite(a_g))
+    assert np.all(c_g >= c_b)
+    assert c_g.sum() > c_b.sum()
+    assert ctx.interaction_count() == c_g.sum()
+    e_b, e_g = rel_err(a_b[sample], ref), rel_err(a_g[sample], ref)
+    assert np.median(e_g) <= np.median(e_b) + 2e-8
+    assert np.median(e_g) <= 1e-5
+
+
+def test_fp32_group_steps_match_single_launches(bh):
+    """The group form through bh_step (graph replays) equals the kernels
+    launched one by one, and its trajectory stays with the FP64 form's."""
+    pos, vel, mass, ids = bh.generate_system(13, 20_000, 0.1, 0.05)
+    out = {}
+    for graphs in (True, False):
+        with bh.Context(len(mass)) as c:
+            c.set_step_graphs(graphs)
+            c.set_bodies(pos, vel, mass, ids)
+            c.step(DT, THETA, G, nsteps=6, mode=bh.MODE_FP32_GROUP, t=0.0)
+            out[graphs] = c.get_bodies()
+    for a, b in zip(out[True], out[False]):
+        assert np.array_equal(a, b)
+    with bh.Context(len(mass)) as c:
+        c.set_bodies(pos, vel, mass, ids)
+        c.step(DT, THETA, G, nsteps=6, mode=bh.MODE_PLAIN_FP64, t=0.0)
+        p64, _, _, i64, _ = c.get_bodies()
+    p, _, _, i, _ = out[True]
+    assert np.abs(p[np.argsort(i)] - p64[np.argsort(i64)]).max() < 1e-10
+
+
 def test_second_moment_spread_matches_fp64(bh):
     """The second-moment pass (learned features): per device node,
     sqrt(Q/m) of the far-field masses, Q = sum m |x - com|^2 over the
