@@ -91,43 +91,6 @@ __global__ void direct_extract_kernel(int64_t n, const double* __restrict__ px, 
 
 namespace {
 
-// Packed FP32 pairs (two floats in one 64-bit register): one f32x2
-// instruction does two FP32 operations, each rounded as the scalar one.
-using f32x2 = unsigned long long;
-
-__device__ __forceinline__ f32x2 pk(float lo, float hi)
-{
-    f32x2 d;
-    asm("mov.b64 %0, {%1, %2};" : "=l"(d) : "f"(lo), "f"(hi));
-    return d;
-}
-
-__device__ __forceinline__ void upk(f32x2 v, float& lo, float& hi)
-{
-    asm("mov.b64 {%0, %1}, %2;" : "=f"(lo), "=f"(hi) : "l"(v));
-}
-
-__device__ __forceinline__ f32x2 sub2(f32x2 a, f32x2 b)
-{
-    f32x2 d;
-    asm("sub.rn.f32x2 %0, %1, %2;" : "=l"(d) : "l"(a), "l"(b));
-    return d;
-}
-
-__device__ __forceinline__ f32x2 mul2(f32x2 a, f32x2 b)
-{
-    f32x2 d;
-    asm("mul.rn.f32x2 %0, %1, %2;" : "=l"(d) : "l"(a), "l"(b));
-    return d;
-}
-
-__device__ __forceinline__ f32x2 fma2(f32x2 a, f32x2 b, f32x2 c)
-{
-    f32x2 d;
-    asm("fma.rn.f32x2 %0, %1, %2, %3;" : "=l"(d) : "l"(a), "l"(b), "l"(c));
-    return d;
-}
-
 template <bool kFP64, int kLearn, bool kGroup = false>
 __global__ void __launch_bounds__(kThreads) traverse_masked_kernel(FParams p)
 {
@@ -167,12 +130,14 @@ __global__ void __launch_bounds__(kThreads) traverse_masked_kernel(FParams p)
     const bool valid = i < p.n;
     const int64_t ii = valid ? i : base;  // idle lanes shadow the group's first body
     const double x = p.px[ii], y = p.py[ii], z = p.pz[ii];
-    const float gx = __double2float_rn(__shfl_sync(0xffffffffu, x, 0));
-    const float gy = __double2float_rn(__shfl_sync(0xffffffffu, y, 0));
-    const float gz = __double2float_rn(__shfl_sync(0xffffffffu, z, 0));
-    const float rx = __double2float_rn(x - (double)gx);
-    const float ry = __double2float_rn(y - (double)gy);
-    const float rz = __double2float_rn(z - (double)gz);
+    // The group centre g: the first body's position truncated to FP32 on the
+    // bit patterns (any float near the group serves).
+    const float gx = narrow_trunc(__shfl_sync(0xffffffffu, x, 0));
+    const float gy = narrow_trunc(__shfl_sync(0xffffffffu, y, 0));
+    const float gz = narrow_trunc(__shfl_sync(0xffffffffu, z, 0));
+    const float rx = __double2float_rn(x - widen(gx));
+    const float ry = __double2float_rn(y - widen(gy));
+    const float rz = __double2float_rn(z - widen(gz));
     float bminx = rx, bminy = ry, bminz = rz, bmaxx = rx, bmaxy = ry, bmaxz = rz;
 #pragma unroll
     for (int off = 16; off > 0; off >>= 1) {
@@ -678,9 +643,12 @@ __global__ void __launch_bounds__(kThreads) traverse_masked_kernel(FParams p)
                 upk(fx, fx0, fx1);
                 upk(fy, fy0, fy1);
                 upk(fz, fz0, fz1);
-                adx += (double)(fx0 + fx1);
-                ady += (double)(fy0 + fy1);
-                adz += (double)(fz0 + fz1);
+                // widen(): the exact conversion on the bit patterns (the
+                // conversion instruction runs on the FP64 pipe, which the
+                // direct terms already load)
+                adx += widen(fx0 + fx1);
+                ady += widen(fy0 + fy1);
+                adz += widen(fz0 + fz1);
             }
             nlist = 0;
             __syncwarp();
@@ -689,9 +657,9 @@ __global__ void __launch_bounds__(kThreads) traverse_masked_kernel(FParams p)
     if (overflow && lane == 0) atomicOr(p.err, kErrOverflow);
     if (kLearn == kLearnCollect) return;
     if (kGroup) {
-        adx += (double)ox;
-        ady += (double)oy;
-        adz += (double)oz;
+        adx += widen(ox);
+        ady += widen(oy);
+        adz += widen(oz);
     }
 
     if (valid) {
