@@ -117,9 +117,6 @@ void layout(bh_context* ctx, Carver& c)
     ctx->slot_top = c.take<uint8_t>(2 * n);
     ctx->depth_off = c.take<int32_t>(32);
     ctx->depth_nodes = c.take<int32_t>(n);
-    ctx->leaf_parent = c.take<int32_t>(n);
-    ctx->node_parent = c.take<int32_t>(n);
-    ctx->node_ctr = c.take<unsigned>(n);
     ctx->rec = c.take<bh::TreeRec>(2 * n);
     ctx->counts = c.take<int32_t>(16);
     const int64_t nblk = (n + 1023) / 1024;

@@ -380,9 +380,6 @@ struct bh_context {
     uint8_t* slot_top = nullptr;
     int32_t* depth_off = nullptr;   // 23 offsets into depth_nodes (by depth)
     int32_t* depth_nodes = nullptr; // node ids bucketed by depth
-    int32_t* leaf_parent = nullptr; // branching node holding each leaf (-1: the root)
-    int32_t* node_parent = nullptr; // branching node holding each branching node (-1: the root)
-    unsigned* node_ctr = nullptr;   // children summed so far (bottom-up pass)
     bh::TreeRec* rec = nullptr;     // traversal records, slot 0 = root
     int32_t* counts = nullptr;      // device scalars: [0]=L, [1]=B, [2]=slots
     int32_t* scan_tmp = nullptr;    // block sums of the device scans

@@ -363,7 +363,6 @@ __global__ void node_place_kernel(const int32_t* __restrict__ counts, const int8
                                   const uint8_t* __restrict__ node_depth, const int32_t* __restrict__ node_cs,
                                   const int32_t* __restrict__ split_node, const int8_t* __restrict__ split_rank,
                                   int32_t* __restrict__ slot_ref, uint8_t* __restrict__ slot_top,
-                                  int32_t* __restrict__ leaf_parent, int32_t* __restrict__ node_parent,
                                   unsigned* __restrict__ err)
 {
     const int L = counts[0], B = counts[1], S = counts[2];
@@ -395,15 +394,13 @@ __global__ void node_place_kernel(const int32_t* __restrict__ counts, const int8
         }
         slot_ref[s] = ref;
         slot_top[s] = (uint8_t)top;
-        if (ref >= 0) leaf_parent[ref] = P;
-        else node_parent[~ref] = P;
     }
 }
 
 // One node's sums from its children, in slot (= octant) order from 0.0
 // (linear_octree.cpp:69-87), and with kMoments the second moment by the
-// parallel-axis rule (see below).  Children may have been written by other
-// threads of this launch: loads bypass L1.
+// parallel-axis rule (see below).  The children's sums were written by the
+// previous level's launch; loads bypass L1.
 __device__ __forceinline__ double4_32a load_sums(const double4_32a* p)
 {
     const double2 a = __ldcg(reinterpret_cast<const double2*>(p));
@@ -464,36 +461,6 @@ __device__ void node_sums(int b, const int32_t* __restrict__ node_cs, const int3
             }
         }
         nq[b] = q;
-    }
-}
-
-constexpr int64_t kUpsweepMaxBodies = 1000000;
-
-// Bottom-up sums without levels: one thread per leaf climbs towards the
-// root; at each node the thread whose arrival completes the node's children
-// (an atomic count) computes the node, the others stop.  No thread waits:
-// each node is computed exactly once, after all its children.  A thread's
-// writes are fenced before its arrival is counted.
-template <bool kMoments>
-__global__ void upsweep_kernel(const int32_t* __restrict__ counts, const int32_t* __restrict__ leaf_parent,
-                               const int32_t* __restrict__ node_parent, const int32_t* __restrict__ node_cs,
-                               const int32_t* __restrict__ node_nchild, const int32_t* __restrict__ slot_ref,
-                               const double4_32a* ls, double4_32a* ns, const double* lq, double* nq,
-                               unsigned* __restrict__ ctr)
-{
-    const int L = counts[0];
-    for (int l = blockIdx.x * blockDim.x + threadIdx.x; l < L; l += gridDim.x * blockDim.x) {
-        int b = leaf_parent[l];
-        bool wrote = false;  // the leaf's sums come from an earlier launch
-        while (b >= 0) {
-            if (wrote) __threadfence();
-            const unsigned arrived = atomicAdd(ctr + b, 1u);
-            if (arrived + 1u != (unsigned)node_nchild[b]) break;
-            __threadfence();
-            node_sums<kMoments>(b, node_cs, node_nchild, slot_ref, ls, ns, lq, nq);
-            wrote = true;
-            b = node_parent[b];
-        }
     }
 }
 
@@ -782,27 +749,13 @@ int launch_build(bh_context* ctx, const double* mass, bool moments, bool far_fus
     BH_LAUNCH_CHECK(ctx);
     node_place_kernel<<<grid_for(2 * n, kThreads, maxb), kThreads, 0, st>>>(
         ctx->counts, ctx->cdep, ctx->node_a, ctx->node_e, ctx->node_depth, ctx->node_cs, ctx->split_node,
-        ctx->split_rank, ctx->slot_ref, ctx->slot_top, ctx->leaf_parent, ctx->node_parent, ctx->err);
+        ctx->split_rank, ctx->slot_ref, ctx->slot_top, ctx->err);
     BH_LAUNCH_CHECK(ctx);
 
-    // 3./4. monopoles (and second moments), deepest first.  Below a
-    // million bodies one launch climbs from the leaves (launch overheads
-    // dominate there); above, the level-synchronous pass keeps more loads in
-    // flight.  Both sum each node's children in slot order from 0.0.
-    if (n < kUpsweepMaxBodies) {
-        BH_CUDA_TRY(cudaMemsetAsync(ctx->node_ctr, 0, sizeof(unsigned) * (size_t)n, st));
-        if (moments)
-            upsweep_kernel<true><<<g, kThreads, 0, st>>>(ctx->counts, ctx->leaf_parent, ctx->node_parent,
-                                                         ctx->node_cs, ctx->node_nchild, ctx->slot_ref,
-                                                         ctx->leaf_s, ctx->node_s, ctx->leaf_q, ctx->node_q,
-                                                         ctx->node_ctr);
-        else
-            upsweep_kernel<false><<<g, kThreads, 0, st>>>(ctx->counts, ctx->leaf_parent, ctx->node_parent,
-                                                          ctx->node_cs, ctx->node_nchild, ctx->slot_ref,
-                                                          ctx->leaf_s, ctx->node_s, ctx->leaf_q, ctx->node_q,
-                                                          ctx->node_ctr);
-        BH_LAUNCH_CHECK(ctx);
-    } else {
+    // 3./4. monopoles (and second moments), level by level, deepest first:
+    // depth buckets of the branching nodes, then one launch per depth; each
+    // node sums its children in slot order from 0.0.  No atomics.
+    {
         const int nblk = (int)((n + kBucketThreads - 1) / kBucketThreads);
         bucket_count_kernel<<<nblk, kBucketThreads, 0, st>>>(ctx->counts, ctx->node_depth, ctx->scan_tmp, nblk);
         BH_LAUNCH_CHECK(ctx);

@@ -152,10 +152,9 @@ def test_300k_against_oracle(bh, ctx, port):
 
 
 def test_level_build_path_against_oracle(bh, port):
-    """A million bodies (trojans included) build through the level-by-level
-    monopole pass (smaller sets climb in one launch, which the tests above
-    cover): the tree, with and without the merge, and the second moments'
-    tree bit for bit and to 1e-12 against the oracle's sums."""
+    """A million bodies (trojans included) through the level-by-level
+    monopole pass that every size uses: the tree, with and without the
+    merge, bit for bit against the oracle's."""
     n = 1_000_000
     pos, vel, mass, ids = bh.generate_system(41, n, 0.1, 0.05)
     bb = port.bbox(pos)
