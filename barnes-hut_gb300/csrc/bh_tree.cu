@@ -138,12 +138,12 @@ __global__ void leaf_sum_kernel(const int32_t* __restrict__ counts, const int32_
 // octants), and the first of them represents it (j is first exactly when
 // max{k < j : d(k) <= d(j)} is pl(j)).  next(j) = min{k > j : d(k) <= d(j)}
 // is j's next split when d(next(j)) = d(j).  These nearest-value queries are
-// answered from ballots: for each of the 22 thresholds t (d <= t - 1,
-// t = 0..21) a warp's ballot marks its positions at or below t - 1; a query
-// looks in its own warp's mask first, then in the other warps of its block
-// (prefix / suffix over the warps' extreme positions), then in the other
-// blocks (prefix / suffix over the blocks' extreme positions, from a pass over
-// block summaries).  No searches and no atomics.
+// answered per warp, block and grid: a query looks inside its own warp first
+// (the lanes below its depth, from ballots on the depth's bits), then in the
+// other warps of its block (prefix / suffix over the warps' last and first
+// positions below each of the 22 thresholds t, d <= t - 1, t = 0..21), then
+// in the other blocks (prefix / suffix over the blocks' extreme positions,
+// from a pass over block summaries).  No searches and no atomics.
 constexpr int kNT = kMaxDepth + 1;  // thresholds t: d <= t - 1
 constexpr int kBT = 1024;           // boundary positions per block
 constexpr int kBW = kBT / 32;
@@ -153,25 +153,49 @@ __device__ __forceinline__ int bnd_depth(const int8_t* __restrict__ cdep, int L,
     return j <= L ? (int)cdep[j] : 127;  // cdep[0] = cdep[L] = -1; past L: no threshold
 }
 
+// A warp's last and first position below each threshold t (v < t, i.e.
+// d <= t - 1), into wl[t] and wf[t] (-1 / INT_MAX where none is): lane l is
+// the last below t exactly for t in (v_l, min of the later lanes' v], and
+// the first for t in (v_l, min of the earlier lanes' v]; thresholds up to
+// the warp's minimum have neither.  Two min-scans and a short loop per lane
+// instead of one ballot per threshold.
+__device__ __forceinline__ void warp_threshold_ends(int v, int lane, int wbase, int* wl, int* wf)
+{
+    int suf = v, pre = v;
+#pragma unroll
+    for (int off = 1; off < 32; off <<= 1) {
+        const int y = __shfl_down_sync(0xffffffffu, suf, off);
+        if (lane + off < 32) suf = min(suf, y);
+        const int z = __shfl_up_sync(0xffffffffu, pre, off);
+        if (lane >= off) pre = min(pre, z);
+    }
+    int s_next = __shfl_down_sync(0xffffffffu, suf, 1);
+    if (lane == 31) s_next = 127;
+    int p_prev = __shfl_up_sync(0xffffffffu, pre, 1);
+    if (lane == 0) p_prev = 127;
+    const int wmin = __shfl_sync(0xffffffffu, pre, 31);
+    if (lane < kNT && lane <= wmin) {
+        wl[lane] = -1;
+        wf[lane] = INT_MAX;
+    }
+    const int lo = v + 1;  // v >= -1
+    for (int t = lo; t <= min(s_next, kNT - 1); ++t) wl[t] = wbase + lane;
+    for (int t = lo; t <= min(p_prev, kNT - 1); ++t) wf[t] = wbase + lane;
+}
+
 // Per block: for every threshold the last and the first position at or below it.
 __global__ void __launch_bounds__(kBT) bnd_summary_kernel(const int32_t* __restrict__ counts,
                                                           const int8_t* __restrict__ cdep,
                                                           int32_t* __restrict__ blast, int32_t* __restrict__ bfirst)
 {
+    static_assert(kNT <= 32, "one lane per threshold");
     __shared__ int wl[kBW][kNT], wf[kBW][kNT];
     const int L = counts[0];
     const int64_t j = (int64_t)blockIdx.x * kBT + threadIdx.x;
     const int v = bnd_depth(cdep, L, j);
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
     const int wbase = (int)(j - lane);
-#pragma unroll
-    for (int t = 0; t < kNT; ++t) {
-        const unsigned m = __ballot_sync(0xffffffffu, v <= t - 1);
-        if (lane == t) {
-            wl[w][t] = m ? wbase + 31 - __clz(m) : -1;
-            wf[w][t] = m ? wbase + __ffs(m) - 1 : INT_MAX;
-        }
-    }
+    warp_threshold_ends(v, lane, wbase, wl[w], wf[w]);
     __syncthreads();
     // Warp t reduces threshold t over the block's warps (lane = warp).
     static_assert(kBW == 32 && kNT <= kBW, "one lane per warp, one warp per threshold");
@@ -258,22 +282,30 @@ __global__ void __launch_bounds__(kBT) bnd_resolve_kernel(const int32_t* __restr
                                                           int32_t* __restrict__ pl, int32_t* __restrict__ pr,
                                                           int32_t* __restrict__ nxt, int64_t cap)
 {
-    __shared__ unsigned wm[kBW][kNT];
     __shared__ int wl[kBW][kNT], wf[kBW][kNT];
     const int L = counts[0];
     const int64_t j = (int64_t)blockIdx.x * kBT + threadIdx.x;
     const int v = bnd_depth(cdep, L, j);
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
     const int wbase = (int)(j - lane);
+    warp_threshold_ends(v, lane, wbase, wl[w], wf[w]);
+    // Inside the warp: the lanes whose depth is below this lane's (LT) and
+    // at or below it (LE), from five ballots on the bits of v + 1 (past the
+    // end, v = 127, counts as 30: above every depth).
+    const int vq = min(v, 30) + 1;
+    unsigned lt_m = 0u, eq_m = 0xffffffffu;
 #pragma unroll
-    for (int t = 0; t < kNT; ++t) {
-        const unsigned m = __ballot_sync(0xffffffffu, v <= t - 1);
-        if (lane == t) {
-            wm[w][t] = m;
-            wl[w][t] = m ? wbase + 31 - __clz(m) : -1;
-            wf[w][t] = m ? wbase + __ffs(m) - 1 : INT_MAX;
+    for (int k = 4; k >= 0; --k) {
+        const bool bit = (vq >> k) & 1;
+        const unsigned b = __ballot_sync(0xffffffffu, bit);
+        if (bit) {
+            lt_m |= eq_m & ~b;
+            eq_m &= b;
+        } else {
+            eq_m &= ~b;
         }
     }
+    const unsigned le_m = lt_m | eq_m;
     __syncthreads();
     // Each warp's answer from outside it: exclusive prefix (max) and suffix
     // (min) over the warps, started from the other blocks'.  Warp t scans
@@ -304,19 +336,19 @@ __global__ void __launch_bounds__(kBT) bnd_resolve_kernel(const int32_t* __restr
     int f = 0;
     if (j >= 1 && j < L) {
         const unsigned below = (1u << lane) - 1u, above = ~below & ~(1u << lane);
-        auto prev = [&](int t) {
-            const unsigned m = wm[w][t] & below;
+        auto prev = [&](unsigned mask, int t) {
+            const unsigned m = mask & below;
             return m ? wbase + 31 - __clz(m) : wl[w][t];
         };
-        auto next = [&](int t) {
-            const unsigned m = wm[w][t] & above;
+        auto next = [&](unsigned mask, int t) {
+            const unsigned m = mask & above;
             return m ? wbase + __ffs(m) - 1 : wf[w][t];
         };
-        const int PL = prev(v), PLE = prev(v + 1);
+        const int PL = prev(lt_m, v), PLE = prev(le_m, v + 1);
         f = PLE == PL ? 1 : 0;
         pl[j] = PL;
-        pr[j] = next(v);
-        nxt[j] = next(v + 1);
+        pr[j] = next(lt_m, v);
+        nxt[j] = next(le_m, v + 1);
     }
     flag[j] = f;
 }
