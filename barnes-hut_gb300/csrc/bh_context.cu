@@ -256,9 +256,8 @@ int step_once(bh_context* ctx, double dt, double theta, double G, int mode)
     if (!rc) rc = bh::launch_permute(ctx);
     phase_end(ctx, 3, e);
     e = phase_begin(ctx);
-    if (!rc && far) rc = bh::launch_far_mass(ctx);
     const bool moments = mode == BH_MODE_LEARNED;
-    if (!rc) rc = bh::launch_build(ctx, far ? ctx->m2 : ctx->m, moments, far, G);
+    if (!rc) rc = bh::launch_build(ctx, ctx->m, moments, far, G, far);
     ctx->tree_far = far;
     ctx->tree_moments = moments;
     phase_end(ctx, 4, e);
@@ -746,7 +745,7 @@ int bh_tree_spread(bh_context* ctx, float* spread)
     if (!ctx->tree_valid) return ctx->n == 0 ? BH_OK : bh_fail(BH_ERR_STATE, "bh_tree_spread: no tree built");
     if (!spread) return bh_fail(BH_ERR_INVALID_ARGUMENT, "bh_tree_spread: null array");
     if (!ctx->tree_far || !ctx->tree_moments) {
-        if ((rc = bh::launch_far_mass(ctx)) || (rc = bh::launch_build(ctx, ctx->m2, true))) return rc;
+        if ((rc = bh::launch_build(ctx, ctx->m, true, false, 0.0, true))) return rc;
         ctx->tree_far = ctx->tree_moments = true;
     }
     int32_t S = 0;
@@ -791,8 +790,7 @@ int bh_compute_accelerations(bh_context* ctx, double theta, double G, double sof
     const bool far = mode >= BH_MODE_FP32_FAR;
     const bool moments = mode == BH_MODE_LEARNED;
     if (far != ctx->tree_far || (moments && !ctx->tree_moments)) {
-        if (far && (rc = bh::launch_far_mass(ctx))) return rc;
-        if ((rc = bh::launch_build(ctx, far ? ctx->m2 : ctx->m, moments))) return rc;
+        if ((rc = bh::launch_build(ctx, ctx->m, moments, false, 0.0, far))) return rc;
         ctx->tree_far = far;
         ctx->tree_moments = moments;
     }

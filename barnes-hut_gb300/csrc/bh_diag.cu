@@ -289,7 +289,7 @@ int bh_invariants(bh_context* ctx, double G, double theta, double out[9])
                 return rc;
         }
         if (!ctx->tree_far) {
-            if ((rc = bh::launch_far_mass(ctx)) || (rc = bh::launch_build(ctx, ctx->m2, ctx->tree_moments))) return rc;
+            if ((rc = bh::launch_build(ctx, ctx->m, ctx->tree_moments, false, 0.0, true))) return rc;
             ctx->tree_far = true;
         }
         if ((rc = bh::launch_direct_extract(ctx, G))) return rc;

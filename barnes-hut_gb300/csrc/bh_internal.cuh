@@ -479,9 +479,11 @@ int sort_passes_raw(int64_t n, const uint64_t* keys_in, uint64_t* keys_out, uint
 // `moments` also computes the second moments (spread per slot).
 // far_fused: the far-field tree of an FP32 form, whose centres of mass need
 // no bit-exact quotient; the FP32 node records for G are written too.
-int launch_build(bh_context* ctx, const double* mass, bool moments = false, bool far_fused = false, double G = 0.0);
+// far_masses: the bodies with id < num_direct count as massless (the FP32
+// forms' far-field tree).
+int launch_build(bh_context* ctx, const double* mass, bool moments = false, bool far_fused = false, double G = 0.0,
+                 bool far_masses = false);
 // FP32 modes: far-field masses (direct bodies zeroed) into ctx->m2.
-int launch_far_mass(bh_context* ctx);
 // Waits for the context's stream and turns a raised device error word into
 // a status (clearing the word).
 int finish(bh_context* ctx, const char* fn);

@@ -199,8 +199,7 @@ int bh_learned_collect(bh_context* ctx, double theta, double theta_label, double
     if (!ctx->tree_valid) return bh_fail(BH_ERR_STATE, "bh_learned_collect: build the tree first");
     int rc;
     if (!ctx->tree_far || !ctx->tree_moments) {
-        if ((rc = launch_far_mass(ctx))) return rc;
-        if ((rc = launch_build(ctx, ctx->m2, true))) return rc;
+        if ((rc = launch_build(ctx, ctx->m, true, false, 0.0, true))) return rc;
         ctx->tree_far = ctx->tree_moments = true;
     }
     cudaStream_t st = ctx->stream;

@@ -41,13 +41,6 @@
 namespace bh {
 namespace {
 
-__global__ void far_mass_kernel(int64_t n, const double* __restrict__ m, const uint64_t* __restrict__ id, int nd,
-                                double* __restrict__ m_far)
-{
-    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
-        m_far[i] = id[i] < (uint64_t)nd ? 0.0 : m[i];
-}
-
 // FP32 node records from the FP64 ones.
 // d4 (FP64 walk only): {cx, cy, cz, G m} per slot, the FP64 evaluation's
 // 32-byte record.
@@ -719,15 +712,6 @@ int launch_fp32_nodes(bh_context* ctx, double G)
     BH_LAUNCH_CHECK(ctx);
     ctx->fnodes_fused = true;
     ctx->fnodes_G = G;
-    return BH_OK;
-}
-
-int launch_far_mass(bh_context* ctx)
-{
-    if (ctx->n == 0) return BH_OK;
-    const int nd = ctx->num_direct < 64 ? ctx->num_direct : 64;
-    far_mass_kernel<<<grid_n(ctx->n), 256, 0, ctx->stream>>>(ctx->n, ctx->m, ctx->id, nd, ctx->m2);
-    BH_LAUNCH_CHECK(ctx);
     return BH_OK;
 }
 

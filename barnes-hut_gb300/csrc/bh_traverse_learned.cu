@@ -60,12 +60,14 @@ __global__ void __launch_bounds__(kThreads, 5) traverse_learned_kernel(FParams p
     const bool valid = i < p.n;
     const int64_t ii = valid ? i : base;  // idle lanes shadow the group's first body
     const double x = p.px[ii], y = p.py[ii], z = p.pz[ii];
-    const float gx = __double2float_rn(__shfl_sync(0xffffffffu, x, 0));
-    const float gy = __double2float_rn(__shfl_sync(0xffffffffu, y, 0));
-    const float gz = __double2float_rn(__shfl_sync(0xffffffffu, z, 0));
-    const float rx = __double2float_rn(x - (double)gx);
-    const float ry = __double2float_rn(y - (double)gy);
-    const float rz = __double2float_rn(z - (double)gz);
+    // The group centre as the collection walk forms it (the features are
+    // group-relative): the first body's position truncated to FP32.
+    const float gx = narrow_trunc(__shfl_sync(0xffffffffu, x, 0));
+    const float gy = narrow_trunc(__shfl_sync(0xffffffffu, y, 0));
+    const float gz = narrow_trunc(__shfl_sync(0xffffffffu, z, 0));
+    const float rx = __double2float_rn(x - widen(gx));
+    const float ry = __double2float_rn(y - widen(gy));
+    const float rz = __double2float_rn(z - widen(gz));
     float bminx = rx, bminy = ry, bminz = rz, bmaxx = rx, bmaxy = ry, bmaxz = rz;
 #pragma unroll
     for (int off = 16; off > 0; off >>= 1) {
@@ -382,9 +384,9 @@ __global__ void __launch_bounds__(kThreads, 5) traverse_learned_kernel(FParams p
                 fz = fmaf(sc, dz, fz);
                 cnt += take ? 1u : 0u;
             }
-            adx += (double)fx;
-            ady += (double)fy;
-            adz += (double)fz;
+            adx += widen(fx);  // exact, on the bit patterns
+            ady += widen(fy);
+            adz += widen(fz);
             nlist = 0;
             __syncwarp();
         }

@@ -82,13 +82,16 @@ __global__ void leaf_scatter_kernel(int64_t n, const uint64_t* __restrict__ key,
 // Leaf sums in body order (linear_octree.cpp:28-38) and boundary depths.
 // kMoments: also the leaf's second moment about its centre of mass (the
 // learned criterion's spread feature), sum_b m_b |x_b - c|^2.
+// nzero > 0: the bodies with id < nzero count as massless (the FP32 forms'
+// far-field tree, which leaves the Sun and planets to the direct terms).
 template <bool kMoments>
 __global__ void leaf_sum_kernel(const int32_t* __restrict__ counts, const int32_t* __restrict__ leaf_first,
                                 const uint64_t* __restrict__ leaf_key, const double* __restrict__ px,
                                 const double* __restrict__ py, const double* __restrict__ pz,
-                                const double* __restrict__ m, double4_32a* __restrict__ ls, int8_t* __restrict__ cdep,
-                                double* __restrict__ lq)
+                                const double* __restrict__ m, const uint64_t* __restrict__ id, int nzero,
+                                double4_32a* __restrict__ ls, int8_t* __restrict__ cdep, double* __restrict__ lq)
 {
+    auto mass = [&](int b) { return nzero > 0 && id[b] < (uint64_t)nzero ? 0.0 : m[b]; };
     const int L = counts[0];
     for (int l = blockIdx.x * blockDim.x + threadIdx.x; l < L; l += gridDim.x * blockDim.x) {
         double sm = 0.0, sx = 0.0, sy = 0.0, sz = 0.0;
@@ -96,14 +99,14 @@ __global__ void leaf_sum_kernel(const int32_t* __restrict__ counts, const int32_
         if (b1 == b0 + 1) {
             // One body: each sum is 0.0 + v, which is v except that -0.0
             // becomes +0.0; decided on the bit patterns (no FP64 addition).
-            const double mb = m[b0];
+            const double mb = mass(b0);
             sm = plus_zero(mb);
             sx = plus_zero(__dmul_rn(px[b0], mb));
             sy = plus_zero(__dmul_rn(py[b0], mb));
             sz = plus_zero(__dmul_rn(pz[b0], mb));
         } else {
             for (int b = b0; b < b1; ++b) {
-                const double mb = m[b];
+                const double mb = mass(b);
                 sm = __dadd_rn(sm, mb);
                 sx = __dadd_rn(sx, __dmul_rn(px[b], mb));
                 sy = __dadd_rn(sy, __dmul_rn(py[b], mb));
@@ -120,7 +123,7 @@ __global__ void leaf_sum_kernel(const int32_t* __restrict__ counts, const int32_
                 const double cx = sx * is, cy = sy * is, cz = sz * is;
                 for (int b = b0; b < b1; ++b) {
                     const double dx = px[b] - cx, dy = py[b] - cy, dz = pz[b] - cz;
-                    q += m[b] * (dx * dx + dy * dy + dz * dz);
+                    q += mass(b) * (dx * dx + dy * dy + dz * dz);
                 }
             }
             lq[l] = q;
@@ -594,6 +597,26 @@ __global__ void monopole_level_kernel(int depth, const int32_t* __restrict__ dep
         node_sums<kMoments>(depth_nodes[k], node_cs, node_nchild, slot_ref, ls, ns, lq, nq);
 }
 
+// The shallowest depths (0..kTopDepth: at most 8^d nodes each, 4,681 in
+// all) in one block, level by level with a block barrier between levels:
+// one launch instead of five nearly empty ones.
+constexpr int kTopDepth = 4;
+constexpr int kTopThreads = 1024;
+
+template <bool kMoments>
+__global__ void __launch_bounds__(kTopThreads) monopole_top_kernel(
+    const int32_t* __restrict__ depth_off, const int32_t* __restrict__ depth_nodes,
+    const int32_t* __restrict__ node_cs, const int32_t* __restrict__ node_nchild, const int32_t* __restrict__ slot_ref,
+    const double4_32a* ls, double4_32a* ns, const double* lq, double* nq)
+{
+    for (int d = kTopDepth; d >= 0; --d) {
+        const int lo = depth_off[d], hi = depth_off[d + 1];
+        for (int k = lo + (int)threadIdx.x; k < hi; k += kTopThreads)
+            node_sums<kMoments>(depth_nodes[k], node_cs, node_nchild, slot_ref, ls, ns, lq, nq);
+        __syncthreads();
+    }
+}
+
 // com = w/m when m > 0 (linear_octree.cpp:95-104), then the merge of
 // linear_octree.cpp:194-202 with m0 = com0 = 0.  A one-body leaf passes its
 // body's position (one = true): its w is 0 + x m, so w/m is merge_div(m, x).
@@ -726,8 +749,9 @@ int64_t boundary_pass_ints(int64_t n)
     return 4 * kNT * nb;
 }
 
-int launch_build(bh_context* ctx, const double* mass, bool moments, bool far_fused, double G)
+int launch_build(bh_context* ctx, const double* mass, bool moments, bool far_fused, double G, bool far_masses)
 {
+    const int nzero = far_masses ? (ctx->num_direct < 64 ? ctx->num_direct : 64) : 0;
     ctx->fnodes_fused = false;
     const int64_t n = ctx->n;
     if (n == 0) return BH_OK;
@@ -744,10 +768,12 @@ int launch_build(bh_context* ctx, const double* mass, bool moments, bool far_fus
     BH_LAUNCH_CHECK(ctx);
     if (moments)
         leaf_sum_kernel<true><<<g, kThreads, 0, st>>>(ctx->counts, ctx->leaf_first, ctx->leaf_key, ctx->px, ctx->py,
-                                                      ctx->pz, mass, ctx->leaf_s, ctx->cdep, ctx->leaf_q);
+                                                      ctx->pz, mass, ctx->id, nzero, ctx->leaf_s, ctx->cdep,
+                                                      ctx->leaf_q);
     else
         leaf_sum_kernel<false><<<g, kThreads, 0, st>>>(ctx->counts, ctx->leaf_first, ctx->leaf_key, ctx->px, ctx->py,
-                                                       ctx->pz, mass, ctx->leaf_s, ctx->cdep, ctx->leaf_q);
+                                                       ctx->pz, mass, ctx->id, nzero, ctx->leaf_s, ctx->cdep,
+                                                       ctx->leaf_q);
     BH_LAUNCH_CHECK(ctx);
 
     // 2. branching nodes: the boundary pass (representative flags, node
@@ -785,8 +811,9 @@ int launch_build(bh_context* ctx, const double* mass, bool moments, bool far_fus
     BH_LAUNCH_CHECK(ctx);
 
     // 3./4. monopoles (and second moments), level by level, deepest first:
-    // depth buckets of the branching nodes, then one launch per depth; each
-    // node sums its children in slot order from 0.0.  No atomics.
+    // depth buckets of the branching nodes, then one launch per depth down to
+    // kTopDepth + 1 and one block for the rest; each node sums its children
+    // in slot order from 0.0.  No atomics.
     {
         const int nblk = (int)((n + kBucketThreads - 1) / kBucketThreads);
         bucket_count_kernel<<<nblk, kBucketThreads, 0, st>>>(ctx->counts, ctx->node_depth, ctx->scan_tmp, nblk);
@@ -797,7 +824,7 @@ int launch_build(bh_context* ctx, const double* mass, bool moments, bool far_fus
         bucket_place_kernel<<<nblk, kBucketThreads, 0, st>>>(ctx->counts, ctx->node_depth, ctx->scan_tmp, nblk,
                                                              depth_tot, ctx->depth_off, ctx->depth_nodes);
         BH_LAUNCH_CHECK(ctx);
-        for (int d = kMaxDepth - 1; d >= 0; --d) {
+        for (int d = kMaxDepth - 1; d > kTopDepth; --d) {
             if (moments)
                 monopole_level_kernel<true><<<g, kThreads, 0, st>>>(d, ctx->depth_off, ctx->depth_nodes,
                                                                     ctx->node_cs, ctx->node_nchild, ctx->slot_ref,
@@ -810,6 +837,15 @@ int launch_build(bh_context* ctx, const double* mass, bool moments, bool far_fus
                                                                      ctx->node_q);
             BH_LAUNCH_CHECK(ctx);
         }
+        if (moments)
+            monopole_top_kernel<true><<<1, kTopThreads, 0, st>>>(ctx->depth_off, ctx->depth_nodes, ctx->node_cs,
+                                                                 ctx->node_nchild, ctx->slot_ref, ctx->leaf_s,
+                                                                 ctx->node_s, ctx->leaf_q, ctx->node_q);
+        else
+            monopole_top_kernel<false><<<1, kTopThreads, 0, st>>>(ctx->depth_off, ctx->depth_nodes, ctx->node_cs,
+                                                                  ctx->node_nchild, ctx->slot_ref, ctx->leaf_s,
+                                                                  ctx->node_s, ctx->leaf_q, ctx->node_q);
+        BH_LAUNCH_CHECK(ctx);
     }
 
     // 5. traversal records
