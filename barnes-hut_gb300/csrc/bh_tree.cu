@@ -597,26 +597,6 @@ __global__ void monopole_level_kernel(int depth, const int32_t* __restrict__ dep
         node_sums<kMoments>(depth_nodes[k], node_cs, node_nchild, slot_ref, ls, ns, lq, nq);
 }
 
-// The shallowest depths (0..kTopDepth: at most 8^d nodes each, 4,681 in
-// all) in one block, level by level with a block barrier between levels:
-// one launch instead of five nearly empty ones.
-constexpr int kTopDepth = 4;
-constexpr int kTopThreads = 1024;
-
-template <bool kMoments>
-__global__ void __launch_bounds__(kTopThreads) monopole_top_kernel(
-    const int32_t* __restrict__ depth_off, const int32_t* __restrict__ depth_nodes,
-    const int32_t* __restrict__ node_cs, const int32_t* __restrict__ node_nchild, const int32_t* __restrict__ slot_ref,
-    const double4_32a* ls, double4_32a* ns, const double* lq, double* nq)
-{
-    for (int d = kTopDepth; d >= 0; --d) {
-        const int lo = depth_off[d], hi = depth_off[d + 1];
-        for (int k = lo + (int)threadIdx.x; k < hi; k += kTopThreads)
-            node_sums<kMoments>(depth_nodes[k], node_cs, node_nchild, slot_ref, ls, ns, lq, nq);
-        __syncthreads();
-    }
-}
-
 // com = w/m when m > 0 (linear_octree.cpp:95-104), then the merge of
 // linear_octree.cpp:194-202 with m0 = com0 = 0.  A one-body leaf passes its
 // body's position (one = true): its w is 0 + x m, so w/m is merge_div(m, x).
@@ -811,9 +791,8 @@ int launch_build(bh_context* ctx, const double* mass, bool moments, bool far_fus
     BH_LAUNCH_CHECK(ctx);
 
     // 3./4. monopoles (and second moments), level by level, deepest first:
-    // depth buckets of the branching nodes, then one launch per depth down to
-    // kTopDepth + 1 and one block for the rest; each node sums its children
-    // in slot order from 0.0.  No atomics.
+    // depth buckets of the branching nodes, then one launch per depth; each
+    // node sums its children in slot order from 0.0.  No atomics.
     {
         const int nblk = (int)((n + kBucketThreads - 1) / kBucketThreads);
         bucket_count_kernel<<<nblk, kBucketThreads, 0, st>>>(ctx->counts, ctx->node_depth, ctx->scan_tmp, nblk);
@@ -824,7 +803,7 @@ int launch_build(bh_context* ctx, const double* mass, bool moments, bool far_fus
         bucket_place_kernel<<<nblk, kBucketThreads, 0, st>>>(ctx->counts, ctx->node_depth, ctx->scan_tmp, nblk,
                                                              depth_tot, ctx->depth_off, ctx->depth_nodes);
         BH_LAUNCH_CHECK(ctx);
-        for (int d = kMaxDepth - 1; d > kTopDepth; --d) {
+        for (int d = kMaxDepth - 1; d >= 0; --d) {
             if (moments)
                 monopole_level_kernel<true><<<g, kThreads, 0, st>>>(d, ctx->depth_off, ctx->depth_nodes,
                                                                     ctx->node_cs, ctx->node_nchild, ctx->slot_ref,
@@ -837,15 +816,6 @@ int launch_build(bh_context* ctx, const double* mass, bool moments, bool far_fus
                                                                      ctx->node_q);
             BH_LAUNCH_CHECK(ctx);
         }
-        if (moments)
-            monopole_top_kernel<true><<<1, kTopThreads, 0, st>>>(ctx->depth_off, ctx->depth_nodes, ctx->node_cs,
-                                                                 ctx->node_nchild, ctx->slot_ref, ctx->leaf_s,
-                                                                 ctx->node_s, ctx->leaf_q, ctx->node_q);
-        else
-            monopole_top_kernel<false><<<1, kTopThreads, 0, st>>>(ctx->depth_off, ctx->depth_nodes, ctx->node_cs,
-                                                                  ctx->node_nchild, ctx->slot_ref, ctx->leaf_s,
-                                                                  ctx->node_s, ctx->leaf_q, ctx->node_q);
-        BH_LAUNCH_CHECK(ctx);
     }
 
     // 5. traversal records
