@@ -628,7 +628,8 @@ def forms_4m(args, dev, params, scale, info):
 # DRAM traffic per launch of the force kernel (dram__bytes_read.sum +
 # dram__bytes_write.sum) from one ncu --set full capture of that kernel on
 # that workload, keyed by (mode, bodies).
-TRAFFIC_BYTES = {("fp64_list", 300_149): 52.33e6 + 1.02e6, ("fp32", 4_000_000): 481.81e6 + 183.69e6}
+TRAFFIC_BYTES = {("fp64_list", 300_149): 52.34e6 + 1.16e6, ("fp32", 4_000_000): 482.41e6 + 183.02e6,
+                 ("fp32_group", 4_000_000): 483.43e6 + 183.40e6}
 
 # Algorithmic bytes per body of the HBM-bound phases: the minimum traffic of
 # each phase's work (reads + writes of its inputs and outputs once).
