@@ -312,7 +312,8 @@ def test_division_free_helpers_match_ieee(bh, which, n):
     assert bh.selftest(which, n, seed=12345) == 0
 
 
-@pytest.mark.parametrize("mode", ["MODE_PLAIN_FP64", "MODE_FP64_LIST", "MODE_FP32_FAR", "MODE_LEARNED"])
+@pytest.mark.parametrize("mode", ["MODE_PLAIN_FP64", "MODE_FP64_LIST", "MODE_FP32_FAR", "MODE_FP32_GROUP",
+                                  "MODE_LEARNED"])
 def test_step_graphs_replay_the_same_kernels(bh, mode):
     """Kicked steps replayed through the captured CUDA graph give the same
     state bit for bit as launching the kernels one by one, with the same
@@ -351,7 +352,7 @@ def test_edge_systems_step_in_every_form(bh, golden, port, name):
     params = (rng.normal(0, 0.2, bh.MLP_PARAMS)).astype(np.float32)
     scale = np.concatenate([np.zeros(8), np.ones(8), np.full(8, -50.0), np.full(8, 50.0),
                             [0.0, 1.0]]).astype(np.float32)
-    for mode in ("MODE_PLAIN_FP64", "MODE_FP64_LIST", "MODE_FP32_FAR", "MODE_LEARNED"):
+    for mode in ("MODE_PLAIN_FP64", "MODE_FP64_LIST", "MODE_FP32_FAR", "MODE_FP32_GROUP", "MODE_LEARNED"):
         res = []
         for graphs in (False, True):
             with bh.Context(max(len(mass), 16)) as c:  # capacity above the bodies count

@@ -161,9 +161,10 @@ def test_simulate_driver_matches_reference_loop(bh, tmp_path):
     rp = np.zeros((len(ids), 3)); rp[ref[:, 0].astype(np.int64)] = ref[:, 1:]
     expect = float(np.sum(np.linalg.norm(pos - rp[ids.astype(np.int64)], axis=1)))
     assert 0.0 < expect < 0.1 and abs(float(err[0].split()[1]) - expect) <= 1e-4
-    r = subprocess.run([str(BUILD / "simulate"), "--generate", "2000", "--seed", "3", "--steps", "2",
-                        "--mode", "fp32"], capture_output=True, text=True, cwd=tmp_path)
-    assert r.returncode == 0 and "Loaded 2000 bodies" in r.stdout
+    for mode in ("fp32", "fp32_group"):
+        r = subprocess.run([str(BUILD / "simulate"), "--generate", "2000", "--seed", "3", "--steps", "2",
+                            "--mode", mode], capture_output=True, text=True, cwd=tmp_path)
+        assert r.returncode == 0 and "Loaded 2000 bodies" in r.stdout, (mode, r.stderr)
 
 
 @pytest.mark.gpu
