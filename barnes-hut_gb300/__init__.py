@@ -91,6 +91,7 @@ def _sig(lib):
     f["bh_interaction_count"] = (C.c_int, [_P, C.POINTER(_I64)])
     f["bh_interaction_counts"] = (C.c_int, [_P, _P])
     f["bh_step"] = (C.c_int, [_P, _D, _D, _D, _I64, C.c_int, C.POINTER(_D)])
+    f["bh_step_host"] = (C.c_int, [_P, _I64, _P, _P, _P, _P, _P, _D, _D, _D, _I64, C.c_int, C.POINTER(_D)])
     f["bh_set_profiling"] = (C.c_int, [_P, C.c_int])
     f["bh_phase_times"] = (C.c_int, [_P, _P, C.POINTER(_I64)])
     f["bh_measure_fma_peak"] = (C.c_int, [_P, C.c_int, C.POINTER(_D)])
@@ -515,6 +516,26 @@ class Context:
     def step(self, dt, theta=THETA_DEFAULT, G=G_DEFAULT, nsteps=1, mode=MODE_PLAIN_FP64, t=None) -> float:
         tv = _D(0.0 if t is None else t)
         _check(library().bh_step(self._h, dt, theta, G, int(nsteps), mode, None if t is None else C.byref(tv)))
+        return tv.value
+
+    def step_host(self, pos, vel, mass, ids, acc, dt, theta=THETA_DEFAULT, G=G_DEFAULT, nsteps=1,
+                  mode=MODE_PLAIN_FP64, t=0.0) -> float:
+        """bh_step_host: `nsteps` steps of a host-resident state, updated in
+        place (pos, vel: (n, 3) float64; mass; ids uint64; acc (n, 3), the
+        previous step's accelerations in, the last step's out), in one call
+        with one synchronisation.  Returns the new time."""
+        arrays = (pos, vel, mass, ids, acc)
+        for a in arrays:
+            if not (isinstance(a, np.ndarray) and a.flags.c_contiguous and a.flags.writeable):
+                raise ValueError("step_host: arrays must be writeable C-contiguous numpy arrays")
+        n = len(mass)
+        if pos.shape != (n, 3) or vel.shape != (n, 3) or acc.shape != (n, 3) or ids.shape != (n,) or \
+                pos.dtype != np.float64 or vel.dtype != np.float64 or acc.dtype != np.float64 or \
+                mass.dtype != np.float64 or ids.dtype != np.uint64:
+            raise ValueError("step_host: expected (n, 3) float64 pos/vel/acc, float64 mass, uint64 ids")
+        tv = _D(t)
+        _check(library().bh_step_host(self._h, n, _ptr(pos), _ptr(vel), _ptr(mass), _ptr(ids), _ptr(acc), dt,
+                                      theta, G, int(nsteps), mode, C.byref(tv)))
         return tv.value
 
 

@@ -506,11 +506,9 @@ int bh_get_bodies(bh_context* ctx, double* pos, double* vel, double* mass, uint6
     if (n == 0) return BH_OK;
     if (pos && (rc = download_vec3(ctx, pos, ctx->px2, ctx->px, ctx->py, ctx->pz, n))) return rc;
     if (vel && (rc = download_vec3(ctx, vel, ctx->vx2, ctx->vx, ctx->vy, ctx->vz, n))) return rc;
-    if (acc) {
-        // The two staging blocks may still be in flight above; wait first.
-        BH_CUDA_TRY(cudaStreamSynchronize(ctx->stream));
-        if ((rc = download_vec3(ctx, acc, ctx->px2, ctx->ax, ctx->ay, ctx->az, n))) return rc;
-    }
+    // The acceleration download reuses the position staging block after the
+    // position copy on the same stream: stream order keeps them apart.
+    if (acc && (rc = download_vec3(ctx, acc, ctx->px2, ctx->ax, ctx->ay, ctx->az, n))) return rc;
     if (mass) BH_CUDA_TRY(cudaMemcpyAsync(mass, ctx->m, sizeof(double) * n, cudaMemcpyDeviceToHost, ctx->stream));
     if (ids) BH_CUDA_TRY(cudaMemcpyAsync(ids, ctx->id, sizeof(uint64_t) * n, cudaMemcpyDeviceToHost, ctx->stream));
     return finish(ctx, "bh_get_bodies");
@@ -835,6 +833,53 @@ int bh_step(bh_context* ctx, double dt, double theta, double G, int64_t nsteps, 
         ctx->t += dt;
     }
     rc = finish(ctx, "bh_step");
+    if (t_io) *t_io = ctx->t;
+    if (nsteps > 0 && ctx->n > 0) {
+        ctx->tree_valid = ctx->sorted_valid = ctx->bbox_valid = rc == BH_OK;
+        ctx->keys_valid = false;
+    }
+    return rc;
+}
+
+int bh_step_host(bh_context* ctx, int64_t n, double* pos, double* vel, double* mass, uint64_t* ids, double* acc,
+                 double dt, double theta, double G, int64_t nsteps, int mode, double* t_io)
+{
+    int rc = check_ctx(ctx, "bh_step_host");
+    if (rc) return rc;
+    if (n < 0 || nsteps < 0 || !(theta >= 0.0))
+        return bh_fail(BH_ERR_INVALID_ARGUMENT, "bh_step_host: bad n, nsteps or theta");
+    if (n > ctx->cap) return bh_fail(BH_ERR_CAPACITY, "bh_step_host: more bodies than the context capacity");
+    if (n > 0 && (!pos || !vel || !mass || !ids || !acc))
+        return bh_fail(BH_ERR_INVALID_ARGUMENT, "bh_step_host: null array");
+    // bh_set_bodies and bh_set_accelerations, without their waits: every
+    // copy and kernel below runs in the order of the context's stream.
+    ctx->n = n;
+    ctx->t = t_io ? *t_io : 0.0;
+    ctx->tree_valid = ctx->keys_valid = ctx->bbox_valid = ctx->sorted_valid = false;
+    if (n > 0) {
+        if ((rc = upload_vec3(ctx, pos, ctx->px2, ctx->px, ctx->py, ctx->pz, n))) return rc;
+        if ((rc = upload_vec3(ctx, vel, ctx->vx2, ctx->vx, ctx->vy, ctx->vz, n))) return rc;
+        BH_CUDA_TRY(cudaMemcpyAsync(ctx->m, mass, sizeof(double) * n, cudaMemcpyHostToDevice, ctx->stream));
+        BH_CUDA_TRY(cudaMemcpyAsync(ctx->id, ids, sizeof(uint64_t) * n, cudaMemcpyHostToDevice, ctx->stream));
+        if ((rc = upload_vec3(ctx, acc, ctx->px2, ctx->ax, ctx->ay, ctx->az, n))) return rc;
+    }
+    // bh_step's loop, without its wait.
+    for (int64_t s = 0; s < nsteps; ++s) {
+        if (ctx->n > 0) {
+            const bool graph = ctx->graphs && !ctx->prof && ctx->t > 0;
+            if ((rc = graph ? step_graph(ctx, dt, theta, G, mode) : step_once(ctx, dt, theta, G, mode))) return rc;
+        }
+        ctx->t += dt;
+    }
+    // bh_get_bodies.
+    if (n > 0) {
+        if ((rc = download_vec3(ctx, pos, ctx->px2, ctx->px, ctx->py, ctx->pz, n))) return rc;
+        if ((rc = download_vec3(ctx, vel, ctx->vx2, ctx->vx, ctx->vy, ctx->vz, n))) return rc;
+        if ((rc = download_vec3(ctx, acc, ctx->px2, ctx->ax, ctx->ay, ctx->az, n))) return rc;
+        BH_CUDA_TRY(cudaMemcpyAsync(mass, ctx->m, sizeof(double) * n, cudaMemcpyDeviceToHost, ctx->stream));
+        BH_CUDA_TRY(cudaMemcpyAsync(ids, ctx->id, sizeof(uint64_t) * n, cudaMemcpyDeviceToHost, ctx->stream));
+    }
+    rc = finish(ctx, "bh_step_host");
     if (t_io) *t_io = ctx->t;
     if (nsteps > 0 && ctx->n > 0) {
         ctx->tree_valid = ctx->sorted_valid = ctx->bbox_valid = rc == BH_OK;

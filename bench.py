@@ -13,8 +13,9 @@ and seeded (the reference's 300k CSV is not part of its repository).
 * value: device time (CUDA events on the engine's stream), state resident in
   HBM, L2 flushed (256 MiB write) before every timed step.
 * e2e: the same steps through the C ABI with the state on the host: each
-  step uploads pos, vel, mass, ids and acc from pinned memory and downloads
-  them again (host clock around upload + step + download).
+  step is one bh_step_host call, which uploads pos, vel, mass, ids and acc
+  from pinned memory, runs the step and downloads them again (host clock
+  around the calls).
 * roofline: the force kernel (the dominant phase) against the FP64 FMA peak
   measured in the same process; algorithmic work = 20 flops per accepted
   interaction (the conventional monopole count), interactions counted on the
@@ -883,10 +884,9 @@ def run_ours(args, rank, ws, local):
     barrier(ws)
     t0 = time.perf_counter()
     for _ in range(e2e_steps):
-        ctx.set_bodies(hp, hv, hm, hi)
-        ctx.set_accelerations(ha)
-        t = ctx.step(DT, theta, G, 1, mode, t=t)
-        ctx.get_bodies(out=(hp, hv, hm, hi, ha))
+        # one C-ABI call per step: the state's upload, the step and the
+        # download of the new state and accelerations (bh_step_host)
+        t = ctx.step_host(hp, hv, hm, hi, ha, DT, theta, G, 1, mode, t=t)
     e2e_s = reduce_max(time.perf_counter() - t0, ws)
     h2d = hp.nbytes + hv.nbytes + hm.nbytes + hi.nbytes + ha.nbytes
     d2h = h2d

@@ -241,6 +241,17 @@ int bh_interaction_counts(bh_context *ctx, int32_t *per_body);
  * t > 0, drift, bbox, keys, sort, build, merge, forces, kick).  *t_io is the
  * simulation time, accumulated as t += dt after every step. */
 int bh_step(bh_context *ctx, double dt, double theta, double G, int64_t nsteps, int mode, double *t_io);
+/* The same loop over a state held on the host, the way the reference's own
+ * driver holds it (src/main.cpp:191-282 keeps the bodies in host memory):
+ * uploads the n bodies (pos, vel: AoS n*3; mass; ids) and the accelerations
+ * of the previous step (acc, n*3, which the first half-kick uses when
+ * *t_io > 0), runs nsteps steps, and writes pos, vel, mass, ids and acc back
+ * in the new body order.  Equivalent to bh_set_bodies, bh_set_accelerations,
+ * bh_step and bh_get_bodies in a row, with one synchronisation instead of
+ * five (page-locked host buffers give the fastest copies).  No reference
+ * counterpart. */
+int bh_step_host(bh_context *ctx, int64_t n, double *pos, double *vel, double *mass, uint64_t *ids, double *acc,
+                 double dt, double theta, double G, int64_t nsteps, int mode, double *t_io);
 
 /* ---- measurement (no reference counterpart) -------------------------- */
 /* Steps with the kick (all but the first of a run) go through a CUDA graph

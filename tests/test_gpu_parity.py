@@ -370,3 +370,31 @@ def test_edge_systems_step_in_every_form(bh, golden, port, name):
             if len(np.unique(g[f"{name}/keys"])) == len(mass):  # ties: the reference's order is unspecified
                 for x, y, what in zip((p, v, i, a), (rp, rv, ri, ra), ("pos", "vel", "ids", "acc")):
                     assert_bits_equal(x, y, f"{name} {what}")
+
+
+def test_step_host_equals_set_step_get(bh):
+    """bh_step_host (upload, steps and download in one call) gives the state
+    and accelerations of bh_set_bodies + bh_set_accelerations + bh_step +
+    bh_get_bodies bit for bit, over two calls in a row and in two forms."""
+    pos, vel, mass, ids = bh.generate_system(17, 30_000, 0.1, 0.05)
+    n = len(mass)
+    for mode in (bh.MODE_FP64_LIST, bh.MODE_FP32_GROUP):
+        with bh.Context(n) as c:
+            c.set_bodies(pos, vel, mass, ids)
+            t = c.step(DT, THETA, G, nsteps=2, mode=mode, t=0.0)
+            state = [np.array(a) for a in c.get_bodies()]
+        ref, host = [np.array(a) for a in state], [np.array(a) for a in state]
+        t_ref = t_host = t
+        with bh.Context(n) as c:
+            for _ in range(2):
+                p, v, m, i, a = ref
+                c.set_bodies(p, v, m, i)
+                c.set_accelerations(a)
+                t_ref = c.step(DT, THETA, G, nsteps=3, mode=mode, t=t_ref)
+                ref = [np.array(x) for x in c.get_bodies()]
+        with bh.Context(n) as c:
+            for _ in range(2):
+                t_host = c.step_host(*host, DT, THETA, G, nsteps=3, mode=mode, t=t_host)
+        assert t_host == t_ref
+        for x, y, what in zip(ref, host, ("pos", "vel", "mass", "ids", "acc")):
+            assert_bits_equal(x, y, f"mode {mode} {what}")
