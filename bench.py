@@ -33,6 +33,9 @@ and seeded (the reference's 300k CSV is not part of its repository).
   the learned run's error) with the FP32 walk's roofline.
 * learned_eval: the learned criterion on 5 unseen 1M-body systems at the
   same budgets against the same theta sweep, with its fallback rate.
+* learned_high_accuracy: the learned criterion with theta = 0.5 as its
+  fallback and a network trained for it, at budgets 3e-9-3e-7, against
+  finer theta sweeps (0.35-0.8) on an unseen 1M-body system.
 * precision_run: the FP32 far-field form on 1M bodies at theta {0.5, 0.8,
   1.05}, then 1,000 steps with error, energy and angular-momentum drift every
   100 steps.
@@ -44,7 +47,7 @@ and seeded (the reference's 300k CSV is not part of its repository).
 * let_exchange: the locally essential tree export and import at 4M bodies
   split over 8 ranks, against the oracle on the host cores.
 * csv_ingest: readCSV of a 1M-body file on the GPU against the host reader.
-  --no-extras skips these six blocks; --blocks a,b runs only those.
+  --no-extras skips these seven blocks; --blocks a,b runs only those.
 
 Multi-GPU: the path does not shard on one GPU per rank; ranks run replicas
 (weak scaling) and value is the sum of their body-steps over the slowest
@@ -76,7 +79,8 @@ N_BODIES = 300_149
 SEED = 2
 FLOPS_PER_INTERACTION = 20
 L2_FLUSH_BYTES = 256 << 20
-EXTRA_BLOCKS = ("forms_4m", "learned_eval", "precision_run", "long_runs", "let_exchange", "csv_ingest")
+EXTRA_BLOCKS = ("forms_4m", "learned_eval", "learned_high_accuracy", "precision_run", "long_runs", "let_exchange",
+                "csv_ingest")
 WORKLOAD = "plain FP64 theta=1.05, dt=1h, 300,149 bodies (Sun, 8 planets, 300,140 asteroids, 10% outer belt)"
 MODES = {"plain": 0, "fp64_list": 1, "fp32": 2, "learned": 3, "fp32_group": 4}
 KERNEL = {0: "traverse_exact_kernel", 1: "traverse_masked_kernel<fp64>", 2: "traverse_masked_kernel<fp32>",
@@ -503,6 +507,68 @@ def learned_eval(args, dev, params, scale):
             "mean_over_seeds": summary, "comparison": _against_theta(summary), "per_seed": rows}
 
 
+def learned_high_accuracy(args, dev):
+    """The learned criterion where the theta test must be fine: theta = 0.5
+    as its fallback, a network trained on pairs collected at theta = 0.5 and
+    labelled by the walk at theta = 0.3 (six seeded 1M-body systems, 90/10),
+    per-body budgets 3e-9 to 3e-7, against the FP32 per-body and group theta
+    sweeps, on an unseen 1M-body system: interactions per body, median error
+    against the FP64 direct sum, and force time (one walk, L2 flushed)."""
+    import torch
+    bh = importlib.import_module("barnes-hut_gb300")
+    learned = importlib.import_module("barnes-hut_gb300.learned")
+    n = min(args.ns_bodies, 1_000_000)
+    t0 = time.perf_counter()
+    F, L = learned.collect_pairs(range(9201, 9207), n, 0.10, 0.0, theta=0.5, theta_label=0.3, theta_max=3.0,
+                                 max_pairs=6_000_000)
+    params, scale, losses = bh.mlp_train(F, L, epochs=6, batch=4096, lr=2e-3, seed=0)
+    info = {"pairs": int(len(L)), "systems": 6, "seeds": "9201-9206", "collect_theta": 0.5, "label_theta": 0.3,
+            "final_loss": float(losses[-1]), "seconds": time.perf_counter() - t0}
+    pos, vel, mass, ids = bh.generate_system(9301, n, 0.10, 0.0)
+    rows = {}
+    with bh.Context(n, dev) as ctx:
+        ext = torch.cuda.ExternalStream(ctx.stream(), device=dev)
+        flush = torch.empty(L2_FLUSH_BYTES // 4, dtype=torch.float32, device=f"cuda:{dev}")
+        _fresh(ctx, pos, vel, mass, ids)
+        err = _sample_error(ctx, n, G)
+        cases = [(f"theta_{th:g}", bh.MODE_FP32_FAR, th, None) for th in (0.35, 0.4, 0.45, 0.5, 0.6, 0.7, 0.8)]
+        cases += [(f"group_theta_{th:g}", bh.MODE_FP32_GROUP, th, None) for th in (0.4, 0.5, 0.6, 0.7, 0.8)]
+        cases += [(f"budget_{b:g}", bh.MODE_LEARNED, 0.5, b) for b in (3e-9, 1e-8, 3e-8, 1e-7, 3e-7)]
+        for name, mode, th, b in cases:
+            if b is not None:
+                ctx.learned_set_model(params, scale, budget=b, theta_max=3.0)
+            med, p99 = err(ctx.compute_accelerations(th, G, 0.0, mode))
+            ipb = ctx.interaction_count() / n
+            ms = []
+            for _ in range(4):
+                flush.fill_(1.0)
+                torch.cuda.synchronize()
+                e0 = torch.cuda.Event(enable_timing=True)
+                e1 = torch.cuda.Event(enable_timing=True)
+                e0.record(ext)
+                ctx.compute_accelerations(th, G, 0.0, mode, download=False)
+                e1.record(ext)
+                e1.synchronize()
+                ms.append(e0.elapsed_time(e1))
+            rows[name] = {"theta": th, "budget": b, "median_rel_err": med, "p99_rel_err": p99,
+                          "interactions_per_body": ipb, "force_ms": sorted(ms)[1]}
+    cmp = {}
+    thetas = {k: r for k, r in rows.items() if not k.startswith("budget_")}
+    for k, r in rows.items():
+        if not k.startswith("budget_"):
+            continue
+        ok = [t for t in thetas.values() if t["median_rel_err"] <= r["median_rel_err"]]
+        if ok:
+            fewest = min(ok, key=lambda t: t["interactions_per_body"])
+            fastest = min(ok, key=lambda t: t["force_ms"])
+            cmp[k] = {"theta_interactions_at_equal_or_lower_error": fewest["interactions_per_body"],
+                      "learned_interactions": r["interactions_per_body"],
+                      "theta_force_ms_at_equal_or_lower_error": fastest["force_ms"],
+                      "learned_force_ms": r["force_ms"]}
+    return {"workload": f"{n:,} bodies (90/10), unseen seed 9301, theta = 0.5 fallback", "training": info,
+            "rows": rows, "comparison": cmp}
+
+
 def _against_theta(rows):
     """Each learned row against the theta-only rows: the fastest theta run
     at equal or lower median error, and the time ratio (above 1: the learned
@@ -900,13 +966,14 @@ def run_ours(args, rank, ws, local):
     accuracy = {"median_rel_err": float(np.median(err)), "p99_rel_err": float(np.quantile(err, 0.99)),
                 "sample": int(len(sample)), "against": "FP64 direct sum"}
 
-    ns = pr = le = runs = let = ingest = None
+    ns = pr = le = lh = runs = let = ingest = None
     blocks = set(EXTRA_BLOCKS) if args.blocks is None else set(args.blocks.split(","))
     if rank == 0 and ws == 1 and not args.no_extras:
         needs_model = blocks & {"forms_4m", "learned_eval", "long_runs"}
         params, scale, info = train_model(args) if needs_model else (None, None, None)
         ns = forms_4m(args, dev, params, scale, info) if "forms_4m" in blocks else None
         le = learned_eval(args, dev, params, scale) if "learned_eval" in blocks else None
+        lh = learned_high_accuracy(args, dev) if "learned_high_accuracy" in blocks else None
         pr = precision_run(args, dev) if "precision_run" in blocks else None
         let = let_exchange(args, dev) if "let_exchange" in blocks else None
         ingest = csv_ingest(args, dev) if "csv_ingest" in blocks else None
@@ -956,6 +1023,7 @@ def run_ours(args, rank, ws, local):
         "north_star": ns.get("north_star") if ns else None,
         "forms_4m": ns,
         "learned_eval": le,
+        "learned_high_accuracy": lh,
         "precision_run": pr,
         "long_runs": runs,
         "let_exchange": let,
