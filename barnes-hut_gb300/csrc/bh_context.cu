@@ -634,6 +634,7 @@ struct HostTree {
 
 int fetch_tree(bh_context* ctx, HostTree& h)
 {
+    if (int rc = bh::ensure_rec(ctx)) return rc;
     int32_t c[4];
     BH_CUDA_TRY(cudaMemcpyAsync(c, ctx->counts, sizeof(c), cudaMemcpyDeviceToHost, ctx->stream));
     BH_CUDA_TRY(cudaStreamSynchronize(ctx->stream));

@@ -292,6 +292,7 @@ int bh_invariants(bh_context* ctx, double G, double theta, double out[9])
             if ((rc = bh::launch_build(ctx, ctx->m, ctx->tree_moments, false, 0.0, true))) return rc;
             ctx->tree_far = true;
         }
+        if ((rc = bh::ensure_rec(ctx))) return rc;
         if ((rc = bh::launch_direct_extract(ctx, G))) return rc;
     }
     // Every kernel below writes one partial per block into its own column.

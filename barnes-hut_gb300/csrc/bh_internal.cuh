@@ -390,6 +390,7 @@ struct bh_context {
 
     bool tree_far = false;      // the tree holds far-field masses (FP32 modes)
     bool tree_moments = false;  // the tree's second moments are current
+    bool tree_rec = false;      // rec holds the tree's FP64 records (a fused far-field build leaves them out)
     bool build_merge = true;    // apply the single-rank exchange merge in builds
     int num_direct = BH_NUM_MASSIVE;  // bodies with id < num_direct: FP64 direct terms in FP32 modes
 
@@ -483,6 +484,9 @@ int sort_passes_raw(int64_t n, const uint64_t* keys_in, uint64_t* keys_out, uint
 // forms' far-field tree).
 int launch_build(bh_context* ctx, const double* mass, bool moments = false, bool far_fused = false, double G = 0.0,
                  bool far_masses = false);
+// The FP64 records of the current tree, written by a rebuild of its node
+// values where the last build left them out (no-op otherwise).
+int ensure_rec(bh_context* ctx);
 // FP32 modes: far-field masses (direct bodies zeroed) into ctx->m2.
 // Waits for the context's stream and turns a raised device error word into
 // a status (clearing the word).
@@ -502,6 +506,9 @@ int launch_fp32_nodes(bh_context* ctx, double G);
 // n_dev != nullptr (device-side count, at most n_max), else n_max is used.
 int device_exclusive_scan(bh_context* ctx, const int32_t* in, int32_t* out, int64_t n_max,
                           const int32_t* n_dev, int32_t* total);
+// Exclusive scan of the head flags of n sorted keys (1 where key[i] differs
+// from key[i - 1]): out[i] = the run id of a head; *total = the run count.
+int device_scan_key_heads(bh_context* ctx, const uint64_t* key, int32_t* out, int64_t n, int32_t* total);
 // The same over a caller's block-sum scratch of scan_tmp_ints(n_max) ints.
 int device_exclusive_scan_tmp(bh_context* ctx, const int32_t* in, int32_t* out, int64_t n_max,
                               const int32_t* n_dev, int32_t* total, int32_t* tmp);

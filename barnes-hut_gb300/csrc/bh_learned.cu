@@ -202,6 +202,7 @@ int bh_learned_collect(bh_context* ctx, double theta, double theta_label, double
         if ((rc = launch_build(ctx, ctx->m, true, false, 0.0, true))) return rc;
         ctx->tree_far = ctx->tree_moments = true;
     }
+    if ((rc = ensure_rec(ctx))) return rc;
     cudaStream_t st = ctx->stream;
     int32_t *grp = nullptr, *slot = nullptr;
     uint32_t* mask = nullptr;

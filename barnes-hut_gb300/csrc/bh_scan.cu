@@ -1,6 +1,7 @@
-// Device-wide exclusive scan of int32 values (reduce, scan of block sums,
-// down-sweep).  Used by the tree build to number leaves, branching nodes and
-// child slots.  No block waits on another block.
+// Device-wide exclusive scan of int32 values: per-block sums, then a
+// down-sweep in which each block adds the sums before its own.  Used by the
+// tree build to number leaves, branching nodes and child slots.  No block
+// waits on another block.
 #include "bh_internal.cuh"
 
 namespace bh {
@@ -45,7 +46,17 @@ __device__ int32_t block_inclusive(int32_t x, int32_t* warp_tot, int32_t* total)
     return r;
 }
 
-__global__ void __launch_bounds__(kScanThreads) scan_reduce_kernel(const int32_t* __restrict__ in, int64_t n_max,
+// The scanned values: in[i], or with `key` the head flags of sorted keys
+// (1 where key[i] starts a new run: the leaf numbering, with no pass to
+// write the flags first).
+__device__ __forceinline__ int32_t scan_value(const int32_t* in, const uint64_t* key, int64_t i)
+{
+    if (key) return (i == 0 || key[i] != key[i - 1]) ? 1 : 0;
+    return in[i];
+}
+
+__global__ void __launch_bounds__(kScanThreads) scan_reduce_kernel(const int32_t* __restrict__ in,
+                                                                  const uint64_t* __restrict__ key, int64_t n_max,
                                                                   const int32_t* __restrict__ n_dev,
                                                                   int32_t* __restrict__ bsum)
 {
@@ -56,44 +67,44 @@ __global__ void __launch_bounds__(kScanThreads) scan_reduce_kernel(const int32_t
     int32_t s = 0;
 #pragma unroll
     for (int k = 0; k < kScanItems; ++k)
-        if (base + k < n) s += in[base + k];
+        if (base + k < n) s += scan_value(in, key, base + k);
     block_inclusive(s, warp_tot, &total);
     if (threadIdx.x == 0) bsum[blockIdx.x] = total;
 }
 
-__global__ void __launch_bounds__(1024) scan_bsum_kernel(int32_t* __restrict__ bsum, int nb, int32_t* __restrict__ total)
-{
-    __shared__ int32_t warp_tot[32];
-    __shared__ int32_t chunk;
-    int32_t carry = 0;
-    for (int base = 0; base < nb; base += blockDim.x) {
-        const int i = base + threadIdx.x;
-        const int32_t v = i < nb ? bsum[i] : 0;
-        const int32_t inc = block_inclusive(v, warp_tot, &chunk);
-        if (i < nb) bsum[i] = carry + inc - v;
-        carry += chunk;
-        __syncthreads();
-    }
-    if (threadIdx.x == 0) *total = carry;
-}
-
-__global__ void __launch_bounds__(kScanThreads) scan_down_kernel(const int32_t* in, int32_t* out, int64_t n_max,
+// Each block's offset is the sum of the block sums before it, read by the
+// block itself (a few thousand at most), so no launch scans them; the last
+// block also writes the total.
+__global__ void __launch_bounds__(kScanThreads) scan_down_kernel(const int32_t* in, const uint64_t* __restrict__ key,
+                                                                int32_t* out, int64_t n_max,
                                                                 const int32_t* __restrict__ n_dev,
-                                                                const int32_t* __restrict__ bsum)
+                                                                const int32_t* __restrict__ bsum,
+                                                                int32_t* __restrict__ total_out)
 {
     __shared__ int32_t warp_tot[32];
     __shared__ int32_t total;
+    __shared__ int32_t before_s;
+    // sum of bsum[0 .. blockIdx.x)
+    {
+        int32_t acc = 0;
+        for (int k = threadIdx.x; k < (int)blockIdx.x; k += kScanThreads) acc += bsum[k];
+        block_inclusive(acc, warp_tot, &total);
+        if (threadIdx.x == 0) before_s = total;
+        __syncthreads();
+    }
+    const int32_t before = before_s;
     const int64_t n = scan_n(n_max, n_dev);
     const int64_t base = (int64_t)blockIdx.x * kScanBlock + (int64_t)threadIdx.x * kScanItems;
     int32_t v[kScanItems];
     int32_t s = 0;
 #pragma unroll
     for (int k = 0; k < kScanItems; ++k) {
-        v[k] = base + k < n ? in[base + k] : 0;
+        v[k] = base + k < n ? scan_value(in, key, base + k) : 0;
         s += v[k];
     }
     const int32_t inc = block_inclusive(s, warp_tot, &total);
-    int32_t run = bsum[blockIdx.x] + inc - s;
+    if (blockIdx.x == gridDim.x - 1 && threadIdx.x == 0) *total_out = before + total;
+    int32_t run = before + inc - s;
 #pragma unroll
     for (int k = 0; k < kScanItems; ++k) {
         if (base + k < n) out[base + k] = run;
@@ -119,11 +130,23 @@ int device_exclusive_scan_tmp(bh_context* ctx, const int32_t* in, int32_t* out, 
         return BH_OK;
     }
     const int nb = (int)((n_max + kScanBlock - 1) / kScanBlock);
-    scan_reduce_kernel<<<nb, kScanThreads, 0, ctx->stream>>>(in, n_max, n_dev, tmp);
+    scan_reduce_kernel<<<nb, kScanThreads, 0, ctx->stream>>>(in, nullptr, n_max, n_dev, tmp);
     BH_LAUNCH_CHECK(ctx);
-    scan_bsum_kernel<<<1, 1024, 0, ctx->stream>>>(tmp, nb, total);
+    scan_down_kernel<<<nb, kScanThreads, 0, ctx->stream>>>(in, nullptr, out, n_max, n_dev, tmp, total);
     BH_LAUNCH_CHECK(ctx);
-    scan_down_kernel<<<nb, kScanThreads, 0, ctx->stream>>>(in, out, n_max, n_dev, tmp);
+    return BH_OK;
+}
+
+int device_scan_key_heads(bh_context* ctx, const uint64_t* key, int32_t* out, int64_t n, int32_t* total)
+{
+    if (n <= 0) {
+        BH_CUDA_TRY(cudaMemsetAsync(total, 0, sizeof(int32_t), ctx->stream));
+        return BH_OK;
+    }
+    const int nb = (int)((n + kScanBlock - 1) / kScanBlock);
+    scan_reduce_kernel<<<nb, kScanThreads, 0, ctx->stream>>>(nullptr, key, n, nullptr, ctx->scan_tmp);
+    BH_LAUNCH_CHECK(ctx);
+    scan_down_kernel<<<nb, kScanThreads, 0, ctx->stream>>>(nullptr, key, out, n, nullptr, ctx->scan_tmp, total);
     BH_LAUNCH_CHECK(ctx);
     return BH_OK;
 }

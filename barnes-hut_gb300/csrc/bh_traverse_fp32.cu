@@ -731,6 +731,7 @@ int prepare_walk(bh_context* ctx, double theta, double G, double soft2, bool fp6
     const int64_t n = ctx->n;
     const int nd = fp64 ? 0 : (ctx->num_direct < 64 ? ctx->num_direct : 64);
     if (fp64 || !ctx->fnodes_fused || ctx->fnodes_G != G) {  // else they are current (the build wrote them)
+        if (int rc = ensure_rec(ctx)) return rc;
         fp32_nodes_kernel<<<grid_n(2 * n), 256, 0, ctx->stream>>>(ctx->counts, ctx->rec, G, ctx->fA, ctx->fB,
                                                                   ctx->fmeta, fp64 ? ctx->d4 : nullptr);
         BH_LAUNCH_CHECK(ctx);

@@ -56,12 +56,6 @@ __device__ inline bool is_head(const uint64_t* __restrict__ key, int64_t i)
     return i == 0 || key[i] != key[i - 1];
 }
 
-__global__ void leaf_head_kernel(int64_t n, const uint64_t* __restrict__ key, int32_t* __restrict__ head)
-{
-    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
-        head[i] = is_head(key, i) ? 1 : 0;
-}
-
 // Leaf ids of bodies, first body and key of each leaf.
 __global__ void leaf_scatter_kernel(int64_t n, const uint64_t* __restrict__ key, const int32_t* __restrict__ excl,
                                     int32_t* __restrict__ body_leaf, int32_t* __restrict__ leaf_first,
@@ -252,27 +246,31 @@ __device__ int block_excl_extreme(int x, int& carry, int* wsum)
     return res;
 }
 
-// One block per threshold: the blocks' exclusive prefix of last positions
-// (max) and exclusive suffix of first positions (min).
+// Two blocks per threshold: the blocks' exclusive prefix of last positions
+// (max; blocks 0..kNT-1) and exclusive suffix of first positions (min;
+// blocks kNT..2 kNT-1).
 __global__ void __launch_bounds__(1024) bnd_scan_kernel(int nblk, const int32_t* __restrict__ blast,
                                                         const int32_t* __restrict__ bfirst,
                                                         int32_t* __restrict__ bpre, int32_t* __restrict__ bsuf)
 {
     __shared__ int wsum[32];
-    const int t = blockIdx.x;
-    int carry = -1;
-    for (int base = 0; base < nblk; base += blockDim.x) {
-        const int b = base + threadIdx.x;
-        const int x = b < nblk ? blast[(int64_t)b * kNT + t] : -1;
-        const int ex = block_excl_extreme<false>(x, carry, wsum);
-        if (b < nblk) bpre[(int64_t)b * kNT + t] = ex;
-    }
-    carry = INT_MAX;
-    for (int base = 0; base < nblk; base += blockDim.x) {
-        const int b = nblk - 1 - (base + (int)threadIdx.x);
-        const int x = b >= 0 ? bfirst[(int64_t)b * kNT + t] : INT_MAX;
-        const int ex = block_excl_extreme<true>(x, carry, wsum);
-        if (b >= 0) bsuf[(int64_t)b * kNT + t] = ex;
+    const int t = blockIdx.x % kNT;
+    if (blockIdx.x < kNT) {
+        int carry = -1;
+        for (int base = 0; base < nblk; base += blockDim.x) {
+            const int b = base + threadIdx.x;
+            const int x = b < nblk ? blast[(int64_t)b * kNT + t] : -1;
+            const int ex = block_excl_extreme<false>(x, carry, wsum);
+            if (b < nblk) bpre[(int64_t)b * kNT + t] = ex;
+        }
+    } else {
+        int carry = INT_MAX;
+        for (int base = 0; base < nblk; base += blockDim.x) {
+            const int b = nblk - 1 - (base + (int)threadIdx.x);
+            const int x = b >= 0 ? bfirst[(int64_t)b * kNT + t] : INT_MAX;
+            const int ex = block_excl_extreme<true>(x, carry, wsum);
+            if (b >= 0) bsuf[(int64_t)b * kNT + t] = ex;
+        }
     }
 }
 
@@ -697,7 +695,10 @@ __global__ void finalize_kernel(const int32_t* __restrict__ counts, const int32_
             o.nchild = (uint8_t)node_nchild[b];
             o.depth = node_depth[b];
         }
-        rec[s] = o;
+        // The fused far-field build feeds only the FP32 walks, which read
+        // the FP32 records below: the FP64 record is left out (ensure_rec
+        // writes it when a diagnostic or export asks for it).
+        if (!kFar) rec[s] = o;
         if (kFar) {  // the FP32 walk's records, as fp32_nodes_kernel makes them
             const bool leaf = o.child < 0;
             far.A[s] = make_float4(narrow_trunc(o.cx), narrow_trunc(o.cy), narrow_trunc(o.cz),
@@ -739,10 +740,8 @@ int launch_build(bh_context* ctx, const double* mass, bool moments, bool far_fus
     const int maxb = 8 * bh::num_sms();
     const int g = grid_for(n, kThreads, maxb);
 
-    // 1. leaves
-    leaf_head_kernel<<<g, kThreads, 0, st>>>(n, ctx->key, ctx->head);
-    BH_LAUNCH_CHECK(ctx);
-    int rc = device_exclusive_scan(ctx, ctx->head, ctx->head, n, nullptr, ctx->counts + 0);
+    // 1. leaves: ids from a scan of the keys' head flags
+    int rc = device_scan_key_heads(ctx, ctx->key, ctx->head, n, ctx->counts + 0);
     if (rc) return rc;
     leaf_scatter_kernel<<<g, kThreads, 0, st>>>(n, ctx->key, ctx->head, ctx->body_leaf, ctx->leaf_first, ctx->leaf_key);
     BH_LAUNCH_CHECK(ctx);
@@ -766,7 +765,7 @@ int launch_build(bh_context* ctx, const double* mass, bool moments, bool far_fus
         int32_t* bsuf = bpre + (int64_t)nb * kNT;
         bnd_summary_kernel<<<nb, kBT, 0, st>>>(ctx->counts, ctx->cdep, blast, bfirst);
         BH_LAUNCH_CHECK(ctx);
-        bnd_scan_kernel<<<kNT, 1024, 0, st>>>(nb, blast, bfirst, bpre, bsuf);
+        bnd_scan_kernel<<<2 * kNT, 1024, 0, st>>>(nb, blast, bfirst, bpre, bsuf);
         BH_LAUNCH_CHECK(ctx);
         bnd_resolve_kernel<<<nb, kBT, 0, st>>>(ctx->counts, ctx->cdep, bpre, bsuf, ctx->head, ctx->bnd_pl, ctx->bnd_pr,
                                                 ctx->bnd_next, n);
@@ -840,7 +839,14 @@ int launch_build(bh_context* ctx, const double* mass, bool moments, bool far_fus
         ctx->fnodes_fused = true;
         ctx->fnodes_G = G;
     }
+    ctx->tree_rec = !far_fused;
     return BH_OK;
+}
+
+int ensure_rec(bh_context* ctx)
+{
+    if (ctx->tree_rec || ctx->n == 0) return BH_OK;
+    return launch_build(ctx, ctx->m, ctx->tree_moments, false, 0.0, ctx->tree_far);
 }
 
 }  // namespace bh

@@ -134,6 +134,40 @@ def test_fp32_group_steps_match_single_launches(bh):
     assert np.abs(p[np.argsort(i)] - p64[np.argsort(i64)]).max() < 1e-10
 
 
+def test_fp32_steps_then_record_readers(bh):
+    """An FP32 step builds only the FP32 walk's node records; the calls that
+    read the FP64 ones (invariants through the tree, the tree export, the
+    learned criterion's pair collection) write them first, and see what a
+    fresh build of the same state gives."""
+    pos, vel, mass, ids = bh.generate_system(23, 40_000, 0.1, 0.05)
+    n = len(mass)
+    with bh.Context(n) as c:
+        c.set_bodies(pos, vel, mass, ids)
+        c.step(DT, THETA, G, nsteps=3, mode=bh.MODE_FP32_GROUP, t=0.0)
+        inv1 = c.invariants(G, THETA)
+        exp1 = c.export_tree()
+        p, v, m, i, _ = c.get_bodies()
+        c.step(DT, THETA, G, nsteps=1, mode=bh.MODE_FP32_FAR, t=1.0)
+        f1, l1 = c.learned_collect(THETA, 0.5, 3.0, G, max_pairs=3_000_000)
+        state = c.get_bodies()
+    with bh.Context(n) as c2:
+        c2.set_bodies(p, v, m, i)
+        c2.compute_bbox(); c2.compute_keys(); c2.sort_bodies(); c2.build_tree()
+        inv2 = c2.invariants(G, THETA)
+        exp2 = c2.export_tree()
+        c2.set_bodies(*state[:4])
+        c2.compute_bbox(); c2.compute_keys(); c2.sort_bodies(); c2.build_tree()
+        f2, l2 = c2.learned_collect(THETA, 0.5, 3.0, G, max_pairs=3_000_000)
+    for a, b in zip(exp1, exp2):
+        assert np.array_equal(a, b)
+    for k in ("E", "K", "U"):
+        assert abs(inv1[k] - inv2[k]) <= 1e-12 * abs(inv2[k])
+    # the pairs come out in the order the warps reach them: compare as sets
+    assert 0 < len(l1) == len(l2) < 3_000_000
+    assert np.allclose(np.sort(l1), np.sort(l2), rtol=0, atol=1e-3)
+    assert np.allclose(np.sort(f1, axis=0), np.sort(f2, axis=0), rtol=0, atol=1e-4)
+
+
 def test_second_moment_spread_matches_fp64(bh):
     """The second-moment pass (learned features): per device node,
     sqrt(Q/m) of the far-field masses, Q = sum m |x - com|^2 over the
