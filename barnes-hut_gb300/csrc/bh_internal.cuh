@@ -506,9 +506,11 @@ int launch_fp32_nodes(bh_context* ctx, double G);
 // n_dev != nullptr (device-side count, at most n_max), else n_max is used.
 int device_exclusive_scan(bh_context* ctx, const int32_t* in, int32_t* out, int64_t n_max,
                           const int32_t* n_dev, int32_t* total);
-// Exclusive scan of the head flags of n sorted keys (1 where key[i] differs
-// from key[i - 1]): out[i] = the run id of a head; *total = the run count.
-int device_scan_key_heads(bh_context* ctx, const uint64_t* key, int32_t* out, int64_t n, int32_t* total);
+// The leaves of n sorted keys (runs of equal keys) from a scan of their head
+// flags: body_leaf[i] (the leaf of body i), leaf_first[l] (its first body,
+// with leaf_first[L] = n), leaf_key[l], and *total = L.
+int device_number_leaves(bh_context* ctx, const uint64_t* key, int64_t n, int32_t* total, int32_t* body_leaf,
+                         int32_t* leaf_first, uint64_t* leaf_key);
 // The same over a caller's block-sum scratch of scan_tmp_ints(n_max) ints.
 int device_exclusive_scan_tmp(bh_context* ctx, const int32_t* in, int32_t* out, int64_t n_max,
                               const int32_t* n_dev, int32_t* total, int32_t* tmp);

@@ -75,11 +75,19 @@ __global__ void __launch_bounds__(kScanThreads) scan_reduce_kernel(const int32_t
 // Each block's offset is the sum of the block sums before it, read by the
 // block itself (a few thousand at most), so no launch scans them; the last
 // block also writes the total.
+// With `key` (the leaf numbering) the sweep writes, instead of the scan, each
+// body's leaf id and each leaf's first body and key (`leaves`).
+struct LeafOut {
+    int32_t* body_leaf;
+    int32_t* leaf_first;  // L + 1 entries: the last is n
+    uint64_t* leaf_key;
+};
+
 __global__ void __launch_bounds__(kScanThreads) scan_down_kernel(const int32_t* in, const uint64_t* __restrict__ key,
                                                                 int32_t* out, int64_t n_max,
                                                                 const int32_t* __restrict__ n_dev,
                                                                 const int32_t* __restrict__ bsum,
-                                                                int32_t* __restrict__ total_out)
+                                                                int32_t* __restrict__ total_out, LeafOut leaves)
 {
     __shared__ int32_t warp_tot[32];
     __shared__ int32_t total;
@@ -105,6 +113,23 @@ __global__ void __launch_bounds__(kScanThreads) scan_down_kernel(const int32_t* 
     const int32_t inc = block_inclusive(s, warp_tot, &total);
     if (blockIdx.x == gridDim.x - 1 && threadIdx.x == 0) *total_out = before + total;
     int32_t run = before + inc - s;
+    if (key) {
+#pragma unroll
+        for (int k = 0; k < kScanItems; ++k) {
+            const int64_t i = base + k;
+            if (i < n) {
+                const int32_t lid = v[k] ? run : run - 1;
+                leaves.body_leaf[i] = lid;
+                if (v[k]) {
+                    leaves.leaf_first[lid] = (int32_t)i;
+                    leaves.leaf_key[lid] = key[i];
+                }
+                if (i == n - 1) leaves.leaf_first[lid + 1] = (int32_t)n;
+            }
+            run += v[k];
+        }
+        return;
+    }
 #pragma unroll
     for (int k = 0; k < kScanItems; ++k) {
         if (base + k < n) out[base + k] = run;
@@ -132,12 +157,13 @@ int device_exclusive_scan_tmp(bh_context* ctx, const int32_t* in, int32_t* out, 
     const int nb = (int)((n_max + kScanBlock - 1) / kScanBlock);
     scan_reduce_kernel<<<nb, kScanThreads, 0, ctx->stream>>>(in, nullptr, n_max, n_dev, tmp);
     BH_LAUNCH_CHECK(ctx);
-    scan_down_kernel<<<nb, kScanThreads, 0, ctx->stream>>>(in, nullptr, out, n_max, n_dev, tmp, total);
+    scan_down_kernel<<<nb, kScanThreads, 0, ctx->stream>>>(in, nullptr, out, n_max, n_dev, tmp, total, LeafOut{});
     BH_LAUNCH_CHECK(ctx);
     return BH_OK;
 }
 
-int device_scan_key_heads(bh_context* ctx, const uint64_t* key, int32_t* out, int64_t n, int32_t* total)
+int device_number_leaves(bh_context* ctx, const uint64_t* key, int64_t n, int32_t* total, int32_t* body_leaf,
+                         int32_t* leaf_first, uint64_t* leaf_key)
 {
     if (n <= 0) {
         BH_CUDA_TRY(cudaMemsetAsync(total, 0, sizeof(int32_t), ctx->stream));
@@ -146,7 +172,8 @@ int device_scan_key_heads(bh_context* ctx, const uint64_t* key, int32_t* out, in
     const int nb = (int)((n + kScanBlock - 1) / kScanBlock);
     scan_reduce_kernel<<<nb, kScanThreads, 0, ctx->stream>>>(nullptr, key, n, nullptr, ctx->scan_tmp);
     BH_LAUNCH_CHECK(ctx);
-    scan_down_kernel<<<nb, kScanThreads, 0, ctx->stream>>>(nullptr, key, out, n, nullptr, ctx->scan_tmp, total);
+    scan_down_kernel<<<nb, kScanThreads, 0, ctx->stream>>>(nullptr, key, nullptr, n, nullptr, ctx->scan_tmp, total,
+                                                           LeafOut{body_leaf, leaf_first, leaf_key});
     BH_LAUNCH_CHECK(ctx);
     return BH_OK;
 }

@@ -51,28 +51,6 @@ inline int grid_for(int64_t n, int threads, int max_blocks)
     return (int)(b > max_blocks ? max_blocks : b);
 }
 
-__device__ inline bool is_head(const uint64_t* __restrict__ key, int64_t i)
-{
-    return i == 0 || key[i] != key[i - 1];
-}
-
-// Leaf ids of bodies, first body and key of each leaf.
-__global__ void leaf_scatter_kernel(int64_t n, const uint64_t* __restrict__ key, const int32_t* __restrict__ excl,
-                                    int32_t* __restrict__ body_leaf, int32_t* __restrict__ leaf_first,
-                                    uint64_t* __restrict__ leaf_key)
-{
-    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
-        const bool h = is_head(key, i);
-        const int32_t lid = h ? excl[i] : excl[i] - 1;
-        body_leaf[i] = lid;
-        if (h) {
-            leaf_first[lid] = (int32_t)i;
-            leaf_key[lid] = key[i];
-        }
-        if (i == n - 1) leaf_first[lid + 1] = (int32_t)n;
-    }
-}
-
 // Leaf sums in body order (linear_octree.cpp:28-38) and boundary depths.
 // kMoments: also the leaf's second moment about its centre of mass (the
 // learned criterion's spread feature), sum_b m_b |x_b - c|^2.
@@ -740,11 +718,9 @@ int launch_build(bh_context* ctx, const double* mass, bool moments, bool far_fus
     const int maxb = 8 * bh::num_sms();
     const int g = grid_for(n, kThreads, maxb);
 
-    // 1. leaves: ids from a scan of the keys' head flags
-    int rc = device_scan_key_heads(ctx, ctx->key, ctx->head, n, ctx->counts + 0);
+    // 1. leaves: ids, first bodies and keys from a scan of the keys' head flags
+    int rc = device_number_leaves(ctx, ctx->key, n, ctx->counts + 0, ctx->body_leaf, ctx->leaf_first, ctx->leaf_key);
     if (rc) return rc;
-    leaf_scatter_kernel<<<g, kThreads, 0, st>>>(n, ctx->key, ctx->head, ctx->body_leaf, ctx->leaf_first, ctx->leaf_key);
-    BH_LAUNCH_CHECK(ctx);
     if (moments)
         leaf_sum_kernel<true><<<g, kThreads, 0, st>>>(ctx->counts, ctx->leaf_first, ctx->leaf_key, ctx->px, ctx->py,
                                                       ctx->pz, mass, ctx->id, nzero, ctx->leaf_s, ctx->cdep,
