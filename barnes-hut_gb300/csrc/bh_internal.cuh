@@ -487,7 +487,6 @@ int launch_build(bh_context* ctx, const double* mass, bool moments = false, bool
 // The FP64 records of the current tree, written by a rebuild of its node
 // values where the last build left them out (no-op otherwise).
 int ensure_rec(bh_context* ctx);
-// FP32 modes: far-field masses (direct bodies zeroed) into ctx->m2.
 // Waits for the context's stream and turns a raised device error word into
 // a status (clearing the word).
 int finish(bh_context* ctx, const char* fn);
