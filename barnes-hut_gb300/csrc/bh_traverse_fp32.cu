@@ -414,8 +414,6 @@ __global__ void __launch_bounds__(kThreads) traverse_masked_kernel(FParams p)
                 // A body never interacts with its own leaf (traversal.cpp:70,
                 // the FP32 form has no chain rule for it): its lanes leave
                 // the leaf's mask here, so the evaluation needs no leaf test.
-                // (The learned walk keeps the test: the extra registers cost
-                // it more occupancy than the test costs.)
                 const bool own_cand = A != 0 && leaf && ref >= leaf_lo && ref <= leaf_hi;
                 unsigned oc = __ballot_sync(0xffffffffu, own_cand);
                 while (oc) {

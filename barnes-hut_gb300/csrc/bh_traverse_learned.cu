@@ -18,6 +18,8 @@
 // each lane of its mask decides for itself, as in the plain walk.
 // Candidates whose features fall outside the training range go the same way
 // and are counted.
+#include <climits>
+
 #include "bh_walk.cuh"
 
 namespace bh {
@@ -80,13 +82,18 @@ __global__ void __launch_bounds__(kThreads, 5) traverse_learned_kernel(FParams p
     }
     const unsigned full = __ballot_sync(0xffffffffu, valid);
     const int my_leaf = valid ? p.body_leaf[i] : -2;
+    // The group's leaf ids span [leaf_lo, leaf_hi] (bodies in key order).
+    int leaf_lo = valid ? my_leaf : INT_MAX, leaf_hi = valid ? my_leaf : INT_MIN;
+#pragma unroll
+    for (int off = 16; off > 0; off >>= 1) {
+        leaf_lo = min(leaf_lo, __shfl_xor_sync(0xffffffffu, leaf_lo, off));
+        leaf_hi = max(leaf_hi, __shfl_xor_sync(0xffffffffu, leaf_hi, off));
+    }
     const float theta2f = (float)p.theta2;
     const float soft2f = (float)p.soft2;
     const double soft2 = p.soft2;
     int2* stk = sm.stack[w];
     float4* L = sm.lst[w];
-    int* LN = sm.lst_node[w];
-    int* LL = sm.lst_leaf[w];
     unsigned* LM = sm.lst_mask[w];
     const unsigned me = 1u << lane;
     const unsigned lt = me - 1u;
@@ -333,29 +340,56 @@ __global__ void __launch_bounds__(kThreads, 5) traverse_learned_kernel(FParams p
                 }
                 __syncwarp();
             }
-            // Mixed nodes: every lane of the mask applies its own test.
-            unsigned mb = __ballot_sync(0xffffffffu, mixed);
-            while (mb) {
-                const int j = __ffs(mb) - 1;
-                mb &= mb - 1;
-                const unsigned Mj = __shfl_sync(0xffffffffu, M, j);
-                const int dj = __shfl_sync(0xffffffffu, depth, j);
-                const float cx = __shfl_sync(0xffffffffu, e.x, j);
-                const float cy = __shfl_sync(0xffffffffu, e.y, j);
-                const float cz = __shfl_sync(0xffffffffu, e.z, j);
-                const float dx = cx - rx, dy = cy - ry, dz = cz - rz;
-                const bool acc = sm.side2f[dj] < theta2f * (dx * dx + dy * dy + dz * dz);
-                const unsigned Aj = __ballot_sync(0xffffffffu, acc) & Mj;
-                if (lane == j) A = Aj;
+            // Mixed nodes: every lane of the mask applies its own test.  The
+            // nodes {c, side^2} go to free entry slots past the staged list
+            // (from the first even position; the list holds at most
+            // kList - 32 entries here), and every lane tests its body against
+            // each of them, read by broadcast.  Lane q keeps the lanes that
+            // accept slot q.
+            const unsigned mb = __ballot_sync(0xffffffffu, mixed);
+            if (mb) {
+                float4* X = L + ((nlist + 1) & ~1);
+                const int nm = __popc(mb);
+                const int slot = __popc(mb & lt);
+                if (mixed) X[slot] = make_float4(e.x, e.y, e.z, sm.side2f[depth]);
+                __syncwarp();
+                unsigned res = 0;
+#pragma unroll 2
+                for (int q = 0; q < nm; ++q) {
+                    const float4 v = X[q];
+                    const float dx = v.x - rx, dy = v.y - ry, dz = v.z - rz;
+                    const unsigned bq = __ballot_sync(0xffffffffu, v.w < theta2f * (dx * dx + dy * dy + dz * dz));
+                    if (lane == q) res = bq;
+                }
+                const unsigned accm = __shfl_sync(0xffffffffu, res, slot & 31);
+                if (mixed) A = accm & M;
+                __syncwarp();
             }
-            // Stage the accepted (node, lanes) entries.
+            // A body never interacts with its own leaf (traversal.cpp:70):
+            // its lanes leave the leaf's mask here, so the evaluation needs
+            // no leaf test.
+            {
+                const bool own_cand = A != 0 && leaf && ref >= leaf_lo && ref <= leaf_hi;
+                unsigned oc = __ballot_sync(0xffffffffu, own_cand);
+                while (oc) {
+                    const int j = __ffs(oc) - 1;
+                    oc &= oc - 1u;
+                    const int lj = __shfl_sync(0xffffffffu, ref, j);
+                    const unsigned own = __ballot_sync(0xffffffffu, my_leaf == lj);
+                    if (lane == j) A &= ~own;
+                }
+            }
+            // Stage the accepted (node, lanes) entries in pairs
+            // {x0, x1, y0, y1}, {z0, z1, w0, w1}.
             const bool stage = A != 0;
             const unsigned am = __ballot_sync(0xffffffffu, stage);
             if (stage) {
                 const int pos = nlist + __popc(am & lt);
-                L[pos] = e;
-                LN[pos] = node;
-                LL[pos] = leaf ? ref : -1;  // for the own-leaf test
+                float* P = reinterpret_cast<float*>(L + (pos & ~1)) + (pos & 1);
+                P[0] = e.x;
+                P[2] = e.y;
+                P[4] = e.z;
+                P[6] = e.w;
                 LM[pos] = A;
             }
             nlist += __popc(am);
@@ -369,24 +403,46 @@ __global__ void __launch_bounds__(kThreads, 5) traverse_learned_kernel(FParams p
             __syncwarp();
         }
         if (nlist > kList - 32 || (sp == 0 && nlist > 0)) {
-            float fx = 0.f, fy = 0.f, fz = 0.f;
-            for (int j = 0; j < nlist; ++j) {
-                const float4 q = L[j];
-                const unsigned mj = LM[j];
-                const bool take = (mj & me) != 0u && LL[j] != my_leaf;
-                const float dx = q.x - rx, dy = q.y - ry, dz = q.z - rz;
-                const float r2 = fmaf(dx, dx, fmaf(dy, dy, fmaf(dz, dz, soft2f)));
-                const float inv = rsqrtf(r2);
-                float sc = q.w * (inv * inv * inv);
-                if (!take) sc = 0.0f;
-                fx = fmaf(sc, dx, fx);
-                fy = fmaf(sc, dy, fy);
-                fz = fmaf(sc, dz, fz);
-                cnt += take ? 1u : 0u;
+            // Two entries per iteration in packed pairs (even, odd); an odd
+            // count is padded with a zero entry taken by no lane.  Each half
+            // rounds as the scalar form; the two halves are separate partial
+            // sums, added at the end.
+            if (nlist & 1) {
+                if (lane == 0) {
+                    float* P = reinterpret_cast<float*>(L + (nlist - 1)) + 1;
+                    P[0] = P[2] = P[4] = P[6] = 0.0f;
+                    LM[nlist] = 0u;
+                }
+                __syncwarp();
             }
-            adx += widen(fx);  // exact, on the bit patterns
-            ady += widen(fy);
-            adz += widen(fz);
+            const f32x2 rx2 = pk(rx, rx), ry2 = pk(ry, ry), rz2 = pk(rz, rz);
+            const f32x2 sf2 = pk(soft2f, soft2f);
+            f32x2 fx = 0ull, fy = 0ull, fz = 0ull;  // +0.0f pairs
+            for (int j = 0; j < nlist; j += 2) {
+                const ulonglong2 xy = *reinterpret_cast<const ulonglong2*>(L + j);
+                const ulonglong2 zw = *reinterpret_cast<const ulonglong2*>(L + j + 1);
+                const uint2 mj = *reinterpret_cast<const uint2*>(LM + j);
+                const f32x2 dx = sub2(xy.x, rx2), dy = sub2(xy.y, ry2), dz = sub2(zw.x, rz2);
+                const f32x2 r2 = fma2(dx, dx, fma2(dy, dy, fma2(dz, dz, sf2)));
+                float r0, r1;
+                upk(r2, r0, r1);
+                const f32x2 inv = pk(rsqrtf(r0), rsqrtf(r1));
+                float s0, s1;
+                upk(mul2(zw.y, mul2(mul2(inv, inv), inv)), s0, s1);
+                const bool t0 = (mj.x & me) != 0u, t1 = (mj.y & me) != 0u;
+                const f32x2 sc = pk(t0 ? s0 : 0.0f, t1 ? s1 : 0.0f);
+                fx = fma2(sc, dx, fx);
+                fy = fma2(sc, dy, fy);
+                fz = fma2(sc, dz, fz);
+                cnt += (t0 ? 1u : 0u) + (t1 ? 1u : 0u);
+            }
+            float fx0, fx1, fy0, fy1, fz0, fz1;
+            upk(fx, fx0, fx1);
+            upk(fy, fy0, fy1);
+            upk(fz, fz0, fz1);
+            adx += widen(fx0 + fx1);  // exact, on the bit patterns
+            ady += widen(fy0 + fy1);
+            adz += widen(fz0 + fz1);
             nlist = 0;
             __syncwarp();
         }

@@ -25,7 +25,7 @@ enum { kLearnNone = 0, kLearnInfer = 1, kLearnCollect = 2 };
 template <bool kFP64, int kLearn>
 struct WalkSmem {
     static constexpr int kW64 = kFP64 ? kWarps : 1;      // FP64-only tables
-    static constexpr bool kLL = kFP64 || kLearn == 1;     // leaf ids kept for the evaluation's own-leaf test
+    static constexpr bool kLL = kFP64;                    // leaf ids kept for the evaluation's own-leaf test
     static constexpr bool kF = kLearn == 1;              // network input rows
     int2 stack[kWarps][kStack];  // sibling ranges: {first | (count - 1) << 28, lane mask}
     // FP32 node data of the staged entries: {x, y, z, G m} per entry, or in
