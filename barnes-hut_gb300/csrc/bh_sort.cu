@@ -95,15 +95,24 @@ __global__ void __launch_bounds__(kSortThreads) onesweep_kernel(
         }
     }
 
-    // Rank within the warp: peers holding the same digit are found with
-    // match.any; the lowest peer bumps the warp's digit counter once.
+    // Rank within the warp: peers holding the same digit are found with one
+    // ballot per digit bit (a fixed cost; match.any takes longer the more
+    // distinct digits a warp holds, as in the low passes); the lowest peer
+    // bumps the warp's digit counter once.
     const unsigned lt = (1u << lane) - 1u;
 #pragma unroll
     for (int k = 0; k < kSortItems; ++k) {
         const int64_t i = base + w * (32 * kSortItems) + k * 32 + lane;
         const bool valid = i < n;
         const uint32_t d = valid ? (uint32_t)((key[k] >> shift) & 0xFF) : 0x100u;
-        const unsigned peers = __match_any_sync(0xffffffffu, d);
+        const unsigned vb = __ballot_sync(0xffffffffu, valid);
+        unsigned peers = valid ? vb : ~vb;
+#pragma unroll
+        for (int b = 0; b < 8; ++b) {
+            const bool bit = (d >> b) & 1u;
+            const unsigned v = __ballot_sync(0xffffffffu, bit);
+            peers &= bit ? v : ~v;
+        }
         const int leader = __ffs(peers) - 1;
         uint32_t old = 0;
         if (valid && lane == leader) {

@@ -57,6 +57,7 @@ port on hosts without the reference checkout) on rank 0 only.
 from __future__ import annotations
 
 import argparse
+import gc
 import importlib
 import json
 import os
@@ -910,6 +911,11 @@ def run_ours(args, rank, ws, local):
         t = t_snap
         barrier(ws)
         l0 = ctx.launches()
+        # No collector pause inside the event-timed steps: a host stall
+        # between the first event and the step's launch would be counted as
+        # device time.
+        gc.collect()
+        gc.disable()
         w0 = time.perf_counter()
         for _ in range(args.steps):
             flush.fill_(1.0)
@@ -925,6 +931,7 @@ def run_ours(args, rank, ws, local):
         torch.cuda.synchronize(dev)
         barrier(ws)
         w1 = time.perf_counter()
+        gc.enable()
         time.sleep(0.25)  # the sample that covers the last timed step
     torch.cuda.synchronize(dev)
     launches = ctx.launches() - l0
@@ -948,12 +955,15 @@ def run_ours(args, rank, ws, local):
     hp[:], hv[:], hm[:], hi[:], ha[:] = ctx.get_bodies()
     e2e_steps = max(1, args.e2e_steps)
     barrier(ws)
+    gc.collect()
+    gc.disable()
     t0 = time.perf_counter()
     for _ in range(e2e_steps):
         # one C-ABI call per step: the state's upload, the step and the
         # download of the new state and accelerations (bh_step_host)
         t = ctx.step_host(hp, hv, hm, hi, ha, DT, theta, G, 1, mode, t=t)
     e2e_s = reduce_max(time.perf_counter() - t0, ws)
+    gc.enable()
     h2d = hp.nbytes + hv.nbytes + hm.nbytes + hi.nbytes + ha.nbytes
     d2h = h2d
 
