@@ -6,7 +6,7 @@
 // sort is a stable 8-pass LSD radix sort (8-bit digits) whose digit
 // histograms for all passes come from the key kernel, and each pass is one
 // kernel: tiles claim an id in launch order, rank their keys with warp
-// match/ballot primitives, publish per-digit tile counts, and obtain their
+// ballots (one per digit bit), publish per-digit tile counts, and obtain their
 // global offsets by a decoupled look-back over earlier tiles.  Every wait
 // in the look-back is bounded; on expiry the kernel raises kErrTimeout
 // and still publishes, so no tile can wait forever.
