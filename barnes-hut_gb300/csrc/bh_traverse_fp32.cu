@@ -242,7 +242,7 @@ __global__ void __launch_bounds__(kThreads) traverse_masked_kernel(FParams p)
             const int s_r = __shfl_sync(0xffffffffu, rstart, rj);
             const unsigned m_r = __shfl_sync(0xffffffffu, rmask, rj);
             pops += T;
-            if (sp - R + T > kStack || pops > p.max_pops) {
+            if (sp - R + T > WalkSmem<kFP64, kLearn>::kStk || pops > p.max_pops) {
                 overflow = true;
                 break;
             }
@@ -470,7 +470,7 @@ __global__ void __launch_bounds__(kThreads) traverse_masked_kernel(FParams p)
             sp += __popc(pm);
             __syncwarp();
         }
-        if (nlist > kList - 32 || (sp == 0 && nlist > 0)) {
+        if (nlist > WalkSmem<kFP64, kLearn>::kLst - 32 || (sp == 0 && nlist > 0)) {
             if (kLearn == kLearnCollect) {
                 nlist = 0;  // collection evaluates nothing
                 __syncwarp();

@@ -13,6 +13,12 @@ constexpr int kWarps = 4;
 constexpr int kThreads = 32 * kWarps;
 constexpr int kStack = 512;   // sibling-range entries per warp
 constexpr int kList = 96;     // staged interactions per warp
+// The FP64 walk's: a longer list, so that each balanced evaluation spreads
+// more pairs over the warp (fewer flushes), and a shorter stack, so that the
+// block still fits 5 per SM.  The deepest stack measured is 202 entries
+// (4M bodies, theta = 0.3); past the bound the walk reports an overflow.
+constexpr int kStack64 = 352;
+constexpr int kList64 = 128;
 constexpr int kSegs = 63;     // FP64 list evaluation: run slots body + thread, 0..62
 constexpr int kSlotBits = 28; // slot index bits of a stack entry (count - 1 in the top 3)
 constexpr float kMargin = 1e-5f;  // relative margin of the FP32 group tests
@@ -21,24 +27,27 @@ constexpr float kAbsErr = 1e-6f;  // bound on FP32 coordinate error, relative to
 enum { kLearnNone = 0, kLearnInfer = 1, kLearnCollect = 2 };
 
 // Per-block shared memory of the walk.  Tables a variant does not use shrink
-// to one element, so that the FP32 walk fits 8 blocks (32 warps) per SM.
+// to one element, so that the FP32 walk fits 8 blocks (32 warps) per SM; the
+// FP64 walk fits 5 (6 ran slower: the FP64 pipe is already 86 % busy).
 template <bool kFP64, int kLearn>
 struct WalkSmem {
     static constexpr int kW64 = kFP64 ? kWarps : 1;      // FP64-only tables
     static constexpr bool kLL = kFP64;                    // leaf ids kept for the evaluation's own-leaf test
     static constexpr bool kF = kLearn == 1;              // network input rows
-    int2 stack[kWarps][kStack];  // sibling ranges: {first | (count - 1) << 28, lane mask}
+    static constexpr int kStk = kFP64 ? kStack64 : kStack;  // stack entries per warp
+    static constexpr int kLst = kFP64 ? kList64 : kList;    // staged entries per warp
+    int2 stack[kWarps][kStk];  // sibling ranges: {first | (count - 1) << 28, lane mask}
     // FP32 node data of the staged entries: {x, y, z, G m} per entry, or in
     // the plain FP32 walk entry pairs {x0, x1, y0, y1}, {z0, z1, w0, w1}
-    float4 lst[kFP64 ? 1 : kWarps][kFP64 ? 1 : kList];
-    int lst_node[kWarps][kList];
-    int lst_leaf[kLL ? kWarps : 1][kLL ? kList : 1];
-    alignas(8) unsigned lst_mask[kWarps][kList];
+    float4 lst[kFP64 ? 1 : kWarps][kFP64 ? 1 : kLst];
+    int lst_node[kWarps][kLst];
+    int lst_leaf[kLL ? kWarps : 1][kLL ? kLst : 1];
+    alignas(8) unsigned lst_mask[kWarps][kLst];
     float side2f[kMaxDepth + 1];
     double side2d[kMaxDepth + 1];
     float2 sthr[kMaxDepth + 1];  // group-test distances per depth: side sqrt(1 + margin) / theta, (1 - margin)
     float feat[kF ? kWarps : 1][kF ? 32 : 1][9];
-    uint8_t plist[kW64][kFP64 ? kList : 1][32];  // FP64: each lane's own entries, in order
+    uint8_t plist[kW64][kFP64 ? kLst : 1][32];  // FP64: each lane's own entries, in order
     // FP64: the balanced evaluation's per-warp tables (see the flush).
     int poff[kW64][33];                     // first pair of each lane, then the total
     double bpos[kW64][3][kFP64 ? 32 : 1];   // the bodies' positions
