@@ -90,7 +90,7 @@ __global__ void __launch_bounds__(kThreads) traverse_masked_kernel(FParams p)
     static_assert(kLearn != kLearnInfer, "the learned walk is traverse_learned_kernel");
     static_assert(!kGroup || (!kFP64 && kLearn == kLearnNone), "the group test is an FP32 far-field walk");
     extern __shared__ __align__(16) unsigned char smem_raw[];
-    WalkSmem<kFP64, kLearn>& sm = *reinterpret_cast<WalkSmem<kFP64, kLearn>*>(smem_raw);
+    WalkSmem<kFP64, kLearn, kGroup>& sm = *reinterpret_cast<WalkSmem<kFP64, kLearn, kGroup>*>(smem_raw);
     if (threadIdx.x <= kMaxDepth) {
         const double dx = __dsub_rn(p.bbox[3], p.bbox[0]);
         const double dy = __dsub_rn(p.bbox[4], p.bbox[1]);
@@ -163,7 +163,7 @@ __global__ void __launch_bounds__(kThreads) traverse_masked_kernel(FParams p)
     int2* stk = sm.stack[w];
     float4* L = kFP64 ? nullptr : sm.lst[w];
     int* LN = sm.lst_node[w];
-    int* LL = WalkSmem<kFP64, kLearn>::kLL ? sm.lst_leaf[w] : nullptr;
+    int* LL = WalkSmem<kFP64, kLearn, kGroup>::kLL ? sm.lst_leaf[w] : nullptr;
     unsigned* LM = sm.lst_mask[w];
     const unsigned me = 1u << lane;
     const unsigned lt = me - 1u;
@@ -242,7 +242,7 @@ __global__ void __launch_bounds__(kThreads) traverse_masked_kernel(FParams p)
             const int s_r = __shfl_sync(0xffffffffu, rstart, rj);
             const unsigned m_r = __shfl_sync(0xffffffffu, rmask, rj);
             pops += T;
-            if (sp - R + T > WalkSmem<kFP64, kLearn>::kStk || pops > p.max_pops) {
+            if (sp - R + T > WalkSmem<kFP64, kLearn, kGroup>::kStk || pops > p.max_pops) {
                 overflow = true;
                 break;
             }
@@ -387,10 +387,10 @@ __global__ void __launch_bounds__(kThreads) traverse_masked_kernel(FParams p)
             } else if (mb) {
                 // The mixed nodes {c, side^2} go to free entry slots past the
                 // staged list (from the first even position, which leaves the
-                // last entry pair whole; the list holds at most kList - 32
-                // entries here), and every lane tests its body against each
-                // of them, read by broadcast.  Lane q keeps the lanes that
-                // accept slot q.
+                // last entry pair whole; the list holds at most its capacity
+                // less 32 entries here), and every lane tests its body
+                // against each of them, read by broadcast.  Lane q keeps the
+                // lanes that accept slot q.
                 float4* X = L + ((nlist + 1) & ~1);
                 const int nm = __popc(mb);
                 const int slot = __popc(mb & lt);
@@ -457,7 +457,7 @@ __global__ void __launch_bounds__(kThreads) traverse_masked_kernel(FParams p)
                     P[6] = e.w;
                 }
                 if (kFP64) LN[pos] = node;
-                if (WalkSmem<kFP64, kLearn>::kLL) LL[pos] = leaf ? ref : -1;  // for the own-leaf test
+                if (WalkSmem<kFP64, kLearn, kGroup>::kLL) LL[pos] = leaf ? ref : -1;  // for the own-leaf test
                 LM[pos] = A;
             }
             nlist += __popc(am);
@@ -470,7 +470,7 @@ __global__ void __launch_bounds__(kThreads) traverse_masked_kernel(FParams p)
             sp += __popc(pm);
             __syncwarp();
         }
-        if (nlist > WalkSmem<kFP64, kLearn>::kLst - 32 || (sp == 0 && nlist > 0)) {
+        if (nlist > WalkSmem<kFP64, kLearn, kGroup>::kLst - 32 || (sp == 0 && nlist > 0)) {
             if (kLearn == kLearnCollect) {
                 nlist = 0;  // collection evaluates nothing
                 __syncwarp();
@@ -682,7 +682,7 @@ int grid_n(int64_t n)
 template <bool kFP64, int kLearn, bool kGroup = false>
 int launch_walk(bh_context* ctx, const FParams& p)
 {
-    const size_t smem = sizeof(WalkSmem<kFP64, kLearn>);
+    const size_t smem = sizeof(WalkSmem<kFP64, kLearn, kGroup>);
     BH_CUDA_TRY(cudaFuncSetAttribute(traverse_masked_kernel<kFP64, kLearn, kGroup>,
                                      cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     // The plain walks keep their working set in shared memory and L2 (L1

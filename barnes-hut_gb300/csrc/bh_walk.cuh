@@ -19,6 +19,10 @@ constexpr int kList = 96;     // staged interactions per warp
 // (4M bodies, theta = 0.3); past the bound the walk reports an overflow.
 constexpr int kStack64 = 352;
 constexpr int kList64 = 128;
+// The group form's list: longer, for fewer flushes (its entries carry no lane
+// masks); 144 keeps 7 blocks per SM.  The per-body FP32 walk ran slower with
+// it, the learned walk no faster.
+constexpr int kListGroup = 144;
 constexpr int kSegs = 63;     // FP64 list evaluation: run slots body + thread, 0..62
 constexpr int kSlotBits = 28; // slot index bits of a stack entry (count - 1 in the top 3)
 constexpr float kMargin = 1e-5f;  // relative margin of the FP32 group tests
@@ -29,13 +33,13 @@ enum { kLearnNone = 0, kLearnInfer = 1, kLearnCollect = 2 };
 // Per-block shared memory of the walk.  Tables a variant does not use shrink
 // to one element, so that the FP32 walk fits 8 blocks (32 warps) per SM; the
 // FP64 walk fits 5 (6 ran slower: the FP64 pipe is already 86 % busy).
-template <bool kFP64, int kLearn>
+template <bool kFP64, int kLearn, bool kGroup = false>
 struct WalkSmem {
     static constexpr int kW64 = kFP64 ? kWarps : 1;      // FP64-only tables
     static constexpr bool kLL = kFP64;                    // leaf ids kept for the evaluation's own-leaf test
     static constexpr bool kF = kLearn == 1;              // network input rows
     static constexpr int kStk = kFP64 ? kStack64 : kStack;  // stack entries per warp
-    static constexpr int kLst = kFP64 ? kList64 : kList;    // staged entries per warp
+    static constexpr int kLst = kFP64 ? kList64 : kGroup ? kListGroup : kList;  // staged entries per warp
     int2 stack[kWarps][kStk];  // sibling ranges: {first | (count - 1) << 28, lane mask}
     // FP32 node data of the staged entries: {x, y, z, G m} per entry, or in
     // the plain FP32 walk entry pairs {x0, x1, y0, y1}, {z0, z1, w0, w1}
