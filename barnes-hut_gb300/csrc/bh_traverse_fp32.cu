@@ -391,18 +391,47 @@ __global__ void __launch_bounds__(kThreads) traverse_masked_kernel(FParams p)
                 // less 32 entries here), and every lane tests its body
                 // against each of them, read by broadcast.  Lane q keeps the
                 // lanes that accept slot q.
+                unsigned res = 0;
                 float4* X = L + ((nlist + 1) & ~1);
                 const int nm = __popc(mb);
                 const int slot = __popc(mb & lt);
-                if (mixed) X[slot] = make_float4(e.x, e.y, e.z, sm.side2f[depth]);
-                __syncwarp();
-                unsigned res = 0;
+                if (kGroup) {
+                    // Slots in the list's entry-pair layout, tested two at a
+                    // time in packed FP32 pairs (an odd count leaves a stale
+                    // second half, whose result no lane reads).  The per-body
+                    // form keeps one slot at a time: the pairs' registers
+                    // would cost it a resident block per SM.
+                    if (mixed) {
+                        float* P = reinterpret_cast<float*>(X + (slot & ~1)) + (slot & 1);
+                        P[0] = e.x;
+                        P[2] = e.y;
+                        P[4] = e.z;
+                        P[6] = sm.side2f[depth];
+                    }
+                    __syncwarp();
+                    const f32x2 qx = pk(rx, rx), qy = pk(ry, ry), qz = pk(rz, rz), qt = pk(theta2f, theta2f);
+                    for (int q = 0; q < nm; q += 2) {
+                        const ulonglong2 xy = *reinterpret_cast<const ulonglong2*>(X + q);
+                        const ulonglong2 zs = *reinterpret_cast<const ulonglong2*>(X + q + 1);
+                        const f32x2 dx = sub2(xy.x, qx), dy = sub2(xy.y, qy), dz = sub2(zs.x, qz);
+                        float t0, t1, s0, s1;
+                        upk(mul2(qt, fma2(dx, dx, fma2(dy, dy, mul2(dz, dz)))), t0, t1);
+                        upk(zs.y, s0, s1);
+                        const unsigned b0 = __ballot_sync(0xffffffffu, s0 < t0);
+                        const unsigned b1 = __ballot_sync(0xffffffffu, s1 < t1);
+                        if (lane == q) res = b0;
+                        if (lane == q + 1) res = b1;
+                    }
+                } else {
+                    if (mixed) X[slot] = make_float4(e.x, e.y, e.z, sm.side2f[depth]);
+                    __syncwarp();
 #pragma unroll 2
-                for (int q = 0; q < nm; ++q) {
-                    const float4 v = X[q];
-                    const float dx = v.x - rx, dy = v.y - ry, dz = v.z - rz;
-                    const unsigned bq = __ballot_sync(0xffffffffu, v.w < theta2f * (dx * dx + dy * dy + dz * dz));
-                    if (lane == q) res = bq;
+                    for (int q = 0; q < nm; ++q) {
+                        const float4 v = X[q];
+                        const float dx = v.x - rx, dy = v.y - ry, dz = v.z - rz;
+                        const unsigned bq = __ballot_sync(0xffffffffu, v.w < theta2f * (dx * dx + dy * dy + dz * dz));
+                        if (lane == q) res = bq;
+                    }
                 }
                 const unsigned acc = __shfl_sync(0xffffffffu, res, slot & 31);
                 // The group form accepts a mixed node only when every body
