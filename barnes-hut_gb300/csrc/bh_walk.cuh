@@ -60,6 +60,14 @@ struct WalkSmem {
     uint16_t segn[kW64][kFP64 ? kSegs : 1];  // and its interaction count
 };
 
+// The resident blocks per SM each layout is sized for, in the SM's 228 KB of
+// shared memory (1 KB of it reserved per block); registers allow no more.
+constexpr size_t kSmemPerSM = 228 * 1024, kSmemReserved = 1024;
+static_assert(5 * (sizeof(WalkSmem<true, kLearnNone>) + kSmemReserved) <= kSmemPerSM, "FP64 walk: 5 blocks per SM");
+static_assert(8 * (sizeof(WalkSmem<false, kLearnNone>) + kSmemReserved) <= kSmemPerSM, "FP32 walk: 8 blocks per SM");
+static_assert(7 * (sizeof(WalkSmem<false, kLearnNone, true>) + kSmemReserved) <= kSmemPerSM,
+              "group walk: 7 blocks per SM");
+
 // Packed FP32 pairs (two floats in one 64-bit register): one f32x2
 // instruction does two FP32 operations, each rounded as the scalar one.
 using f32x2 = unsigned long long;
