@@ -104,7 +104,8 @@ __global__ void __launch_bounds__(kSortThreads) onesweep_kernel(
     for (int k = 0; k < kSortItems; ++k) {
         const int64_t i = base + w * (32 * kSortItems) + k * 32 + lane;
         const bool valid = i < n;
-        const uint32_t d = valid ? (uint32_t)((key[k] >> shift) & 0xFF) : 0x100u;
+        const uint32_t d = valid ? (uint32_t)((key[k] >> shift) & 0xFF) : 0u;
+        // lanes past the end form their own peer set, apart from every digit
         const unsigned vb = __ballot_sync(0xffffffffu, valid);
         unsigned peers = valid ? vb : ~vb;
 #pragma unroll
